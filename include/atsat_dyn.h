@@ -1,0 +1,262 @@
+/*
+ * atsat_dyn.h -- C ABI of the GB300 dynamical core for the ATSAT Saturn model.
+ *
+ * The library replaces two member functions of cSaturnModel behind plain C entry points:
+ *
+ *   cSaturnModel::RungeKuttaSat()              planet/RungeKutta_Sat_Turb.cpp:110-387
+ *     (with computeBuoyancyRefLevel :31-50, computeMetricPressure :60-108 and the per-cell
+ *      right-hand side cSaturnModel::RHSSat, planet/RHS_Sat_Turb.cpp:25-1016)
+ *   PressureSolver<cSaturnModel>::run()        planet/PressureSolver.h:145-766
+ *     (with its model hook cSaturnModel::prepareProjectionBoundaries, planet/Pressure_Sat.cpp:78-194)
+ *
+ * and, as device glue for resident multi-step runs, computeMixtureDensity (Pressure_Sat.cpp:49-62),
+ * restoreVar (planet/cSaturnModel.cpp:1551-1600) and the boundary passes of BC_Sat.
+ *
+ * Conventions
+ *   - Every entry point returns an int status: ATSAT_DYN_OK (0) or a negative ATSAT_DYN_E_* code.
+ *     Nothing in the library calls exit(), abort() or traps on the device. atsat_dyn_last_error()
+ *     gives a one-line reason for the last failure on a handle.
+ *   - A handle owns one CUDA stream and all of its device memory. A handle is not thread-safe;
+ *     different handles may be driven from different threads.
+ *   - Fields are bound to HOST storage, either as the reference's ragged rows (Array::x[i][j] is
+ *     one row of km doubles) or as one contiguous [im][jm][km] block. upload/download copy between
+ *     the bound host storage and the device copy; every compute entry point works on the device copy
+ *     only and returns when the device work is complete (ATSAT_DYN_ASYNC unset).
+ *   - There is no CPU fallback: a knob value the device path does not implement makes
+ *     atsat_dyn_create return ATSAT_DYN_E_UNSUPPORTED.
+ */
+#ifndef ATSAT_DYN_H
+#define ATSAT_DYN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ATSAT_DYN_ABI_VERSION 1
+
+/* ---- status codes ---- */
+enum {
+    ATSAT_DYN_OK                 =  0,
+    ATSAT_DYN_E_INVALID          = -1,  /* bad argument, size or field id */
+    ATSAT_DYN_E_UNSUPPORTED      = -2,  /* a knob value the device path does not implement */
+    ATSAT_DYN_E_CUDA             = -3,  /* a CUDA runtime call failed */
+    ATSAT_DYN_E_TIMEOUT          = -4,  /* a bounded device wait gave up */
+    ATSAT_DYN_E_NONFINITE_INPUT  = -5,  /* atsat_dyn_check_finite found NaN/Inf in an input */
+    ATSAT_DYN_E_NOMEM            = -6,  /* device or pinned host allocation failed */
+    ATSAT_DYN_E_UNBOUND          = -7   /* upload/download of a field with no host binding */
+};
+
+/* ---- arithmetic of the step ---- */
+enum {
+    ATSAT_DYN_FP64  = 0,   /* plain FP64 drop-in: every operation in double */
+    ATSAT_DYN_MIXED = 1    /* FP32 stencils on FP32 stage inputs; FP64 state, accumulator,
+                              level-mean reductions and Poisson defect correction */
+};
+
+/* ---- field ids ----
+ * The 17 prognostic fields in the order RHSSat differentiates them (RHS_Sat_Turb.cpp:137-153). */
+enum {
+    ATSAT_F_U = 0, ATSAT_F_V, ATSAT_F_W, ATSAT_F_T,
+    ATSAT_F_H2O, ATSAT_F_H2O_CLOUD, ATSAT_F_H2O_ICE, ATSAT_F_H2S,
+    ATSAT_F_NH3, ATSAT_F_NH3_CLOUD, ATSAT_F_NH3_ICE,
+    ATSAT_F_CH4, ATSAT_F_CH4_CLOUD, ATSAT_F_CH4_ICE, ATSAT_F_NH4SH,
+    ATSAT_F_TKE, ATSAT_F_DIS,
+    ATSAT_NPROG = 17,
+
+    /* start-of-step copies y_n (un, vn, ..., tken, disn), same order */
+    ATSAT_F_N_BASE = 17,
+    ATSAT_F_UN = 17, ATSAT_F_VN, ATSAT_F_WN, ATSAT_F_TN,
+    ATSAT_F_H2ON, ATSAT_F_H2O_CLOUDN, ATSAT_F_H2O_ICEN, ATSAT_F_H2SN,
+    ATSAT_F_NH3N, ATSAT_F_NH3_CLOUDN, ATSAT_F_NH3_ICEN,
+    ATSAT_F_CH4N, ATSAT_F_CH4_CLOUDN, ATSAT_F_CH4_ICEN, ATSAT_F_NH4SHN,
+    ATSAT_F_TKEN, ATSAT_F_DISN,
+
+    /* pressures and density */
+    ATSAT_F_P_DYN = 34, ATSAT_F_P_STAT, ATSAT_F_P_METRIC, ATSAT_F_RHO_MIX,
+
+    /* point inputs of RHSSat */
+    ATSAT_F_NUE = 38, ATSAT_F_Q_PRECIP, ATSAT_F_Q_RAD, ATSAT_F_TKE_SOURCE, ATSAT_F_DIS_SOURCE,
+    ATSAT_F_S_PRECIP_H2O, ATSAT_F_S_PRECIP_H2O_CLOUD, ATSAT_F_S_PRECIP_H2O_ICE,
+    ATSAT_F_S_PRECIP_NH3, ATSAT_F_S_PRECIP_NH3_CLOUD, ATSAT_F_S_PRECIP_NH3_ICE,
+    ATSAT_F_S_PRECIP_CH4, ATSAT_F_S_PRECIP_CH4_CLOUD, ATSAT_F_S_PRECIP_CH4_ICE,
+    ATSAT_F_MASSFLUX_H2S, ATSAT_F_MASSFLUX_NH3, ATSAT_F_MASSFLUX_NH4SH,
+    ATSAT_F_FLUXLIM_NH4SH, ATSAT_F_THERMALMASSFLUX,
+
+    /* tendencies rhs_* in prognostic order, then aux_u/v/w */
+    ATSAT_F_RHS_BASE = 57,
+    ATSAT_F_RHS_U = 57, ATSAT_F_RHS_V, ATSAT_F_RHS_W, ATSAT_F_RHS_T,
+    ATSAT_F_RHS_H2O, ATSAT_F_RHS_H2O_CLOUD, ATSAT_F_RHS_H2O_ICE, ATSAT_F_RHS_H2S,
+    ATSAT_F_RHS_NH3, ATSAT_F_RHS_NH3_CLOUD, ATSAT_F_RHS_NH3_ICE,
+    ATSAT_F_RHS_CH4, ATSAT_F_RHS_CH4_CLOUD, ATSAT_F_RHS_CH4_ICE, ATSAT_F_RHS_NH4SH,
+    ATSAT_F_RHS_TKE, ATSAT_F_RHS_DIS,
+    ATSAT_F_AUX_U = 74, ATSAT_F_AUX_V, ATSAT_F_AUX_W,
+
+    /* previous-iteration dynamic pressure, written by restoreVar */
+    ATSAT_F_P_DYNN = 77,
+
+    ATSAT_NFIELDS = 78
+};
+
+/* ---- grid ----
+ * rad_z and the_z are cSaturnModel::rad.z and the.z as the reference builds them
+ * (Array_1D::Coordinates, lib/Array_1D.cpp:50-61: a running sum of dr / dthe). The arrays are
+ * copied at create time. */
+typedef struct atsat_dyn_grid {
+    int32_t im, jm, km;
+    int32_t reserved0;
+    const double* rad_z;      /* im values */
+    const double* the_z;      /* jm values, colatitude in radians */
+    double dr, dthe, dphi;
+} atsat_dyn_grid;
+
+/* ---- constants and resolved knobs ----
+ * The constants are cSaturnModel members after LoadConfig and ThermalPropertiesSat; the knobs
+ * are the ATSAT_* environment switches resolved the way the reference resolves them
+ * (atsat_dyn_params_from_env does that). */
+typedef struct atsat_dyn_params {
+    /* model constants */
+    double re, pr;
+    double sc_h2o, sc_nh3, sc_h2s, sc_ch4, sc_nh4sh;
+    double u_0, t_ref, L_atm, g, omega;
+    double Coriolis, centrifugal, buoyancy, chemical_reaction;
+    double cp_mix, r_mix, R_mix;
+    double dt;
+    /* real-valued knobs */
+    double metric_radius_km;   /* ATSAT_METRIC_RADIUS, 58232 (cSaturnModel.h:164-169) */
+    double sinthe_min;         /* ATSAT_SINTHE_MIN, 0 (cSaturnModel.h:458-465) */
+    double buoy_scale;         /* ATSAT_BUOY_SCALE, 1 (RHS_Sat_Turb.cpp:268-269) */
+    double turb_coupling;      /* ATSAT_TURB_COUPLING, 1 (RHS_Sat_Turb.cpp:577-578) */
+    double rad_coupling;       /* ATSAT_RAD_COUPLING, 0 (RHS_Sat_Turb.cpp:611-612) */
+    double precip_coupling;    /* ATSAT_PRECIP_COUPLING, 1 (RHS_Sat_Turb.cpp:645-650) */
+    double thermal_massflux;   /* ATSAT_THERMAL_MASSFLUX, 0 (RHS_Sat_Turb.cpp:749-750) */
+    double species_divu;       /* ATSAT_SPECIES_DIVU, 0 (RHS_Sat_Turb.cpp:979) */
+    double pdyn_cap;           /* ATSAT_PDYN_CAP, 0.2 (PressureSolver.h:168) */
+    /* switches, each resolved to 0 or 1 */
+    int32_t phi_periodic;      /* ATSAT_BC_PHI_PERIODIC, 1 (ATPhys.h:124-129) */
+    int32_t metric_split;      /* ATSAT_METRIC_SPLIT, 1 */
+    int32_t coriolis_split;    /* ATSAT_CORIOLIS_SPLIT && metric_split, 1 */
+    int32_t hydro_buoy;        /* ATSAT_HYDRO_BUOY && metric_split, 0 */
+    int32_t nd_cor;            /* Coriolis at L/u_0 scale: ATSAT_ND_COR, else GEO_BALANCE, else NONDIM; 1 */
+    int32_t nd_cent;           /* ATSAT_ND_CENT, else NONDIM; 0 */
+    int32_t nd_buoy;           /* ATSAT_ND_BUOY, else NONDIM; 0 */
+    int32_t cell_hold;         /* ATSAT_CELL_HOLD, else GEO_BALANCE; 1 */
+    int32_t adiabatic;         /* ATSAT_ADIABATIC, 1 */
+    int32_t adiabatic_rho;     /* ATSAT_ADIABATIC_RHO, 1 */
+    int32_t turb_active;       /* cSaturnModel::turb_active, 1 with turb_model k_omega_SST */
+    int32_t t_limiter;         /* ATSAT_T_LIMITER, 0 */
+    int32_t buoy_legacy;       /* ATSAT_BUOY_LEGACY, 0 */
+    int32_t chrom;             /* ATSAT_CHROM, 0 (1 is not implemented: UNSUPPORTED) */
+    int32_t cp_h2_dyn;         /* ATSAT_CP_H2 / _CP_GAS in the RHS, 0 (1: UNSUPPORTED) */
+    int32_t print_diag;        /* any of ATSAT_TB/UB/CWB_DIAG, 0 (1: UNSUPPORTED) */
+    int32_t coord_stretching;  /* cSaturnModel::coord_stretching, 0 */
+    int32_t press_src;         /* ATSAT_PRESS_SRC, 1 */
+    int32_t press_incr;        /* ATSAT_PRESS_INCR, 1 (Run() sets it under GEO_BALANCE) */
+    int32_t press_sweeps;      /* ATSAT_PRESS_SWEEPS, 1 (values < 1 mean 1) */
+    int32_t press_wall;        /* ATSAT_PRESS_WALL, 0 (ATSAT has no solid body) */
+    int32_t rigid_lid;         /* ATSAT_BC_RIGID_LID, 1 */
+    int32_t press_line;        /* ATSAT_PRESS_LINE, 0 */
+    int32_t press_baro;        /* ATSAT_PRESS_BAROTROPIC (effective), 0 */
+    int32_t precision;         /* ATSAT_DYN_FP64 or ATSAT_DYN_MIXED */
+    int32_t reserved[9];
+} atsat_dyn_params;
+
+/* statistics of one pressure call */
+typedef struct atsat_dyn_pstats {
+    int32_t sweeps;            /* red-black sweeps done */
+    int32_t reserved0;
+    double  src_clamped;       /* cells whose source hit +-den*PDYN_CAP or was non-finite */
+    double  max_abs_update;    /* max |p_new - p_old| over the interior, last sweep */
+} atsat_dyn_pstats;
+
+/* device-side diagnostics */
+typedef struct atsat_dyn_diag {
+    int64_t launches;          /* kernels launched by this handle since create */
+    int64_t nonfinite;         /* non-finite cells found by the last atsat_dyn_check_finite */
+    int32_t timeout;           /* a bounded device wait gave up */
+    int32_t reserved[5];
+} atsat_dyn_diag;
+
+typedef struct atsat_dyn* atsat_dyn_t;
+
+/* ---- set-up ---- */
+
+/* The reference's defaults: constants of the committed configuration (cSaturnDefaults.cpp.inc,
+ * cSaturnModel.h member initialisers) and every knob at its default. cp_mix, r_mix and R_mix are
+ * filled with the values ChemistrySat::ThermalPropertiesSat computes from the default composition. */
+int atsat_dyn_params_default(atsat_dyn_params* p);
+
+/* Overwrite the knob fields of *p from the ATSAT_* environment variables, resolved as the reference
+ * resolves them (defaults where a variable is unset). Constants are left alone. */
+int atsat_dyn_params_from_env(atsat_dyn_params* p);
+
+int  atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_dyn_t* out);
+void atsat_dyn_destroy(atsat_dyn_t h);
+const char* atsat_dyn_last_error(atsat_dyn_t h);
+int  atsat_dyn_abi_version(void);
+
+/* ---- host bindings and transfers ---- */
+
+/* rows[i*jm + j] points to km doubles: the layout of Array::x (lib/Array.cpp:62-70). */
+int atsat_dyn_bind_host_rows(atsat_dyn_t h, int32_t field, double* const* rows);
+/* base points to im*jm*km doubles, k fastest. */
+int atsat_dyn_bind_host_array(atsat_dyn_t h, int32_t field, double* base);
+int atsat_dyn_upload(atsat_dyn_t h, const int32_t* fields, int32_t n);
+int atsat_dyn_download(atsat_dyn_t h, const int32_t* fields, int32_t n);
+
+/* cell_vbar0 / cell_ubar0: im*jm values or NULL (empty vectors); p_baro: im*jm*km values or NULL. */
+int atsat_dyn_set_tables(atsat_dyn_t h, const double* cell_vbar0, const double* cell_ubar0,
+                         const double* p_baro);
+/* buoy_ref_level[im] of the last computeBuoyancyRefLevel on the device */
+int atsat_dyn_get_buoy_ref_level(atsat_dyn_t h, double* out);
+
+/* ---- the hot path ---- */
+
+int atsat_dyn_mixture_density(atsat_dyn_t h);          /* Pressure_Sat.cpp:49-62 */
+int atsat_dyn_buoyancy_ref_level(atsat_dyn_t h);       /* RungeKutta_Sat_Turb.cpp:31-50 */
+int atsat_dyn_metric_pressure(atsat_dyn_t h);          /* RungeKutta_Sat_Turb.cpp:60-108 */
+/* One RHSSat pass over the RK interior (RungeKutta_Sat_Turb.cpp:220-247) on the live fields:
+ * writes all rhs_* and aux_u/v/w. Uses the buoyancy level and p_metric already on the device. */
+int atsat_dyn_rhs(atsat_dyn_t h);
+int atsat_dyn_rk4_step(atsat_dyn_t h);                 /* RungeKutta_Sat_Turb.cpp:110-387 */
+int atsat_dyn_prepare_projection_boundaries(atsat_dyn_t h);   /* Pressure_Sat.cpp:78-194 */
+int atsat_dyn_pressure(atsat_dyn_t h, atsat_dyn_pstats* out); /* PressureSolver.h:145-766 */
+
+/* ---- device glue for resident multi-step runs ---- */
+int atsat_dyn_restore_var(atsat_dyn_t h);              /* restoreVar(1.0), cSaturnModel.cpp:1551-1600 */
+
+/* ---- diagnostics and timing ---- */
+int atsat_dyn_sync(atsat_dyn_t h);
+int atsat_dyn_status(atsat_dyn_t h, atsat_dyn_diag* out);
+/* Count non-finite cells of a field on the device (the reference's NaN census, FileIO_Sat.cpp:418). */
+int atsat_dyn_count_nonfinite(atsat_dyn_t h, int32_t field, int64_t* count);
+/* Per-kernel CUDA-event timing on the handle's stream: enable, reset, and read the launch count
+ * and summed milliseconds of kernel class `kclass` (ATSAT_K_*). */
+enum {
+    ATSAT_K_RK_STAGE = 0,   /* fused RHS + stage update (one per RK stage) */
+    ATSAT_K_LEVEL_MEAN,     /* buoyancy level mean */
+    ATSAT_K_METRIC_SCAN,    /* p_metric radial prefix sum */
+    ATSAT_K_PRESS_SOURCE,   /* projection source + lc_old */
+    ATSAT_K_PRESS_SWEEP,    /* red-black half-sweep */
+    ATSAT_K_PRESS_BOUNDARY, /* Neumann planes, seam, projection boundary prep */
+    ATSAT_K_GLUE,           /* density, restoreVar, boundary conditions */
+    ATSAT_K_RHS,            /* standalone RHS pass */
+    ATSAT_K_NCLASS
+};
+int atsat_dyn_profile(atsat_dyn_t h, int32_t enable);
+int atsat_dyn_profile_reset(atsat_dyn_t h);
+int atsat_dyn_profile_read(atsat_dyn_t h, int32_t kclass, int64_t* launches, double* ms);
+/* Device-side pointer and row pitch (in elements) of a field's device copy. */
+int atsat_dyn_device_field(atsat_dyn_t h, int32_t field, double** dptr, int64_t* pitch);
+
+/* Pinned host memory for bound arrays (cudaHostAlloc / cudaFreeHost). */
+void* atsat_dyn_host_alloc(size_t bytes);
+void  atsat_dyn_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ATSAT_DYN_H */

@@ -1,0 +1,790 @@
+/*
+ * ORACLE -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C, FP64, OpenMP restatement of the ATSAT dynamical core, used by tests/ and bench.py's
+ * CPU-baseline leg as the checker of the CUDA path. It is never linked into, called by or shipped
+ * with the product library (atsat_gb300/csrc), which fails loudly when its CUDA build is missing.
+ *
+ * It restates, operation by operation and in the reference's evaluation order, so that on a
+ * machine without FMA contraction it agrees with the reference bit for bit (build with
+ * -ffp-contract=off):
+ *   cSaturnModel::computeBuoyancyRefLevel   planet/RungeKutta_Sat_Turb.cpp:31-50
+ *   cSaturnModel::computeMetricPressure     planet/RungeKutta_Sat_Turb.cpp:60-108
+ *   cSaturnModel::RHSSat                    planet/RHS_Sat_Turb.cpp:25-1016
+ *   cSaturnModel::RungeKuttaSat             planet/RungeKutta_Sat_Turb.cpp:110-387
+ *   cSaturnModel::computeMixtureDensity     planet/Pressure_Sat.cpp:49-62
+ *   cSaturnModel::prepareProjectionBoundaries planet/Pressure_Sat.cpp:78-194
+ *   PressureSolver<cSaturnModel>::run       planet/PressureSolver.h:145-766 (pointwise sweep)
+ *   cSaturnModel::restoreVar(1.0)           planet/cSaturnModel.cpp:1551-1600
+ * Parity of this file with the reference is pinned by tests/test_oracle_golden.py against
+ * fixtures produced by the reference itself (oracle/ref_harness.cpp).
+ *
+ * Storage: each field is one contiguous [im][jm][km] block of doubles (k fastest), indexed by the
+ * field ids of include/atsat_dyn.h. The reference's ragged rows hold the same numbers.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/atsat_dyn.h"
+
+typedef struct {
+    int im, jm, km;
+    const double *rad_z, *the_z;
+    double dr, dthe, dphi;
+    const atsat_dyn_params* p;
+    double** f;                 /* ATSAT_NFIELDS pointers */
+    const double *vbar0, *ubar0, *p_baro;
+    double* buoy;               /* im */
+    double* acc[ATSAT_NPROG];   /* RK4 accumulators */
+} M;
+
+#define IDX(m, i, j, k) ((((size_t)(i)) * (m)->jm + (size_t)(j)) * (m)->km + (size_t)(k))
+#define X(m, fid, i, j, k) ((m)->f[fid][IDX(m, i, j, k)])
+
+/* std::max / std::min as the reference evaluates them (NaN passes through the same way). */
+static inline double smax(double a, double b) { return (a < b) ? b : a; }
+static inline double smin(double a, double b) { return (b < a) ? b : a; }
+
+/* cSaturnModel::metricRadius, cSaturnModel.h:164-169 */
+static inline double metric_radius(const M* m, double r) {
+    const double R_km = m->p->metric_radius_km;
+    if (!(R_km > 0.0)) return r;
+    return r + (R_km / m->p->L_atm - 1.0);
+}
+
+static inline int phi_wrap(int periodic, int kk, int km) {
+    if (!periodic) return kk;
+    const int n = km - 1;
+    return kk < 0 ? kk + n : (kk >= n ? kk - n : kk);
+}
+
+typedef struct {
+    double rm, rm2, exp_rm, exp_2_rm;
+    double sinthe, sinthe2, costhe, cotanthe;
+    double inv_rm, inv_rm2;
+    double inv_rmsinthe, inv_rm2sinthe, inv_rm2sinthe2;
+    double costhe_inv_rm2sinthe;
+    double inv_2dr, inv_2dthe, inv_2dphi;
+    double inv_dr2, inv_dthe2, inv_dphi2;
+} Geo;
+
+/* RungeKutta_Sat_Turb.cpp:223-243 */
+static void make_geo(const M* m, int i, double sinthe, double costhe, Geo* g) {
+    g->rm = metric_radius(m, m->rad_z[i]);
+    g->rm2 = g->rm * g->rm;
+    g->exp_rm = m->p->coord_stretching ? 1.0 / (g->rm + 1.0) : 1.0;
+    g->exp_2_rm = g->exp_rm * g->exp_rm;
+    g->sinthe = sinthe;
+    g->sinthe2 = g->sinthe * g->sinthe;
+    g->costhe = costhe;
+    g->cotanthe = g->costhe / g->sinthe;
+    g->inv_rm = 1.0 / g->rm;
+    g->inv_rm2 = 1.0 / g->rm2;
+    g->inv_rmsinthe = 1.0 / (g->rm * g->sinthe);
+    g->inv_rm2sinthe = g->inv_rm2 / g->sinthe;
+    g->inv_rm2sinthe2 = g->inv_rm2 / g->sinthe2;
+    g->costhe_inv_rm2sinthe = g->costhe * g->inv_rm2sinthe;
+    g->inv_2dr = 1.0 / (2.0 * m->dr);
+    g->inv_2dthe = 1.0 / (2.0 * m->dthe);
+    g->inv_2dphi = 1.0 / (2.0 * m->dphi);
+    g->inv_dr2 = 1.0 / (m->dr * m->dr);
+    g->inv_dthe2 = 1.0 / (m->dthe * m->dthe);
+    g->inv_dphi2 = 1.0 / (m->dphi * m->dphi);
+}
+
+/* ---------------- RungeKutta_Sat_Turb.cpp:31-50 ---------------- */
+static void buoyancy_ref_level(M* m) {
+    const atsat_dyn_params* p = m->p;
+    #pragma omp parallel for schedule(static)
+    for (int i = 0; i < m->im; i++) {
+        double sum = 0.0, wsum = 0.0;
+        for (int j = 0; j < m->jm; j++) {
+            const double wgt = sin(m->the_z[j]);
+            for (int k = 0; k < m->km; k++) {
+                const double t = X(m, ATSAT_F_T, i, j, k);
+                if (!(t > 0.0)) continue;
+                const double b = p->g * X(m, ATSAT_F_P_STAT, i, j, k) / (p->r_mix * p->R_mix * t * p->t_ref);
+                if (!isfinite(b)) continue;
+                sum += wgt * b;
+                wsum += wgt;
+            }
+        }
+        m->buoy[i] = (wsum > 0.0) ? sum / wsum : 0.0;
+    }
+}
+
+/* ---------------- RungeKutta_Sat_Turb.cpp:60-108 ---------------- */
+static void metric_pressure(M* m) {
+    const atsat_dyn_params* p = m->p;
+    const int im = m->im, jm = m->jm, km = m->km;
+    const int hb = p->hydro_buoy;
+    const double hb_coeff = hb ? p->g * (p->L_atm * 1.0e3) / (p->u_0 * p->u_0) : 0.0;
+    double* tbar = (double*)calloc((size_t)im, sizeof(double));
+    if (hb) {
+        for (int i = 0; i < im; i++) {
+            double s = 0.0, sw = 0.0;
+            for (int j = 0; j < jm; j++) {
+                const double wgt = fabs(sin(m->the_z[j]));
+                for (int k = 0; k < km - 1; k++) { s += wgt * X(m, ATSAT_F_T, i, j, k); sw += wgt; }
+            }
+            tbar[i] = (sw > 0.0) ? s / sw : 1.0;
+        }
+    }
+    #pragma omp parallel for collapse(2) schedule(static)
+    for (int j = 0; j < jm; j++) {
+        for (int k = 0; k < km; k++) {
+            const double cor_ = p->coriolis_split
+                ? p->Coriolis * (p->nd_cor ? p->L_atm * 1.0e3 / p->u_0 : 1.0) * 2.0 * p->omega * fabs(sin(m->the_z[j]))
+                : 0.0;
+            double f_prev = 0.0;
+            for (int i = 0; i < im; i++) {
+                const double rm_ = metric_radius(m, m->rad_z[i]);
+                const double exp_rm_ = p->coord_stretching ? 1.0 / (rm_ + 1.0) : 1.0;
+                const double v = X(m, ATSAT_F_V, i, j, k), w = X(m, ATSAT_F_W, i, j, k);
+                double f;
+                if (!hb) {
+                    f = ((v * v + w * w) / rm_ + cor_ * w) / exp_rm_;
+                } else {
+                    const double tb_ = tbar[i], t = X(m, ATSAT_F_T, i, j, k);
+                    const double b_ = (tb_ > 0.0 && isfinite(t)) ? hb_coeff * (t - tb_) / tb_ : 0.0;
+                    f = ((v * v + w * w) / rm_ + cor_ * w + b_) / exp_rm_;
+                }
+                if (i == 0) X(m, ATSAT_F_P_METRIC, 0, j, k) = 0.0;
+                else X(m, ATSAT_F_P_METRIC, i, j, k) = X(m, ATSAT_F_P_METRIC, i - 1, j, k) + 0.5 * (f_prev + f) * m->dr;
+                f_prev = f;
+            }
+            if (m->p_baro)
+                for (int i = 0; i < im; i++) X(m, ATSAT_F_P_METRIC, i, j, k) += m->p_baro[IDX(m, i, j, k)];
+        }
+    }
+    free(tbar);
+}
+
+/* ---------------- RHS_Sat_Turb.cpp:25-1016 ---------------- */
+
+/* One transported scalar: central first and second differences in r, theta, phi
+ * (RHS_Sat_Turb.cpp:133-207). */
+typedef struct { double dr, d2r, dthe, d2the, dphi, d2phi; } D6;
+
+static inline void derivs(const M* m, int fid, int i, int j, int k, int kw, int ke, const Geo* g, D6* d) {
+    const double c = X(m, fid, i, j, k);
+    const double rp = X(m, fid, i + 1, j, k), rmn = X(m, fid, i - 1, j, k);
+    const double tp = X(m, fid, i, j + 1, k), tmn = X(m, fid, i, j - 1, k);
+    const double pe = X(m, fid, i, j, ke), pw = X(m, fid, i, j, kw);
+    d->dr = (rp - rmn) * g->inv_2dr * g->exp_rm;
+    d->d2r = (rp - 2.0 * c + rmn) * g->inv_dr2 * g->exp_2_rm;
+    d->dthe = (tp - tmn) * g->inv_2dthe;
+    d->d2the = (tp - 2.0 * c + tmn) * g->inv_dthe2;
+    d->dphi = (pe - pw) * g->inv_2dphi;
+    d->d2phi = (pe - 2.0 * c + pw) * g->inv_dphi2;
+}
+
+static inline double transport(double u, double v, double w, const D6* d, const Geo* g) {
+    return u * d->dr + v * d->dthe * g->inv_rm + w * d->dphi * g->inv_rmsinthe;
+}
+
+static inline double diffusion(const D6* d, double two_inv_rm, const Geo* g) {
+    return d->d2r + d->dr * two_inv_rm + d->d2the * g->inv_rm2
+         + d->dthe * g->costhe_inv_rm2sinthe + d->d2phi * g->inv_rm2sinthe2;
+}
+
+static void rhs_cell(M* m, int i, int j, int k, const Geo* g) {
+    const atsat_dyn_params* p = m->p;
+    const int per = p->phi_periodic;
+    const int kw = phi_wrap(per, k - 1, m->km);
+    const int ke = phi_wrap(per, k + 1, m->km);
+    const size_t c = IDX(m, i, j, k);
+    double** f = m->f;
+
+    const double costhe = g->costhe, cotanthe = g->cotanthe;
+    const double inv_rm = g->inv_rm, inv_rm2 = g->inv_rm2, inv_rmsinthe = g->inv_rmsinthe;
+    const double inv_rm2sinthe = g->inv_rm2sinthe, inv_rm2sinthe2 = g->inv_rm2sinthe2;
+    const double costhe_inv_rm2sinthe = g->costhe_inv_rm2sinthe;
+
+    const double u_ijk = f[ATSAT_F_U][c], v_ijk = f[ATSAT_F_V][c], w_ijk = f[ATSAT_F_W][c];
+
+    D6 d[ATSAT_NPROG];
+    for (int q = 0; q < ATSAT_NPROG; q++) derivs(m, q, i, j, k, kw, ke, g, &d[q]);
+    const double dpdr = (X(m, ATSAT_F_P_DYN, i + 1, j, k) - X(m, ATSAT_F_P_DYN, i - 1, j, k)) * g->inv_2dr * g->exp_rm;
+    const double dpdthe = (X(m, ATSAT_F_P_DYN, i, j + 1, k) - X(m, ATSAT_F_P_DYN, i, j - 1, k)) * g->inv_2dthe;
+    const double dpdphi = (X(m, ATSAT_F_P_DYN, i, j, ke) - X(m, ATSAT_F_P_DYN, i, j, kw)) * g->inv_2dphi;
+
+    /* body-force scale factors, RHS_Sat_Turb.cpp:260-277 */
+    const double L_m = p->L_atm * 1.0e3;
+    const double nd_cor = p->nd_cor ? L_m / p->u_0 : 1.0;
+    const double nd_cent = p->nd_cent ? L_m * L_m / (p->u_0 * p->u_0) : 1.0;
+    const double nd_buoy = p->nd_buoy ? 1.0e5 * L_m / (p->u_0 * p->u_0) : 1.0;
+
+    /* Coriolis, :310-321 */
+    const double sinthe_true = sqrt(smax(0.0, 1.0 - costhe * costhe));
+    const double Coriolis_rad = nd_cor * -2.0 * p->omega * sinthe_true * w_ijk;
+    const double Coriolis_the = nd_cor * -2.0 * p->omega * costhe * w_ijk;
+    double v_cor = v_ijk, u_cor = u_ijk;
+    if (p->cell_hold && m->vbar0) {
+        v_cor -= m->vbar0[(size_t)i * m->jm + j];
+        u_cor -= m->ubar0[(size_t)i * m->jm + j];
+    }
+    const double Coriolis_phi = nd_cor * +2.0 * p->omega * (+costhe * v_cor + sinthe_true * u_cor);
+
+    /* centrifugal, :349-350 */
+    const double centrifugal_rad = nd_cent * p->omega * p->omega * g->rm * sinthe_true * sinthe_true;
+    const double centrifugal_the = nd_cent * p->omega * p->omega * g->rm * sinthe_true * costhe;
+
+    const double coeff_energy_p = p->u_0 * p->u_0 / (p->cp_mix * p->t_ref);
+
+    /* adiabatic compression work, :368-378 */
+    double dpstatdr = 0.0;
+    if (p->adiabatic) {
+        const double to_nd = 1.0 / (p->r_mix * p->u_0 * p->u_0 * 1.0e-5);
+        dpstatdr = (X(m, ATSAT_F_P_STAT, i + 1, j, k) - X(m, ATSAT_F_P_STAT, i - 1, j, k)) * g->inv_2dr * g->exp_rm * to_nd;
+        const double rho_l = f[ATSAT_F_RHO_MIX][c];
+        if (p->adiabatic_rho && rho_l > 0.0 && isfinite(rho_l)) dpstatdr *= p->r_mix / rho_l;
+    }
+
+    const double pressure_t = coeff_energy_p * (u_ijk * (dpdr + dpstatdr)
+        + v_ijk * dpdthe * inv_rm + w_ijk * dpdphi * inv_rmsinthe);
+    const double transport_t = transport(u_ijk, v_ijk, w_ijk, &d[ATSAT_F_T], g);
+
+    const double metric_on = p->metric_split ? 0.0 : 1.0;
+    const double cor_rad_on = p->coriolis_split ? 0.0 : 1.0;
+    const D6 *du = &d[ATSAT_F_U], *dv = &d[ATSAT_F_V], *dw = &d[ATSAT_F_W];
+    const double transport_u = u_ijk * du->dr + v_ijk * du->dthe * inv_rm + w_ijk * du->dphi * inv_rmsinthe
+        - metric_on * (v_ijk * v_ijk + w_ijk * w_ijk) * inv_rm;
+    const double transport_v = u_ijk * dv->dr + v_ijk * dv->dthe * inv_rm + w_ijk * dv->dphi * inv_rmsinthe
+        + (u_ijk * v_ijk - w_ijk * w_ijk * cotanthe) * inv_rm;
+    const double transport_w = u_ijk * dw->dr + v_ijk * dw->dthe * inv_rm + w_ijk * dw->dphi * inv_rmsinthe
+        + (w_ijk * u_ijk + v_ijk * w_ijk * cotanthe) * inv_rm;
+
+    /* diffusion, :435-491 */
+    const double two_inv_rm = 2.0 * inv_rm;
+    const double v_metric = (1.0 + costhe / g->sinthe2) * inv_rm2;
+    const double diffusion_t = diffusion(&d[ATSAT_F_T], two_inv_rm, g);
+    const double diffusion_u = du->d2r + 2.0 * u_ijk * inv_rm2 + du->d2the * inv_rm2
+        + 4.0 * du->dr * inv_rm + du->dthe * costhe_inv_rm2sinthe + du->d2phi * inv_rm2sinthe2;
+    const double diffusion_v = dv->d2r + dv->dr * two_inv_rm + dv->d2the * inv_rm2
+        + dv->dthe * costhe_inv_rm2sinthe - v_metric * v_ijk
+        + dv->d2phi * inv_rm2sinthe2 + 2.0 * du->dthe * inv_rm2
+        - dw->dphi * 2.0 * costhe * inv_rm2sinthe2;
+    const double diffusion_w = dw->d2r + dw->dr * two_inv_rm + dw->d2the * inv_rm2
+        + dw->dthe * costhe_inv_rm2sinthe - v_metric * w_ijk
+        + dw->d2phi * inv_rm2sinthe2 + 2.0 * du->dphi * inv_rm2sinthe
+        + dv->dphi * 2.0 * costhe * inv_rm2sinthe2;
+
+    /* k-omega transport, :511-538 */
+    if (p->turb_active) {
+        const double sig_k = 0.85, sig_w = 0.5;
+        const double nue_here = f[ATSAT_F_NUE][c];
+        const double transport_tke = transport(u_ijk, v_ijk, w_ijk, &d[ATSAT_F_TKE], g);
+        const double transport_dis = transport(u_ijk, v_ijk, w_ijk, &d[ATSAT_F_DIS], g);
+        const double diffusion_tke = diffusion(&d[ATSAT_F_TKE], two_inv_rm, g);
+        const double diffusion_dis = diffusion(&d[ATSAT_F_DIS], two_inv_rm, g);
+        f[ATSAT_F_RHS_TKE][c] = -transport_tke + diffusion_tke * (1.0 / p->re + nue_here / sig_k) + f[ATSAT_F_TKE_SOURCE][c];
+        f[ATSAT_F_RHS_DIS][c] = -transport_dis + diffusion_dis * (1.0 / p->re + nue_here / sig_w) + f[ATSAT_F_DIS_SOURCE][c];
+    } else {
+        f[ATSAT_F_RHS_TKE][c] = 0.0;
+        f[ATSAT_F_RHS_DIS][c] = 0.0;
+    }
+
+    /* eddy coupling, :577-582 */
+    const double Pr_t = 0.9;
+    const double nue_c = f[ATSAT_F_NUE][c];
+    const double nue_t = (p->turb_coupling != 0.0 && isfinite(nue_c)) ? p->turb_coupling * smax(0.0, nue_c) : 0.0;
+    const double nue_t_s = nue_t / Pr_t;
+
+    /* radiation, :611-629 */
+    double radiation_t = 0.0;
+    if (p->rad_coupling != 0.0) {
+        const double rho_f = f[ATSAT_F_RHO_MIX][c];
+        const double rho = (rho_f > 0.0 && isfinite(rho_f)) ? rho_f : p->r_mix;
+        const double L_rad = p->L_atm * 1.0e3;
+        if (rho > 0.0 && p->cp_mix > 0.0) {
+            radiation_t = p->rad_coupling * f[ATSAT_F_Q_RAD][c] * L_rad / (rho * p->cp_mix * p->u_0 * p->t_ref);
+            if (!isfinite(radiation_t)) radiation_t = 0.0;
+            else if (radiation_t > 0.5) radiation_t = 0.5;
+            else if (radiation_t < -0.5) radiation_t = -0.5;
+        }
+    }
+
+    /* precipitation latent heat, :645-665 */
+    const double pc = p->precip_coupling;
+    double precip_t = 0.0;
+    if (pc != 0.0) {
+        const double L_rad = p->L_atm * 1.0e3;
+        if (p->r_mix > 0.0 && p->cp_mix > 0.0) {
+            precip_t = pc * f[ATSAT_F_Q_PRECIP][c] * L_rad / (p->r_mix * p->cp_mix * p->u_0 * p->t_ref);
+            if (!isfinite(precip_t)) precip_t = 0.0;
+            else if (precip_t > 0.5) precip_t = 0.5;
+            else if (precip_t < -0.5) precip_t = -0.5;
+        }
+    }
+
+    /* buoyancy anomaly, :700-714 */
+    double buoyancy_u = 0.0;
+    const double t_c = f[ATSAT_F_T][c];
+    if (t_c > 0.0 && !p->hydro_buoy) {
+        if (p->buoy_legacy) {
+            buoyancy_u = +p->buoyancy * p->g * (f[ATSAT_F_P_STAT][c] + f[ATSAT_F_P_DYN][c])
+                       / (p->r_mix * p->R_mix * t_c * p->t_ref);
+        } else {
+            buoyancy_u = -nd_buoy * p->buoy_scale * p->buoyancy
+                * (p->g * f[ATSAT_F_P_STAT][c] / (p->r_mix * p->R_mix * t_c * p->t_ref) - m->buoy[i]);
+        }
+    }
+
+    /* assembly, :752-937 */
+    const double tmf = p->thermal_massflux;
+    f[ATSAT_F_RHS_T][c] = +pressure_t - transport_t + diffusion_t / (p->re * p->pr) + diffusion_t * nue_t_s
+        - tmf * p->chemical_reaction * f[ATSAT_F_THERMALMASSFLUX][c] + radiation_t + precip_t;
+
+    f[ATSAT_F_RHS_U][c] = -dpdr + buoyancy_u - transport_u + diffusion_u / p->re + diffusion_u * nue_t
+        - cor_rad_on * p->Coriolis * Coriolis_rad + p->centrifugal * centrifugal_rad;
+
+    double dpmdthe = 0.0, dpmdphi = 0.0;
+    if (p->metric_split) {
+        dpmdthe = (X(m, ATSAT_F_P_METRIC, i, j + 1, k) - X(m, ATSAT_F_P_METRIC, i, j - 1, k)) * g->inv_2dthe;
+        dpmdphi = (X(m, ATSAT_F_P_METRIC, i, j, ke) - X(m, ATSAT_F_P_METRIC, i, j, kw)) * g->inv_2dphi;
+    }
+    f[ATSAT_F_RHS_V][c] = -dpdthe * inv_rm - dpmdthe * inv_rm - transport_v + diffusion_v / p->re + diffusion_v * nue_t
+        - p->Coriolis * Coriolis_the + p->centrifugal * centrifugal_the;
+    f[ATSAT_F_RHS_W][c] = -dpdphi * inv_rmsinthe - dpmdphi * inv_rmsinthe - transport_w + diffusion_w / p->re
+        + diffusion_w * nue_t - p->Coriolis * Coriolis_phi;
+
+#define SPECIES(FID, SC, EXTRA) do { \
+        const double tr_ = transport(u_ijk, v_ijk, w_ijk, &d[FID], g); \
+        const double df_ = diffusion(&d[FID], two_inv_rm, g); \
+        f[ATSAT_F_RHS_BASE + FID][c] = -tr_ + df_ / ((SC) * p->re) + df_ * nue_t_s EXTRA; \
+    } while (0)
+    SPECIES(ATSAT_F_CH4, p->sc_ch4, + pc * f[ATSAT_F_S_PRECIP_CH4][c]);
+    SPECIES(ATSAT_F_CH4_CLOUD, p->sc_ch4, + pc * f[ATSAT_F_S_PRECIP_CH4_CLOUD][c]);
+    SPECIES(ATSAT_F_CH4_ICE, p->sc_ch4, + pc * f[ATSAT_F_S_PRECIP_CH4_ICE][c]);
+    SPECIES(ATSAT_F_H2O, p->sc_h2o, + pc * f[ATSAT_F_S_PRECIP_H2O][c]);
+    SPECIES(ATSAT_F_H2O_CLOUD, p->sc_h2o, + pc * f[ATSAT_F_S_PRECIP_H2O_CLOUD][c]);
+    SPECIES(ATSAT_F_H2O_ICE, p->sc_h2o, + pc * f[ATSAT_F_S_PRECIP_H2O_ICE][c]);
+    SPECIES(ATSAT_F_H2S, p->sc_h2s, + p->chemical_reaction * f[ATSAT_F_MASSFLUX_H2S][c]);
+    SPECIES(ATSAT_F_NH3, p->sc_nh3, + p->chemical_reaction * f[ATSAT_F_MASSFLUX_NH3][c] + pc * f[ATSAT_F_S_PRECIP_NH3][c]);
+    SPECIES(ATSAT_F_NH3_CLOUD, p->sc_nh3, + pc * f[ATSAT_F_S_PRECIP_NH3_CLOUD][c]);
+    SPECIES(ATSAT_F_NH3_ICE, p->sc_nh3, + pc * f[ATSAT_F_S_PRECIP_NH3_ICE][c]);
+#undef SPECIES
+    {   /* nh4sh carries the flux-limiter correction between transport and diffusion, :932-937 */
+        const double tr_ = transport(u_ijk, v_ijk, w_ijk, &d[ATSAT_F_NH4SH], g);
+        const double df_ = diffusion(&d[ATSAT_F_NH4SH], two_inv_rm, g);
+        f[ATSAT_F_RHS_NH4SH][c] = -tr_ + f[ATSAT_F_FLUXLIM_NH4SH][c] + df_ / (p->sc_nh4sh * p->re) + df_ * nue_t_s
+            + p->chemical_reaction * f[ATSAT_F_MASSFLUX_NH4SH][c];
+    }
+
+    /* flux-form species term, :979-1009 */
+    if (p->species_divu != 0.0) {
+        const double sd = p->species_divu * (du->dr + 2.0 * u_ijk * inv_rm + dv->dthe * inv_rm
+                                             + v_ijk * cotanthe * inv_rm + dw->dphi * inv_rmsinthe);
+        static const int sp[11] = { ATSAT_F_H2O, ATSAT_F_H2O_CLOUD, ATSAT_F_H2O_ICE, ATSAT_F_H2S, ATSAT_F_NH3,
+                                    ATSAT_F_NH3_CLOUD, ATSAT_F_NH3_ICE, ATSAT_F_CH4, ATSAT_F_CH4_CLOUD,
+                                    ATSAT_F_CH4_ICE, ATSAT_F_NH4SH };
+        for (int s = 0; s < 11; s++) f[ATSAT_F_RHS_BASE + sp[s]][c] -= sd * f[sp[s]][c];
+    }
+
+    f[ATSAT_F_AUX_U][c] = f[ATSAT_F_RHS_U][c] + dpdr;
+    f[ATSAT_F_AUX_V][c] = f[ATSAT_F_RHS_V][c] + dpdthe * inv_rm;
+    f[ATSAT_F_AUX_W][c] = f[ATSAT_F_RHS_W][c] + dpdphi * inv_rmsinthe;
+}
+
+static void rhs_pass(M* m) {
+    const int im = m->im, jm = m->jm, km = m->km;
+    const int k_first = m->p->phi_periodic ? 0 : 1;
+    #pragma omp parallel for collapse(2) schedule(static)
+    for (int i = 1; i < im - 1; i++) {
+        for (int j = 2; j < jm - 2; j++) {
+            double st = sin(m->the_z[j]);
+            if (st < m->p->sinthe_min) st = m->p->sinthe_min;
+            Geo g;
+            make_geo(m, i, st, cos(m->the_z[j]), &g);
+            for (int k = k_first; k < km - 1; k++) rhs_cell(m, i, j, k, &g);
+        }
+    }
+}
+
+/* ---------------- RungeKutta_Sat_Turb.cpp:110-387 ---------------- */
+static void rk4_step(M* m) {
+    const atsat_dyn_params* p = m->p;
+    const int im = m->im, jm = m->jm, km = m->km;
+    buoyancy_ref_level(m);
+    if (p->metric_split) metric_pressure(m);
+    const int k_first = p->phi_periodic ? 0 : 1;
+    const int turb = p->turb_active;
+    const double tke_max_nd = 1000.0 / (p->u_0 * p->u_0);
+    const double dis_min_nd = 1.0e-10;
+    const double dt = p->dt;
+
+    for (int stage = 0; stage < 4; stage++) {
+        const double c_in = (stage == 0 || stage == 1) ? 0.5 * dt : (stage == 2 ? dt : 0.0);
+        const double wgt = (stage == 0 || stage == 3) ? 1.0 : 2.0;
+        rhs_pass(m);
+        #pragma omp parallel for collapse(2) schedule(static)
+        for (int i = 1; i < im - 1; i++) {
+            for (int j = 2; j < jm - 2; j++) {
+                for (int k = k_first; k < km - 1; k++) {
+                    const size_t c = IDX(m, i, j, k);
+                    for (int q = 0; q < ATSAT_NPROG; q++) {
+                        if ((q == ATSAT_F_TKE || q == ATSAT_F_DIS) && !turb) continue;
+                        const double r = m->f[ATSAT_F_RHS_BASE + q][c];
+                        m->acc[q][c] = (stage == 0) ? wgt * r : m->acc[q][c] + wgt * r;
+                    }
+                    if (stage < 3) {
+                        for (int q = 0; q < ATSAT_F_TKE; q++)
+                            m->f[q][c] = m->f[ATSAT_F_N_BASE + q][c] + c_in * m->f[ATSAT_F_RHS_BASE + q][c];
+                        if (turb) {
+                            m->f[ATSAT_F_TKE][c] = smin(smax(m->f[ATSAT_F_TKEN][c] + c_in * m->f[ATSAT_F_RHS_TKE][c], 0.0), tke_max_nd);
+                            m->f[ATSAT_F_DIS][c] = smax(m->f[ATSAT_F_DISN][c] + c_in * m->f[ATSAT_F_RHS_DIS][c], dis_min_nd);
+                        }
+                    }
+                }
+            }
+        }
+    }
+
+    const double sixth_dt = dt / 6.0;
+    /* the t limiter reads the OLD state tn only, so it can run in the same pass */
+    #pragma omp parallel for collapse(2) schedule(static)
+    for (int i = 1; i < im - 1; i++) {
+        for (int j = 2; j < jm - 2; j++) {
+            for (int k = k_first; k < km - 1; k++) {
+                const size_t c = IDX(m, i, j, k);
+                const double tn = m->f[ATSAT_F_TN][c];
+                double t_new = tn + sixth_dt * m->acc[ATSAT_F_T][c];
+                if (p->t_limiter) {
+                    double lo = tn, hi = tn;
+                    const size_t nb[6] = { IDX(m, i - 1, j, k), IDX(m, i + 1, j, k), IDX(m, i, j - 1, k),
+                                           IDX(m, i, j + 1, k), IDX(m, i, j, k - 1), IDX(m, i, j, k + 1) };
+                    for (int q = 0; q < 6; q++) {
+                        const double val = m->f[ATSAT_F_TN][nb[q]];
+                        if (val < lo) lo = val;
+                        if (val > hi) hi = val;
+                    }
+                    if (t_new < lo) t_new = lo;
+                    else if (t_new > hi) t_new = hi;
+                }
+                m->f[ATSAT_F_T][c] = t_new;
+                if (turb) {
+                    m->f[ATSAT_F_TKE][c] = smin(smax(m->f[ATSAT_F_TKEN][c] + sixth_dt * m->acc[ATSAT_F_TKE][c], 0.0), tke_max_nd);
+                    m->f[ATSAT_F_DIS][c] = smax(m->f[ATSAT_F_DISN][c] + sixth_dt * m->acc[ATSAT_F_DIS][c], dis_min_nd);
+                }
+                for (int q = 0; q < ATSAT_F_TKE; q++) {
+                    if (q == ATSAT_F_T) continue;
+                    m->f[q][c] = m->f[ATSAT_F_N_BASE + q][c] + sixth_dt * m->acc[q][c];
+                }
+            }
+        }
+    }
+}
+
+/* ---------------- Pressure_Sat.cpp:49-62 ---------------- */
+static void mixture_density(M* m) {
+    const atsat_dyn_params* p = m->p;
+    const size_t n = (size_t)m->im * m->jm * m->km;
+    #pragma omp parallel for schedule(static)
+    for (size_t c = 0; c < n; c++) {
+        const double T = m->f[ATSAT_F_T][c] * p->t_ref;
+        if (!(T > 0.0) || !(p->R_mix > 0.0)) { m->f[ATSAT_F_RHO_MIX][c] = 0.0; continue; }
+        const double rho = (m->f[ATSAT_F_P_STAT][c] * 1.0e5) / (p->R_mix * T);
+        m->f[ATSAT_F_RHO_MIX][c] = isfinite(rho) ? rho : 0.0;
+    }
+}
+
+/* ---------------- Pressure_Sat.cpp:78-194 ---------------- */
+static void prepare_projection_boundaries(M* m, int rigid_lid) {
+    const int im = m->im, jm = m->jm, km = m->km;
+    const int per = m->p->phi_periodic;
+    const int k_first = per ? 0 : 1;
+    const double c43 = 4.0 / 3.0, c13 = 1.0 / 3.0;
+    const int au = ATSAT_F_AUX_U, av = ATSAT_F_AUX_V, aw = ATSAT_F_AUX_W;
+    const int ru = ATSAT_F_RHS_U, rv = ATSAT_F_RHS_V, rw = ATSAT_F_RHS_W;
+#define CUB_R(F_, I0, A, B, C) X(m, F_, I0, j, k) = X(m, F_, C, j, k) - 3.0 * X(m, F_, B, j, k) + 3.0 * X(m, F_, A, j, k)
+#define CUB_T(F_, J0, A, B, C) X(m, F_, i, J0, k) = X(m, F_, i, C, k) - 3.0 * X(m, F_, i, B, k) + 3.0 * X(m, F_, i, A, k)
+    #pragma omp parallel for
+    for (int j = 1; j < jm - 1; j++) {
+        for (int k = k_first; k < km - 1; k++) {
+            if (rigid_lid) { X(m, au, 0, j, k) = 0.0; X(m, au, im - 1, j, k) = 0.0; }
+            else { CUB_R(au, 0, 1, 2, 3); CUB_R(au, im - 1, im - 2, im - 3, im - 4); }
+            CUB_R(av, 0, 1, 2, 3); CUB_R(av, im - 1, im - 2, im - 3, im - 4);
+            CUB_R(aw, 0, 1, 2, 3); CUB_R(aw, im - 1, im - 2, im - 3, im - 4);
+            CUB_R(ru, 0, 1, 2, 3); CUB_R(ru, im - 1, im - 2, im - 3, im - 4);
+            CUB_R(rv, 0, 1, 2, 3); CUB_R(rv, im - 1, im - 2, im - 3, im - 4);
+            CUB_R(rw, 0, 1, 2, 3); CUB_R(rw, im - 1, im - 2, im - 3, im - 4);
+        }
+    }
+    #pragma omp parallel for
+    for (int k = k_first; k < km - 1; k++) {
+        for (int i = 1; i < im - 1; i++) {
+            CUB_T(au, 0, 1, 2, 3);
+            X(m, av, i, 0, k) = 0.0; X(m, aw, i, 0, k) = 0.0;
+            CUB_T(au, jm - 1, jm - 2, jm - 3, jm - 4);
+            X(m, av, i, jm - 1, k) = 0.0; X(m, aw, i, jm - 1, k) = 0.0;
+            CUB_T(ru, 0, 1, 2, 3);
+            X(m, rv, i, 0, k) = 0.0; X(m, rw, i, 0, k) = 0.0;
+            CUB_T(ru, jm - 1, jm - 2, jm - 3, jm - 4);
+            X(m, rv, i, jm - 1, k) = 0.0; X(m, rw, i, jm - 1, k) = 0.0;
+        }
+    }
+#undef CUB_R
+#undef CUB_T
+    const int six[6] = { au, av, aw, ru, rv, rw };
+    #pragma omp parallel for
+    for (int i = 0; i < im; i++) {
+        for (int j = 0; j < jm; j++) {
+            for (int s = 0; s < 6; s++) {
+                if (per) { X(m, six[s], i, j, km - 1) = X(m, six[s], i, j, 0); continue; }
+                double a0 = c43 * X(m, six[s], i, j, 1) - c13 * X(m, six[s], i, j, 2);
+                double a1 = c43 * X(m, six[s], i, j, km - 2) - c13 * X(m, six[s], i, j, km - 3);
+                X(m, six[s], i, j, 0) = a0;
+                X(m, six[s], i, j, km - 1) = a1;
+                X(m, six[s], i, j, 0) = X(m, six[s], i, j, km - 1) = (X(m, six[s], i, j, 0) + X(m, six[s], i, j, km - 1)) / 2.0;
+            }
+        }
+    }
+}
+
+/* ---------------- PressureSolver.h:145-766 (pointwise red-black sweeps) ---------------- */
+static void pressure(M* m, atsat_dyn_pstats* st) {
+    const atsat_dyn_params* p = m->p;
+    const int im = m->im, jm = m->jm, km = m->km;
+    const double c43 = 4.0 / 3.0, c13 = 1.0 / 3.0;
+    double* sinthe_table = (double*)malloc(sizeof(double) * (size_t)jm);
+    for (int j = 0; j < jm; j++) {
+        sinthe_table[j] = sin(m->the_z[j]);
+        if (sinthe_table[j] < p->sinthe_min) sinthe_table[j] = p->sinthe_min;
+        if (sinthe_table[j] == 0.0) sinthe_table[j] = 1.0e-5;
+    }
+    const double p_dyn_cap = p->pdyn_cap;
+    const int src_projection = p->press_src;
+    const int n_sweeps = p->press_sweeps > 0 ? p->press_sweeps : 1;
+    const int press_wall = p->press_wall;
+    const int rigid_lid = p->rigid_lid;
+    prepare_projection_boundaries(m, rigid_lid);
+
+    const double inv_2dr = 1.0 / (2.0 * m->dr), inv_2dthe = 1.0 / (2.0 * m->dthe), inv_2dphi = 1.0 / (2.0 * m->dphi);
+    const double inv_dr2 = 1.0 / (m->dr * m->dr), inv_dthe2 = 1.0 / (m->dthe * m->dthe), inv_dphi2 = 1.0 / (m->dphi * m->dphi);
+    const int per = p->phi_periodic;
+    const int k_first = per ? 0 : 1;
+    const int press_incr = p->press_incr && src_projection != 0;
+    const int Su = press_incr ? ATSAT_F_RHS_U : ATSAT_F_AUX_U;
+    const int Sv = press_incr ? ATSAT_F_RHS_V : ATSAT_F_AUX_V;
+    const int Sw = press_incr ? ATSAT_F_RHS_W : ATSAT_F_AUX_W;
+    const size_t n = (size_t)im * jm * km;
+    double* lc_old = NULL;
+    const int P = ATSAT_F_P_DYN;
+
+    if (press_incr) {
+        lc_old = (double*)calloc(n, sizeof(double));
+        #pragma omp parallel for collapse(2) schedule(static)
+        for (int i = 1; i < im - 1; i++) {
+            for (int j = 1; j < jm - 1; j++) {
+                const double rm = metric_radius(m, m->rad_z[i]);
+                const double exp_rm = p->coord_stretching ? 1.0 / (rm + 1.0) : 1.0;
+                const double num1 = exp_rm * exp_rm * inv_dr2;
+                const double num2 = inv_dthe2 / (rm * rm);
+                const double num3 = inv_dphi2 / (rm * rm * sinthe_table[j] * sinthe_table[j]);
+                for (int k = k_first; k < km - 1; k++) {
+                    const int kw = phi_wrap(per, k - 1, km), ke = phi_wrap(per, k + 1, km);
+                    const double p0 = X(m, P, i, j, k);
+                    double l_;
+                    if (press_wall) {
+                        l_ = 0.0;
+                        l_ += num1 * (X(m, P, i + 1, j, k) - p0);
+                        l_ += num1 * (X(m, P, i - 1, j, k) - p0);
+                        l_ += num2 * (X(m, P, i, j + 1, k) - p0);
+                        l_ += num2 * (X(m, P, i, j - 1, k) - p0);
+                        l_ += num3 * (X(m, P, i, j, ke) - p0);
+                        l_ += num3 * (X(m, P, i, j, kw) - p0);
+                    } else {
+                        l_ = num1 * (X(m, P, i + 1, j, k) + X(m, P, i - 1, j, k) - 2.0 * p0)
+                           + num2 * (X(m, P, i, j + 1, k) + X(m, P, i, j - 1, k) - 2.0 * p0)
+                           + num3 * (X(m, P, i, j, ke) + X(m, P, i, j, kw) - 2.0 * p0);
+                    }
+                    lc_old[IDX(m, i, j, k)] = l_;
+                }
+            }
+        }
+    }
+
+    double clamped = 0.0, maxupd = 0.0;
+    for (int sweep = 0; sweep < n_sweeps; sweep++) {
+        double mu = 0.0;
+        for (int colour = 0; colour < 2; colour++) {
+            #pragma omp parallel for collapse(2) schedule(static) reduction(+:clamped) reduction(max:mu)
+            for (int i = 1; i < im - 1; i++) {
+                for (int j = 1; j < jm - 1; j++) {
+                    Geo g;
+                    make_geo(m, i, sinthe_table[j], cos(m->the_z[j]), &g);
+                    const double num1 = g.exp_2_rm * inv_dr2;
+                    const double num2 = g.inv_rm2 * inv_dthe2;
+                    const double num3 = g.inv_rm2sinthe2 * inv_dphi2;
+                    const double denom = 2.0 * num1 + 2.0 * num2 + 2.0 * num3;
+                    for (int k = k_first; k < km - 1; k++) {
+                        if (((i + j + k) & 1) != colour) continue;
+                        const int kw = phi_wrap(per, k - 1, km), ke = phi_wrap(per, k + 1, km);
+                        double du_dr, dv_dthe, dw_dphi;
+                        if (src_projection == 0) {
+                            du_dr = ((X(m, ATSAT_F_AUX_U, i + 1, j, k) - X(m, ATSAT_F_AUX_U, i - 1, j, k))
+                                   - (X(m, ATSAT_F_RHS_U, i + 1, j, k) - X(m, ATSAT_F_RHS_U, i - 1, j, k))) * inv_2dr;
+                            dv_dthe = ((X(m, ATSAT_F_AUX_V, i, j + 1, k) - X(m, ATSAT_F_AUX_V, i, j - 1, k))
+                                     - (X(m, ATSAT_F_RHS_V, i, j + 1, k) - X(m, ATSAT_F_RHS_V, i, j - 1, k))) * inv_2dthe;
+                            dw_dphi = ((X(m, ATSAT_F_AUX_W, i, j, ke) - X(m, ATSAT_F_AUX_W, i, j, kw))
+                                     - (X(m, ATSAT_F_RHS_W, i, j, ke) - X(m, ATSAT_F_RHS_W, i, j, kw))) * inv_2dphi;
+                        } else {
+                            const double sup = (press_incr && rigid_lid && (i + 1 == im - 1)) ? 0.0 : X(m, Su, i + 1, j, k);
+                            const double sum_ = (press_incr && rigid_lid && (i - 1 == 0)) ? 0.0 : X(m, Su, i - 1, j, k);
+                            du_dr = (sup - sum_) * inv_2dr;
+                            dv_dthe = (X(m, Sv, i, j + 1, k) - X(m, Sv, i, j - 1, k)) * inv_2dthe;
+                            dw_dphi = (X(m, Sw, i, j, ke) - X(m, Sw, i, j, kw)) * inv_2dphi;
+                        }
+                        double div_src = du_dr * g.exp_rm + dv_dthe * g.inv_rm + dw_dphi * g.inv_rmsinthe;
+                        double acc = 0.0, den = denom;
+                        if (press_wall) {
+                            acc = den = 0.0;
+                            acc += num1 * X(m, P, i + 1, j, k); den += num1;
+                            acc += num1 * X(m, P, i - 1, j, k); den += num1;
+                            acc += num2 * X(m, P, i, j + 1, k); den += num2;
+                            acc += num2 * X(m, P, i, j - 1, k); den += num2;
+                            acc += num3 * X(m, P, i, j, ke); den += num3;
+                            acc += num3 * X(m, P, i, j, kw); den += num3;
+                            if (den <= 0.0) continue;
+                        } else {
+                            acc = (X(m, P, i + 1, j, k) + X(m, P, i - 1, j, k)) * num1
+                                + (X(m, P, i, j + 1, k) + X(m, P, i, j - 1, k)) * num2
+                                + (X(m, P, i, j, ke) + X(m, P, i, j, kw)) * num3;
+                        }
+                        const double src_max = den * p_dyn_cap;
+                        if (!isfinite(div_src)) { div_src = 0.0; clamped += 1.0; }
+                        else if (div_src > src_max) { div_src = src_max; clamped += 1.0; }
+                        else if (div_src < -src_max) { div_src = -src_max; clamped += 1.0; }
+                        if (press_incr) div_src += lc_old[IDX(m, i, j, k)];
+                        const double old = X(m, P, i, j, k);
+                        const double nv = (acc - div_src) / den;
+                        X(m, P, i, j, k) = nv;
+                        const double dd = fabs(nv - old);
+                        if (dd > mu) mu = dd;
+                    }
+                }
+            }
+        }
+        maxupd = mu;
+        /* outer boundary of the relaxation, PressureSolver.h:718-746 */
+        #pragma omp parallel for collapse(2)
+        for (int k = 0; k < km; k++) {
+            for (int j = 0; j < jm; j++) {
+                X(m, P, 0, j, k) = c43 * X(m, P, 1, j, k) - c13 * X(m, P, 2, j, k);
+                X(m, P, im - 1, j, k) = c43 * X(m, P, im - 2, j, k) - c13 * X(m, P, im - 3, j, k);
+            }
+        }
+        #pragma omp parallel for collapse(2)
+        for (int k = 0; k < km; k++) {
+            for (int i = 0; i < im; i++) {
+                X(m, P, i, 0, k) = c43 * X(m, P, i, 1, k) - c13 * X(m, P, i, 2, k);
+                X(m, P, i, jm - 1, k) = c43 * X(m, P, i, jm - 2, k) - c13 * X(m, P, i, jm - 3, k);
+            }
+        }
+        #pragma omp parallel for collapse(2)
+        for (int i = 0; i < im; i++) {
+            for (int j = 0; j < jm; j++) {
+                if (per) { X(m, P, i, j, km - 1) = X(m, P, i, j, 0); continue; }
+                X(m, P, i, j, 0) = c43 * X(m, P, i, j, 1) - c13 * X(m, P, i, j, 2);
+                X(m, P, i, j, km - 1) = c43 * X(m, P, i, j, km - 2) - c13 * X(m, P, i, j, km - 3);
+                X(m, P, i, j, 0) = X(m, P, i, j, km - 1) = (X(m, P, i, j, 0) + X(m, P, i, j, km - 1)) / 2.0;
+            }
+        }
+    }
+    if (st) { st->sweeps = n_sweeps; st->src_clamped = clamped; st->max_abs_update = maxupd; }
+    free(lc_old);
+    free(sinthe_table);
+}
+
+/* ---------------- cSaturnModel.cpp:1551-1600 ---------------- */
+static void restore_var(M* m) {
+    const size_t n = (size_t)m->im * m->jm * m->km;
+    for (int q = 0; q < ATSAT_NPROG; q++) memcpy(m->f[ATSAT_F_N_BASE + q], m->f[q], n * sizeof(double));
+    memcpy(m->f[ATSAT_F_P_DYNN], m->f[ATSAT_F_P_DYN], n * sizeof(double));
+}
+
+/* ---------------- exported entry points ---------------- */
+
+static int setup(M* m, const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields,
+                 const double* vbar0, const double* ubar0, const double* p_baro, double* buoy) {
+    if (!g || !p || !fields || g->im < 4 || g->jm < 5 || g->km < 4) return ATSAT_DYN_E_INVALID;
+    if (p->chrom || p->cp_h2_dyn || p->print_diag || p->press_line || p->press_baro) return ATSAT_DYN_E_UNSUPPORTED;
+    memset(m, 0, sizeof(*m));
+    m->im = g->im; m->jm = g->jm; m->km = g->km;
+    m->rad_z = g->rad_z; m->the_z = g->the_z;
+    m->dr = g->dr; m->dthe = g->dthe; m->dphi = g->dphi;
+    m->p = p; m->f = fields;
+    m->vbar0 = vbar0; m->ubar0 = ubar0; m->p_baro = p_baro;
+    m->buoy = buoy;
+    return ATSAT_DYN_OK;
+}
+
+int orc_buoyancy_ref_level(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields, double* buoy) {
+    M m; int rc = setup(&m, g, p, fields, NULL, NULL, NULL, buoy);
+    if (rc) return rc;
+    buoyancy_ref_level(&m);
+    return 0;
+}
+
+int orc_metric_pressure(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields, const double* p_baro) {
+    M m; int rc = setup(&m, g, p, fields, NULL, NULL, p_baro, NULL);
+    if (rc) return rc;
+    metric_pressure(&m);
+    return 0;
+}
+
+/* buoyancy level + p_metric + one RHS pass, as ref_harness "rhs" */
+int orc_rhs(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields, const double* vbar0,
+            const double* ubar0, const double* p_baro, double* buoy) {
+    M m; int rc = setup(&m, g, p, fields, vbar0, ubar0, p_baro, buoy);
+    if (rc) return rc;
+    buoyancy_ref_level(&m);
+    if (p->metric_split) metric_pressure(&m);
+    rhs_pass(&m);
+    return 0;
+}
+
+int orc_rk4_step(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields, const double* vbar0,
+                 const double* ubar0, const double* p_baro, double* buoy) {
+    M m; int rc = setup(&m, g, p, fields, vbar0, ubar0, p_baro, buoy);
+    if (rc) return rc;
+    const size_t n = (size_t)g->im * g->jm * g->km;
+    for (int q = 0; q < ATSAT_NPROG; q++) {
+        m.acc[q] = (double*)calloc(n, sizeof(double));
+        if (!m.acc[q]) { for (int r = 0; r < q; r++) free(m.acc[r]); return ATSAT_DYN_E_NOMEM; }
+    }
+    rk4_step(&m);
+    for (int q = 0; q < ATSAT_NPROG; q++) free(m.acc[q]);
+    return 0;
+}
+
+int orc_mixture_density(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields) {
+    M m; int rc = setup(&m, g, p, fields, NULL, NULL, NULL, NULL);
+    if (rc) return rc;
+    mixture_density(&m);
+    return 0;
+}
+
+int orc_prepare_projection_boundaries(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields) {
+    M m; int rc = setup(&m, g, p, fields, NULL, NULL, NULL, NULL);
+    if (rc) return rc;
+    prepare_projection_boundaries(&m, p->rigid_lid);
+    return 0;
+}
+
+int orc_pressure(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields, atsat_dyn_pstats* st) {
+    M m; int rc = setup(&m, g, p, fields, NULL, NULL, NULL, NULL);
+    if (rc) return rc;
+    pressure(&m, st);
+    return 0;
+}
+
+int orc_restore_var(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields) {
+    M m; int rc = setup(&m, g, p, fields, NULL, NULL, NULL, NULL);
+    if (rc) return rc;
+    restore_var(&m);
+    return 0;
+}

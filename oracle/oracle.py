@@ -1,0 +1,118 @@
+"""ORACLE -- TEST INFRASTRUCTURE ONLY: ctypes wrapper of oracle/atsat_oracle.c.
+
+Used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the checker of the CUDA
+path; the product never imports it. Every function works on a synth.State in place (its arrays are
+the FP64 fields the reference's Array members hold).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from atsat_gb300 import abi, fields as F
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "atsat_oracle.c")
+LIB = os.path.join(HERE, "liboracle.so")
+CFLAGS = ["-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c99", "-Wall"]
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        subprocess.run(["gcc", *CFLAGS, SRC, "-o", LIB, "-lm"], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(LIB)
+    return _lib
+
+
+class _Call:
+    def __init__(self, state, params: dict):
+        self.state = state
+        g = state.grid
+        self.gh = abi.GridHold(g)
+        self.p = abi.make_params(params)
+        shape = g.shape
+        for fid in range(F.NFIELDS):
+            if fid not in state.arrays:
+                state.arrays[fid] = np.zeros(shape)
+        self.ptrs = (C.POINTER(C.c_double) * F.NFIELDS)()
+        for fid in range(F.NFIELDS):
+            a = state.arrays[fid]
+            assert a.dtype == np.float64 and a.flags.c_contiguous and a.shape == shape
+            self.ptrs[fid] = abi.dptr(a)
+        self.buoy = np.zeros(g.im)
+
+    def tables(self):
+        s = self.state
+        return (abi.dptr(s.cell_vbar0), abi.dptr(s.cell_ubar0), abi.dptr(s.p_baro))
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError(f"oracle {what} failed with status {rc}")
+
+
+def rhs(state, params) -> np.ndarray:
+    c = _Call(state, params)
+    _check(lib().orc_rhs(C.byref(c.gh.s), C.byref(c.p), c.ptrs, *c.tables(), abi.dptr(c.buoy)), "rhs")
+    return c.buoy
+
+
+def rk4_step(state, params) -> np.ndarray:
+    c = _Call(state, params)
+    _check(lib().orc_rk4_step(C.byref(c.gh.s), C.byref(c.p), c.ptrs, *c.tables(), abi.dptr(c.buoy)), "rk4")
+    return c.buoy
+
+
+def pressure(state, params) -> abi.PStats:
+    c = _Call(state, params)
+    st = abi.PStats()
+    _check(lib().orc_pressure(C.byref(c.gh.s), C.byref(c.p), c.ptrs, C.byref(st)), "pressure")
+    return st
+
+
+def mixture_density(state, params):
+    c = _Call(state, params)
+    _check(lib().orc_mixture_density(C.byref(c.gh.s), C.byref(c.p), c.ptrs), "density")
+
+
+def restore_var(state, params):
+    c = _Call(state, params)
+    _check(lib().orc_restore_var(C.byref(c.gh.s), C.byref(c.p), c.ptrs), "restore_var")
+
+
+def buoyancy_ref_level(state, params) -> np.ndarray:
+    c = _Call(state, params)
+    _check(lib().orc_buoyancy_ref_level(C.byref(c.gh.s), C.byref(c.p), c.ptrs, abi.dptr(c.buoy)), "buoy")
+    return c.buoy
+
+
+def metric_pressure(state, params):
+    c = _Call(state, params)
+    _check(lib().orc_metric_pressure(C.byref(c.gh.s), C.byref(c.p), c.ptrs, abi.dptr(state.p_baro)), "metric")
+
+
+def steps(state, params, nsteps: int, iter0: int = 1, bc=None):
+    """The dycore sequence of cSaturnModel::Run (cSaturnModel.cpp:864-1111 restricted to the dycore):
+    density + pressure on even iterations, RK4, boundary conditions (bc(state) when given),
+    restoreVar."""
+    for it in range(iter0, iter0 + nsteps):
+        if it % 2 == 0:
+            mixture_density(state, params)
+            pressure(state, params)
+        rk4_step(state, params)
+        if bc is not None:
+            bc(state)
+        restore_var(state, params)
