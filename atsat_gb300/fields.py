@@ -65,4 +65,7 @@ PARAM_INTS = [
     ("chrom", 0), ("cp_h2_dyn", 0), ("print_diag", 0), ("coord_stretching", 0),
     ("press_src", 1), ("press_incr", 1), ("press_sweeps", 1), ("press_wall", 0),
     ("rigid_lid", 1), ("press_line", 0), ("press_baro", 0), ("precision", 0),
+    ("bc_radius_form", 2), ("bc_bottom_form", 3), ("bc_pole_form", 1), ("bc_pole_fill", 1),
+    ("bc_lid_u", 1), ("bc_top_taper", 2), ("bc_species_lid_copy", 1), ("bc_species_wall_copy", 2),
+    ("local_rho", 1),
 ]

@@ -160,7 +160,17 @@ typedef struct atsat_dyn_params {
     int32_t press_line;        /* ATSAT_PRESS_LINE, 0 */
     int32_t press_baro;        /* ATSAT_PRESS_BAROTROPIC (effective), 0 */
     int32_t precision;         /* ATSAT_DYN_FP64 or ATSAT_DYN_MIXED */
-    int32_t reserved[9];
+    /* boundary conditions of BC_Sat / BoundaryConditions.h, used by atsat_dyn_boundary_conditions */
+    int32_t bc_radius_form;    /* ATSAT_BC_RADIUS_COPY, 2 = Neumann (1 copy, 2 Neumann, 3 cubic, 0 cubic) */
+    int32_t bc_bottom_form;    /* ATSAT_BC_BOTTOM_FORM, 3 = cubic on i = 0 (0 = as the lid) */
+    int32_t bc_pole_form;      /* ATSAT_BC_POLE_COPY, 1 = copy */
+    int32_t bc_pole_fill;      /* ATSAT_BC_POLE_FILL, 1 */
+    int32_t bc_lid_u;          /* ATSAT_BC_LID_U (default: BC_RIGID_LID), 1 */
+    int32_t bc_top_taper;      /* ATSAT_BC_TOP_TAPER, 2 */
+    int32_t bc_species_lid_copy;  /* ATSAT_BC_SPECIES_LID_COPY, 1 */
+    int32_t bc_species_wall_copy; /* ATSAT_BC_SPECIES_WALL_COPY, 2 (mass-fraction copy) */
+    int32_t local_rho;         /* ATSAT_LOCAL_RHO, 1 (rho_at reads rho_mix) */
+    int32_t reserved[7];
 } atsat_dyn_params;
 
 /* statistics of one pressure call */

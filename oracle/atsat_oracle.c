@@ -706,6 +706,186 @@ static void restore_var(M* m) {
     memcpy(m->f[ATSAT_F_P_DYNN], m->f[ATSAT_F_P_DYN], n * sizeof(double));
 }
 
+/* ---------------- BoundaryConditions.h:150-518 with BC_Sat.cpp:61-179 ----------------
+ * bcTheta, bcPhi, bcRadius (and BC_Sat's species lid/wall copies) in the order cSaturnModel::Run
+ * calls them (cSaturnModel.cpp:1091-1093), restricted to the fields of the dycore. */
+static inline double bc_form(int form, double a, double b, double c) {
+    const double c43 = 4.0 / 3.0, c13 = 1.0 / 3.0;
+    const int f = (form == 0) ? 3 : form;          /* ATSAT's bc_default_form() is CUBIC */
+    if (f == 1) return a;
+    if (f == 2) return c43 * a - c13 * b;
+    return c - 3.0 * b + 3.0 * a;
+}
+
+static const int BC_RADIUS[] = { ATSAT_F_T, ATSAT_F_U, ATSAT_F_V, ATSAT_F_W, ATSAT_F_CH4, ATSAT_F_CH4_CLOUD,
+    ATSAT_F_CH4_ICE, ATSAT_F_H2O, ATSAT_F_H2O_CLOUD, ATSAT_F_H2O_ICE, ATSAT_F_H2S, ATSAT_F_NH3, ATSAT_F_NH3_CLOUD,
+    ATSAT_F_NH3_ICE, ATSAT_F_NH4SH, ATSAT_F_MASSFLUX_H2S, ATSAT_F_MASSFLUX_NH3, ATSAT_F_MASSFLUX_NH4SH,
+    ATSAT_F_FLUXLIM_NH4SH, ATSAT_F_THERMALMASSFLUX };
+static const int BC_THETA_EXTRAP[] = { ATSAT_F_T, ATSAT_F_U, ATSAT_F_CH4, ATSAT_F_CH4_CLOUD, ATSAT_F_CH4_ICE,
+    ATSAT_F_H2O, ATSAT_F_H2O_CLOUD, ATSAT_F_H2O_ICE, ATSAT_F_H2S, ATSAT_F_NH3, ATSAT_F_NH3_CLOUD, ATSAT_F_NH3_ICE,
+    ATSAT_F_NH4SH, ATSAT_F_MASSFLUX_H2S, ATSAT_F_MASSFLUX_NH3, ATSAT_F_MASSFLUX_NH4SH, ATSAT_F_THERMALMASSFLUX };
+static const int BC_THETA_ZERO[] = { ATSAT_F_V, ATSAT_F_W, ATSAT_F_FLUXLIM_NH4SH };
+static const int BC_TURB[] = { ATSAT_F_TKE, ATSAT_F_DIS, ATSAT_F_NUE };
+static const double BC_TURB_FLOOR[] = { 0.0, 1.0e-10, 0.0 };
+static const int BC_SPECIES[] = { ATSAT_F_H2O, ATSAT_F_H2O_CLOUD, ATSAT_F_H2O_ICE, ATSAT_F_H2S, ATSAT_F_NH3,
+    ATSAT_F_NH3_CLOUD, ATSAT_F_NH3_ICE, ATSAT_F_CH4, ATSAT_F_CH4_CLOUD, ATSAT_F_CH4_ICE, ATSAT_F_NH4SH };
+#define NELEM(a) ((int)(sizeof(a) / sizeof((a)[0])))
+
+static void bc_theta(M* m) {
+    const atsat_dyn_params* p = m->p;
+    const int im = m->im, jm = m->jm, km = m->km;
+    const double c43 = 4.0 / 3.0, c13 = 1.0 / 3.0;
+    const int form = p->bc_pole_form;
+    const int nfill = p->bc_pole_fill ? 1 : 0;
+    const int turb = p->turb_active;
+    const int k_lo = p->phi_periodic ? 0 : 1;
+    #pragma omp parallel for
+    for (int k = k_lo; k < km - 1; k++) {
+        for (int i = 1; i < im - 1; i++) {
+            if (nfill > 0) {
+                const int jf = nfill + 1;
+                for (int r = 1; r <= nfill; r++) {
+                    const double ramp = (double)r / (double)jf;
+                    for (int q = 0; q < NELEM(BC_THETA_EXTRAP); q++) {
+                        const int F_ = BC_THETA_EXTRAP[q];
+                        X(m, F_, i, r, k) = X(m, F_, i, jf, k);
+                        X(m, F_, i, jm - 1 - r, k) = X(m, F_, i, jm - 1 - jf, k);
+                    }
+                    for (int q = 0; q < NELEM(BC_THETA_ZERO); q++) {
+                        const int F_ = BC_THETA_ZERO[q];
+                        X(m, F_, i, r, k) = ramp * X(m, F_, i, jf, k);
+                        X(m, F_, i, jm - 1 - r, k) = ramp * X(m, F_, i, jm - 1 - jf, k);
+                    }
+                    if (turb)
+                        for (int q = 0; q < NELEM(BC_TURB); q++) {
+                            const int F_ = BC_TURB[q];
+                            X(m, F_, i, r, k) = smax(BC_TURB_FLOOR[q], X(m, F_, i, jf, k));
+                            X(m, F_, i, jm - 1 - r, k) = smax(BC_TURB_FLOOR[q], X(m, F_, i, jm - 1 - jf, k));
+                        }
+                }
+            }
+            for (int q = 0; q < NELEM(BC_THETA_ZERO); q++) {
+                X(m, BC_THETA_ZERO[q], i, 0, k) = 0.0;
+                X(m, BC_THETA_ZERO[q], i, jm - 1, k) = 0.0;
+            }
+            for (int q = 0; q < NELEM(BC_THETA_EXTRAP); q++) {
+                const int F_ = BC_THETA_EXTRAP[q];
+                X(m, F_, i, 0, k) = bc_form(form, X(m, F_, i, 1, k), X(m, F_, i, 2, k), X(m, F_, i, 3, k));
+                X(m, F_, i, jm - 1, k) = bc_form(form, X(m, F_, i, jm - 2, k), X(m, F_, i, jm - 3, k), X(m, F_, i, jm - 4, k));
+            }
+            if (turb)
+                for (int q = 0; q < NELEM(BC_TURB); q++) {
+                    const int F_ = BC_TURB[q];
+                    X(m, F_, i, 0, k) = smax(BC_TURB_FLOOR[q], c43 * X(m, F_, i, 1, k) - c13 * X(m, F_, i, 2, k));
+                    X(m, F_, i, jm - 1, k) = smax(BC_TURB_FLOOR[q], c43 * X(m, F_, i, jm - 2, k) - c13 * X(m, F_, i, jm - 3, k));
+                }
+        }
+    }
+}
+
+static void bc_phi(M* m) {
+    const atsat_dyn_params* p = m->p;
+    const int im = m->im, jm = m->jm, km = m->km;
+    const double c43 = 4.0 / 3.0, c13 = 1.0 / 3.0;
+    const int turb = p->turb_active;
+    /* the phi list is the radius list (same fields) */
+    #pragma omp parallel for
+    for (int i = 0; i < im; i++) {
+        for (int j = 0; j < jm; j++) {
+            for (int q = 0; q < NELEM(BC_RADIUS); q++) {
+                const int F_ = BC_RADIUS[q];
+                if (p->phi_periodic) X(m, F_, i, j, km - 1) = X(m, F_, i, j, 0);
+                else {
+                    const double lo = c43 * X(m, F_, i, j, 1) - c13 * X(m, F_, i, j, 2);
+                    const double hi = c43 * X(m, F_, i, j, km - 2) - c13 * X(m, F_, i, j, km - 3);
+                    X(m, F_, i, j, 0) = X(m, F_, i, j, km - 1) = 0.5 * (lo + hi);
+                }
+            }
+            if (turb)
+                for (int q = 0; q < NELEM(BC_TURB); q++) {
+                    const int F_ = BC_TURB[q];
+                    if (p->phi_periodic) X(m, F_, i, j, 0) = X(m, F_, i, j, km - 1) = smax(BC_TURB_FLOOR[q], X(m, F_, i, j, 0));
+                    else {
+                        const double lo = c43 * X(m, F_, i, j, 1) - c13 * X(m, F_, i, j, 2);
+                        const double hi = c43 * X(m, F_, i, j, km - 2) - c13 * X(m, F_, i, j, km - 3);
+                        X(m, F_, i, j, 0) = X(m, F_, i, j, km - 1) = smax(BC_TURB_FLOOR[q], 0.5 * (lo + hi));
+                    }
+                }
+        }
+    }
+}
+
+static inline double rho_at(const M* m, int i, int j, int k) {
+    if (!m->p->local_rho) return m->p->r_mix;
+    const double rho = X(m, ATSAT_F_RHO_MIX, i, j, k);
+    return (rho > 0.0 && isfinite(rho)) ? rho : m->p->r_mix;
+}
+
+static void bc_radius(M* m) {
+    const atsat_dyn_params* p = m->p;
+    const int im = m->im, jm = m->jm, km = m->km;
+    const double c43 = 4.0 / 3.0, c13 = 1.0 / 3.0;
+    const int form = p->bc_radius_form, bform = p->bc_bottom_form;
+    const int turb = p->turb_active;
+    const int k_lo = p->phi_periodic ? 0 : 1;
+    #pragma omp parallel for
+    for (int j = 1; j < jm - 1; j++) {
+        for (int k = k_lo; k < km - 1; k++) {
+            for (int q = 0; q < NELEM(BC_RADIUS); q++) {
+                const int F_ = BC_RADIUS[q];
+                const int fb = (bform != 0 && F_ != ATSAT_F_U) ? bform : form;
+                X(m, F_, 0, j, k) = bc_form(fb, X(m, F_, 1, j, k), X(m, F_, 2, j, k), X(m, F_, 3, j, k));
+                X(m, F_, im - 1, j, k) = bc_form(form, X(m, F_, im - 2, j, k), X(m, F_, im - 3, j, k), X(m, F_, im - 4, j, k));
+            }
+            if (turb)
+                for (int q = 0; q < NELEM(BC_TURB); q++) {
+                    const int F_ = BC_TURB[q];
+                    X(m, F_, 0, j, k) = smax(BC_TURB_FLOOR[q], c43 * X(m, F_, 1, j, k) - c13 * X(m, F_, 2, j, k));
+                    X(m, F_, im - 1, j, k) = smax(BC_TURB_FLOOR[q], c43 * X(m, F_, im - 2, j, k) - c13 * X(m, F_, im - 3, j, k));
+                }
+        }
+    }
+    if (p->bc_lid_u) {
+        #pragma omp parallel for
+        for (int j = 0; j < jm; j++)
+            for (int k = 0; k < km; k++) { X(m, ATSAT_F_U, 0, j, k) = 0.0; X(m, ATSAT_F_U, im - 1, j, k) = 0.0; }
+    }
+    if (p->bc_top_taper) {
+        const int iml = im - 1;
+        #pragma omp parallel for
+        for (int j = 0; j < jm; j++) {
+            for (int k = 0; k < km; k++) {
+                X(m, ATSAT_F_V, iml, j, k) = 0.0;
+                X(m, ATSAT_F_W, iml, j, k) = 0.0;
+                if (p->bc_top_taper == 2) {
+                    X(m, ATSAT_F_V, iml - 1, j, k) = (1.0 / 3.0) * X(m, ATSAT_F_V, iml - 3, j, k);
+                    X(m, ATSAT_F_W, iml - 1, j, k) = (1.0 / 3.0) * X(m, ATSAT_F_W, iml - 3, j, k);
+                    X(m, ATSAT_F_V, iml - 2, j, k) = (2.0 / 3.0) * X(m, ATSAT_F_V, iml - 3, j, k);
+                    X(m, ATSAT_F_W, iml - 2, j, k) = (2.0 / 3.0) * X(m, ATSAT_F_W, iml - 3, j, k);
+                } else {
+                    X(m, ATSAT_F_V, iml - 1, j, k) *= (1.0 / 3.0);
+                    X(m, ATSAT_F_W, iml - 1, j, k) *= (1.0 / 3.0);
+                    X(m, ATSAT_F_V, iml - 2, j, k) *= (2.0 / 3.0);
+                    X(m, ATSAT_F_W, iml - 2, j, k) *= (2.0 / 3.0);
+                }
+            }
+        }
+    }
+    /* BC_Sat::bcRadius, BC_Sat.cpp:61-105 */
+    const int lid_copy = p->bc_species_lid_copy, wall_copy = p->bc_species_wall_copy;
+    if (lid_copy == 0 && wall_copy == 0) return;
+    #pragma omp parallel for
+    for (int j = 0; j < jm; j++)
+        for (int k = 0; k < km; k++) {
+            const double fr = (wall_copy == 2) ? rho_at(m, 0, j, k) / rho_at(m, 1, j, k) : 1.0;
+            for (int q = 0; q < NELEM(BC_SPECIES); q++) {
+                const int F_ = BC_SPECIES[q];
+                if (lid_copy != 0) X(m, F_, im - 1, j, k) = X(m, F_, im - 2, j, k);
+                if (wall_copy != 0) X(m, F_, 0, j, k) = X(m, F_, 1, j, k) * fr;
+            }
+        }
+}
+
 /* ---------------- exported entry points ---------------- */
 
 static int setup(M* m, const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields,
@@ -786,5 +966,14 @@ int orc_restore_var(const atsat_dyn_grid* g, const atsat_dyn_params* p, double**
     M m; int rc = setup(&m, g, p, fields, NULL, NULL, NULL, NULL);
     if (rc) return rc;
     restore_var(&m);
+    return 0;
+}
+
+int orc_boundary_conditions(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields) {
+    M m; int rc = setup(&m, g, p, fields, NULL, NULL, NULL, NULL);
+    if (rc) return rc;
+    bc_theta(&m);
+    bc_phi(&m);
+    bc_radius(&m);
     return 0;
 }

@@ -104,15 +104,19 @@ def metric_pressure(state, params):
     _check(lib().orc_metric_pressure(C.byref(c.gh.s), C.byref(c.p), c.ptrs, abi.dptr(state.p_baro)), "metric")
 
 
-def steps(state, params, nsteps: int, iter0: int = 1, bc=None):
+def boundary_conditions(state, params):
+    """bcTheta, bcPhi, bcRadius of BC_Sat on the dycore fields (cSaturnModel.cpp:1091-1093)."""
+    c = _Call(state, params)
+    _check(lib().orc_boundary_conditions(C.byref(c.gh.s), C.byref(c.p), c.ptrs), "bc")
+
+
+def steps(state, params, nsteps: int, iter0: int = 1):
     """The dycore sequence of cSaturnModel::Run (cSaturnModel.cpp:864-1111 restricted to the dycore):
-    density + pressure on even iterations, RK4, boundary conditions (bc(state) when given),
-    restoreVar."""
+    density + pressure on even iterations, RK4, boundary conditions, restoreVar."""
     for it in range(iter0, iter0 + nsteps):
         if it % 2 == 0:
             mixture_density(state, params)
             pressure(state, params)
         rk4_step(state, params)
-        if bc is not None:
-            bc(state)
+        boundary_conditions(state, params)
         restore_var(state, params)
