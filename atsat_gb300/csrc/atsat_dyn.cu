@@ -1,0 +1,862 @@
+// Host side of the C ABI declared in include/atsat_dyn.h.
+//
+// A handle owns its CUDA stream, one device allocation that holds every field in the pitched SoA
+// layout of dyn_common.cuh, the per-column geometry table, and the host bindings. Compute entry
+// points enqueue kernels on the handle's stream and synchronise before returning.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <omp.h>
+
+#include "dyn_common.cuh"
+
+using namespace atsat;
+
+namespace {
+
+enum BindKind { BIND_NONE = 0, BIND_ARRAY = 1, BIND_ROWS = 2 };
+
+struct ProfEvent {
+    int cls;
+    cudaEvent_t a, b;
+};
+
+}  // namespace
+
+struct atsat_dyn {
+    atsat_dyn_grid g{};
+    std::vector<double> rad_z, the_z;
+    atsat_dyn_params p{};
+    KConst kc{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+
+    double* slab = nullptr;              // one allocation for every device array below
+    double* f[ATSAT_NFIELDS] = {};
+    double* stage[NPROG] = {};
+    double* acc[NPROG] = {};
+    double* src = nullptr;
+    double* p_baro = nullptr;            // null unless set
+    double* partial = nullptr;
+    double* buoy = nullptr;
+    double* sin_j = nullptr;
+    double* rm_tab = nullptr;
+    double* cor_j = nullptr;
+    ColGeo* geo = nullptr;
+    double** six = nullptr;              // device array: aux_u, aux_v, aux_w, rhs_u, rhs_v, rhs_w
+    unsigned long long* counter = nullptr;
+    std::vector<ColGeo> geo_h;
+    bool has_pbaro = false;
+
+    int bind_kind[ATSAT_NFIELDS] = {};
+    double* bind_base[ATSAT_NFIELDS] = {};
+    std::vector<double*> bind_rows[ATSAT_NFIELDS];
+    double* pinned = nullptr;            // staging for ragged rows, fsz doubles
+
+    int64_t launches = 0;
+    bool profiling = false;
+    std::vector<ProfEvent> pend;
+    std::vector<cudaEvent_t> pool;
+    int64_t prof_n[ATSAT_K_NCLASS] = {};
+    double prof_ms[ATSAT_K_NCLASS] = {};
+
+    int write_all_rhs = 0;
+    std::string err;
+};
+
+namespace {
+
+int fail(atsat_dyn* h, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (h) h->err = buf;
+    return code;
+}
+
+#define CK(h, call)                                                                                     \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            return fail(h, ATSAT_DYN_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                        __LINE__);                                                                      \
+    } while (0)
+
+cudaEvent_t ev_get(atsat_dyn* h) {
+    if (!h->pool.empty()) {
+        cudaEvent_t e = h->pool.back();
+        h->pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Bracket the launches of one kernel class with events when profiling is on.
+struct Timed {
+    atsat_dyn* h;
+    int cls;
+    cudaEvent_t a = nullptr, b = nullptr;
+    Timed(atsat_dyn* h_, int cls_) : h(h_), cls(cls_) {
+        if (h->profiling) {
+            a = ev_get(h);
+            b = ev_get(h);
+            cudaEventRecord(a, h->stream);
+        }
+    }
+    ~Timed() {
+        if (h->profiling) {
+            cudaEventRecord(b, h->stream);
+            h->pend.push_back({cls, a, b});
+        }
+    }
+};
+
+int resolve_profile(atsat_dyn* h) {
+    if (h->pend.empty()) return ATSAT_DYN_OK;
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (auto& e : h->pend) {
+        float ms = 0.f;
+        CK(h, cudaEventElapsedTime(&ms, e.a, e.b));
+        h->prof_n[e.cls] += 1;
+        h->prof_ms[e.cls] += ms;
+        h->pool.push_back(e.a);
+        h->pool.push_back(e.b);
+    }
+    h->pend.clear();
+    return ATSAT_DYN_OK;
+}
+
+double metric_radius(const atsat_dyn_params& p, double r) {
+    const double R_km = p.metric_radius_km;
+    if (!(R_km > 0.0)) return r;
+    return r + (R_km / p.L_atm - 1.0);
+}
+
+int check_supported(atsat_dyn* h, const atsat_dyn_params& p) {
+    struct { int bad; const char* what; } rules[] = {
+        {p.phi_periodic == 0, "ATSAT_BC_PHI_PERIODIC=0 (the non-periodic seam)"},
+        {p.chrom != 0, "ATSAT_CHROM (chromophore tracer)"},
+        {p.cp_h2_dyn != 0, "ATSAT_CP_H2 / ATSAT_CP_GAS in the dynamics"},
+        {p.print_diag != 0, "ATSAT_TB/UB/CWB_DIAG print-only accumulators"},
+        {p.coord_stretching != 0, "radial coordinate stretching"},
+        {p.hydro_buoy != 0, "ATSAT_HYDRO_BUOY"},
+        {p.t_limiter != 0, "ATSAT_T_LIMITER (reads tn at k-1 = -1 on the periodic seam in the reference)"},
+        {p.press_wall != 0, "ATSAT_PRESS_WALL (no solid body exists in ATSAT)"},
+        {p.press_line != 0, "ATSAT_PRESS_LINE"},
+        {p.press_baro != 0, "ATSAT_PRESS_BAROTROPIC"},
+        {p.precision != ATSAT_DYN_FP64, "precision other than FP64"},
+    };
+    for (auto& r : rules)
+        if (r.bad) return fail(h, ATSAT_DYN_E_UNSUPPORTED, "not implemented on the device: %s", r.what);
+    return ATSAT_DYN_OK;
+}
+
+void build_constants(atsat_dyn* h) {
+    const atsat_dyn_params& p = h->p;
+    const atsat_dyn_grid& g = h->g;
+    KConst& K = h->kc;
+    K.im = g.im; K.jm = g.jm; K.km = g.km;
+    K.kp = (g.km + 31) / 32 * 32;
+    K.plane = (int64_t)g.jm * K.kp;
+    K.fsz = (int64_t)g.im * K.plane;
+    K.periodic = p.phi_periodic;
+    K.turb = p.turb_active;
+    K.metric_split = p.metric_split;
+    K.coriolis_split = p.coriolis_split;
+    K.adiabatic = p.adiabatic;
+    K.adiabatic_rho = p.adiabatic_rho;
+    K.buoy_legacy = p.buoy_legacy;
+    K.hydro_buoy = p.hydro_buoy;
+    K.t_limiter = p.t_limiter;
+    K.cell_hold = p.cell_hold;
+    K.rad_on = (p.rad_coupling != 0.0 && p.cp_mix > 0.0);
+    K.precip_on = (p.precip_coupling != 0.0 && p.r_mix > 0.0 && p.cp_mix > 0.0);
+    K.tmf_on = (p.thermal_massflux != 0.0);
+    K.divu_on = (p.species_divu != 0.0);
+    K.press_incr = (p.press_incr != 0 && p.press_src != 0);
+    K.press_src = p.press_src;
+    K.rigid_lid = p.rigid_lid;
+    K.press_wall = p.press_wall;
+    K.dr = g.dr;
+    K.inv_2dr = 1.0 / (2.0 * g.dr);
+    K.inv_2dthe = 1.0 / (2.0 * g.dthe);
+    K.inv_2dphi = 1.0 / (2.0 * g.dphi);
+    K.inv_dr2 = 1.0 / (g.dr * g.dr);
+    K.inv_dthe2 = 1.0 / (g.dthe * g.dthe);
+    K.inv_dphi2 = 1.0 / (g.dphi * g.dphi);
+    K.coeff_energy_p = p.u_0 * p.u_0 / (p.cp_mix * p.t_ref);
+    K.to_nd = 1.0 / (p.r_mix * p.u_0 * p.u_0 * 1.0e-5);
+    K.r_mix = p.r_mix;
+    K.rR = p.r_mix * p.R_mix;
+    K.t_ref = p.t_ref;
+    K.g = p.g;
+    const double L_m = p.L_atm * 1.0e3;
+    const double nd_buoy = p.nd_buoy ? 1.0e5 * L_m / (p.u_0 * p.u_0) : 1.0;
+    K.kbuoy = -nd_buoy * p.buoy_scale * p.buoyancy;
+    K.legacy_buoy = p.buoyancy * p.g;
+    K.inv_re = 1.0 / p.re;
+    K.inv_re_pr = 1.0 / (p.re * p.pr);
+    K.inv_sc_re_ch4 = 1.0 / (p.sc_ch4 * p.re);
+    K.inv_sc_re_h2o = 1.0 / (p.sc_h2o * p.re);
+    K.inv_sc_re_h2s = 1.0 / (p.sc_h2s * p.re);
+    K.inv_sc_re_nh3 = 1.0 / (p.sc_nh3 * p.re);
+    K.inv_sc_re_nh4sh = 1.0 / (p.sc_nh4sh * p.re);
+    K.inv_sig_k = 1.0 / 0.85;
+    K.inv_sig_w = 1.0 / 0.5;
+    K.turb_coupling = p.turb_coupling;
+    K.inv_pr_t = 1.0 / 0.9;
+    K.Coriolis = p.Coriolis;
+    K.centrifugal = p.centrifugal;
+    K.chem = p.chemical_reaction;
+    K.metric_on = p.metric_split ? 0.0 : 1.0;
+    K.cor_rad_on = p.coriolis_split ? 0.0 : 1.0;
+    K.rad_coupling = p.rad_coupling;
+    K.rad_num = L_m;
+    K.rad_den_c = p.cp_mix * p.u_0 * p.t_ref;
+    K.precip_coupling = p.precip_coupling;
+    K.precip_num = L_m;
+    K.precip_den = 1.0 / (p.r_mix * p.cp_mix * p.u_0 * p.t_ref);
+    K.tmf_chem = p.thermal_massflux * p.chemical_reaction;
+    K.species_divu = p.species_divu;
+    K.tke_max = 1000.0 / (p.u_0 * p.u_0);
+    K.dis_min = 1.0e-10;
+    K.dt = p.dt;
+    K.pdyn_cap = p.pdyn_cap;
+    K.c43 = 4.0 / 3.0;
+    K.c13 = 1.0 / 3.0;
+}
+
+// Per-column geometry (RungeKutta_Sat_Turb.cpp:129-142, 223-243; PressureSolver.h:156-162, 255-259, 326-353)
+void build_geometry(atsat_dyn* h, const double* vbar0, const double* ubar0) {
+    const atsat_dyn_params& p = h->p;
+    const atsat_dyn_grid& g = h->g;
+    const int im = g.im, jm = g.jm;
+    h->geo_h.assign((size_t)im * jm, ColGeo{});
+    const double L_m = p.L_atm * 1.0e3;
+    const double nd_cor = p.nd_cor ? L_m / p.u_0 : 1.0;
+    const double nd_cent = p.nd_cent ? L_m * L_m / (p.u_0 * p.u_0) : 1.0;
+    const double inv_dr2 = 1.0 / (g.dr * g.dr), inv_dthe2 = 1.0 / (g.dthe * g.dthe);
+    const double inv_dphi2 = 1.0 / (g.dphi * g.dphi);
+    for (int i = 0; i < im; i++) {
+        for (int j = 0; j < jm; j++) {
+            ColGeo& c = h->geo_h[(size_t)i * jm + j];
+            double st = std::sin(h->the_z[j]);
+            if (st < p.sinthe_min) st = p.sinthe_min;
+            const double ct = std::cos(h->the_z[j]);
+            const double rm = metric_radius(p, h->rad_z[i]);
+            const double rm2 = rm * rm;
+            const double sinthe2 = st * st;
+            c.rm = rm;
+            c.inv_rm = 1.0 / rm;
+            c.inv_rm2 = 1.0 / rm2;
+            c.inv_rmsinthe = 1.0 / (rm * st);
+            c.inv_rm2sinthe = c.inv_rm2 / st;
+            c.inv_rm2sinthe2 = c.inv_rm2 / sinthe2;
+            c.costhe_inv_rm2sinthe = ct * c.inv_rm2sinthe;
+            c.cotanthe = ct / st;
+            c.costhe = ct;
+            c.two_inv_rm = 2.0 * c.inv_rm;
+            c.v_metric = (1.0 + ct / sinthe2) * c.inv_rm2;
+            c.exp_rm = 1.0;
+            c.exp_2_rm = 1.0;
+            const double s_true = std::sqrt(std::max(0.0, 1.0 - ct * ct));
+            c.sinthe_true = s_true;
+            c.cor_rad = nd_cor * -2.0 * p.omega * s_true;
+            c.cor_the = nd_cor * -2.0 * p.omega * ct;
+            c.cor_phi = nd_cor * +2.0 * p.omega;
+            c.cent_rad = nd_cent * p.omega * p.omega * rm * s_true * s_true;
+            c.cent_the = nd_cent * p.omega * p.omega * rm * s_true * ct;
+            const bool hold = p.cell_hold && vbar0 && ubar0;
+            c.vbar0 = hold ? vbar0[(size_t)i * jm + j] : 0.0;
+            c.ubar0 = hold ? ubar0[(size_t)i * jm + j] : 0.0;
+            // pressure solver: its own sine table with the exact-zero guard
+            double sp = std::sin(h->the_z[j]);
+            if (sp < p.sinthe_min) sp = p.sinthe_min;
+            if (sp == 0.0) sp = 1.0e-5;
+            const double inv_rm2 = 1.0 / rm2;
+            const double inv_rm2sinthe2 = inv_rm2 / (sp * sp);
+            c.p_num1 = 1.0 * inv_dr2;
+            c.p_num2 = inv_rm2 * inv_dthe2;
+            c.p_num3 = inv_rm2sinthe2 * inv_dphi2;
+            c.p_den = 2.0 * c.p_num1 + 2.0 * c.p_num2 + 2.0 * c.p_num3;
+            c.lc_num1 = 1.0 * 1.0 * inv_dr2;
+            c.lc_num2 = inv_dthe2 / (rm * rm);
+            c.lc_num3 = inv_dphi2 / (rm * rm * sp * sp);
+            c.p_exp_rm = 1.0;
+            c.p_inv_rm = 1.0 / rm;
+            c.p_inv_rmsinthe = 1.0 / (rm * sp);
+        }
+    }
+}
+
+bool valid_field(int f) { return f >= 0 && f < ATSAT_NFIELDS; }
+
+int upload_one(atsat_dyn* h, int fid) {
+    const KConst& K = h->kc;
+    const int im = K.im, jm = K.jm, km = K.km, kp = K.kp;
+    if (h->bind_kind[fid] == BIND_ARRAY) {
+        CK(h, cudaMemcpy2DAsync(h->f[fid], (size_t)kp * 8, h->bind_base[fid], (size_t)km * 8, (size_t)km * 8,
+                                (size_t)im * jm, cudaMemcpyHostToDevice, h->stream));
+    } else if (h->bind_kind[fid] == BIND_ROWS) {
+        CK(h, cudaStreamSynchronize(h->stream));     // the staging buffer is free again
+        double* const* rows = h->bind_rows[fid].data();
+        double* st = h->pinned;
+        const int nrows = im * jm;
+#pragma omp parallel for schedule(static)
+        for (int r = 0; r < nrows; r++) memcpy(st + (size_t)r * kp, rows[r], (size_t)km * 8);
+        CK(h, cudaMemcpyAsync(h->f[fid], st, (size_t)K.fsz * 8, cudaMemcpyHostToDevice, h->stream));
+    } else {
+        return fail(h, ATSAT_DYN_E_UNBOUND, "field %d has no host binding", fid);
+    }
+    return ATSAT_DYN_OK;
+}
+
+int download_one(atsat_dyn* h, int fid) {
+    const KConst& K = h->kc;
+    const int im = K.im, jm = K.jm, km = K.km, kp = K.kp;
+    if (h->bind_kind[fid] == BIND_ARRAY) {
+        CK(h, cudaMemcpy2DAsync(h->bind_base[fid], (size_t)km * 8, h->f[fid], (size_t)kp * 8, (size_t)km * 8,
+                                (size_t)im * jm, cudaMemcpyDeviceToHost, h->stream));
+    } else if (h->bind_kind[fid] == BIND_ROWS) {
+        CK(h, cudaMemcpyAsync(h->pinned, h->f[fid], (size_t)K.fsz * 8, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        double* const* rows = h->bind_rows[fid].data();
+        const double* st = h->pinned;
+        const int nrows = im * jm;
+#pragma omp parallel for schedule(static)
+        for (int r = 0; r < nrows; r++) memcpy(rows[r], st + (size_t)r * kp, (size_t)km * 8);
+    } else {
+        return fail(h, ATSAT_DYN_E_UNBOUND, "field %d has no host binding", fid);
+    }
+    return ATSAT_DYN_OK;
+}
+
+int finish(atsat_dyn* h) {
+    CK(h, cudaGetLastError());
+    CK(h, cudaStreamSynchronize(h->stream));
+    return ATSAT_DYN_OK;
+}
+
+StageIO<double> make_io(atsat_dyn* h, double* const* in, double* const* out) {
+    StageIO<double> io{};
+    for (int q = 0; q < NPROG; q++) {
+        io.in[q] = in[q];
+        io.out[q] = out ? out[q] : nullptr;
+        io.yn[q] = h->f[ATSAT_F_N_BASE + q];
+        io.acc[q] = h->acc[q];
+        io.rhs[q] = h->f[ATSAT_F_RHS_BASE + q];
+    }
+    io.p_dyn = h->f[ATSAT_F_P_DYN];
+    io.p_stat = h->f[ATSAT_F_P_STAT];
+    io.p_metric = h->f[ATSAT_F_P_METRIC];
+    io.rho_mix = h->f[ATSAT_F_RHO_MIX];
+    io.nue = h->f[ATSAT_F_NUE];
+    io.q_precip = h->f[ATSAT_F_Q_PRECIP];
+    io.q_rad = h->f[ATSAT_F_Q_RAD];
+    io.tke_source = h->f[ATSAT_F_TKE_SOURCE];
+    io.dis_source = h->f[ATSAT_F_DIS_SOURCE];
+    for (int s = 0; s < 9; s++) io.s_precip[s] = h->f[ATSAT_F_S_PRECIP_H2O + s];
+    io.massflux_h2s = h->f[ATSAT_F_MASSFLUX_H2S];
+    io.massflux_nh3 = h->f[ATSAT_F_MASSFLUX_NH3];
+    io.massflux_nh4sh = h->f[ATSAT_F_MASSFLUX_NH4SH];
+    io.fluxlim_nh4sh = h->f[ATSAT_F_FLUXLIM_NH4SH];
+    io.thermalmassflux = h->f[ATSAT_F_THERMALMASSFLUX];
+    io.aux[0] = h->f[ATSAT_F_AUX_U];
+    io.aux[1] = h->f[ATSAT_F_AUX_V];
+    io.aux[2] = h->f[ATSAT_F_AUX_W];
+    io.buoy = h->buoy;
+    io.geo = h->geo;
+    return io;
+}
+
+int do_level_mean(atsat_dyn* h) {
+    Timed t(h, ATSAT_K_LEVEL_MEAN);
+    CK(h, launch_level_mean(h->kc, h->f[ATSAT_F_T], h->f[ATSAT_F_P_STAT], h->sin_j, h->partial, h->buoy, h->stream));
+    h->launches += 2;
+    return ATSAT_DYN_OK;
+}
+
+int do_metric(atsat_dyn* h) {
+    Timed t(h, ATSAT_K_METRIC_SCAN);
+    CK(h, launch_metric_scan(h->kc, h->f[ATSAT_F_V], h->f[ATSAT_F_W], h->rm_tab, h->cor_j,
+                             h->has_pbaro ? h->p_baro : nullptr, h->f[ATSAT_F_P_METRIC], h->stream));
+    h->launches += 1;
+    return ATSAT_DYN_OK;
+}
+
+int enqueue_rk4(atsat_dyn* h) {
+    int rc;
+    if ((rc = do_level_mean(h))) return rc;
+    if (h->p.metric_split && (rc = do_metric(h))) return rc;
+    double* L[NPROG];
+    double* S[NPROG];
+    for (int q = 0; q < NPROG; q++) { L[q] = h->f[q]; S[q] = h->stage[q]; }
+    const double dt = h->p.dt;
+    for (int stage = 0; stage < 4; stage++) {
+        StageParams sp{};
+        sp.stage = stage;
+        sp.write_all_rhs = h->write_all_rhs;
+        sp.c_in = (stage == 0 || stage == 1) ? 0.5 * dt : (stage == 2 ? dt : 0.0);
+        sp.wgt = (stage == 0 || stage == 3) ? 1.0 : 2.0;
+        sp.sixth_dt = dt / 6.0;
+        double* const* in = (stage & 1) ? S : L;
+        double* const* out = (stage & 1) ? L : S;
+        StageIO<double> io = make_io(h, in, out);
+        Timed t(h, ATSAT_K_RK_STAGE);
+        CK(h, launch_rk_stage_fp64(h->kc, io, sp, stage == 3 ? MODE_FINAL : MODE_STAGE, h->stream));
+        h->launches += 1;
+    }
+    return ATSAT_DYN_OK;
+}
+
+int enqueue_pressure(atsat_dyn* h, int sweeps) {
+    const KConst& K = h->kc;
+    {
+        Timed t(h, ATSAT_K_PRESS_BOUNDARY);
+        CK(h, launch_projection_prep(K, h->six, h->stream));
+        h->launches += 2;
+    }
+    CK(h, cudaMemsetAsync(h->counter, 0, sizeof(unsigned long long), h->stream));
+    const bool incr = K.press_incr;
+    {
+        Timed t(h, ATSAT_K_PRESS_SOURCE);
+        CK(h, launch_press_source(K, h->geo, incr ? h->f[ATSAT_F_RHS_U] : h->f[ATSAT_F_AUX_U],
+                                  incr ? h->f[ATSAT_F_RHS_V] : h->f[ATSAT_F_AUX_V],
+                                  incr ? h->f[ATSAT_F_RHS_W] : h->f[ATSAT_F_AUX_W], h->f[ATSAT_F_AUX_U],
+                                  h->f[ATSAT_F_AUX_V], h->f[ATSAT_F_AUX_W], h->f[ATSAT_F_RHS_U], h->f[ATSAT_F_RHS_V],
+                                  h->f[ATSAT_F_RHS_W], h->f[ATSAT_F_P_DYN], h->src, h->counter, h->stream));
+        h->launches += 1;
+    }
+    for (int s = 0; s < sweeps; s++) {
+        for (int colour = 0; colour < 2; colour++) {
+            Timed t(h, ATSAT_K_PRESS_SWEEP);
+            CK(h, launch_press_sweep(K, h->geo, h->src, h->f[ATSAT_F_P_DYN], colour, h->stream));
+            h->launches += 1;
+        }
+        Timed t(h, ATSAT_K_PRESS_BOUNDARY);
+        CK(h, launch_press_boundary(K, h->f[ATSAT_F_P_DYN], h->stream));
+        h->launches += 1;
+    }
+    return ATSAT_DYN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int atsat_dyn_abi_version(void) { return ATSAT_DYN_ABI_VERSION; }
+
+int atsat_dyn_params_default(atsat_dyn_params* p) {
+    if (!p) return ATSAT_DYN_E_INVALID;
+    memset(p, 0, sizeof(*p));
+    // the committed configuration (cli/config_atsat.xml) and cSaturnModel.h member initialisers
+    p->re = 100000.0; p->pr = 69.0;
+    p->sc_h2o = 0.61; p->sc_nh3 = 0.61; p->sc_h2s = 0.94; p->sc_ch4 = 0.99; p->sc_nh4sh = 0.7;
+    p->u_0 = 470.0; p->t_ref = 134.0; p->L_atm = 500.0; p->g = 10.0; p->omega = 0.000163;
+    p->Coriolis = 1.0; p->centrifugal = 1.0; p->buoyancy = 1.0; p->chemical_reaction = 1.0;
+    // ChemistrySat::ThermalPropertiesSat of the default composition (ChemistrySat.h:475-530)
+    p->cp_mix = 0x1.3a544e8a8f013p+13;
+    p->r_mix = 1.382;
+    p->R_mix = 0x1.6ba7dd06e410fp+11;
+    p->dt = 0.01;
+    p->metric_radius_km = 58232.0; p->sinthe_min = 0.0; p->buoy_scale = 1.0; p->turb_coupling = 1.0;
+    p->rad_coupling = 0.0; p->precip_coupling = 1.0; p->thermal_massflux = 0.0; p->species_divu = 0.0;
+    p->pdyn_cap = 0.2;
+    p->phi_periodic = 1; p->metric_split = 1; p->coriolis_split = 1; p->hydro_buoy = 0;
+    p->nd_cor = 1; p->nd_cent = 0; p->nd_buoy = 0; p->cell_hold = 1; p->adiabatic = 1; p->adiabatic_rho = 1;
+    p->turb_active = 1; p->t_limiter = 0; p->buoy_legacy = 0; p->chrom = 0; p->cp_h2_dyn = 0; p->print_diag = 0;
+    p->coord_stretching = 0;
+    p->press_src = 1; p->press_incr = 1; p->press_sweeps = 1; p->press_wall = 0; p->rigid_lid = 1;
+    p->press_line = 0; p->press_baro = 0; p->precision = ATSAT_DYN_FP64;
+    p->bc_radius_form = 2; p->bc_bottom_form = 3; p->bc_pole_form = 1; p->bc_pole_fill = 1; p->bc_lid_u = 1;
+    p->bc_top_taper = 2; p->bc_species_lid_copy = 1; p->bc_species_wall_copy = 2; p->local_rho = 1;
+    return ATSAT_DYN_OK;
+}
+
+static const char* envs(const char* n) { return getenv(n); }
+static int env_i(const char* n, int d) { const char* e = envs(n); return e ? atoi(e) : d; }
+static double env_d(const char* n, double d) { const char* e = envs(n); return e ? atof(e) : d; }
+
+int atsat_dyn_params_from_env(atsat_dyn_params* p) {
+    if (!p) return ATSAT_DYN_E_INVALID;
+    // the knobs as the reference resolves them; see the file:line of each field in atsat_dyn.h
+    p->metric_radius_km = env_d("ATSAT_METRIC_RADIUS", 58232.0);
+    { const double x = env_d("ATSAT_SINTHE_MIN", 0.0); p->sinthe_min = (x >= 0.0 && x < 1.0) ? x : 0.0; }
+    p->buoy_scale = env_d("ATSAT_BUOY_SCALE", 1.0);
+    p->turb_coupling = env_d("ATSAT_TURB_COUPLING", 1.0);
+    p->rad_coupling = env_d("ATSAT_RAD_COUPLING", 0.0);
+    p->precip_coupling = env_d("ATSAT_PRECIP_COUPLING", 1.0);
+    p->thermal_massflux = env_d("ATSAT_THERMAL_MASSFLUX", 0.0);
+    p->species_divu = env_d("ATSAT_SPECIES_DIVU", 0.0);
+    p->pdyn_cap = env_d("ATSAT_PDYN_CAP", 0.2);
+    p->phi_periodic = env_i("ATSAT_BC_PHI_PERIODIC", 1) != 0;
+    p->metric_split = envs("ATSAT_METRIC_SPLIT") ? (env_i("ATSAT_METRIC_SPLIT", 1) != 0) : 1;
+    p->coriolis_split = (envs("ATSAT_CORIOLIS_SPLIT") ? (env_i("ATSAT_CORIOLIS_SPLIT", 1) != 0) : 1) && p->metric_split;
+    const int geo = envs("ATSAT_GEO_BALANCE") ? (env_i("ATSAT_GEO_BALANCE", 1) != 0) : 1;
+    p->hydro_buoy = (envs("ATSAT_HYDRO_BUOY") ? (env_i("ATSAT_HYDRO_BUOY", 0) != 0) : 0) && p->metric_split;
+    const int nd_all = env_i("ATSAT_NONDIM", 0);
+    const int c_cor = envs("ATSAT_ND_COR") ? env_i("ATSAT_ND_COR", 0) : (geo ? 1 : -1);
+    const int c_cent = env_i("ATSAT_ND_CENT", -1);
+    const int c_buoy = env_i("ATSAT_ND_BUOY", -1);
+    p->nd_cor = ((c_cor >= 0 ? c_cor : nd_all) != 0);
+    p->nd_cent = ((c_cent >= 0 ? c_cent : nd_all) != 0);
+    p->nd_buoy = ((c_buoy >= 0 ? c_buoy : nd_all) != 0);
+    p->cell_hold = envs("ATSAT_CELL_HOLD") ? (env_i("ATSAT_CELL_HOLD", 0) != 0) : geo;
+    p->adiabatic = envs("ATSAT_ADIABATIC") ? (env_i("ATSAT_ADIABATIC", 1) != 0) : 1;
+    p->adiabatic_rho = envs("ATSAT_ADIABATIC_RHO") ? (env_i("ATSAT_ADIABATIC_RHO", 1) != 0) : 1;
+    {
+        const int turb_env = env_i("ATSAT_TURB", -1);
+        const char* tm = envs("ATSAT_TURB_MODEL");
+        const std::string model = tm ? tm : "k_omega_SST";
+        p->turb_active = (turb_env != 0) && !(model.empty() || model == "none" || model == "laminar");
+    }
+    p->t_limiter = env_i("ATSAT_T_LIMITER", 0) != 0;
+    p->buoy_legacy = env_i("ATSAT_BUOY_LEGACY", 0) != 0;
+    p->chrom = envs("ATSAT_CHROM") && env_i("ATSAT_CHROM", 0) != 0;
+    p->cp_h2_dyn = (env_i("ATSAT_CP_H2", 0) != 0) || (env_i("ATSAT_CP_GAS", 0) != 0);
+    p->print_diag = env_i("ATSAT_TB_DIAG", 0) > 0 || env_i("ATSAT_UB_DIAG", 0) > 0 || env_i("ATSAT_CWB_DIAG", 0) > 0;
+    p->press_src = env_i("ATSAT_PRESS_SRC", 1);
+    // Run() sets ATSAT_PRESS_INCR=1 under GEO_BALANCE unless it is given (cSaturnModel.cpp:612)
+    p->press_incr = envs("ATSAT_PRESS_INCR") ? (env_i("ATSAT_PRESS_INCR", 0) != 0) : geo;
+    { const int n = env_i("ATSAT_PRESS_SWEEPS", 1); p->press_sweeps = n > 0 ? n : 1; }
+    p->press_wall = env_i("ATSAT_PRESS_WALL", 0) != 0;
+    p->rigid_lid = env_i("ATSAT_BC_RIGID_LID", 1) != 0;
+    p->press_line = env_i("ATSAT_PRESS_LINE", 0) != 0;
+    {   // under HYDRO_BUOY Run() sets ATSAT_PRESS_BAROTROPIC=1 unless given (cSaturnModel.cpp:615)
+        const int raw = envs("ATSAT_PRESS_BAROTROPIC") ? env_i("ATSAT_PRESS_BAROTROPIC", 0) : (p->hydro_buoy ? 1 : 0);
+        p->press_baro = (raw != 0) && p->phi_periodic && !p->press_wall;
+    }
+    p->bc_radius_form = env_i("ATSAT_BC_RADIUS_COPY", 2);
+    p->bc_bottom_form = env_i("ATSAT_BC_BOTTOM_FORM", 3);
+    p->bc_pole_form = env_i("ATSAT_BC_POLE_COPY", 1);
+    p->bc_pole_fill = env_i("ATSAT_BC_POLE_FILL", 1);
+    p->bc_lid_u = env_i("ATSAT_BC_LID_U", p->rigid_lid);
+    p->bc_top_taper = env_i("ATSAT_BC_TOP_TAPER", 2);
+    p->bc_species_lid_copy = env_i("ATSAT_BC_SPECIES_LID_COPY", 1);
+    p->bc_species_wall_copy = env_i("ATSAT_BC_SPECIES_WALL_COPY", 2);
+    p->local_rho = envs("ATSAT_LOCAL_RHO") ? (env_i("ATSAT_LOCAL_RHO", 1) != 0) : 1;
+    if (env_i("ATSAT_BC_SEAM_DAMP", 0) != 0 || env_i("ATSAT_BC_T_LID_PIN", 0) != 0) return ATSAT_DYN_E_UNSUPPORTED;
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_dyn_t* out) {
+    if (!g || !p || !out || !g->rad_z || !g->the_z) return ATSAT_DYN_E_INVALID;
+    *out = nullptr;
+    if (g->im < 5 || g->jm < 7 || g->km < 5 || g->im > 4096 || g->jm > 65536 || g->km > 65536)
+        return ATSAT_DYN_E_INVALID;
+    atsat_dyn* h = new atsat_dyn();
+    h->g = *g;
+    h->rad_z.assign(g->rad_z, g->rad_z + g->im);
+    h->the_z.assign(g->the_z, g->the_z + g->jm);
+    h->g.rad_z = h->rad_z.data();
+    h->g.the_z = h->the_z.data();
+    h->p = *p;
+    int rc = check_supported(h, *p);
+    if (rc) { *out = h; return rc; }
+    build_constants(h);
+    build_geometry(h, nullptr, nullptr);
+    const KConst& K = h->kc;
+    auto cuda_fail = [&](cudaError_t e, const char* what) {
+        fail(h, e == cudaErrorMemoryAllocation ? ATSAT_DYN_E_NOMEM : ATSAT_DYN_E_CUDA, "%s: %s", what,
+             cudaGetErrorString(e));
+        *out = h;
+        return e == cudaErrorMemoryAllocation ? ATSAT_DYN_E_NOMEM : ATSAT_DYN_E_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaGetDevice(&h->device)) != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_fail(e, "cudaStreamCreate");
+    // fields, stage buffers, accumulators, source; then the small tables
+    const int64_t nbig = ATSAT_NFIELDS + 2 * NPROG + 2;
+    const int64_t nsmall = 2LL * K.im * 16 + K.im + K.jm + K.im + K.jm + 64;
+    const size_t bytes = (size_t)(nbig * K.fsz + nsmall) * 8 + sizeof(ColGeo) * (size_t)K.im * K.jm + 4096;
+    if ((e = cudaMalloc(&h->slab, bytes)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    if ((e = cudaMemsetAsync(h->slab, 0, bytes, h->stream)) != cudaSuccess) return cuda_fail(e, "cudaMemset");
+    double* q = h->slab;
+    for (int f = 0; f < ATSAT_NFIELDS; f++) { h->f[f] = q; q += K.fsz; }
+    for (int s = 0; s < NPROG; s++) { h->stage[s] = q; q += K.fsz; }
+    for (int s = 0; s < NPROG; s++) { h->acc[s] = q; q += K.fsz; }
+    h->src = q; q += K.fsz;
+    h->p_baro = q; q += K.fsz;
+    h->partial = q; q += 2LL * K.im * 16;
+    h->buoy = q; q += K.im;
+    h->sin_j = q; q += K.jm;
+    h->rm_tab = q; q += K.im;
+    h->cor_j = q; q += K.jm;
+    h->counter = reinterpret_cast<unsigned long long*>(q); q += 8;
+    h->six = reinterpret_cast<double**>(q); q += 8;
+    q = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(q) + 255) & ~uintptr_t(255));
+    h->geo = reinterpret_cast<ColGeo*>(q);
+    // small host tables
+    std::vector<double> sin_j(K.jm), rm_tab(K.im), cor_j(K.jm);
+    const double nd = p->nd_cor ? p->L_atm * 1.0e3 / p->u_0 : 1.0;
+    for (int j = 0; j < K.jm; j++) {
+        sin_j[j] = std::sin(h->the_z[j]);
+        cor_j[j] = p->coriolis_split ? p->Coriolis * nd * 2.0 * p->omega * std::fabs(std::sin(h->the_z[j])) : 0.0;
+    }
+    for (int i = 0; i < K.im; i++) rm_tab[i] = metric_radius(*p, h->rad_z[i]);
+    double* six_h[6] = {h->f[ATSAT_F_AUX_U], h->f[ATSAT_F_AUX_V], h->f[ATSAT_F_AUX_W],
+                        h->f[ATSAT_F_RHS_U], h->f[ATSAT_F_RHS_V], h->f[ATSAT_F_RHS_W]};
+    if ((e = cudaMemcpyAsync(h->sin_j, sin_j.data(), 8 * K.jm, cudaMemcpyHostToDevice, h->stream)) ||
+        (e = cudaMemcpyAsync(h->rm_tab, rm_tab.data(), 8 * K.im, cudaMemcpyHostToDevice, h->stream)) ||
+        (e = cudaMemcpyAsync(h->cor_j, cor_j.data(), 8 * K.jm, cudaMemcpyHostToDevice, h->stream)) ||
+        (e = cudaMemcpyAsync(h->six, six_h, sizeof(six_h), cudaMemcpyHostToDevice, h->stream)) ||
+        (e = cudaMemcpyAsync(h->geo, h->geo_h.data(), sizeof(ColGeo) * h->geo_h.size(), cudaMemcpyHostToDevice,
+                             h->stream)) ||
+        (e = cudaStreamSynchronize(h->stream)))
+        return cuda_fail(e, "table upload");
+    *out = h;
+    return ATSAT_DYN_OK;
+}
+
+void atsat_dyn_destroy(atsat_dyn_t h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (auto& e : h->pend) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+    for (auto e : h->pool) cudaEventDestroy(e);
+    if (h->slab) cudaFree(h->slab);
+    if (h->pinned) cudaFreeHost(h->pinned);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+const char* atsat_dyn_last_error(atsat_dyn_t h) { return h ? h->err.c_str() : "null handle"; }
+
+int atsat_dyn_bind_host_rows(atsat_dyn_t h, int32_t field, double* const* rows) {
+    if (!h || !h->slab) return ATSAT_DYN_E_INVALID;
+    if (!valid_field(field) || !rows) return fail(h, ATSAT_DYN_E_INVALID, "bad field %d or rows", field);
+    const size_t n = (size_t)h->kc.im * h->kc.jm;
+    for (size_t r = 0; r < n; r++)
+        if (!rows[r]) return fail(h, ATSAT_DYN_E_INVALID, "row %zu of field %d is null", r, field);
+    if (!h->pinned) {
+        cudaError_t e = cudaHostAlloc(&h->pinned, (size_t)h->kc.fsz * 8, cudaHostAllocDefault);
+        if (e != cudaSuccess) { h->pinned = nullptr; return fail(h, ATSAT_DYN_E_NOMEM, "pinned staging: %s", cudaGetErrorString(e)); }
+    }
+    h->bind_rows[field].assign(rows, rows + n);
+    h->bind_kind[field] = BIND_ROWS;
+    h->bind_base[field] = nullptr;
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_bind_host_array(atsat_dyn_t h, int32_t field, double* base) {
+    if (!h || !h->slab) return ATSAT_DYN_E_INVALID;
+    if (!valid_field(field)) return fail(h, ATSAT_DYN_E_INVALID, "bad field %d", field);
+    h->bind_kind[field] = base ? BIND_ARRAY : BIND_NONE;
+    h->bind_base[field] = base;
+    h->bind_rows[field].clear();
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_upload(atsat_dyn_t h, const int32_t* fields, int32_t n) {
+    if (!h || !h->slab || (n > 0 && !fields)) return ATSAT_DYN_E_INVALID;
+    CK(h, cudaSetDevice(h->device));
+    for (int32_t q = 0; q < n; q++) {
+        if (!valid_field(fields[q])) return fail(h, ATSAT_DYN_E_INVALID, "bad field %d", fields[q]);
+        int rc = upload_one(h, fields[q]);
+        if (rc) return rc;
+    }
+    return finish(h);
+}
+
+int atsat_dyn_download(atsat_dyn_t h, const int32_t* fields, int32_t n) {
+    if (!h || !h->slab || (n > 0 && !fields)) return ATSAT_DYN_E_INVALID;
+    CK(h, cudaSetDevice(h->device));
+    for (int32_t q = 0; q < n; q++) {
+        if (!valid_field(fields[q])) return fail(h, ATSAT_DYN_E_INVALID, "bad field %d", fields[q]);
+        int rc = download_one(h, fields[q]);
+        if (rc) return rc;
+    }
+    return finish(h);
+}
+
+int atsat_dyn_set_tables(atsat_dyn_t h, const double* cell_vbar0, const double* cell_ubar0, const double* p_baro) {
+    if (!h || !h->slab) return ATSAT_DYN_E_INVALID;
+    if ((cell_vbar0 == nullptr) != (cell_ubar0 == nullptr))
+        return fail(h, ATSAT_DYN_E_INVALID, "cell_vbar0 and cell_ubar0 must both be given or both be null");
+    CK(h, cudaSetDevice(h->device));
+    build_geometry(h, cell_vbar0, cell_ubar0);
+    CK(h, cudaMemcpyAsync(h->geo, h->geo_h.data(), sizeof(ColGeo) * h->geo_h.size(), cudaMemcpyHostToDevice,
+                          h->stream));
+    h->has_pbaro = (p_baro != nullptr);
+    if (p_baro) {
+        const KConst& K = h->kc;
+        CK(h, cudaMemcpy2DAsync(h->p_baro, (size_t)K.kp * 8, p_baro, (size_t)K.km * 8, (size_t)K.km * 8,
+                                (size_t)K.im * K.jm, cudaMemcpyHostToDevice, h->stream));
+    }
+    return finish(h);
+}
+
+int atsat_dyn_get_buoy_ref_level(atsat_dyn_t h, double* out) {
+    if (!h || !h->slab || !out) return ATSAT_DYN_E_INVALID;
+    CK(h, cudaSetDevice(h->device));
+    CK(h, cudaMemcpyAsync(out, h->buoy, 8 * (size_t)h->kc.im, cudaMemcpyDeviceToHost, h->stream));
+    return finish(h);
+}
+
+#define ENTRY(h)                                              \
+    if (!h || !h->slab) return ATSAT_DYN_E_INVALID;           \
+    CK(h, cudaSetDevice(h->device))
+
+int atsat_dyn_mixture_density(atsat_dyn_t h) {
+    ENTRY(h);
+    {
+        Timed t(h, ATSAT_K_GLUE);
+        CK(h, launch_density(h->kc, h->f[ATSAT_F_T], h->f[ATSAT_F_P_STAT], h->p.R_mix, h->f[ATSAT_F_RHO_MIX], h->stream));
+        h->launches += 1;
+    }
+    return finish(h);
+}
+
+int atsat_dyn_buoyancy_ref_level(atsat_dyn_t h) {
+    ENTRY(h);
+    int rc = do_level_mean(h);
+    return rc ? rc : finish(h);
+}
+
+int atsat_dyn_metric_pressure(atsat_dyn_t h) {
+    ENTRY(h);
+    int rc = do_metric(h);
+    return rc ? rc : finish(h);
+}
+
+int atsat_dyn_rhs(atsat_dyn_t h) {
+    ENTRY(h);
+    double* L[NPROG];
+    for (int q = 0; q < NPROG; q++) L[q] = h->f[q];
+    StageIO<double> io = make_io(h, L, nullptr);
+    StageParams sp{};
+    {
+        Timed t(h, ATSAT_K_RHS);
+        CK(h, launch_rk_stage_fp64(h->kc, io, sp, MODE_RHS, h->stream));
+        h->launches += 1;
+    }
+    return finish(h);
+}
+
+int atsat_dyn_rk4_step(atsat_dyn_t h) {
+    ENTRY(h);
+    int rc = enqueue_rk4(h);
+    return rc ? rc : finish(h);
+}
+
+int atsat_dyn_prepare_projection_boundaries(atsat_dyn_t h) {
+    ENTRY(h);
+    {
+        Timed t(h, ATSAT_K_PRESS_BOUNDARY);
+        CK(h, launch_projection_prep(h->kc, h->six, h->stream));
+        h->launches += 2;
+    }
+    return finish(h);
+}
+
+int atsat_dyn_pressure(atsat_dyn_t h, atsat_dyn_pstats* out) {
+    ENTRY(h);
+    const int sweeps = h->p.press_sweeps > 0 ? h->p.press_sweeps : 1;
+    int rc = enqueue_pressure(h, sweeps);
+    if (rc) return rc;
+    rc = finish(h);
+    if (rc) return rc;
+    if (out) {
+        unsigned long long n = 0;
+        CK(h, cudaMemcpy(&n, h->counter, sizeof(n), cudaMemcpyDeviceToHost));
+        out->sweeps = sweeps;
+        out->src_clamped = (double)n;
+        out->max_abs_update = -1.0;      // not tracked on the device
+    }
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_restore_var(atsat_dyn_t h) {
+    ENTRY(h);
+    {
+        Timed t(h, ATSAT_K_GLUE);
+        const size_t bytes = (size_t)h->kc.fsz * 8;
+        for (int q = 0; q < NPROG; q++)
+            CK(h, cudaMemcpyAsync(h->f[ATSAT_F_N_BASE + q], h->f[q], bytes, cudaMemcpyDeviceToDevice, h->stream));
+        CK(h, cudaMemcpyAsync(h->f[ATSAT_F_P_DYNN], h->f[ATSAT_F_P_DYN], bytes, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    return finish(h);
+}
+
+int atsat_dyn_sync(atsat_dyn_t h) {
+    ENTRY(h);
+    return finish(h);
+}
+
+int atsat_dyn_status(atsat_dyn_t h, atsat_dyn_diag* out) {
+    if (!h || !out) return ATSAT_DYN_E_INVALID;
+    memset(out, 0, sizeof(*out));
+    out->launches = h->launches;
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_count_nonfinite(atsat_dyn_t h, int32_t field, int64_t* count) {
+    ENTRY(h);
+    if (!valid_field(field) || !count) return fail(h, ATSAT_DYN_E_INVALID, "bad field %d", field);
+    CK(h, cudaMemsetAsync(h->counter, 0, sizeof(unsigned long long), h->stream));
+    CK(h, launch_count_nonfinite(h->kc, h->f[field], h->counter, h->stream));
+    h->launches += 1;
+    unsigned long long n = 0;
+    CK(h, cudaMemcpyAsync(&n, h->counter, sizeof(n), cudaMemcpyDeviceToHost, h->stream));
+    int rc = finish(h);
+    *count = (int64_t)n;
+    return rc;
+}
+
+int atsat_dyn_profile(atsat_dyn_t h, int32_t enable) {
+    if (!h) return ATSAT_DYN_E_INVALID;
+    int rc = resolve_profile(h);
+    h->profiling = enable != 0;
+    return rc;
+}
+
+int atsat_dyn_profile_reset(atsat_dyn_t h) {
+    if (!h) return ATSAT_DYN_E_INVALID;
+    int rc = resolve_profile(h);
+    for (int c = 0; c < ATSAT_K_NCLASS; c++) { h->prof_n[c] = 0; h->prof_ms[c] = 0.0; }
+    return rc;
+}
+
+int atsat_dyn_profile_read(atsat_dyn_t h, int32_t kclass, int64_t* launches, double* ms) {
+    if (!h || kclass < 0 || kclass >= ATSAT_K_NCLASS) return ATSAT_DYN_E_INVALID;
+    int rc = resolve_profile(h);
+    if (launches) *launches = h->prof_n[kclass];
+    if (ms) *ms = h->prof_ms[kclass];
+    return rc;
+}
+
+int atsat_dyn_device_field(atsat_dyn_t h, int32_t field, double** dptr, int64_t* pitch) {
+    if (!h || !h->slab || !valid_field(field)) return ATSAT_DYN_E_INVALID;
+    if (dptr) *dptr = h->f[field];
+    if (pitch) *pitch = h->kc.kp;
+    return ATSAT_DYN_OK;
+}
+
+void* atsat_dyn_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+    return p;
+}
+
+void atsat_dyn_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+// test hook: write every rhs_* at the last RK stage, as RHSSat does at every stage
+int atsat_dyn_set_write_all_rhs(atsat_dyn_t h, int32_t on) {
+    if (!h) return ATSAT_DYN_E_INVALID;
+    h->write_all_rhs = on != 0;
+    return ATSAT_DYN_OK;
+}
+
+}  // extern "C"

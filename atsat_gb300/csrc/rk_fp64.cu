@@ -1,0 +1,399 @@
+// FP64 drop-in kernels of RungeKuttaSat (planet/RungeKutta_Sat_Turb.cpp:110-387) and RHSSat
+// (planet/RHS_Sat_Turb.cpp:25-1016).
+//
+// One fused kernel per RK stage: every thread owns one cell of the RK interior
+// (i = 1..im-2, j = 2..jm-3, k = 0..km-2 with the periodic seam), evaluates the full right-hand side
+// of the 17 prognostic fields from the stage input Y_s, folds it into the FP64 accumulator and
+// writes the next stage input Y_{s+1} = y_n + c_in * rhs (the reference's pass A and pass B,
+// :220-320, in one pass over memory). The last stage writes y_{n+1} = y_n + dt/6 * acc directly
+// (:324-375). Y_s and Y_{s+1} live in different buffers, so no cell reads a half-updated
+// neighbour -- the property the reference's separated passes exist for (:178-202).
+//
+// The arithmetic follows the reference's expressions. Divisions by configuration constants are
+// multiplications by reciprocals formed on the host, and exp_rm (identically 1: ATSAT has no radial
+// stretching) is not multiplied; both change results by at most an ulp per operation.
+#include "dyn_common.cuh"
+
+namespace atsat {
+
+namespace {
+
+struct D6 { double dr, d2r, dthe, d2the, dphi, d2phi; };
+
+__device__ __forceinline__ double ldg(const double* p) { return __ldg(p); }
+
+__device__ __forceinline__ void derivs(const double* __restrict__ f, int64_t c, int64_t plane, int kp,
+                                       int dkw, int dke, const KConst& K, D6& d) {
+    const double x = ldg(f + c);
+    const double rp = ldg(f + c + plane), rn = ldg(f + c - plane);
+    const double tp = ldg(f + c + kp), tn = ldg(f + c - kp);
+    const double pe = ldg(f + c + dke), pw = ldg(f + c + dkw);
+    d.dr = (rp - rn) * K.inv_2dr;
+    d.d2r = (rp - 2.0 * x + rn) * K.inv_dr2;
+    d.dthe = (tp - tn) * K.inv_2dthe;
+    d.d2the = (tp - 2.0 * x + tn) * K.inv_dthe2;
+    d.dphi = (pe - pw) * K.inv_2dphi;
+    d.d2phi = (pe - 2.0 * x + pw) * K.inv_dphi2;
+}
+
+struct GeoR {
+    double inv_rm, inv_rm2, inv_rmsinthe, inv_rm2sinthe, inv_rm2sinthe2, costhe_inv_rm2sinthe, cotanthe;
+    double costhe, two_inv_rm, v_metric;
+};
+
+__device__ __forceinline__ double transport(double u, double v, double w, const D6& d, const GeoR& g) {
+    return u * d.dr + v * d.dthe * g.inv_rm + w * d.dphi * g.inv_rmsinthe;
+}
+
+__device__ __forceinline__ double diffusion(const D6& d, const GeoR& g) {
+    return d.d2r + d.dr * g.two_inv_rm + d.d2the * g.inv_rm2 + d.dthe * g.costhe_inv_rm2sinthe
+         + d.d2phi * g.inv_rm2sinthe2;
+}
+
+__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
+
+template <int MODE>
+__device__ __forceinline__ void emit(const StageIO<double>& io, const StageParams& sp, const KConst& K, int q,
+                                     int64_t c, double r) {
+    if (MODE == MODE_RHS) {
+        io.rhs[q][c] = r;
+        return;
+    }
+    double y;
+    if (MODE == MODE_STAGE) {
+        const double a = (sp.stage == 0) ? sp.wgt * r : io.acc[q][c] + sp.wgt * r;
+        io.acc[q][c] = a;
+        y = ldg(io.yn[q] + c) + sp.c_in * r;
+    } else {
+        const double a = io.acc[q][c] + sp.wgt * r;
+        y = ldg(io.yn[q] + c) + sp.sixth_dt * a;
+        if (sp.write_all_rhs || q < 3) io.rhs[q][c] = r;
+    }
+    if (q == ATSAT_F_TKE) y = smin(smax(y, 0.0), K.tke_max);
+    else if (q == ATSAT_F_DIS) y = smax(y, K.dis_min);
+    io.out[q][c] = y;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) rk_stage_fp64_kernel(const KConst K, const StageIO<double> io,
+                                                            const StageParams sp) {
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= K.km || j >= K.jm) return;
+    const int64_t plane = K.plane;
+    const int kp = K.kp;
+    const int64_t c = ((int64_t)i * K.jm + j) * kp + k;
+    const bool interior = (i >= 1 && i <= K.im - 2 && j >= 2 && j <= K.jm - 3 && k <= K.km - 2);
+    if (!interior) {
+        // Cells the step does not integrate keep their values: the stage buffer takes them once.
+        if (MODE == MODE_STAGE && sp.stage == 0) {
+#pragma unroll 1
+            for (int q = 0; q < NPROG; q++) io.out[q][c] = ldg(io.in[q] + c);
+        }
+        return;
+    }
+    const int kw = (k == 0) ? K.km - 2 : k - 1;
+    const int ke = (k == K.km - 2) ? 0 : k + 1;
+    const int dkw = kw - k, dke = ke - k;
+
+    const ColGeo* gp = io.geo + ((int64_t)i * K.jm + j);
+    GeoR g;
+    g.inv_rm = ldg(&gp->inv_rm);
+    g.inv_rm2 = ldg(&gp->inv_rm2);
+    g.inv_rmsinthe = ldg(&gp->inv_rmsinthe);
+    g.inv_rm2sinthe = ldg(&gp->inv_rm2sinthe);
+    g.inv_rm2sinthe2 = ldg(&gp->inv_rm2sinthe2);
+    g.costhe_inv_rm2sinthe = ldg(&gp->costhe_inv_rm2sinthe);
+    g.cotanthe = ldg(&gp->cotanthe);
+    g.costhe = ldg(&gp->costhe);
+    g.two_inv_rm = ldg(&gp->two_inv_rm);
+    g.v_metric = ldg(&gp->v_metric);
+
+    const double u = ldg(io.in[ATSAT_F_U] + c);
+    const double v = ldg(io.in[ATSAT_F_V] + c);
+    const double w = ldg(io.in[ATSAT_F_W] + c);
+
+    D6 du, dv, dw;
+    derivs(io.in[ATSAT_F_U], c, plane, kp, dkw, dke, K, du);
+    derivs(io.in[ATSAT_F_V], c, plane, kp, dkw, dke, K, dv);
+    derivs(io.in[ATSAT_F_W], c, plane, kp, dkw, dke, K, dw);
+    const double dpdr = (ldg(io.p_dyn + c + plane) - ldg(io.p_dyn + c - plane)) * K.inv_2dr;
+    const double dpdthe = (ldg(io.p_dyn + c + kp) - ldg(io.p_dyn + c - kp)) * K.inv_2dthe;
+    const double dpdphi = (ldg(io.p_dyn + c + dke) - ldg(io.p_dyn + c + dkw)) * K.inv_2dphi;
+
+    // eddy viscosity as the momentum / scalar equations read it (RHS_Sat_Turb.cpp:577-582)
+    const double nue_c = ldg(io.nue + c);
+    const double nue_t = (K.turb_coupling != 0.0 && isfinite(nue_c)) ? K.turb_coupling * smax(0.0, nue_c) : 0.0;
+    const double nue_t_s = nue_t * K.inv_pr_t;
+
+    // ---- momentum (RHS_Sat_Turb.cpp:310-350, 388-399, 435-456, 700-714, 780-835) ----
+    {
+        const double cor_rad = ldg(&gp->cor_rad) * w;
+        const double cor_the = ldg(&gp->cor_the) * w;
+        const double v_cor = v - ldg(&gp->vbar0), u_cor = u - ldg(&gp->ubar0);
+        const double cor_phi = ldg(&gp->cor_phi) * (g.costhe * v_cor + ldg(&gp->sinthe_true) * u_cor);
+
+        double transport_u = u * du.dr + v * du.dthe * g.inv_rm + w * du.dphi * g.inv_rmsinthe;
+        if (!K.metric_split) transport_u = transport_u - K.metric_on * (v * v + w * w) * g.inv_rm;
+        const double transport_v = u * dv.dr + v * dv.dthe * g.inv_rm + w * dv.dphi * g.inv_rmsinthe
+                                 + (u * v - w * w * g.cotanthe) * g.inv_rm;
+        const double transport_w = u * dw.dr + v * dw.dthe * g.inv_rm + w * dw.dphi * g.inv_rmsinthe
+                                 + (w * u + v * w * g.cotanthe) * g.inv_rm;
+        const double diffusion_u = du.d2r + 2.0 * u * g.inv_rm2 + du.d2the * g.inv_rm2 + 4.0 * du.dr * g.inv_rm
+                                 + du.dthe * g.costhe_inv_rm2sinthe + du.d2phi * g.inv_rm2sinthe2;
+        const double diffusion_v = dv.d2r + dv.dr * g.two_inv_rm + dv.d2the * g.inv_rm2
+                                 + dv.dthe * g.costhe_inv_rm2sinthe - g.v_metric * v
+                                 + dv.d2phi * g.inv_rm2sinthe2 + 2.0 * du.dthe * g.inv_rm2
+                                 - dw.dphi * 2.0 * g.costhe * g.inv_rm2sinthe2;
+        const double diffusion_w = dw.d2r + dw.dr * g.two_inv_rm + dw.d2the * g.inv_rm2
+                                 + dw.dthe * g.costhe_inv_rm2sinthe - g.v_metric * w
+                                 + dw.d2phi * g.inv_rm2sinthe2 + 2.0 * du.dphi * g.inv_rm2sinthe
+                                 + dv.dphi * 2.0 * g.costhe * g.inv_rm2sinthe2;
+
+        double buoyancy_u = 0.0;
+        const double t_c = ldg(io.in[ATSAT_F_T] + c);
+        if (t_c > 0.0 && !K.hydro_buoy) {
+            const double ps = ldg(io.p_stat + c);
+            if (K.buoy_legacy) buoyancy_u = K.legacy_buoy * (ps + ldg(io.p_dyn + c)) / (K.rR * t_c * K.t_ref);
+            else buoyancy_u = K.kbuoy * (K.g * ps / (K.rR * t_c * K.t_ref) - ldg(io.buoy + i));
+        }
+        const double rhs_u = -dpdr + buoyancy_u - transport_u + diffusion_u * K.inv_re + diffusion_u * nue_t
+                           - K.cor_rad_on * K.Coriolis * cor_rad + K.centrifugal * ldg(&gp->cent_rad);
+        double dpmdthe = 0.0, dpmdphi = 0.0;
+        if (K.metric_split) {
+            dpmdthe = (ldg(io.p_metric + c + kp) - ldg(io.p_metric + c - kp)) * K.inv_2dthe;
+            dpmdphi = (ldg(io.p_metric + c + dke) - ldg(io.p_metric + c + dkw)) * K.inv_2dphi;
+        }
+        const double rhs_v = -dpdthe * g.inv_rm - dpmdthe * g.inv_rm - transport_v + diffusion_v * K.inv_re
+                           + diffusion_v * nue_t - K.Coriolis * cor_the + K.centrifugal * ldg(&gp->cent_the);
+        const double rhs_w = -dpdphi * g.inv_rmsinthe - dpmdphi * g.inv_rmsinthe - transport_w
+                           + diffusion_w * K.inv_re + diffusion_w * nue_t - K.Coriolis * cor_phi;
+        emit<MODE>(io, sp, K, ATSAT_F_U, c, rhs_u);
+        emit<MODE>(io, sp, K, ATSAT_F_V, c, rhs_v);
+        emit<MODE>(io, sp, K, ATSAT_F_W, c, rhs_w);
+        if (MODE != MODE_STAGE) {
+            io.aux[0][c] = rhs_u + dpdr;
+            io.aux[1][c] = rhs_v + dpdthe * g.inv_rm;
+            io.aux[2][c] = rhs_w + dpdphi * g.inv_rmsinthe;
+        }
+    }
+
+    // flux-form factor of the species (RHS_Sat_Turb.cpp:979-1009), 0 unless ATSAT_SPECIES_DIVU
+    const double sd = K.divu_on ? K.species_divu * (du.dr + 2.0 * u * g.inv_rm + dv.dthe * g.inv_rm
+                                                    + v * g.cotanthe * g.inv_rm + dw.dphi * g.inv_rmsinthe)
+                                : 0.0;
+
+    // ---- temperature (RHS_Sat_Turb.cpp:368-386, 409, 435-437, 611-665, 752-759) ----
+    {
+        double dpstatdr = 0.0;
+        if (K.adiabatic) {
+            dpstatdr = (ldg(io.p_stat + c + plane) - ldg(io.p_stat + c - plane)) * K.inv_2dr * K.to_nd;
+            const double rho_l = ldg(io.rho_mix + c);
+            if (K.adiabatic_rho && rho_l > 0.0 && isfinite(rho_l)) dpstatdr *= K.r_mix / rho_l;
+        }
+        const double pressure_t = K.coeff_energy_p * (u * (dpdr + dpstatdr) + v * dpdthe * g.inv_rm
+                                                      + w * dpdphi * g.inv_rmsinthe);
+        D6 d;
+        derivs(io.in[ATSAT_F_T], c, plane, kp, dkw, dke, K, d);
+        const double transport_t = transport(u, v, w, d, g);
+        const double diffusion_t = diffusion(d, g);
+        double radiation_t = 0.0;
+        if (K.rad_on) {
+            const double rho_f = ldg(io.rho_mix + c);
+            const double rho = (rho_f > 0.0 && isfinite(rho_f)) ? rho_f : K.r_mix;
+            if (rho > 0.0) {
+                radiation_t = K.rad_coupling * ldg(io.q_rad + c) * K.rad_num / (rho * K.rad_den_c);
+                if (!isfinite(radiation_t)) radiation_t = 0.0;
+                else if (radiation_t > 0.5) radiation_t = 0.5;
+                else if (radiation_t < -0.5) radiation_t = -0.5;
+            }
+        }
+        double precip_t = 0.0;
+        if (K.precip_on) {
+            precip_t = K.precip_coupling * ldg(io.q_precip + c) * K.precip_num * K.precip_den;
+            if (!isfinite(precip_t)) precip_t = 0.0;
+            else if (precip_t > 0.5) precip_t = 0.5;
+            else if (precip_t < -0.5) precip_t = -0.5;
+        }
+        double rhs_t = pressure_t - transport_t + diffusion_t * K.inv_re_pr + diffusion_t * nue_t_s;
+        if (K.tmf_on) rhs_t = rhs_t - K.tmf_chem * ldg(io.thermalmassflux + c);
+        rhs_t = rhs_t + radiation_t + precip_t;
+        emit<MODE>(io, sp, K, ATSAT_F_T, c, rhs_t);
+    }
+
+    // ---- species (RHS_Sat_Turb.cpp:409-431, 457-491, 839-937) ----
+    const double pc = K.precip_coupling;
+#define ATSAT_SPECIES(FID, INV_SC_RE, EXTRA)                                                   \
+    {                                                                                          \
+        D6 d;                                                                                  \
+        derivs(io.in[FID], c, plane, kp, dkw, dke, K, d);                                      \
+        const double df = diffusion(d, g);                                                     \
+        double r = -transport(u, v, w, d, g) + df * (INV_SC_RE) + df * nue_t_s EXTRA;          \
+        if (K.divu_on) r -= sd * ldg(io.in[FID] + c);                                          \
+        emit<MODE>(io, sp, K, FID, c, r);                                                      \
+    }
+    ATSAT_SPECIES(ATSAT_F_H2O, K.inv_sc_re_h2o, +pc * ldg(io.s_precip[0] + c))
+    ATSAT_SPECIES(ATSAT_F_H2O_CLOUD, K.inv_sc_re_h2o, +pc * ldg(io.s_precip[1] + c))
+    ATSAT_SPECIES(ATSAT_F_H2O_ICE, K.inv_sc_re_h2o, +pc * ldg(io.s_precip[2] + c))
+    ATSAT_SPECIES(ATSAT_F_H2S, K.inv_sc_re_h2s, +K.chem * ldg(io.massflux_h2s + c))
+    ATSAT_SPECIES(ATSAT_F_NH3, K.inv_sc_re_nh3, +K.chem * ldg(io.massflux_nh3 + c) + pc * ldg(io.s_precip[3] + c))
+    ATSAT_SPECIES(ATSAT_F_NH3_CLOUD, K.inv_sc_re_nh3, +pc * ldg(io.s_precip[4] + c))
+    ATSAT_SPECIES(ATSAT_F_NH3_ICE, K.inv_sc_re_nh3, +pc * ldg(io.s_precip[5] + c))
+    ATSAT_SPECIES(ATSAT_F_CH4, K.inv_sc_re_ch4, +pc * ldg(io.s_precip[6] + c))
+    ATSAT_SPECIES(ATSAT_F_CH4_CLOUD, K.inv_sc_re_ch4, +pc * ldg(io.s_precip[7] + c))
+    ATSAT_SPECIES(ATSAT_F_CH4_ICE, K.inv_sc_re_ch4, +pc * ldg(io.s_precip[8] + c))
+#undef ATSAT_SPECIES
+    {   // nh4sh carries the flux-limiter correction (RHS_Sat_Turb.cpp:932-937)
+        D6 d;
+        derivs(io.in[ATSAT_F_NH4SH], c, plane, kp, dkw, dke, K, d);
+        const double df = diffusion(d, g);
+        double r = -transport(u, v, w, d, g) + ldg(io.fluxlim_nh4sh + c) + df * K.inv_sc_re_nh4sh + df * nue_t_s
+                 + K.chem * ldg(io.massflux_nh4sh + c);
+        if (K.divu_on) r -= sd * ldg(io.in[ATSAT_F_NH4SH] + c);
+        emit<MODE>(io, sp, K, ATSAT_F_NH4SH, c, r);
+    }
+
+    // ---- k-omega transport (RHS_Sat_Turb.cpp:511-538) ----
+    if (K.turb) {
+        {
+            D6 d;
+            derivs(io.in[ATSAT_F_TKE], c, plane, kp, dkw, dke, K, d);
+            const double r = -transport(u, v, w, d, g) + diffusion(d, g) * (K.inv_re + nue_c * K.inv_sig_k)
+                           + ldg(io.tke_source + c);
+            emit<MODE>(io, sp, K, ATSAT_F_TKE, c, r);
+        }
+        {
+            D6 d;
+            derivs(io.in[ATSAT_F_DIS], c, plane, kp, dkw, dke, K, d);
+            const double r = -transport(u, v, w, d, g) + diffusion(d, g) * (K.inv_re + nue_c * K.inv_sig_w)
+                           + ldg(io.dis_source + c);
+            emit<MODE>(io, sp, K, ATSAT_F_DIS, c, r);
+        }
+    } else if (MODE == MODE_RHS || (MODE == MODE_FINAL && sp.write_all_rhs)) {
+        io.rhs[ATSAT_F_TKE][c] = 0.0;
+        io.rhs[ATSAT_F_DIS][c] = 0.0;
+    }
+}
+
+// ---- computeBuoyancyRefLevel (RungeKutta_Sat_Turb.cpp:31-50): two-level deterministic reduction ----
+constexpr int LM_CHUNKS = 16;
+constexpr int LM_THREADS = 256;
+
+__global__ void __launch_bounds__(LM_THREADS) level_mean_partial_kernel(const KConst K, const double* __restrict__ t,
+                                                                         const double* __restrict__ ps,
+                                                                         const double* __restrict__ sin_j,
+                                                                         double* __restrict__ partial) {
+    const int i = blockIdx.x, chunk = blockIdx.y;
+    const int j0 = (int)((int64_t)K.jm * chunk / LM_CHUNKS), j1 = (int)((int64_t)K.jm * (chunk + 1) / LM_CHUNKS);
+    double sum = 0.0, wsum = 0.0;
+    const int n = (j1 - j0) * K.km;
+    for (int e = threadIdx.x; e < n; e += LM_THREADS) {
+        const int j = j0 + e / K.km, k = e % K.km;
+        const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
+        const double tc = __ldg(t + c);
+        if (!(tc > 0.0)) continue;
+        const double b = K.g * __ldg(ps + c) / (K.rR * tc * K.t_ref);
+        if (!isfinite(b)) continue;
+        const double wgt = __ldg(sin_j + j);
+        sum += wgt * b;
+        wsum += wgt;
+    }
+    __shared__ double s_sum[LM_THREADS / 32], s_w[LM_THREADS / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_down_sync(0xffffffffu, sum, o);
+        wsum += __shfl_down_sync(0xffffffffu, wsum, o);
+    }
+    if ((threadIdx.x & 31) == 0) { s_sum[threadIdx.x >> 5] = sum; s_w[threadIdx.x >> 5] = wsum; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < LM_THREADS / 32; q++) { a += s_sum[q]; b += s_w[q]; }
+        partial[((int64_t)i * LM_CHUNKS + chunk) * 2 + 0] = a;
+        partial[((int64_t)i * LM_CHUNKS + chunk) * 2 + 1] = b;
+    }
+}
+
+__global__ void level_mean_final_kernel(const KConst K, const double* __restrict__ partial, double* __restrict__ buoy) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= K.im) return;
+    double s = 0.0, w = 0.0;
+    for (int q = 0; q < LM_CHUNKS; q++) {
+        s += partial[((int64_t)i * LM_CHUNKS + q) * 2 + 0];
+        w += partial[((int64_t)i * LM_CHUNKS + q) * 2 + 1];
+    }
+    buoy[i] = (w > 0.0) ? s / w : 0.0;
+}
+
+// ---- computeMetricPressure (RungeKutta_Sat_Turb.cpp:60-108): one radial trapezoid scan per column ----
+__global__ void __launch_bounds__(256) metric_scan_kernel(const KConst K, const double* __restrict__ v,
+                                                          const double* __restrict__ w,
+                                                          const double* __restrict__ rm_tab,
+                                                          const double* __restrict__ cor_j,
+                                                          const double* __restrict__ p_baro,
+                                                          double* __restrict__ pm, double dr) {
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    if (k >= K.km || j >= K.jm) return;
+    const double cor = __ldg(cor_j + j);
+    double f_prev = 0.0, acc = 0.0;
+    for (int i = 0; i < K.im; i++) {
+        const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
+        const double vv = __ldg(v + c), ww = __ldg(w + c);
+        const double f = (vv * vv + ww * ww) / __ldg(rm_tab + i) + cor * ww;
+        if (i > 0) acc = acc + 0.5 * (f_prev + f) * dr;
+        f_prev = f;
+        pm[c] = p_baro ? acc + __ldg(p_baro + c) : acc;
+    }
+}
+
+// ---- computeMixtureDensity (Pressure_Sat.cpp:49-62) ----
+__global__ void __launch_bounds__(256) density_kernel(const KConst K, const double* __restrict__ t,
+                                                      const double* __restrict__ ps, double R_mix,
+                                                      double* __restrict__ rho) {
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= K.km || j >= K.jm) return;
+    const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
+    const double T = __ldg(t + c) * K.t_ref;
+    if (!(T > 0.0) || !(R_mix > 0.0)) { rho[c] = 0.0; return; }
+    const double r = (__ldg(ps + c) * 1.0e5) / (R_mix * T);
+    rho[c] = isfinite(r) ? r : 0.0;
+}
+
+}  // namespace
+
+cudaError_t launch_rk_stage_fp64(const KConst& kc, const StageIO<double>& io, const StageParams& sp, int mode,
+                                 cudaStream_t s) {
+    dim3 block(32, 8);
+    dim3 grid((kc.km + 31) / 32, (kc.jm + 7) / 8, kc.im);
+    if (mode == MODE_RHS) rk_stage_fp64_kernel<MODE_RHS><<<grid, block, 0, s>>>(kc, io, sp);
+    else if (mode == MODE_STAGE) rk_stage_fp64_kernel<MODE_STAGE><<<grid, block, 0, s>>>(kc, io, sp);
+    else rk_stage_fp64_kernel<MODE_FINAL><<<grid, block, 0, s>>>(kc, io, sp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_level_mean(const KConst& kc, const double* t, const double* p_stat, const double* sin_j,
+                              double* partial, double* buoy, cudaStream_t s) {
+    level_mean_partial_kernel<<<dim3(kc.im, LM_CHUNKS), LM_THREADS, 0, s>>>(kc, t, p_stat, sin_j, partial);
+    level_mean_final_kernel<<<(kc.im + 63) / 64, 64, 0, s>>>(kc, partial, buoy);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_metric_scan(const KConst& kc, const double* v, const double* w, const double* rm_tab,
+                               const double* cor_j, const double* p_baro, double* p_metric, cudaStream_t s) {
+    dim3 block(32, 8), grid((kc.km + 31) / 32, (kc.jm + 7) / 8);
+    metric_scan_kernel<<<grid, block, 0, s>>>(kc, v, w, rm_tab, cor_j, p_baro, p_metric, kc.dr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_density(const KConst& kc, const double* t, const double* p_stat, double R_mix, double* rho,
+                           cudaStream_t s) {
+    dim3 block(32, 8), grid((kc.km + 31) / 32, (kc.jm + 7) / 8, kc.im);
+    density_kernel<<<grid, block, 0, s>>>(kc, t, p_stat, R_mix, rho);
+    return cudaGetLastError();
+}
+
+}  // namespace atsat

@@ -1,0 +1,255 @@
+"""Host-side mirror of the ATSAT dynamical-core interface over the C ABI (include/atsat_dyn.h).
+
+`Dycore` stands for the part of cSaturnModel this library replaces. Its methods keep the reference's
+names and meaning:
+
+    RungeKuttaSat()                 cSaturnModel::RungeKuttaSat        RungeKutta_Sat_Turb.cpp:110-387
+    PressureSolver_run()            PressureSolver<cSaturnModel>::run  PressureSolver.h:145-766
+    computeMixtureDensity()         cSaturnModel::computeMixtureDensity Pressure_Sat.cpp:49-62
+    computeBuoyancyRefLevel()       RungeKutta_Sat_Turb.cpp:31-50
+    computeMetricPressure()         RungeKutta_Sat_Turb.cpp:60-108
+    RHSSat_pass()                   one RHSSat pass over the RK interior (:220-247)
+    prepareProjectionBoundaries()   Pressure_Sat.cpp:78-194
+    restoreVar()                    cSaturnModel::restoreVar(1.0)      cSaturnModel.cpp:1551-1600
+    boundary_conditions()           BC_Sat bcTheta, bcPhi, bcRadius    cSaturnModel.cpp:1091-1093
+
+Fields live on the device; `bind`/`upload`/`download` move them to and from host numpy arrays (the
+reference's Array storage). Every call raises DycoreError on a non-zero status: there is no CPU
+fallback, and a missing CUDA build is an ImportError-like failure at load time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi, fields as F
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libatsat_dyn.so")
+
+_lib = None
+
+
+class DycoreError(RuntimeError):
+    def __init__(self, status: int, what: str, msg: str):
+        super().__init__(f"{what}: status {status}: {msg}")
+        self.status = status
+
+
+def lib():
+    """The loaded CUDA library. Raises if it has not been built: the product has no CPU path."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libatsat_dyn.so is not built ({LIB_PATH}); run "
+                               "`python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        H = C.c_void_p
+        L.atsat_dyn_create.argtypes = [C.POINTER(abi.Grid), C.POINTER(abi.Params), C.POINTER(H)]
+        L.atsat_dyn_destroy.argtypes = [H]
+        L.atsat_dyn_destroy.restype = None
+        L.atsat_dyn_last_error.argtypes = [H]
+        L.atsat_dyn_last_error.restype = C.c_char_p
+        L.atsat_dyn_params_default.argtypes = [C.POINTER(abi.Params)]
+        L.atsat_dyn_params_from_env.argtypes = [C.POINTER(abi.Params)]
+        L.atsat_dyn_bind_host_rows.argtypes = [H, C.c_int32, C.POINTER(C.POINTER(C.c_double))]
+        L.atsat_dyn_bind_host_array.argtypes = [H, C.c_int32, C.POINTER(C.c_double)]
+        L.atsat_dyn_upload.argtypes = [H, C.POINTER(C.c_int32), C.c_int32]
+        L.atsat_dyn_download.argtypes = [H, C.POINTER(C.c_int32), C.c_int32]
+        L.atsat_dyn_set_tables.argtypes = [H, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.atsat_dyn_get_buoy_ref_level.argtypes = [H, C.POINTER(C.c_double)]
+        for n in ("mixture_density", "buoyancy_ref_level", "metric_pressure", "rhs", "rk4_step",
+                  "prepare_projection_boundaries", "restore_var", "sync", "boundary_conditions"):
+            fn = getattr(L, "atsat_dyn_" + n, None)
+            if fn is not None:
+                fn.argtypes = [H]
+        L.atsat_dyn_pressure.argtypes = [H, C.POINTER(abi.PStats)]
+        L.atsat_dyn_status.argtypes = [H, C.POINTER(abi.Diag)]
+        L.atsat_dyn_count_nonfinite.argtypes = [H, C.c_int32, C.POINTER(C.c_int64)]
+        L.atsat_dyn_profile.argtypes = [H, C.c_int32]
+        L.atsat_dyn_profile_reset.argtypes = [H]
+        L.atsat_dyn_profile_read.argtypes = [H, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_double)]
+        L.atsat_dyn_device_field.argtypes = [H, C.c_int32, C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_int64)]
+        L.atsat_dyn_host_alloc.argtypes = [C.c_size_t]
+        L.atsat_dyn_host_alloc.restype = C.c_void_p
+        L.atsat_dyn_host_free.argtypes = [C.c_void_p]
+        L.atsat_dyn_host_free.restype = None
+        L.atsat_dyn_set_write_all_rhs.argtypes = [H, C.c_int32]
+        _lib = L
+    return _lib
+
+
+def params_from_env(base: dict | None = None) -> dict:
+    """The reference's constants (`base`, default: its committed configuration) with every knob
+    resolved from the ATSAT_* environment as the reference resolves it."""
+    p = abi.make_params(base or abi.default_params())
+    rc = lib().atsat_dyn_params_from_env(C.byref(p))
+    if rc != 0:
+        raise DycoreError(rc, "atsat_dyn_params_from_env", "an ATSAT_* knob is set to a value with no device path")
+    out = {n: getattr(p, n) for n, _ in F.PARAM_DOUBLES}
+    out.update({n: getattr(p, n) for n, _ in F.PARAM_INTS})
+    return out
+
+
+class PinnedArray:
+    """A numpy array over page-locked host memory (cudaHostAlloc), for fast host<->device copies."""
+
+    def __init__(self, shape, dtype=np.float64):
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self._p = lib().atsat_dyn_host_alloc(max(n, 8))
+        if not self._p:
+            raise MemoryError("cudaHostAlloc failed")
+        buf = (C.c_char * n).from_address(self._p)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def free(self):
+        if self._p:
+            self.array = None
+            lib().atsat_dyn_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Dycore:
+    def __init__(self, grid, params: dict):
+        self.grid = grid
+        self._gh = abi.GridHold(grid)
+        self._p = abi.make_params(params)
+        self.params = dict(params)
+        self.h = C.c_void_p()
+        self._bound = {}
+        rc = lib().atsat_dyn_create(C.byref(self._gh.s), C.byref(self._p), C.byref(self.h))
+        if rc != 0:
+            msg = lib().atsat_dyn_last_error(self.h).decode() if self.h else ""
+            self.close()
+            raise DycoreError(rc, "atsat_dyn_create", msg)
+
+    # ---- plumbing ----
+    def _ck(self, rc, what):
+        if rc != 0:
+            raise DycoreError(rc, what, lib().atsat_dyn_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            lib().atsat_dyn_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def bind(self, fid: int, arr: np.ndarray):
+        assert arr.dtype == np.float64 and arr.flags.c_contiguous and arr.shape == self.grid.shape
+        self._bound[fid] = arr
+        self._ck(lib().atsat_dyn_bind_host_array(self.h, fid, abi.dptr(arr)), "bind_host_array")
+
+    def bind_rows(self, fid: int, rows: list):
+        """Bind the reference's ragged storage: rows[i*jm + j] is a float64 array of km values."""
+        n = self.grid.im * self.grid.jm
+        assert len(rows) == n
+        ptrs = (C.POINTER(C.c_double) * n)(*[abi.dptr(r) for r in rows])
+        self._bound[fid] = (rows, ptrs)
+        self._ck(lib().atsat_dyn_bind_host_rows(self.h, fid, ptrs), "bind_host_rows")
+
+    def bind_state(self, state, fids=None):
+        for fid in (fids if fids is not None else range(F.NFIELDS)):
+            if fid not in state.arrays:
+                state.arrays[fid] = np.zeros(self.grid.shape)
+            self.bind(fid, state.arrays[fid])
+
+    def upload(self, fids):
+        ids = (C.c_int32 * len(fids))(*fids)
+        self._ck(lib().atsat_dyn_upload(self.h, ids, len(fids)), "upload")
+
+    def download(self, fids):
+        ids = (C.c_int32 * len(fids))(*fids)
+        self._ck(lib().atsat_dyn_download(self.h, ids, len(fids)), "download")
+
+    def set_tables(self, cell_vbar0=None, cell_ubar0=None, p_baro=None):
+        self._tables = [None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+                        for a in (cell_vbar0, cell_ubar0, p_baro)]
+        self._ck(lib().atsat_dyn_set_tables(self.h, *[abi.dptr(a) for a in self._tables]), "set_tables")
+
+    def load_state(self, state):
+        """Bind every field of a synth.State, upload it and set its tables."""
+        self.bind_state(state)
+        self.upload(list(range(F.NFIELDS)))
+        self.set_tables(state.cell_vbar0, state.cell_ubar0, state.p_baro)
+
+    def buoy_ref_level(self) -> np.ndarray:
+        out = np.zeros(self.grid.im)
+        self._ck(lib().atsat_dyn_get_buoy_ref_level(self.h, abi.dptr(out)), "get_buoy_ref_level")
+        return out
+
+    def set_write_all_rhs(self, on: bool):
+        self._ck(lib().atsat_dyn_set_write_all_rhs(self.h, int(bool(on))), "set_write_all_rhs")
+
+    # ---- the reference's entry points ----
+    def computeMixtureDensity(self):
+        self._ck(lib().atsat_dyn_mixture_density(self.h), "mixture_density")
+
+    def computeBuoyancyRefLevel(self):
+        self._ck(lib().atsat_dyn_buoyancy_ref_level(self.h), "buoyancy_ref_level")
+
+    def computeMetricPressure(self):
+        self._ck(lib().atsat_dyn_metric_pressure(self.h), "metric_pressure")
+
+    def RHSSat_pass(self):
+        self._ck(lib().atsat_dyn_rhs(self.h), "rhs")
+
+    def RungeKuttaSat(self):
+        self._ck(lib().atsat_dyn_rk4_step(self.h), "rk4_step")
+
+    def prepareProjectionBoundaries(self):
+        self._ck(lib().atsat_dyn_prepare_projection_boundaries(self.h), "prepare_projection_boundaries")
+
+    def PressureSolver_run(self) -> abi.PStats:
+        st = abi.PStats()
+        self._ck(lib().atsat_dyn_pressure(self.h, C.byref(st)), "pressure")
+        return st
+
+    def restoreVar(self):
+        self._ck(lib().atsat_dyn_restore_var(self.h), "restore_var")
+
+    def boundary_conditions(self):
+        self._ck(lib().atsat_dyn_boundary_conditions(self.h), "boundary_conditions")
+
+    # ---- diagnostics ----
+    def sync(self):
+        self._ck(lib().atsat_dyn_sync(self.h), "sync")
+
+    def launches(self) -> int:
+        d = abi.Diag()
+        self._ck(lib().atsat_dyn_status(self.h, C.byref(d)), "status")
+        return int(d.launches)
+
+    def count_nonfinite(self, fid: int) -> int:
+        n = C.c_int64()
+        self._ck(lib().atsat_dyn_count_nonfinite(self.h, fid, C.byref(n)), "count_nonfinite")
+        return int(n.value)
+
+    def profile(self, on: bool):
+        self._ck(lib().atsat_dyn_profile(self.h, int(on)), "profile")
+
+    def profile_reset(self):
+        self._ck(lib().atsat_dyn_profile_reset(self.h), "profile_reset")
+
+    def profile_read(self, kclass: int):
+        n, ms = C.c_int64(), C.c_double()
+        self._ck(lib().atsat_dyn_profile_read(self.h, kclass, C.byref(n), C.byref(ms)), "profile_read")
+        return int(n.value), float(ms.value)

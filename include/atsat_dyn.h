@@ -261,6 +261,10 @@ int atsat_dyn_profile_read(atsat_dyn_t h, int32_t kclass, int64_t* launches, dou
 /* Device-side pointer and row pitch (in elements) of a field's device copy. */
 int atsat_dyn_device_field(atsat_dyn_t h, int32_t field, double** dptr, int64_t* pitch);
 
+/* Write every rhs_* at the last RK stage (RHSSat writes all of them at every stage); off by default
+ * because only rhs_u/v/w are read outside the step (the projection source and the restart file). */
+int atsat_dyn_set_write_all_rhs(atsat_dyn_t h, int32_t on);
+
 /* Pinned host memory for bound arrays (cudaHostAlloc / cudaFreeHost). */
 void* atsat_dyn_host_alloc(size_t bytes);
 void  atsat_dyn_host_free(void* p);

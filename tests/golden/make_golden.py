@@ -1,0 +1,85 @@
+"""Generate the golden fixtures of the dynamical core from the REFERENCE itself.
+
+Each case runs the reference's own code (oracle/_ref/ref_harness, built from the reference sources
+by oracle/build_ref.py) on a seeded synthetic state at the reference's compile-time grid
+41x181x361, and stores per output field:
+  - values at 512 seeded sample cells (flat indices),
+  - the whole-field sum, sum of |x| and max |x|,
+plus the sum of every input field, so a drifting generator is detected before any comparison.
+
+Run here (where the reference tree exists): python tests/golden/make_golden.py
+The fixtures are small .npz files; the tests regenerate the inputs with atsat_gb300.synth.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from atsat_gb300 import abi, fields as F, synth  # noqa: E402
+
+NSAMPLE = 512
+
+# name: (op, nsteps, seed, exercise, params override)
+CASES = {
+    "rhs_s1": ("rhs", 1, 1, True, {}),
+    "rk_s1": ("rk", 1, 1, True, {}),
+    "pressure_s1": ("pressure", 1, 1, True, {}),
+    "density_s1": ("density", 1, 1, True, {}),
+    "steps4_s2": ("steps", 4, 2, True, {}),
+    "rk_plain_s0": ("rk", 1, 0, False, {}),
+}
+
+OUTPUTS = {
+    "rhs": F.RHS_FIELDS + F.AUX_FIELDS + [F.P_METRIC],
+    "rk": F.PROG + F.RHS_FIELDS + F.AUX_FIELDS + [F.P_METRIC],
+    "pressure": [F.P_DYN] + F.AUX_FIELDS + [F.RHS_U, F.RHS_V, F.RHS_W],
+    "density": [F.RHO_MIX],
+    "steps": F.PROG + F.PROG_N + [F.P_DYN, F.P_DYNN, F.RHO_MIX, F.P_METRIC, F.NUE] + F.AUX_FIELDS
+             + [F.RHS_U, F.RHS_V, F.RHS_W],
+}
+
+
+def make_state(name):
+    op, nsteps, seed, exercise, over = CASES[name]
+    g = synth.make_grid()
+    P = abi.default_params(**over)
+    return g, P, synth.saturn_state(g, P, seed=seed, exercise=exercise)
+
+
+def sample_index(name, n_cells):
+    rng = np.random.default_rng(abs(hash(name)) % (2 ** 32) if False else sum(map(ord, name)) * 7919)
+    return np.sort(rng.choice(n_cells, size=NSAMPLE, replace=False))
+
+
+def input_sums(st):
+    return np.array([float(np.sum(st.arrays[f])) for f in range(F.NFIELDS)])
+
+
+def main():
+    from oracle import refrun
+    if not refrun.available():
+        sys.exit("the reference harness is not built: python oracle/build_ref.py")
+    for name, (op, nsteps, seed, exercise, over) in CASES.items():
+        g, P, st = make_state(name)
+        out = refrun.run(st, op, nsteps=nsteps)
+        idx = sample_index(name, g.cells)
+        rec = {"input_sums": input_sums(st), "index": idx}
+        for fid in OUTPUTS[op]:
+            a = out[fid].ravel()
+            rec[f"s_{fid}"] = a[idx]
+            rec[f"sum_{fid}"] = np.array([np.sum(a), np.sum(np.abs(a)), np.max(np.abs(a))])
+        if "buoy_ref_level" in out and op in ("rhs", "rk"):
+            rec["buoy_ref_level"] = out["buoy_ref_level"]
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **rec)
+        print(name, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()

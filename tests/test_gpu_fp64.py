@@ -1,0 +1,182 @@
+"""FP64 drop-in parity: the CUDA path through the C ABI against the oracle, on the same seeded inputs.
+
+The bar (TOL_FP64) is 1e-10 of max|oracle| per field after one call; the oracle itself is pinned
+bit for bit to the reference by test_oracle_golden.py.
+"""
+import numpy as np
+import pytest
+
+from atsat_gb300 import fields as F
+from oracle import oracle
+
+from helpers import TOL_FP64, case, compare
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(9, 13, 17), (21, 91, 181)]
+ALL = list(range(F.NFIELDS))
+
+
+def run_gpu(op, g, P, st):
+    from atsat_gb300 import dyn
+    s = st.copy()
+    with dyn.Dycore(g, P) as d:
+        d.load_state(s)
+        d.set_write_all_rhs(True)
+        if op == "rhs":
+            d.computeBuoyancyRefLevel()
+            if P["metric_split"]:
+                d.computeMetricPressure()
+            d.RHSSat_pass()
+        elif op == "rk":
+            d.RungeKuttaSat()
+        elif op == "pressure":
+            d.PressureSolver_run()
+        elif op == "density":
+            d.computeMixtureDensity()
+        elif op == "prep":
+            d.prepareProjectionBoundaries()
+        d.download(ALL)
+        buoy = d.buoy_ref_level()
+    return s, buoy
+
+
+def run_oracle(op, P, st):
+    s = st.copy()
+    buoy = None
+    if op == "rhs":
+        buoy = oracle.rhs(s, P)
+    elif op == "rk":
+        buoy = oracle.rk4_step(s, P)
+    elif op == "pressure":
+        oracle.pressure(s, P)
+    elif op == "density":
+        oracle.mixture_density(s, P)
+    elif op == "prep":
+        from oracle.oracle import _Call, lib, _check
+        import ctypes as C
+        c = _Call(s, P)
+        _check(lib().orc_prepare_projection_boundaries(C.byref(c.gh.s), C.byref(c.p), c.ptrs), "prep")
+    return s, buoy
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("op", ["rhs", "rk", "pressure", "density", "prep"])
+def test_parity_default_knobs(shape, op):
+    g, P, st = case(shape, seed=5)
+    got, gb = run_gpu(op, g, P, st)
+    ref, rb = run_oracle(op, P, st)
+    compare(got.arrays, ref.arrays, ALL, TOL_FP64, f"{op} {shape}")
+    if rb is not None:
+        assert np.max(np.abs(gb - rb)) <= TOL_FP64 * np.max(np.abs(rb))
+
+
+RK_VARIANTS = [
+    dict(metric_split=0, coriolis_split=0),
+    dict(coriolis_split=0),
+    dict(turb_active=0),
+    dict(nd_buoy=1, nd_cent=1),
+    dict(nd_cor=0),
+    dict(species_divu=0.5),
+    dict(thermal_massflux=1.0),
+    dict(rad_coupling=1.0),
+    dict(buoy_legacy=1),
+    dict(adiabatic=0),
+    dict(adiabatic_rho=0),
+    dict(cell_hold=0),
+    dict(precip_coupling=0.0),
+    dict(turb_coupling=0.0),
+    dict(re=1000.0, pr=0.69),
+    dict(sinthe_min=0.3),
+]
+
+
+@pytest.mark.parametrize("over", RK_VARIANTS, ids=lambda d: ",".join(f"{k}={v}" for k, v in d.items()))
+def test_rk4_knob_variants(over):
+    g, P, st = case((9, 13, 17), seed=7, **over)
+    got, _ = run_gpu("rk", g, P, st)
+    ref, _ = run_oracle("rk", P, st)
+    compare(got.arrays, ref.arrays, ALL, TOL_FP64, f"rk {over}")
+
+
+P_VARIANTS = [
+    dict(press_incr=0),
+    dict(press_src=0),
+    dict(rigid_lid=0),
+    dict(press_sweeps=4),
+    dict(pdyn_cap=1e-6),
+    dict(press_incr=0, rigid_lid=0, press_sweeps=3),
+]
+
+
+@pytest.mark.parametrize("over", P_VARIANTS, ids=lambda d: ",".join(f"{k}={v}" for k, v in d.items()))
+def test_pressure_knob_variants(over):
+    g, P, st = case((21, 91, 181), seed=9, **over)
+    got, _ = run_gpu("pressure", g, P, st)
+    ref, _ = run_oracle("pressure", P, st)
+    compare(got.arrays, ref.arrays, ALL, TOL_FP64, f"pressure {over}")
+
+
+def test_pressure_clamp_count():
+    from atsat_gb300 import dyn
+    g, P, st = case((9, 13, 17), seed=9, pdyn_cap=1e-9)
+    with dyn.Dycore(g, P) as d:
+        d.load_state(st.copy())
+        stats = d.PressureSolver_run()
+    assert stats.sweeps == 1 and stats.src_clamped > 0
+
+
+def test_dropin_sequence_host_bcs():
+    """Four iterations of the dycore part of cSaturnModel::Run with the device doing density,
+    pressure, RK4 and restoreVar, and the host doing the boundary conditions between them -- the
+    drop-in arrangement, where the driver's own BC_Sat code stays on the CPU."""
+    from atsat_gb300 import dyn
+    g, P, st = case((21, 91, 181), seed=13)
+    ref = st.copy()
+    oracle.steps(ref, P, 4)
+    s = st.copy()
+    with dyn.Dycore(g, P) as d:
+        d.load_state(s)
+        for it in range(1, 5):
+            if it % 2 == 0:
+                d.computeMixtureDensity()
+                d.PressureSolver_run()
+            d.RungeKuttaSat()
+            d.download(ALL)
+            oracle.boundary_conditions(s, P)          # the driver's host-side BC_Sat
+            d.upload(ALL)
+            d.restoreVar()
+        d.download(ALL)
+    compare(s.arrays, ref.arrays, F.PROG + F.PROG_N + [F.P_DYN, F.RHO_MIX, F.P_METRIC] + F.AUX_FIELDS,
+            TOL_FP64, "4 iterations")
+
+
+def test_ragged_rows_binding():
+    """The reference's own storage (one row of km doubles per (i, j)) through bind_host_rows."""
+    from atsat_gb300 import dyn
+    g, P, st = case((9, 13, 17), seed=17)
+    ref, _ = run_oracle("rk", P, st)
+    s = st.copy()
+    with dyn.Dycore(g, P) as d:
+        rows = {}
+        for fid in range(F.NFIELDS):
+            a = s.arrays[fid]
+            rows[fid] = [np.array(a[i, j], copy=True) for i in range(g.im) for j in range(g.jm)]
+            d.bind_rows(fid, rows[fid])
+        d.upload(ALL)
+        d.set_tables(s.cell_vbar0, s.cell_ubar0)
+        d.RungeKuttaSat()
+        d.download(ALL)
+    got = {fid: np.stack(rows[fid]).reshape(g.shape) for fid in range(F.NFIELDS)}
+    compare(got, ref.arrays, F.PROG + [F.RHS_U, F.RHS_V, F.RHS_W, F.AUX_U], TOL_FP64, "rows")
+
+
+def test_nonfinite_census():
+    from atsat_gb300 import dyn
+    g, P, st = case((9, 13, 17), seed=19)
+    st.arrays[F.T][3, 4, 5] = np.nan
+    st.arrays[F.T][2, 6, 1] = np.inf
+    with dyn.Dycore(g, P) as d:
+        d.load_state(st)
+        assert d.count_nonfinite(F.T) == 2
+        assert d.count_nonfinite(F.U) == 0
