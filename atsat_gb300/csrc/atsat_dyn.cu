@@ -67,6 +67,7 @@ struct atsat_dyn {
     double prof_ms[ATSAT_K_NCLASS] = {};
 
     int write_all_rhs = 0;
+    cudaEvent_t timer[2] = {nullptr, nullptr};
     std::string err;
 };
 
@@ -450,6 +451,22 @@ int enqueue_pressure(atsat_dyn* h, int sweeps) {
     return ATSAT_DYN_OK;
 }
 
+int enqueue_restore(atsat_dyn* h) {
+    Timed t(h, ATSAT_K_GLUE);
+    const size_t bytes = (size_t)h->kc.fsz * 8;
+    for (int q = 0; q < NPROG; q++)
+        CK(h, cudaMemcpyAsync(h->f[ATSAT_F_N_BASE + q], h->f[q], bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->f[ATSAT_F_P_DYNN], h->f[ATSAT_F_P_DYN], bytes, cudaMemcpyDeviceToDevice, h->stream));
+    return ATSAT_DYN_OK;
+}
+
+int enqueue_bc(atsat_dyn* h) {
+    Timed t(h, ATSAT_K_GLUE);
+    CK(h, launch_boundary_conditions(h->kc, h->p, h->f, h->stream));
+    h->launches += 3;
+    return ATSAT_DYN_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -624,6 +641,7 @@ void atsat_dyn_destroy(atsat_dyn_t h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (auto& e : h->pend) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
     for (auto e : h->pool) cudaEventDestroy(e);
+    for (auto e : h->timer) if (e) cudaEventDestroy(e);
     if (h->slab) cudaFree(h->slab);
     if (h->pinned) cudaFreeHost(h->pinned);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -778,12 +796,33 @@ int atsat_dyn_pressure(atsat_dyn_t h, atsat_dyn_pstats* out) {
 
 int atsat_dyn_restore_var(atsat_dyn_t h) {
     ENTRY(h);
-    {
-        Timed t(h, ATSAT_K_GLUE);
-        const size_t bytes = (size_t)h->kc.fsz * 8;
-        for (int q = 0; q < NPROG; q++)
-            CK(h, cudaMemcpyAsync(h->f[ATSAT_F_N_BASE + q], h->f[q], bytes, cudaMemcpyDeviceToDevice, h->stream));
-        CK(h, cudaMemcpyAsync(h->f[ATSAT_F_P_DYNN], h->f[ATSAT_F_P_DYN], bytes, cudaMemcpyDeviceToDevice, h->stream));
+    int rc = enqueue_restore(h);
+    return rc ? rc : finish(h);
+}
+
+int atsat_dyn_boundary_conditions(atsat_dyn_t h) {
+    ENTRY(h);
+    int rc = enqueue_bc(h);
+    return rc ? rc : finish(h);
+}
+
+int atsat_dyn_iterate(atsat_dyn_t h, int32_t iter0, int32_t n) {
+    ENTRY(h);
+    if (n < 0) return fail(h, ATSAT_DYN_E_INVALID, "negative iteration count");
+    for (int32_t it = iter0; it < iter0 + n; it++) {
+        int rc;
+        if (it % 2 == 0) {
+            {
+                Timed t(h, ATSAT_K_GLUE);
+                CK(h, launch_density(h->kc, h->f[ATSAT_F_T], h->f[ATSAT_F_P_STAT], h->p.R_mix, h->f[ATSAT_F_RHO_MIX],
+                                     h->stream));
+                h->launches += 1;
+            }
+            if ((rc = enqueue_pressure(h, h->p.press_sweeps > 0 ? h->p.press_sweeps : 1))) return rc;
+        }
+        if ((rc = enqueue_rk4(h))) return rc;
+        if ((rc = enqueue_bc(h))) return rc;
+        if ((rc = enqueue_restore(h))) return rc;
     }
     return finish(h);
 }
@@ -833,6 +872,27 @@ int atsat_dyn_profile_read(atsat_dyn_t h, int32_t kclass, int64_t* launches, dou
     if (launches) *launches = h->prof_n[kclass];
     if (ms) *ms = h->prof_ms[kclass];
     return rc;
+}
+
+int atsat_dyn_timer_start(atsat_dyn_t h) {
+    ENTRY(h);
+    if (!h->timer[0]) {
+        CK(h, cudaEventCreate(&h->timer[0]));
+        CK(h, cudaEventCreate(&h->timer[1]));
+    }
+    CK(h, cudaEventRecord(h->timer[0], h->stream));
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_timer_stop(atsat_dyn_t h, double* ms) {
+    ENTRY(h);
+    if (!h->timer[0] || !ms) return fail(h, ATSAT_DYN_E_INVALID, "timer_stop without timer_start");
+    CK(h, cudaEventRecord(h->timer[1], h->stream));
+    CK(h, cudaEventSynchronize(h->timer[1]));
+    float f = 0.f;
+    CK(h, cudaEventElapsedTime(&f, h->timer[0], h->timer[1]));
+    *ms = f;
+    return ATSAT_DYN_OK;
 }
 
 int atsat_dyn_device_field(atsat_dyn_t h, int32_t field, double** dptr, int64_t* pitch) {

@@ -66,6 +66,7 @@ def lib():
             if fn is not None:
                 fn.argtypes = [H]
         L.atsat_dyn_pressure.argtypes = [H, C.POINTER(abi.PStats)]
+        L.atsat_dyn_iterate.argtypes = [H, C.c_int32, C.c_int32]
         L.atsat_dyn_status.argtypes = [H, C.POINTER(abi.Diag)]
         L.atsat_dyn_count_nonfinite.argtypes = [H, C.c_int32, C.POINTER(C.c_int64)]
         L.atsat_dyn_profile.argtypes = [H, C.c_int32]
@@ -77,6 +78,8 @@ def lib():
         L.atsat_dyn_host_free.argtypes = [C.c_void_p]
         L.atsat_dyn_host_free.restype = None
         L.atsat_dyn_set_write_all_rhs.argtypes = [H, C.c_int32]
+        L.atsat_dyn_timer_start.argtypes = [H]
+        L.atsat_dyn_timer_stop.argtypes = [H, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -229,6 +232,10 @@ class Dycore:
     def boundary_conditions(self):
         self._ck(lib().atsat_dyn_boundary_conditions(self.h), "boundary_conditions")
 
+    def iterate(self, iter0: int, n: int):
+        """n iterations of the dycore part of cSaturnModel::Run, resident on the device."""
+        self._ck(lib().atsat_dyn_iterate(self.h, iter0, n), "iterate")
+
     # ---- diagnostics ----
     def sync(self):
         self._ck(lib().atsat_dyn_sync(self.h), "sync")
@@ -242,6 +249,14 @@ class Dycore:
         n = C.c_int64()
         self._ck(lib().atsat_dyn_count_nonfinite(self.h, fid, C.byref(n)), "count_nonfinite")
         return int(n.value)
+
+    def timer_start(self):
+        self._ck(lib().atsat_dyn_timer_start(self.h), "timer_start")
+
+    def timer_stop(self) -> float:
+        ms = C.c_double()
+        self._ck(lib().atsat_dyn_timer_stop(self.h, C.byref(ms)), "timer_stop")
+        return float(ms.value)
 
     def profile(self, on: bool):
         self._ck(lib().atsat_dyn_profile(self.h, int(on)), "profile")

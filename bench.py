@@ -1,0 +1,318 @@
+#!/usr/bin/env python3
+"""Throughput of the ATSAT dynamical core on GB300, in cell-steps per second.
+
+One step is one iteration of the dycore part of cSaturnModel::Run on the reference's default grid
+41x181x361 (planet/cSaturnModel.cpp:864-1111): on even iterations computeMixtureDensity and the
+red-black pressure call (PressureSolver<cSaturnModel>::run), then RungeKuttaSat (four RHSSat stages
+and the RK4 update), the boundary conditions and restoreVar -- all resident on the device
+(atsat_dyn_iterate). Cells per step = im * jm * km.
+
+  value   device-resident throughput, the state already in HBM (2.6 GB, far larger than L2, so no
+          L2 flush is needed between iterations)
+  e2e     the same metric through the C ABI with HOST buffers, as a drop-in driver calls it: every
+          step uploads the step's inputs from pinned host memory, runs the pressure call (even
+          steps) and the RK4 step, and downloads what the host reads back
+  roofline  the fused RK stage kernel (the dominant kernel): algorithmic bytes per launch over its
+          mean launch time from CUDA events in the timed region, against the measured HBM copy peak
+  cpu_baseline  this repository's C restatement of the reference's OpenMP path, timed on the host
+          cores on a bounded sample of the same workload (rank 0, N = 1)
+
+--impl reference times the reference's CPU path (the C restatement with all host threads; the
+reference's own build cannot travel to this machine) on the same workload and metric.
+Multi-GPU runs are independent replicas (one per rank, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-steps/s, 1 GB300: mixed-prec vs FP64 GPU at ≤1e-6 rel err; %HBM peak"
+UNIT = "Mcell-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--shape", default="41,181,361")
+    ap.add_argument("--e2e-steps", type=int, default=6)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    a = ap.parse_args()
+    a.warmup = max(a.warmup, 3)
+    a.shape = tuple(int(x) for x in a.shape.split(","))
+    return a
+
+
+def dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+        if vis:
+            ids = vis.split(",")
+            os.environ["CUDA_VISIBLE_DEVICES"] = ids[local % len(ids)]
+        else:
+            os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        import torch.distributed as td
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        td.init_process_group("gloo", rank=rank, world_size=world)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as td
+        td.barrier()
+
+
+def reduce_max(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([x], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.p = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.t.join(timeout=2)
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9 or (vis.isdigit() and f[0] != vis):
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_per_launch(kernel: str):
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def interior_rk(g):
+    return (g.im - 2) * (g.jm - 4) * (g.km - 1)
+
+
+# FP64 words moved per interior-RK cell by the four fused stage launches (the layout shipped here):
+# stage 0 reads Y_s, y_n and the 21 auxiliary inputs (3 stencil, 18 point) and writes acc and Y_1;
+# stages 1-2 also read acc; stage 3 writes y_{n+1}, rhs_u/v/w and aux_u/v/w instead of acc and Y.
+RK_WORDS_PER_CELL = (17 + 17 + 21 + 34) + 2 * (17 + 21 + 17 + 17 + 34) + (17 + 21 + 17 + 17 + 23)
+
+
+def cpu_baseline(g, P, seed, target_s=3.0):
+    """The C restatement of the reference's OpenMP path on this host, all cores, bounded sample."""
+    from atsat_gb300 import synth
+    from oracle import oracle
+    st = synth.saturn_state(g, P, seed=seed)
+    oracle.lib()
+    t0 = time.perf_counter()
+    n = 0
+    while n < 2 or (time.perf_counter() - t0 < target_s and n < 8):
+        oracle.steps(st, P, 1, iter0=1 + n)
+        n += 1
+    dt = time.perf_counter() - t0
+    return {"value": n * g.cells / dt / 1e6, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{n} dycore iterations at {g.im}x{g.jm}x{g.km} (pressure on the even ones), "
+                      f"{dt:.2f} s wall on {os.cpu_count()} OpenMP threads"}
+
+
+def run_reference(a, rank, world):
+    if rank != 0:
+        return None
+    from atsat_gb300 import abi, synth
+    from oracle import oracle
+    g = synth.make_grid(*a.shape)
+    P = abi.default_params()
+    st = synth.saturn_state(g, P, seed=0)
+    oracle.lib()
+    for it in range(1, a.warmup + 1):
+        oracle.steps(st, P, 1, iter0=it)
+    t0 = time.perf_counter()
+    oracle.steps(st, P, a.steps, iter0=a.warmup + 1)
+    dt = time.perf_counter() - t0
+    v = a.steps * g.cells / dt / 1e6
+    return {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": dt * 1e3 / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config(g, "fp64"),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"{a.steps} full dycore iterations after {a.warmup} warm-up"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def config(g, precision):
+    return {"workload": f"ATSAT dycore iteration (RK4 step + red-black pressure call on even steps + "
+                        f"boundary conditions + restoreVar) at {g.im}x{g.jm}x{g.km}",
+            "grid": f"{g.im}x{g.jm}x{g.km}", "cells_per_step": g.cells, "interior_rk_cells": interior_rk(g),
+            "precision": precision, "press_sweeps": 1, "l2": "state of 2.6 GB resident, larger than L2: no flush",
+            "parallelism": "replicas"}
+
+
+def run_ours(a, rank, world):
+    from atsat_gb300 import abi, dyn, fields as F, synth
+    g = synth.make_grid(*a.shape)
+    P = abi.default_params()
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        cpu = cpu_baseline(g, P, seed=0)          # before the first CUDA call
+    st = synth.saturn_state(g, P, seed=rank)
+
+    # pinned host copies of every field, bound to the handle (the e2e leg copies from them)
+    pinned = {}
+    d = dyn.Dycore(g, P)
+    for fid in range(F.NFIELDS):
+        pa = dyn.PinnedArray(g.shape)
+        src = st.arrays.get(fid)
+        pa.array[...] = 0.0 if src is None else src
+        pinned[fid] = pa
+        d.bind(fid, pa.array)
+    d.upload(list(range(F.NFIELDS)))
+    d.set_tables(st.cell_vbar0, st.cell_ubar0, st.p_baro)
+
+    # ---- device-resident throughput ----
+    d.iterate(1, a.warmup)
+    it0 = a.warmup + 1
+    d.profile(True)
+    d.profile_reset()
+    l0 = d.launches()
+    clocks = Clocks()
+    clocks.start()
+    barrier(world)
+    d.timer_start()
+    d.iterate(it0, a.steps)
+    ms = d.timer_stop()
+    barrier(world)
+    clk = clocks.stop()
+    launches = d.launches() - l0
+    n_rk, ms_rk = d.profile_read(abi.K_RK_STAGE)
+    kern = {abi.K_NAMES[c]: dict(zip(("launches", "ms"), d.profile_read(c))) for c in range(len(abi.K_NAMES))}
+    d.profile(False)
+    ms = reduce_max(world, ms)
+    value = world * a.steps * g.cells / (ms / 1e3) / 1e6
+
+    # ---- end to end through the C ABI with host buffers ----
+    ins = F.STEP_INPUTS
+    outs = F.STEP_OUTPUTS
+    h2d = d2h = 0
+    it = it0 + a.steps
+    barrier(world)
+    t0 = time.perf_counter()
+    for s in range(a.e2e_steps):
+        d.upload(ins)
+        h2d += len(ins) * g.cells * 8
+        if it % 2 == 0:
+            d.computeMixtureDensity()
+            d.PressureSolver_run()
+            d.download([F.P_DYN])
+            d2h += g.cells * 8
+        d.RungeKuttaSat()
+        d.download(outs)
+        d2h += len(outs) * g.cells * 8
+        it += 1
+    e2e_s = reduce_max(world, time.perf_counter() - t0)
+    e2e = {"value": world * a.e2e_steps * g.cells / e2e_s / 1e6, "unit": UNIT,
+           "h2d_bytes_per_step": h2d // a.e2e_steps, "d2h_bytes_per_step": d2h // a.e2e_steps,
+           "steps": a.e2e_steps, "ms_per_step": e2e_s * 1e3 / a.e2e_steps}
+
+    peak, peak_kind = peaks()
+    bytes_per_launch = RK_WORDS_PER_CELL / 4 * 8 * interior_rk(g)
+    avg_ms = ms_rk / max(n_rk, 1)
+    achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9
+    roof = {"kernel": "rk_stage_fp64 (fused RHSSat + RK4 stage)", "bound": "hbm", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+            "traffic": traffic_per_launch("rk_stage_fp64"), "algorithmic_bytes_per_launch": bytes_per_launch,
+            "launches": n_rk, "mean_launch_ms": avg_ms,
+            "note": "FP64 path: bound by the FP64 pipe, not HBM (see DESIGN.md)"}
+    d.close()
+    for pa in pinned.values():
+        pa.free()
+    if rank != 0:
+        return None
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+           "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(g, "fp64"),
+           "e2e": e2e, "roofline": roof, "gpu_launches": launches, "clocks": clk, "kernels_ms": kern}
+    if cpu:
+        out["cpu_baseline"] = cpu
+    return out
+
+
+def main():
+    a = parse()
+    rank, world, _ = dist()
+    res = run_reference(a, rank, world) if a.impl == "reference" else run_ours(a, rank, world)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch.distributed as td
+        td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

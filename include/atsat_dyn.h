@@ -236,6 +236,14 @@ int atsat_dyn_pressure(atsat_dyn_t h, atsat_dyn_pstats* out); /* PressureSolver.
 
 /* ---- device glue for resident multi-step runs ---- */
 int atsat_dyn_restore_var(atsat_dyn_t h);              /* restoreVar(1.0), cSaturnModel.cpp:1551-1600 */
+/* BC_Sat bcTheta, bcPhi, bcRadius (cSaturnModel.cpp:1091-1093; BoundaryConditions.h:150-518,
+ * BC_Sat.cpp:61-179) on the dycore's fields: the 17 prognostic fields, nue, massflux_*, fluxlim_nh4sh
+ * and thermalmassflux. */
+int atsat_dyn_boundary_conditions(atsat_dyn_t h);
+/* n iterations of the dycore part of cSaturnModel::Run, iterations iter0 .. iter0+n-1, resident on
+ * the device (cSaturnModel.cpp:864-1111): on even iterations computeMixtureDensity and the pressure
+ * call; then RungeKuttaSat, the boundary conditions and restoreVar. */
+int atsat_dyn_iterate(atsat_dyn_t h, int32_t iter0, int32_t n);
 
 /* ---- diagnostics and timing ---- */
 int atsat_dyn_sync(atsat_dyn_t h);
@@ -258,6 +266,11 @@ enum {
 int atsat_dyn_profile(atsat_dyn_t h, int32_t enable);
 int atsat_dyn_profile_reset(atsat_dyn_t h);
 int atsat_dyn_profile_read(atsat_dyn_t h, int32_t kclass, int64_t* launches, double* ms);
+/* Wall time of the handle's stream between two marks, from CUDA events recorded on that stream:
+ * timer_start records the first, timer_stop records the second, waits for it and returns the
+ * elapsed milliseconds. */
+int atsat_dyn_timer_start(atsat_dyn_t h);
+int atsat_dyn_timer_stop(atsat_dyn_t h, double* ms);
 /* Device-side pointer and row pitch (in elements) of a field's device copy. */
 int atsat_dyn_device_field(atsat_dyn_t h, int32_t field, double** dptr, int64_t* pitch);
 

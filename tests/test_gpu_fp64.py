@@ -180,3 +180,37 @@ def test_nonfinite_census():
         d.load_state(st)
         assert d.count_nonfinite(F.T) == 2
         assert d.count_nonfinite(F.U) == 0
+
+
+@pytest.mark.parametrize("over", [dict(), dict(turb_active=0), dict(bc_top_taper=1, bc_species_wall_copy=1),
+                                  dict(bc_radius_form=3, bc_bottom_form=0, bc_pole_form=2, bc_pole_fill=0),
+                                  dict(local_rho=0, bc_lid_u=0)],
+                         ids=lambda d: ",".join(f"{k}={v}" for k, v in d.items()) or "default")
+def test_device_boundary_conditions(over):
+    from atsat_gb300 import dyn
+    g, P, st = case((9, 13, 17), seed=23, **over)
+    ref = st.copy()
+    oracle.boundary_conditions(ref, P)
+    s = st.copy()
+    with dyn.Dycore(g, P) as d:
+        d.load_state(s)
+        d.boundary_conditions()
+        d.download(ALL)
+    # only products and sums of two or three terms: an FMA-contracted ulp is all that may differ
+    compare(s.arrays, ref.arrays, ALL, 1e-13, f"bc {over}")
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_resident_iterations(shape):
+    """Six iterations of the dycore loop with everything on the device (atsat_dyn_iterate)."""
+    from atsat_gb300 import dyn
+    g, P, st = case(shape, seed=29)
+    ref = st.copy()
+    oracle.steps(ref, P, 6)
+    s = st.copy()
+    with dyn.Dycore(g, P) as d:
+        d.load_state(s)
+        d.iterate(1, 6)
+        d.download(ALL)
+    compare(s.arrays, ref.arrays, F.PROG + F.PROG_N + [F.P_DYN, F.P_DYNN, F.RHO_MIX, F.P_METRIC, F.NUE]
+            + F.AUX_FIELDS + [F.RHS_U, F.RHS_V, F.RHS_W], TOL_FP64, f"6 iterations {shape}")
