@@ -46,7 +46,8 @@ enum {
     ATSAT_DYN_E_TIMEOUT          = -4,  /* a bounded device wait gave up */
     ATSAT_DYN_E_NONFINITE_INPUT  = -5,  /* atsat_dyn_check_finite found NaN/Inf in an input */
     ATSAT_DYN_E_NOMEM            = -6,  /* device or pinned host allocation failed */
-    ATSAT_DYN_E_UNBOUND          = -7   /* upload/download of a field with no host binding */
+    ATSAT_DYN_E_UNBOUND          = -7,  /* upload/download of a field with no host binding */
+    ATSAT_DYN_E_TOO_LARGE        = -8   /* a grid beyond the fixed scratch of a no-allocation call */
 };
 
 /* ---- arithmetic of the step ---- */
@@ -281,6 +282,34 @@ int atsat_dyn_set_write_all_rhs(atsat_dyn_t h, int32_t on);
 /* Pinned host memory for bound arrays (cudaHostAlloc / cudaFreeHost). */
 void* atsat_dyn_host_alloc(size_t bytes);
 void  atsat_dyn_host_free(void* p);
+
+/* ---- no-allocation variant ----
+ * No counterpart in the reference: the reference is host code and never faces this.
+ *
+ * computeBuoyancyRefLevel for callers that cannot call cudaMalloc -- a host program whose pool
+ * allocator owns the whole device memory, or a time-stepping loop that must not pay cudaMalloc /
+ * cudaFree (and the device synchronisation they can cause) on its critical path. The caller passes
+ * its own device inputs and output; the reduction's scratch is a fixed array compiled into the library
+ * (192 KB of static device memory on every GPU that loads it, held until the process exits), so the call
+ * allocates nothing, host or device.
+ *   t, p_stat  device arrays, element (i, j, k) at (i*jm + j)*pitch + k (the layout atsat_dyn_device_field
+ *              reports), pitch >= km
+ *   the_z      HOST array of the jm colatitudes (cSaturnModel::the.z); sin(the_z) weights each row
+ *   buoy_out   DEVICE array of im doubles: the level means
+ *   stream     the CUDA stream to run on (NULL: the default stream); the call waits for it before
+ *              returning
+ * Limits: im <= ATSAT_DYN_NOALLOC_MAX_IM and jm <= ATSAT_DYN_NOALLOC_MAX_JM, else ATSAT_DYN_E_TOO_LARGE.
+ * The first call on a device looks up the scratch array's device address there (once per device), so
+ * make that first call before capturing any stream into a CUDA graph. All calls share the one scratch
+ * array: calls whose GPU work overlaps (different streams or host threads at once) race on it and must
+ * be serialised by the caller. Each call rewrites the scratch it reads, so nothing carries over from the
+ * previous call. */
+#define ATSAT_DYN_NOALLOC_MAX_IM 512
+#define ATSAT_DYN_NOALLOC_MAX_JM 8192
+int atsat_dyn_buoyancy_ref_level_noalloc(const double* t, const double* p_stat, int64_t pitch,
+                                         int32_t im, int32_t jm, int32_t km, const double* the_z,
+                                         double g, double r_mix, double R_mix, double t_ref,
+                                         double* buoy_out, void* stream);
 
 #ifdef __cplusplus
 }
