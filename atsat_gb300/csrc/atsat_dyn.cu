@@ -68,6 +68,14 @@ struct atsat_dyn {
 
     int write_all_rhs = 0;
     cudaEvent_t timer[2] = {nullptr, nullptr};
+
+    // mixed precision: FP32 copy of y_n, two FP32 increment buffers, FP32 copies of the point inputs
+    float* slab32 = nullptr;
+    float* yn32[NPROG] = {};
+    float* dlA[NPROG] = {};
+    float* dlB[NPROG] = {};
+    float* conv32[NCONV] = {};
+    bool conv_dirty[NCONV] = {};
     std::string err;
 };
 
@@ -155,7 +163,7 @@ int check_supported(atsat_dyn* h, const atsat_dyn_params& p) {
         {p.press_wall != 0, "ATSAT_PRESS_WALL (no solid body exists in ATSAT)"},
         {p.press_line != 0, "ATSAT_PRESS_LINE"},
         {p.press_baro != 0, "ATSAT_PRESS_BAROTROPIC"},
-        {p.precision != ATSAT_DYN_FP64, "precision other than FP64"},
+        {p.precision != ATSAT_DYN_FP64 && p.precision != ATSAT_DYN_MIXED, "unknown precision"},
     };
     for (auto& r : rules)
         if (r.bad) return fail(h, ATSAT_DYN_E_UNSUPPORTED, "not implemented on the device: %s", r.what);
@@ -302,8 +310,22 @@ void build_geometry(atsat_dyn* h, const double* vbar0, const double* ubar0) {
 
 bool valid_field(int f) { return f >= 0 && f < ATSAT_NFIELDS; }
 
+// FP32 copies kept for the mixed path: rho_mix and the point inputs nue .. thermalmassflux.
+int conv_slot(int fid) {
+    if (fid == ATSAT_F_RHO_MIX) return 0;
+    if (fid >= ATSAT_F_NUE && fid <= ATSAT_F_THERMALMASSFLUX) return 1 + (fid - ATSAT_F_NUE);
+    return -1;
+}
+int conv_field(int slot) { return slot == 0 ? ATSAT_F_RHO_MIX : ATSAT_F_NUE + slot - 1; }
+
+void mark_dirty(atsat_dyn* h, int fid) {
+    const int s = conv_slot(fid);
+    if (s >= 0) h->conv_dirty[s] = true;
+}
+
 int upload_one(atsat_dyn* h, int fid) {
     const KConst& K = h->kc;
+    mark_dirty(h, fid);
     const int im = K.im, jm = K.jm, km = K.km, kp = K.kp;
     if (h->bind_kind[fid] == BIND_ARRAY) {
         CK(h, cudaMemcpy2DAsync(h->f[fid], (size_t)kp * 8, h->bind_base[fid], (size_t)km * 8, (size_t)km * 8,
@@ -395,7 +417,10 @@ int do_metric(atsat_dyn* h) {
     return ATSAT_DYN_OK;
 }
 
+int enqueue_rk4_mixed(atsat_dyn* h);
+
 int enqueue_rk4(atsat_dyn* h) {
+    if (h->p.precision == ATSAT_DYN_MIXED) return enqueue_rk4_mixed(h);
     int rc;
     if ((rc = do_level_mean(h))) return rc;
     if (h->p.metric_split && (rc = do_metric(h))) return rc;
@@ -415,6 +440,92 @@ int enqueue_rk4(atsat_dyn* h) {
         StageIO<double> io = make_io(h, in, out);
         Timed t(h, ATSAT_K_RK_STAGE);
         CK(h, launch_rk_stage_fp64(h->kc, io, sp, stage == 3 ? MODE_FINAL : MODE_STAGE, h->stream));
+        h->launches += 1;
+    }
+    return ATSAT_DYN_OK;
+}
+
+MixedIO make_mixed_io(atsat_dyn* h, float* const* dl_in, float* const* dl_out, double* const* out64) {
+    MixedIO io{};
+    for (int q = 0; q < NPROG; q++) {
+        io.yn64[q] = h->f[ATSAT_F_N_BASE + q];
+        io.yn32[q] = h->yn32[q];
+        io.dl_in[q] = dl_in ? dl_in[q] : nullptr;
+        io.dl_out[q] = dl_out ? dl_out[q] : nullptr;
+        io.acc[q] = h->acc[q];
+        io.out64[q] = out64 ? out64[q] : nullptr;
+        io.out32[q] = nullptr;
+        io.rhs[q] = h->f[ATSAT_F_RHS_BASE + q];
+    }
+    io.p_dyn = h->f[ATSAT_F_P_DYN];
+    io.p_stat64 = h->f[ATSAT_F_P_STAT];
+    io.p_metric = h->f[ATSAT_F_P_METRIC];
+    io.rho_mix = h->conv32[conv_slot(ATSAT_F_RHO_MIX)];
+    io.nue = h->conv32[conv_slot(ATSAT_F_NUE)];
+    io.q_precip = h->conv32[conv_slot(ATSAT_F_Q_PRECIP)];
+    io.q_rad = h->conv32[conv_slot(ATSAT_F_Q_RAD)];
+    io.tke_source = h->conv32[conv_slot(ATSAT_F_TKE_SOURCE)];
+    io.dis_source = h->conv32[conv_slot(ATSAT_F_DIS_SOURCE)];
+    for (int q = 0; q < 9; q++) io.s_precip[q] = h->conv32[conv_slot(ATSAT_F_S_PRECIP_H2O + q)];
+    io.massflux_h2s = h->conv32[conv_slot(ATSAT_F_MASSFLUX_H2S)];
+    io.massflux_nh3 = h->conv32[conv_slot(ATSAT_F_MASSFLUX_NH3)];
+    io.massflux_nh4sh = h->conv32[conv_slot(ATSAT_F_MASSFLUX_NH4SH)];
+    io.fluxlim_nh4sh = h->conv32[conv_slot(ATSAT_F_FLUXLIM_NH4SH)];
+    io.thermalmassflux = h->conv32[conv_slot(ATSAT_F_THERMALMASSFLUX)];
+    io.aux[0] = h->f[ATSAT_F_AUX_U];
+    io.aux[1] = h->f[ATSAT_F_AUX_V];
+    io.aux[2] = h->f[ATSAT_F_AUX_W];
+    io.buoy = h->buoy;
+    io.geo = h->geo;
+    return io;
+}
+
+// yn32 <- y_n (from `base`), dl0 <- live - y_n when asked, and the dirty FP32 input copies.
+int enqueue_mixed_prepare(atsat_dyn* h, double* const* base, bool with_dl0) {
+    MixedPrep pr{};
+    for (int q = 0; q < NPROG; q++) {
+        pr.yn64[q] = base[q];
+        pr.live64[q] = h->f[q];
+        pr.yn32[q] = h->yn32[q];
+        pr.dl0[q] = with_dl0 ? h->dlB[q] : nullptr;
+    }
+    int n = 0;
+    for (int sl = 0; sl < NCONV; sl++) {
+        if (!h->conv_dirty[sl]) continue;
+        pr.conv_src[n] = h->f[conv_field(sl)];
+        pr.conv_dst[n] = h->conv32[sl];
+        n++;
+        h->conv_dirty[sl] = false;
+    }
+    pr.nconv = n;
+    Timed t(h, ATSAT_K_GLUE);
+    CK(h, launch_mixed_prepare(h->kc, pr, h->stream));
+    h->launches += 1;
+    return ATSAT_DYN_OK;
+}
+
+int enqueue_rk4_mixed(atsat_dyn* h) {
+    int rc;
+    if ((rc = do_level_mean(h))) return rc;
+    if (h->p.metric_split && (rc = do_metric(h))) return rc;
+    double* yn[NPROG];
+    double* L[NPROG];
+    for (int q = 0; q < NPROG; q++) { yn[q] = h->f[ATSAT_F_N_BASE + q]; L[q] = h->f[q]; }
+    if ((rc = enqueue_mixed_prepare(h, yn, true))) return rc;
+    const double dt = h->p.dt;
+    for (int stage = 0; stage < 4; stage++) {
+        StageParams sp{};
+        sp.stage = stage;
+        sp.write_all_rhs = h->write_all_rhs;
+        sp.c_in = (stage == 0 || stage == 1) ? 0.5 * dt : (stage == 2 ? dt : 0.0);
+        sp.wgt = (stage == 0 || stage == 3) ? 1.0 : 2.0;
+        sp.sixth_dt = dt / 6.0;
+        // dl_0 sits in B; stage 0: B -> A, 1: A -> B, 2: B -> A, 3 reads A
+        float* const* in = (stage == 1 || stage == 3) ? h->dlA : h->dlB;
+        float* const* out = (stage == 1) ? h->dlB : h->dlA;
+        MixedIO io = make_mixed_io(h, in, stage == 3 ? nullptr : out, stage == 3 ? L : nullptr);
+        Timed t(h, ATSAT_K_RK_STAGE);
+        CK(h, launch_rk_stage_mixed(h->kc, io, sp, stage == 3 ? MODE_FINAL : MODE_STAGE, h->stream));
         h->launches += 1;
     }
     return ATSAT_DYN_OK;
@@ -464,6 +575,9 @@ int enqueue_bc(atsat_dyn* h) {
     Timed t(h, ATSAT_K_GLUE);
     CK(h, launch_boundary_conditions(h->kc, h->p, h->f, h->stream));
     h->launches += 3;
+    for (int fid : {ATSAT_F_NUE, ATSAT_F_MASSFLUX_H2S, ATSAT_F_MASSFLUX_NH3, ATSAT_F_MASSFLUX_NH4SH,
+                    ATSAT_F_FLUXLIM_NH4SH, ATSAT_F_THERMALMASSFLUX})
+        mark_dirty(h, fid);
     return ATSAT_DYN_OK;
 }
 
@@ -614,6 +728,16 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
     h->six = reinterpret_cast<double**>(q); q += 8;
     q = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(q) + 255) & ~uintptr_t(255));
     h->geo = reinterpret_cast<ColGeo*>(q);
+    if (p->precision == ATSAT_DYN_MIXED) {
+        const size_t n32 = (size_t)(3 * NPROG + NCONV) * K.fsz;
+        if ((e = cudaMalloc(&h->slab32, n32 * 4)) != cudaSuccess) return cuda_fail(e, "cudaMalloc (FP32)");
+        if ((e = cudaMemsetAsync(h->slab32, 0, n32 * 4, h->stream)) != cudaSuccess) return cuda_fail(e, "cudaMemset");
+        float* r = h->slab32;
+        for (int s = 0; s < NPROG; s++) { h->yn32[s] = r; r += K.fsz; }
+        for (int s = 0; s < NPROG; s++) { h->dlA[s] = r; r += K.fsz; }
+        for (int s = 0; s < NPROG; s++) { h->dlB[s] = r; r += K.fsz; }
+        for (int s = 0; s < NCONV; s++) { h->conv32[s] = r; r += K.fsz; h->conv_dirty[s] = true; }
+    }
     // small host tables
     std::vector<double> sin_j(K.jm), rm_tab(K.im), cor_j(K.jm);
     const double nd = p->nd_cor ? p->L_atm * 1.0e3 / p->u_0 : 1.0;
@@ -643,6 +767,7 @@ void atsat_dyn_destroy(atsat_dyn_t h) {
     for (auto e : h->pool) cudaEventDestroy(e);
     for (auto e : h->timer) if (e) cudaEventDestroy(e);
     if (h->slab) cudaFree(h->slab);
+    if (h->slab32) cudaFree(h->slab32);
     if (h->pinned) cudaFreeHost(h->pinned);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -731,6 +856,7 @@ int atsat_dyn_mixture_density(atsat_dyn_t h) {
         Timed t(h, ATSAT_K_GLUE);
         CK(h, launch_density(h->kc, h->f[ATSAT_F_T], h->f[ATSAT_F_P_STAT], h->p.R_mix, h->f[ATSAT_F_RHO_MIX], h->stream));
         h->launches += 1;
+        mark_dirty(h, ATSAT_F_RHO_MIX);
     }
     return finish(h);
 }
@@ -751,6 +877,19 @@ int atsat_dyn_rhs(atsat_dyn_t h) {
     ENTRY(h);
     double* L[NPROG];
     for (int q = 0; q < NPROG; q++) L[q] = h->f[q];
+    if (h->p.precision == ATSAT_DYN_MIXED) {
+        int rc = enqueue_mixed_prepare(h, L, false);       // the stencils read the live fields
+        if (rc) return rc;
+        MixedIO io = make_mixed_io(h, nullptr, nullptr, nullptr);
+        for (int q = 0; q < NPROG; q++) io.yn64[q] = L[q];
+        StageParams sp{};
+        {
+            Timed t(h, ATSAT_K_RHS);
+            CK(h, launch_rk_stage_mixed(h->kc, io, sp, MODE_RHS, h->stream));
+            h->launches += 1;
+        }
+        return finish(h);
+    }
     StageIO<double> io = make_io(h, L, nullptr);
     StageParams sp{};
     {
@@ -817,6 +956,7 @@ int atsat_dyn_iterate(atsat_dyn_t h, int32_t iter0, int32_t n) {
                 CK(h, launch_density(h->kc, h->f[ATSAT_F_T], h->f[ATSAT_F_P_STAT], h->p.R_mix, h->f[ATSAT_F_RHO_MIX],
                                      h->stream));
                 h->launches += 1;
+                mark_dirty(h, ATSAT_F_RHO_MIX);
             }
             if ((rc = enqueue_pressure(h, h->p.press_sweeps > 0 ? h->p.press_sweeps : 1))) return rc;
         }

@@ -94,6 +94,49 @@ struct StageIO {
     const ColGeo* geo;             // [im * jm]
 };
 
+// The mixed-precision stage kernel's view (rk_mixed.cu). Point inputs are FP32 copies of the FP64
+// fields; p_dyn, p_stat, p_metric are read in FP64.
+constexpr int NCONV = 20;          // rho_mix and the 19 point inputs from nue to thermalmassflux
+
+struct MixedIO {
+    const double* yn64[NPROG];
+    const float* yn32[NPROG];
+    const float* dl_in[NPROG];     // null entries: Y_s = y_n
+    float* dl_out[NPROG];
+    double* acc[NPROG];
+    double* out64[NPROG];          // y_{n+1} (final stage)
+    float* out32[NPROG];           // optional FP32 copy of y_{n+1}
+    const double* p_dyn;
+    const double* p_stat64;
+    const double* p_metric;
+    const float* rho_mix;
+    const float* nue;
+    const float* q_precip;
+    const float* q_rad;
+    const float* tke_source;
+    const float* dis_source;
+    const float* s_precip[9];
+    const float* massflux_h2s;
+    const float* massflux_nh3;
+    const float* massflux_nh4sh;
+    const float* fluxlim_nh4sh;
+    const float* thermalmassflux;
+    double* rhs[NPROG];
+    double* aux[3];
+    const double* buoy;
+    const ColGeo* geo;
+};
+
+struct MixedPrep {
+    const double* yn64[NPROG];
+    const double* live64[NPROG];
+    float* yn32[NPROG];
+    float* dl0[NPROG];             // null: not written
+    const double* conv_src[NCONV];
+    float* conv_dst[NCONV];
+    int nconv;
+};
+
 enum StageMode {
     MODE_RHS = 0,       // tendencies only: all rhs_* and aux_*
     MODE_STAGE = 1,     // stages 0..2: acc and the next stage input
@@ -109,6 +152,9 @@ struct StageParams {
 // ---- kernel launchers (each returns cudaGetLastError()) ----
 cudaError_t launch_rk_stage_fp64(const KConst& kc, const StageIO<double>& io, const StageParams& sp,
                                  int mode, cudaStream_t s);
+cudaError_t launch_rk_stage_mixed(const KConst& kc, const MixedIO& io, const StageParams& sp, int mode,
+                                  cudaStream_t s);
+cudaError_t launch_mixed_prepare(const KConst& kc, const MixedPrep& pr, cudaStream_t s);
 cudaError_t launch_level_mean(const KConst& kc, const double* t, const double* p_stat,
                               const double* sin_j, double* partial, double* buoy, cudaStream_t s);
 cudaError_t launch_metric_scan(const KConst& kc, const double* v, const double* w, const double* rm_tab,
