@@ -34,18 +34,69 @@ __device__ __forceinline__ float ys(const float* __restrict__ yn, const float* _
     return dl ? ldf(yn + c) + ldf(dl + c) : ldf(yn + c);
 }
 
+// Differences of Y_s = y_n + dl are taken on the two parts separately and then added: y_n's FP32 copy
+// carries a fixed rounding of the field, dl the small increment at its own precision. Summing first would
+// round the increment against the field (0.85 + 1e-5 loses the increment's low digits), and the stencil
+// would difference that rounding noise.
+__device__ __forceinline__ void diff7(const float* f, int64_t c, int64_t P, int kp, int dkw, int dke, float* e) {
+    const float x = ldf(f + c);
+    const float rp = ldf(f + c + P), rn = ldf(f + c - P);
+    const float tp = ldf(f + c + kp), tn = ldf(f + c - kp);
+    const float pe = ldf(f + c + dke), pw = ldf(f + c + dkw);
+    e[0] = rp - rn;
+    e[1] = rp - 2.0f * x + rn;
+    e[2] = tp - tn;
+    e[3] = tp - 2.0f * x + tn;
+    e[4] = pe - pw;
+    e[5] = pe - 2.0f * x + pw;
+}
+
 __device__ __forceinline__ void derivs32(const float* yn, const float* dl, int64_t c, int64_t P, int kp, int dkw,
                                          int dke, const KF& K, D6f& d) {
-    const float x = ys(yn, dl, c);
-    const float rp = ys(yn, dl, c + P), rn = ys(yn, dl, c - P);
-    const float tp = ys(yn, dl, c + kp), tn = ys(yn, dl, c - kp);
-    const float pe = ys(yn, dl, c + dke), pw = ys(yn, dl, c + dkw);
-    d.dr = (rp - rn) * K.inv_2dr;
-    d.d2r = (rp - 2.0f * x + rn) * K.inv_dr2;
-    d.dthe = (tp - tn) * K.inv_2dthe;
-    d.d2the = (tp - 2.0f * x + tn) * K.inv_dthe2;
-    d.dphi = (pe - pw) * K.inv_2dphi;
-    d.d2phi = (pe - 2.0f * x + pw) * K.inv_dphi2;
+    float a[6];
+    diff7(yn, c, P, kp, dkw, dke, a);
+    if (dl) {
+        float b[6];
+        diff7(dl, c, P, kp, dkw, dke, b);
+#pragma unroll
+        for (int q = 0; q < 6; q++) a[q] += b[q];
+    }
+    d.dr = a[0] * K.inv_2dr;
+    d.d2r = a[1] * K.inv_dr2;
+    d.dthe = a[2] * K.inv_2dthe;
+    d.d2the = a[3] * K.inv_dthe2;
+    d.dphi = a[4] * K.inv_2dphi;
+    d.d2phi = a[5] * K.inv_dphi2;
+}
+
+// The zonal wind w (|w| up to ~0.85, with small zonal variations) is differenced from its FP64 y_n: an
+// FP32 copy would round w by 3e-8 independently per cell, and near the poles w * dw/dphi / (r sin theta)
+// turns that rounding into a tendency error larger than the FP32 arithmetic of every other term.
+__device__ __forceinline__ void derivs_wide(const double* yn, const float* dl, int64_t c, int64_t P, int kp,
+                                            int dkw, int dke, const KF& K, D6f& d) {
+    const double x = ldd(yn + c);
+    const double rp = ldd(yn + c + P), rn = ldd(yn + c - P);
+    const double tp = ldd(yn + c + kp), tn = ldd(yn + c - kp);
+    const double pe = ldd(yn + c + dke), pw = ldd(yn + c + dkw);
+    float a[6];
+    a[0] = (float)(rp - rn);
+    a[1] = (float)(rp - 2.0 * x + rn);
+    a[2] = (float)(tp - tn);
+    a[3] = (float)(tp - 2.0 * x + tn);
+    a[4] = (float)(pe - pw);
+    a[5] = (float)(pe - 2.0 * x + pw);
+    if (dl) {
+        float b[6];
+        diff7(dl, c, P, kp, dkw, dke, b);
+#pragma unroll
+        for (int q = 0; q < 6; q++) a[q] += b[q];
+    }
+    d.dr = a[0] * K.inv_2dr;
+    d.d2r = a[1] * K.inv_dr2;
+    d.dthe = a[2] * K.inv_2dthe;
+    d.d2the = a[3] * K.inv_dthe2;
+    d.dphi = a[4] * K.inv_2dphi;
+    d.d2phi = a[5] * K.inv_dphi2;
 }
 
 struct GeoF {
@@ -150,7 +201,7 @@ __global__ void __launch_bounds__(256) rk_stage_mixed_kernel(const KConst K, con
     D6f du, dv, dw;
     derivs32(io.yn32[ATSAT_F_U], dlq(ATSAT_F_U), c, P, kp, dkw, dke, KF_, du);
     derivs32(io.yn32[ATSAT_F_V], dlq(ATSAT_F_V), c, P, kp, dkw, dke, KF_, dv);
-    derivs32(io.yn32[ATSAT_F_W], dlq(ATSAT_F_W), c, P, kp, dkw, dke, KF_, dw);
+    derivs_wide(io.yn64[ATSAT_F_W], dlq(ATSAT_F_W), c, P, kp, dkw, dke, KF_, dw);
 
     const double dpdr = (ldd(io.p_dyn + c + P) - ldd(io.p_dyn + c - P)) * K.inv_2dr;
     const double dpdthe = (ldd(io.p_dyn + c + kp) - ldd(io.p_dyn + c - kp)) * K.inv_2dthe;
@@ -164,14 +215,17 @@ __global__ void __launch_bounds__(256) rk_stage_mixed_kernel(const KConst K, con
     // ---- momentum ----
     {
         const double cor_the = ldd(&gp->cor_the) * w;
-        const float v_cor = vf - (float)ldd(&gp->vbar0), u_cor = uf - (float)ldd(&gp->ubar0);
-        const float cor_phi = (float)ldd(&gp->cor_phi) * (g.costhe * v_cor + g.sinthe_true * u_cor);
+        // the zonal Coriolis force and the metric terms of the v and w equations are FP64: they are as
+        // large as rhs_v / rhs_w themselves near the poles
+        const double cot = ldd(&gp->cotanthe);
+        const double cor_phi = ldd(&gp->cor_phi) * (ldd(&gp->costhe) * (v - ldd(&gp->vbar0))
+                                                    + ldd(&gp->sinthe_true) * (u - ldd(&gp->ubar0)));
 
         const float tr_u = uf * du.dr + vf * du.dthe * g.inv_rm + wf * du.dphi * g.inv_rmsinthe;
         const float tr_v = uf * dv.dr + vf * dv.dthe * g.inv_rm + wf * dv.dphi * g.inv_rmsinthe;
-        const float tr_w = uf * dw.dr + vf * dw.dthe * g.inv_rm + wf * dw.dphi * g.inv_rmsinthe
-                         + (wf * uf + vf * wf * g.cotanthe) * g.inv_rm;
-        const double tr_v_metric = (u * v - w * w * ldd(&gp->cotanthe)) * inv_rm;
+        const float tr_w = uf * dw.dr + vf * dw.dthe * g.inv_rm + wf * dw.dphi * g.inv_rmsinthe;
+        const double tr_v_metric = (u * v - w * w * cot) * inv_rm;
+        const double tr_w_metric = (w * u + v * w * cot) * inv_rm;
         const float diffusion_u = du.d2r + 2.0f * uf * g.inv_rm2 + du.d2the * g.inv_rm2 + 4.0f * du.dr * g.inv_rm
                                 + du.dthe * g.costhe_inv_rm2sinthe + du.d2phi * g.inv_rm2sinthe2;
         const float diffusion_v = dv.d2r + dv.dr * g.two_inv_rm + dv.d2the * g.inv_rm2
@@ -202,8 +256,8 @@ __global__ void __launch_bounds__(256) rk_stage_mixed_kernel(const KConst K, con
         const double rhs_v = -dpdthe * inv_rm - dpmdthe * inv_rm - (double)tr_v - tr_v_metric
                            + (double)(diffusion_v * inv_re + diffusion_v * nue_t)
                            - K.Coriolis * cor_the + K.centrifugal * ldd(&gp->cent_the);
-        const double rhs_w = -dpdphi * inv_rmsinthe - dpmdphi * inv_rmsinthe - (double)tr_w
-                           + (double)(diffusion_w * inv_re + diffusion_w * nue_t) - K.Coriolis * (double)cor_phi;
+        const double rhs_w = -dpdphi * inv_rmsinthe - dpmdphi * inv_rmsinthe - (double)tr_w - tr_w_metric
+                           + (double)(diffusion_w * inv_re + diffusion_w * nue_t) - K.Coriolis * cor_phi;
         emit<MODE>(io, sp, K, ATSAT_F_U, c, rhs_u, 0.0f);
         emit<MODE>(io, sp, K, ATSAT_F_V, c, rhs_v, 0.0f);
         emit<MODE>(io, sp, K, ATSAT_F_W, c, rhs_w, 0.0f);
