@@ -72,10 +72,15 @@ struct atsat_dyn {
     // mixed precision: FP32 copy of y_n, two FP32 increment buffers, FP32 copies of the point inputs
     float* slab32 = nullptr;
     float* yn32[NPROG] = {};
+    float* wlo = nullptr;
     float* dlA[NPROG] = {};
     float* dlB[NPROG] = {};
+    float* acc32[NPROG - 4] = {};
+    float* fz[NFZ] = {};
     float* conv32[NCONV] = {};
     bool conv_dirty[NCONV] = {};
+    ColGeoF* geof = nullptr;
+    MixedConstF kf{};
     std::string err;
 };
 
@@ -308,6 +313,55 @@ void build_geometry(atsat_dyn* h, const double* vbar0, const double* ubar0) {
     }
 }
 
+// FP32 constants of the mixed stage kernel, formed from the FP64 ones.
+void build_mixed_constants(atsat_dyn* h) {
+    const KConst& K = h->kc;
+    const atsat_dyn_params& p = h->p;
+    MixedConstF& F = h->kf;
+    F.im = K.im; F.jm = K.jm; F.km = K.km; F.kp = K.kp; F.plane = K.plane;
+    F.metric_split = K.metric_split; F.hydro_buoy = K.hydro_buoy; F.turb = K.turb; F.rad_on = K.rad_on;
+    F.precip_on = K.precip_on; F.tmf_on = K.tmf_on; F.divu_on = K.divu_on;
+    F.inv_2dr = (float)K.inv_2dr; F.inv_2dthe = (float)K.inv_2dthe; F.inv_2dphi = (float)K.inv_2dphi;
+    F.inv_dr2 = (float)K.inv_dr2; F.inv_dthe2 = (float)K.inv_dthe2; F.inv_dphi2 = (float)K.inv_dphi2;
+    F.coeff_energy_p = (float)K.coeff_energy_p; F.inv_re = (float)K.inv_re; F.inv_re_pr = (float)K.inv_re_pr;
+    F.inv_sc_re_ch4 = (float)K.inv_sc_re_ch4; F.inv_sc_re_h2o = (float)K.inv_sc_re_h2o;
+    F.inv_sc_re_h2s = (float)K.inv_sc_re_h2s; F.inv_sc_re_nh3 = (float)K.inv_sc_re_nh3;
+    F.inv_sc_re_nh4sh = (float)K.inv_sc_re_nh4sh;
+    F.inv_sig_k = (float)K.inv_sig_k; F.inv_sig_w = (float)K.inv_sig_w;
+    F.turb_coupling = (float)K.turb_coupling; F.inv_pr_t = (float)K.inv_pr_t;
+    F.chem = (float)K.chem; F.precip_coupling = (float)K.precip_coupling;
+    F.precip_factor = (float)(K.precip_coupling * K.precip_num * K.precip_den);
+    F.rad_factor = (float)(K.rad_coupling * K.rad_num / K.rad_den_c);
+    F.r_mix = (float)K.r_mix;
+    F.tke_max = (float)K.tke_max; F.dis_min = (float)K.dis_min;
+    F.species_divu = (float)K.species_divu; F.tmf_chem = (float)K.tmf_chem;
+    F.metric_on = (float)K.metric_on; F.cor_rad_on = (float)K.cor_rad_on;
+    F.kb = p.buoy_legacy ? 1.0f : (float)K.kbuoy;
+    F.bref_scale = p.buoy_legacy ? 0.0f : 1.0f;
+    F.tke_max_d = K.tke_max; F.dis_min_d = K.dis_min;
+}
+
+cudaError_t upload_geof(atsat_dyn* h) {
+    const atsat_dyn_params& p = h->p;
+    std::vector<ColGeoF> gf(h->geo_h.size());
+    for (size_t n = 0; n < gf.size(); n++) {
+        const ColGeo& c = h->geo_h[n];
+        ColGeoF& f = gf[n];
+        f.inv_rm = (float)c.inv_rm; f.inv_rm2 = (float)c.inv_rm2; f.inv_rmsinthe = (float)c.inv_rmsinthe;
+        f.inv_rm2sinthe = (float)c.inv_rm2sinthe; f.inv_rm2sinthe2 = (float)c.inv_rm2sinthe2;
+        f.costhe_inv_rm2sinthe = (float)c.costhe_inv_rm2sinthe; f.cotanthe = (float)c.cotanthe;
+        f.costhe = (float)c.costhe; f.two_inv_rm = (float)c.two_inv_rm; f.v_metric = (float)c.v_metric;
+        f.sinthe_true = (float)c.sinthe_true;
+        f.cor_the_c = (float)(p.Coriolis * c.cor_the);
+        f.cor_phi_c = (float)(p.Coriolis * c.cor_phi);
+        f.cor_rad_c = (float)(p.Coriolis * c.cor_rad);
+        f.vbar0 = (float)c.vbar0; f.ubar0 = (float)c.ubar0;
+    }
+    cudaError_t e = cudaMemcpyAsync(h->geof, gf.data(), sizeof(ColGeoF) * gf.size(), cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(h->stream);
+}
+
 bool valid_field(int f) { return f >= 0 && f < ATSAT_NFIELDS; }
 
 // FP32 copies kept for the mixed path: rho_mix and the point inputs nue .. thermalmassflux.
@@ -452,14 +506,15 @@ MixedIO make_mixed_io(atsat_dyn* h, float* const* dl_in, float* const* dl_out, d
         io.yn32[q] = h->yn32[q];
         io.dl_in[q] = dl_in ? dl_in[q] : nullptr;
         io.dl_out[q] = dl_out ? dl_out[q] : nullptr;
-        io.acc[q] = h->acc[q];
         io.out64[q] = out64 ? out64[q] : nullptr;
         io.out32[q] = nullptr;
         io.rhs[q] = h->f[ATSAT_F_RHS_BASE + q];
     }
-    io.p_dyn = h->f[ATSAT_F_P_DYN];
-    io.p_stat64 = h->f[ATSAT_F_P_STAT];
-    io.p_metric = h->f[ATSAT_F_P_METRIC];
+    io.wlo = h->wlo;
+    io.wlo_out = nullptr;
+    for (int q = 0; q < 4; q++) io.acc64[q] = h->acc[q];
+    for (int q = 0; q < NPROG - 4; q++) io.acc32[q] = h->acc32[q];
+    for (int q = 0; q < NFZ; q++) io.fz[q] = h->fz[q];
     io.rho_mix = h->conv32[conv_slot(ATSAT_F_RHO_MIX)];
     io.nue = h->conv32[conv_slot(ATSAT_F_NUE)];
     io.q_precip = h->conv32[conv_slot(ATSAT_F_Q_PRECIP)];
@@ -475,20 +530,25 @@ MixedIO make_mixed_io(atsat_dyn* h, float* const* dl_in, float* const* dl_out, d
     io.aux[0] = h->f[ATSAT_F_AUX_U];
     io.aux[1] = h->f[ATSAT_F_AUX_V];
     io.aux[2] = h->f[ATSAT_F_AUX_W];
+    io.geof = h->geof;
     io.buoy = h->buoy;
-    io.geo = h->geo;
     return io;
 }
 
-// yn32 <- y_n (from `base`), dl0 <- live - y_n when asked, and the dirty FP32 input copies.
+// Once per RK step: yn32 / wlo <- y_n (`base`), dl_0 <- live - y_n when asked, the dirty FP32 input
+// copies, and the frozen FP64 momentum terms.
 int enqueue_mixed_prepare(atsat_dyn* h, double* const* base, bool with_dl0) {
     MixedPrep pr{};
+    pr.write_yn32 = 1;
     for (int q = 0; q < NPROG; q++) {
         pr.yn64[q] = base[q];
         pr.live64[q] = h->f[q];
         pr.yn32[q] = h->yn32[q];
+        pr.yn32_b[q] = nullptr;
         pr.dl0[q] = with_dl0 ? h->dlB[q] : nullptr;
     }
+    pr.wlo = h->wlo;
+    pr.wlo_b = nullptr;
     int n = 0;
     for (int sl = 0; sl < NCONV; sl++) {
         if (!h->conv_dirty[sl]) continue;
@@ -498,6 +558,13 @@ int enqueue_mixed_prepare(atsat_dyn* h, double* const* base, bool with_dl0) {
         h->conv_dirty[sl] = false;
     }
     pr.nconv = n;
+    for (int q = 0; q < NFZ; q++) pr.fz[q] = h->fz[q];
+    pr.p_dyn = h->f[ATSAT_F_P_DYN];
+    pr.p_metric = h->f[ATSAT_F_P_METRIC];
+    pr.p_stat = h->f[ATSAT_F_P_STAT];
+    pr.rho_mix = h->f[ATSAT_F_RHO_MIX];
+    pr.buoy = h->buoy;
+    pr.geo = h->geo;
     Timed t(h, ATSAT_K_GLUE);
     CK(h, launch_mixed_prepare(h->kc, pr, h->stream));
     h->launches += 1;
@@ -525,7 +592,7 @@ int enqueue_rk4_mixed(atsat_dyn* h) {
         float* const* out = (stage == 1) ? h->dlB : h->dlA;
         MixedIO io = make_mixed_io(h, in, stage == 3 ? nullptr : out, stage == 3 ? L : nullptr);
         Timed t(h, ATSAT_K_RK_STAGE);
-        CK(h, launch_rk_stage_mixed(h->kc, io, sp, stage == 3 ? MODE_FINAL : MODE_STAGE, h->stream));
+        CK(h, launch_rk_stage_mixed(h->kf, io, sp, stage == 3 ? MODE_FINAL : MODE_STAGE, h->stream));
         h->launches += 1;
     }
     return ATSAT_DYN_OK;
@@ -696,6 +763,7 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
     if (rc) { *out = h; return rc; }
     build_constants(h);
     build_geometry(h, nullptr, nullptr);
+    build_mixed_constants(h);
     const KConst& K = h->kc;
     auto cuda_fail = [&](cudaError_t e, const char* what) {
         fail(h, e == cudaErrorMemoryAllocation ? ATSAT_DYN_E_NOMEM : ATSAT_DYN_E_CUDA, "%s: %s", what,
@@ -729,14 +797,21 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
     q = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(q) + 255) & ~uintptr_t(255));
     h->geo = reinterpret_cast<ColGeo*>(q);
     if (p->precision == ATSAT_DYN_MIXED) {
-        const size_t n32 = (size_t)(3 * NPROG + NCONV) * K.fsz;
+        const size_t ngeo = ((size_t)K.im * K.jm * sizeof(ColGeoF) + 4095) / 4 + 1024;
+        const size_t n32 = (size_t)(3 * NPROG + 1 + (NPROG - 4) + NFZ + NCONV) * K.fsz + ngeo;
         if ((e = cudaMalloc(&h->slab32, n32 * 4)) != cudaSuccess) return cuda_fail(e, "cudaMalloc (FP32)");
         if ((e = cudaMemsetAsync(h->slab32, 0, n32 * 4, h->stream)) != cudaSuccess) return cuda_fail(e, "cudaMemset");
         float* r = h->slab32;
         for (int s = 0; s < NPROG; s++) { h->yn32[s] = r; r += K.fsz; }
+        h->wlo = r; r += K.fsz;
         for (int s = 0; s < NPROG; s++) { h->dlA[s] = r; r += K.fsz; }
         for (int s = 0; s < NPROG; s++) { h->dlB[s] = r; r += K.fsz; }
+        for (int s = 0; s < NPROG - 4; s++) { h->acc32[s] = r; r += K.fsz; }
+        for (int s = 0; s < NFZ; s++) { h->fz[s] = r; r += K.fsz; }
         for (int s = 0; s < NCONV; s++) { h->conv32[s] = r; r += K.fsz; h->conv_dirty[s] = true; }
+        r = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(r) + 255) & ~uintptr_t(255));
+        h->geof = reinterpret_cast<ColGeoF*>(r);
+        if ((e = upload_geof(h)) != cudaSuccess) return cuda_fail(e, "FP32 geometry upload");
     }
     // small host tables
     std::vector<double> sin_j(K.jm), rm_tab(K.im), cor_j(K.jm);
@@ -830,6 +905,7 @@ int atsat_dyn_set_tables(atsat_dyn_t h, const double* cell_vbar0, const double* 
     build_geometry(h, cell_vbar0, cell_ubar0);
     CK(h, cudaMemcpyAsync(h->geo, h->geo_h.data(), sizeof(ColGeo) * h->geo_h.size(), cudaMemcpyHostToDevice,
                           h->stream));
+    if (h->geof) CK(h, upload_geof(h));
     h->has_pbaro = (p_baro != nullptr);
     if (p_baro) {
         const KConst& K = h->kc;
@@ -885,7 +961,7 @@ int atsat_dyn_rhs(atsat_dyn_t h) {
         StageParams sp{};
         {
             Timed t(h, ATSAT_K_RHS);
-            CK(h, launch_rk_stage_mixed(h->kc, io, sp, MODE_RHS, h->stream));
+            CK(h, launch_rk_stage_mixed(h->kf, io, sp, MODE_RHS, h->stream));
             h->launches += 1;
         }
         return finish(h);

@@ -94,21 +94,48 @@ struct StageIO {
     const ColGeo* geo;             // [im * jm]
 };
 
-// The mixed-precision stage kernel's view (rk_mixed.cu). Point inputs are FP32 copies of the FP64
-// fields; p_dyn, p_stat, p_metric are read in FP64.
-constexpr int NCONV = 20;          // rho_mix and the 19 point inputs from nue to thermalmassflux
+// ---- mixed precision (rk_mixed.cu) ----
+constexpr int NCONV = 20;          // FP32 copies: rho_mix and the 19 point inputs nue .. thermalmassflux
+
+// frozen FP32 fields formed in FP64 once per RK step
+enum { FZ_DPR = 0, FZ_DPTH, FZ_DPPH, FZ_DPS, FZ_GU, FZ_GV, FZ_GW, FZ_BAN, FZ_BPS, NFZ };
+
+// per-(i,j) geometry in FP32 for the stage kernel
+struct alignas(16) ColGeoF {
+    float inv_rm, inv_rm2, inv_rmsinthe, inv_rm2sinthe;
+    float inv_rm2sinthe2, costhe_inv_rm2sinthe, cotanthe, costhe;
+    float two_inv_rm, v_metric, sinthe_true, cor_the_c;     // cor_*_c include Coriolis and nd_cor
+    float cor_phi_c, cor_rad_c, vbar0, ubar0;
+};
+static_assert(sizeof(ColGeoF) == 16 * 4, "ColGeoF layout");
+
+struct MixedConstF {
+    int im, jm, km, kp;
+    int64_t plane;
+    int metric_split, hydro_buoy, turb, rad_on;
+    int precip_on, tmf_on, divu_on, pad0;
+    float inv_2dr, inv_2dthe, inv_2dphi, inv_dr2, inv_dthe2, inv_dphi2;
+    float coeff_energy_p, inv_re, inv_re_pr;
+    float inv_sc_re_ch4, inv_sc_re_h2o, inv_sc_re_h2s, inv_sc_re_nh3, inv_sc_re_nh4sh;
+    float inv_sig_k, inv_sig_w, turb_coupling, inv_pr_t;
+    float chem, precip_coupling, precip_factor, rad_factor, r_mix;
+    float tke_max, dis_min, species_divu, tmf_chem;
+    float metric_on, cor_rad_on, kb, bref_scale;
+    double tke_max_d, dis_min_d;
+};
 
 struct MixedIO {
-    const double* yn64[NPROG];
-    const float* yn32[NPROG];
-    const float* dl_in[NPROG];     // null entries: Y_s = y_n
+    const float* yn32[NPROG];      // FP32 copy of y_n
+    const float* wlo;              // y_n(w) - yn32(w)
+    const float* dl_in[NPROG];     // stage increments; null entries: Y_s = y_n
     float* dl_out[NPROG];
-    double* acc[NPROG];
+    double* acc64[4];              // u, v, w, t
+    float* acc32[NPROG - 4];       // the 13 scalars
+    const double* yn64[NPROG];
     double* out64[NPROG];          // y_{n+1} (final stage)
     float* out32[NPROG];           // optional FP32 copy of y_{n+1}
-    const double* p_dyn;
-    const double* p_stat64;
-    const double* p_metric;
+    float* wlo_out;
+    const float* fz[NFZ];
     const float* rho_mix;
     const float* nue;
     const float* q_precip;
@@ -123,18 +150,29 @@ struct MixedIO {
     const float* thermalmassflux;
     double* rhs[NPROG];
     double* aux[3];
+    const ColGeoF* geof;
     const double* buoy;
-    const ColGeo* geo;
 };
 
 struct MixedPrep {
+    int write_yn32;
     const double* yn64[NPROG];
     const double* live64[NPROG];
     float* yn32[NPROG];
+    float* yn32_b[NPROG];          // optional second copy
+    float* wlo;
+    float* wlo_b;
     float* dl0[NPROG];             // null: not written
     const double* conv_src[NCONV];
     float* conv_dst[NCONV];
     int nconv;
+    float* fz[NFZ];
+    const double* p_dyn;
+    const double* p_metric;
+    const double* p_stat;
+    const double* rho_mix;
+    const double* buoy;
+    const ColGeo* geo;
 };
 
 enum StageMode {
@@ -152,7 +190,7 @@ struct StageParams {
 // ---- kernel launchers (each returns cudaGetLastError()) ----
 cudaError_t launch_rk_stage_fp64(const KConst& kc, const StageIO<double>& io, const StageParams& sp,
                                  int mode, cudaStream_t s);
-cudaError_t launch_rk_stage_mixed(const KConst& kc, const MixedIO& io, const StageParams& sp, int mode,
+cudaError_t launch_rk_stage_mixed(const MixedConstF& kf, const MixedIO& io, const StageParams& sp, int mode,
                                   cudaStream_t s);
 cudaError_t launch_mixed_prepare(const KConst& kc, const MixedPrep& pr, cudaStream_t s);
 cudaError_t launch_level_mean(const KConst& kc, const double* t, const double* p_stat,

@@ -48,9 +48,13 @@ def parse():
     ap.add_argument("--shape", default="41,181,361")
     ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", default="mixed,fp64",
+                    help="comma list; the first is the headline value, the others are reported beside it")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     a.shape = tuple(int(x) for x in a.shape.split(","))
+    a.precisions = [p.strip() for p in a.precision.split(",") if p.strip()]
+    assert all(p in ("mixed", "fp64") for p in a.precisions), a.precisions
     return a
 
 
@@ -159,10 +163,20 @@ def interior_rk(g):
     return (g.im - 2) * (g.jm - 4) * (g.km - 1)
 
 
-# FP64 words moved per interior-RK cell by the four fused stage launches (the layout shipped here):
-# stage 0 reads Y_s, y_n and the 21 auxiliary inputs (3 stencil, 18 point) and writes acc and Y_1;
+# Bytes moved per interior-RK cell by the four stage launches of one RK4 step, as laid out here.
+# FP64: stage 0 reads Y_s, y_n and the 21 auxiliary inputs (3 stencil, 18 point) and writes acc and Y_1;
 # stages 1-2 also read acc; stage 3 writes y_{n+1}, rhs_u/v/w and aux_u/v/w instead of acc and Y.
-RK_WORDS_PER_CELL = (17 + 17 + 21 + 34) + 2 * (17 + 21 + 17 + 17 + 34) + (17 + 21 + 17 + 17 + 23)
+RK_BYTES_FP64 = 8 * ((17 + 17 + 21 + 34) + 2 * (17 + 21 + 17 + 17 + 34) + (17 + 21 + 17 + 17 + 23))
+# mixed: every stage reads the FP32 copy of y_n of all 17 fields and w's low word (72 B), the FP32 stage
+# increment (68 B), the 9 frozen FP32 momentum terms (36 B) and the 17 point inputs read at the default
+# knobs in FP32 (68 B); stages 0-2 write the accumulators (FP64 for u, v, w, t, FP32 for the 13 scalars:
+# 84 B) and the next increment (68 B), stages 1-3 read the accumulators; stage 3 reads y_n in FP64
+# (136 B) and writes y_{n+1} (136 B), rhs_u/v/w and aux_u/v/w (48 B).
+_MIX_IN = 72 + 68 + 36 + 68
+RK_BYTES_MIXED = (_MIX_IN + 84 + 68) + 2 * (_MIX_IN + 84 + 84 + 68) + (_MIX_IN + 84 + 136 + 136 + 48)
+RK_BYTES = {"fp64": RK_BYTES_FP64, "mixed": RK_BYTES_MIXED}
+KERNEL_NAME = {"fp64": "rk_stage_fp64_kernel (fused RHSSat + RK4 stage, FP64)",
+               "mixed": "rk_stage_mixed_kernel (fused RHSSat + RK4 stage, FP32 stencils / FP64 state)"}
 
 
 def cpu_baseline(g, P, seed, target_s=3.0):
@@ -214,24 +228,13 @@ def config(g, precision):
             "parallelism": "replicas"}
 
 
-def run_ours(a, rank, world):
-    from atsat_gb300 import abi, dyn, fields as F, synth
-    g = synth.make_grid(*a.shape)
-    P = abi.default_params()
-    cpu = None
-    if rank == 0 and world == 1 and not a.no_cpu_baseline:
-        cpu = cpu_baseline(g, P, seed=0)          # before the first CUDA call
-    st = synth.saturn_state(g, P, seed=rank)
-
-    # pinned host copies of every field, bound to the handle (the e2e leg copies from them)
-    pinned = {}
-    d = dyn.Dycore(g, P)
+def measure(a, rank, world, g, P, st, pinned, precision):
+    """Resident throughput, e2e throughput and the stage kernel's roofline of one precision."""
+    from atsat_gb300 import abi, dyn, fields as F
+    d = dyn.Dycore(g, dict(P, precision=1 if precision == "mixed" else 0))
     for fid in range(F.NFIELDS):
-        pa = dyn.PinnedArray(g.shape)
-        src = st.arrays.get(fid)
-        pa.array[...] = 0.0 if src is None else src
-        pinned[fid] = pa
-        d.bind(fid, pa.array)
+        pinned[fid].array[...] = 0.0 if st.arrays.get(fid) is None else st.arrays[fid]
+        d.bind(fid, pinned[fid].array)
     d.upload(list(range(F.NFIELDS)))
     d.set_tables(st.cell_vbar0, st.cell_ubar0, st.p_baro)
 
@@ -281,23 +284,44 @@ def run_ours(a, rank, world):
            "steps": a.e2e_steps, "ms_per_step": e2e_s * 1e3 / a.e2e_steps}
 
     peak, peak_kind = peaks()
-    bytes_per_launch = RK_WORDS_PER_CELL / 4 * 8 * interior_rk(g)
+    bytes_per_launch = RK_BYTES[precision] / 4 * interior_rk(g)
     avg_ms = ms_rk / max(n_rk, 1)
     achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9
-    roof = {"kernel": "rk_stage_fp64 (fused RHSSat + RK4 stage)", "bound": "hbm", "achieved": achieved,
+    roof = {"kernel": KERNEL_NAME[precision], "bound": "hbm", "achieved": achieved,
             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-            "traffic": traffic_per_launch("rk_stage_fp64"), "algorithmic_bytes_per_launch": bytes_per_launch,
-            "launches": n_rk, "mean_launch_ms": avg_ms,
-            "note": "FP64 path: bound by the FP64 pipe, not HBM (see DESIGN.md)"}
+            "traffic": traffic_per_launch("rk_stage_" + precision), "algorithmic_bytes_per_launch": bytes_per_launch,
+            "launches": n_rk, "mean_launch_ms": avg_ms}
+    if precision == "fp64":
+        roof["note"] = "bound by GB300's FP64 pipe (2 DFMA per SM per cycle), not by HBM"
     d.close()
+    return {"value": value, "ms_per_step": ms / a.steps, "e2e": e2e, "roofline": roof, "gpu_launches": launches,
+            "clocks": clk, "kernels_ms": kern}
+
+
+def run_ours(a, rank, world):
+    from atsat_gb300 import abi, dyn, fields as F, synth
+    g = synth.make_grid(*a.shape)
+    P = abi.default_params()
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        cpu = cpu_baseline(g, P, seed=0)          # before the first CUDA call
+    st = synth.saturn_state(g, P, seed=rank)
+    pinned = {fid: dyn.PinnedArray(g.shape) for fid in range(F.NFIELDS)}
+    res = {p: measure(a, rank, world, g, P, st, pinned, p) for p in a.precisions}
     for pa in pinned.values():
         pa.free()
     if rank != 0:
         return None
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
-           "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(g, "fp64"),
-           "e2e": e2e, "roofline": roof, "gpu_launches": launches, "clocks": clk, "kernels_ms": kern}
+    head = a.precisions[0]
+    r = res[head]
+    out = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
+           "warmup": a.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64" if head == "mixed" else "f64", "data": "synthetic",
+           "config": config(g, head), "e2e": r["e2e"], "roofline": r["roofline"],
+           "gpu_launches": r["gpu_launches"], "clocks": r["clocks"], "kernels_ms": r["kernels_ms"]}
+    for p in a.precisions[1:]:
+        out[p] = {k: res[p][k] for k in ("value", "ms_per_step", "e2e", "roofline", "gpu_launches", "clocks")}
+        out["mixed_over_" + p] = r["value"] / res[p]["value"]
     if cpu:
         out["cpu_baseline"] = cpu
     return out
