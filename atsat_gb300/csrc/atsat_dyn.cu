@@ -71,8 +71,16 @@ struct atsat_dyn {
 
     // mixed precision: FP32 copy of y_n, two FP32 increment buffers, FP32 copies of the point inputs
     float* slab32 = nullptr;
-    float* yn32[NPROG] = {};
+    float* yn32[NPROG] = {};             // FP32 copy of y_n read by this step's stencils
     float* wlo = nullptr;
+    float* yo32[NPROG] = {};             // the other copy: receives y_{n+1} in a resident run
+    float* wlo_o = nullptr;
+    // Resident mixed runs (atsat_dyn_iterate): the live and n-level FP64 fields share one buffer
+    // (restoreVar makes them equal and the mixed stages never write the live fields before the final
+    // update, which reads y_n only at the cell it writes), and the FP32 copies are swapped, not rebuilt.
+    bool aliased = false;
+    bool shadow_valid = false;
+    double* spare_n[NPROG] = {};
     float* dlA[NPROG] = {};
     float* dlB[NPROG] = {};
     float* acc32[NPROG - 4] = {};
@@ -471,10 +479,10 @@ int do_metric(atsat_dyn* h) {
     return ATSAT_DYN_OK;
 }
 
-int enqueue_rk4_mixed(atsat_dyn* h);
+int enqueue_rk4_mixed(atsat_dyn* h, bool resident);
 
-int enqueue_rk4(atsat_dyn* h) {
-    if (h->p.precision == ATSAT_DYN_MIXED) return enqueue_rk4_mixed(h);
+int enqueue_rk4(atsat_dyn* h, bool resident = false) {
+    if (h->p.precision == ATSAT_DYN_MIXED) return enqueue_rk4_mixed(h, resident);
     int rc;
     if ((rc = do_level_mean(h))) return rc;
     if (h->p.metric_split && (rc = do_metric(h))) return rc;
@@ -537,15 +545,15 @@ MixedIO make_mixed_io(atsat_dyn* h, float* const* dl_in, float* const* dl_out, d
 
 // Once per RK step: yn32 / wlo <- y_n (`base`), dl_0 <- live - y_n when asked, the dirty FP32 input
 // copies, and the frozen FP64 momentum terms.
-int enqueue_mixed_prepare(atsat_dyn* h, double* const* base, bool with_dl0) {
+int enqueue_mixed_prepare(atsat_dyn* h, double* const* base, bool with_dl0, bool resident) {
     MixedPrep pr{};
-    pr.write_yn32 = 1;
+    pr.write_yn32 = resident ? 0 : 1;
     for (int q = 0; q < NPROG; q++) {
         pr.yn64[q] = base[q];
         pr.live64[q] = h->f[q];
         pr.yn32[q] = h->yn32[q];
         pr.yn32_b[q] = nullptr;
-        pr.dl0[q] = with_dl0 ? h->dlB[q] : nullptr;
+        pr.dl0[q] = (with_dl0 && !resident) ? h->dlB[q] : nullptr;
     }
     pr.wlo = h->wlo;
     pr.wlo_b = nullptr;
@@ -571,14 +579,27 @@ int enqueue_mixed_prepare(atsat_dyn* h, double* const* base, bool with_dl0) {
     return ATSAT_DYN_OK;
 }
 
-int enqueue_rk4_mixed(atsat_dyn* h) {
+// resident: called from atsat_dyn_iterate, which keeps the FP32 copies of the next y_n up to date and
+// ends each iteration with the live and n-level fields equal.
+int enqueue_rk4_mixed(atsat_dyn* h, bool resident) {
     int rc;
     if ((rc = do_level_mean(h))) return rc;
     if (h->p.metric_split && (rc = do_metric(h))) return rc;
     double* yn[NPROG];
     double* L[NPROG];
     for (int q = 0; q < NPROG; q++) { yn[q] = h->f[ATSAT_F_N_BASE + q]; L[q] = h->f[q]; }
-    if ((rc = enqueue_mixed_prepare(h, yn, true))) return rc;
+    const bool fast = resident && h->aliased && h->shadow_valid;
+    if ((rc = enqueue_mixed_prepare(h, yn, true, fast))) return rc;
+    if (resident && !fast) {
+        // the copies of y_{n+1} start as (float) live: cells the step and the BCs leave alone keep them
+        MixedPrep pr{};
+        pr.write_yn32 = 1;
+        for (int q = 0; q < NPROG; q++) { pr.yn64[q] = L[q]; pr.live64[q] = L[q]; pr.yn32[q] = h->yo32[q]; }
+        pr.wlo = h->wlo_o;
+        pr.skip_frozen = 1;
+        CK(h, launch_mixed_prepare(h->kc, pr, h->stream));
+        h->launches += 1;
+    }
     const double dt = h->p.dt;
     for (int stage = 0; stage < 4; stage++) {
         StageParams sp{};
@@ -590,7 +611,12 @@ int enqueue_rk4_mixed(atsat_dyn* h) {
         // dl_0 sits in B; stage 0: B -> A, 1: A -> B, 2: B -> A, 3 reads A
         float* const* in = (stage == 1 || stage == 3) ? h->dlA : h->dlB;
         float* const* out = (stage == 1) ? h->dlB : h->dlA;
-        MixedIO io = make_mixed_io(h, in, stage == 3 ? nullptr : out, stage == 3 ? L : nullptr);
+        MixedIO io = make_mixed_io(h, (stage == 0 && fast) ? nullptr : in, stage == 3 ? nullptr : out,
+                                   stage == 3 ? L : nullptr);
+        if (stage == 3 && resident) {
+            for (int q = 0; q < NPROG; q++) io.out32[q] = h->yo32[q];
+            io.wlo_out = h->wlo_o;
+        }
         Timed t(h, ATSAT_K_RK_STAGE);
         CK(h, launch_rk_stage_mixed(h->kf, io, sp, stage == 3 ? MODE_FINAL : MODE_STAGE, h->stream));
         h->launches += 1;
@@ -629,18 +655,57 @@ int enqueue_pressure(atsat_dyn* h, int sweeps) {
     return ATSAT_DYN_OK;
 }
 
-int enqueue_restore(atsat_dyn* h) {
+// restoreVar. In a resident mixed run the n-level fields become aliases of the live ones (no copy)
+// and the FP32 copy of y_{n+1} becomes the next step's copy of y_n.
+int enqueue_restore(atsat_dyn* h, bool resident = false) {
     Timed t(h, ATSAT_K_GLUE);
     const size_t bytes = (size_t)h->kc.fsz * 8;
-    for (int q = 0; q < NPROG; q++)
-        CK(h, cudaMemcpyAsync(h->f[ATSAT_F_N_BASE + q], h->f[q], bytes, cudaMemcpyDeviceToDevice, h->stream));
+    if (resident && h->p.precision == ATSAT_DYN_MIXED) {
+        if (!h->aliased) {
+            for (int q = 0; q < NPROG; q++) {
+                h->spare_n[q] = h->f[ATSAT_F_N_BASE + q];
+                h->f[ATSAT_F_N_BASE + q] = h->f[q];
+            }
+            h->aliased = true;
+            // both FP32 copies must agree on the cells no step or boundary pass writes
+            const size_t b32 = (size_t)h->kc.fsz * 4;
+            for (int q = 0; q < NPROG; q++)
+                CK(h, cudaMemcpyAsync(h->yn32[q], h->yo32[q], b32, cudaMemcpyDeviceToDevice, h->stream));
+            CK(h, cudaMemcpyAsync(h->wlo, h->wlo_o, b32, cudaMemcpyDeviceToDevice, h->stream));
+        }
+        for (int q = 0; q < NPROG; q++) std::swap(h->yn32[q], h->yo32[q]);
+        std::swap(h->wlo, h->wlo_o);
+        h->shadow_valid = true;
+    } else {
+        for (int q = 0; q < NPROG; q++)
+            CK(h, cudaMemcpyAsync(h->f[ATSAT_F_N_BASE + q], h->f[q], bytes, cudaMemcpyDeviceToDevice, h->stream));
+    }
     CK(h, cudaMemcpyAsync(h->f[ATSAT_F_P_DYNN], h->f[ATSAT_F_P_DYN], bytes, cudaMemcpyDeviceToDevice, h->stream));
     return ATSAT_DYN_OK;
 }
 
-int enqueue_bc(atsat_dyn* h) {
+// Give the n-level fields their own buffers again (a copy of the shared values) before any call that
+// can observe the live and n-level fields separately.
+int unalias(atsat_dyn* h) {
+    if (!h->aliased) return ATSAT_DYN_OK;
+    const size_t bytes = (size_t)h->kc.fsz * 8;
+    for (int q = 0; q < NPROG; q++) {
+        CK(h, cudaMemcpyAsync(h->spare_n[q], h->f[q], bytes, cudaMemcpyDeviceToDevice, h->stream));
+        h->f[ATSAT_F_N_BASE + q] = h->spare_n[q];
+    }
+    h->aliased = false;
+    h->shadow_valid = false;
+    return ATSAT_DYN_OK;
+}
+
+int enqueue_bc(atsat_dyn* h, bool resident = false) {
     Timed t(h, ATSAT_K_GLUE);
-    CK(h, launch_boundary_conditions(h->kc, h->p, h->f, h->stream));
+    float* s32[ATSAT_NFIELDS] = {};
+    const bool shadows = resident && h->p.precision == ATSAT_DYN_MIXED;
+    if (shadows)
+        for (int q = 0; q < NPROG; q++) s32[q] = h->yo32[q];
+    CK(h, launch_boundary_conditions(h->kc, h->p, h->f, shadows ? s32 : nullptr, shadows ? h->wlo_o : nullptr,
+                                     h->stream));
     h->launches += 3;
     for (int fid : {ATSAT_F_NUE, ATSAT_F_MASSFLUX_H2S, ATSAT_F_MASSFLUX_NH3, ATSAT_F_MASSFLUX_NH4SH,
                     ATSAT_F_FLUXLIM_NH4SH, ATSAT_F_THERMALMASSFLUX})
@@ -798,12 +863,14 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
     h->geo = reinterpret_cast<ColGeo*>(q);
     if (p->precision == ATSAT_DYN_MIXED) {
         const size_t ngeo = ((size_t)K.im * K.jm * sizeof(ColGeoF) + 4095) / 4 + 1024;
-        const size_t n32 = (size_t)(3 * NPROG + 1 + (NPROG - 4) + NFZ + NCONV) * K.fsz + ngeo;
+        const size_t n32 = (size_t)(4 * NPROG + 2 + (NPROG - 4) + NFZ + NCONV) * K.fsz + ngeo;
         if ((e = cudaMalloc(&h->slab32, n32 * 4)) != cudaSuccess) return cuda_fail(e, "cudaMalloc (FP32)");
         if ((e = cudaMemsetAsync(h->slab32, 0, n32 * 4, h->stream)) != cudaSuccess) return cuda_fail(e, "cudaMemset");
         float* r = h->slab32;
         for (int s = 0; s < NPROG; s++) { h->yn32[s] = r; r += K.fsz; }
         h->wlo = r; r += K.fsz;
+        for (int s = 0; s < NPROG; s++) { h->yo32[s] = r; r += K.fsz; }
+        h->wlo_o = r; r += K.fsz;
         for (int s = 0; s < NPROG; s++) { h->dlA[s] = r; r += K.fsz; }
         for (int s = 0; s < NPROG; s++) { h->dlB[s] = r; r += K.fsz; }
         for (int s = 0; s < NPROG - 4; s++) { h->acc32[s] = r; r += K.fsz; }
@@ -878,6 +945,12 @@ int atsat_dyn_bind_host_array(atsat_dyn_t h, int32_t field, double* base) {
 int atsat_dyn_upload(atsat_dyn_t h, const int32_t* fields, int32_t n) {
     if (!h || !h->slab || (n > 0 && !fields)) return ATSAT_DYN_E_INVALID;
     CK(h, cudaSetDevice(h->device));
+    for (int32_t q = 0; q < n; q++)
+        if (fields[q] >= 0 && fields[q] < ATSAT_F_N_BASE + NPROG) {
+            int rc = unalias(h);
+            if (rc) return rc;
+            break;
+        }
     for (int32_t q = 0; q < n; q++) {
         if (!valid_field(fields[q])) return fail(h, ATSAT_DYN_E_INVALID, "bad field %d", fields[q]);
         int rc = upload_one(h, fields[q]);
@@ -951,10 +1024,11 @@ int atsat_dyn_metric_pressure(atsat_dyn_t h) {
 
 int atsat_dyn_rhs(atsat_dyn_t h) {
     ENTRY(h);
+    { int rc0 = unalias(h); if (rc0) return rc0; }
     double* L[NPROG];
     for (int q = 0; q < NPROG; q++) L[q] = h->f[q];
     if (h->p.precision == ATSAT_DYN_MIXED) {
-        int rc = enqueue_mixed_prepare(h, L, false);       // the stencils read the live fields
+        int rc = enqueue_mixed_prepare(h, L, false, false);   // the stencils read the live fields
         if (rc) return rc;
         MixedIO io = make_mixed_io(h, nullptr, nullptr, nullptr);
         for (int q = 0; q < NPROG; q++) io.yn64[q] = L[q];
@@ -978,6 +1052,7 @@ int atsat_dyn_rhs(atsat_dyn_t h) {
 
 int atsat_dyn_rk4_step(atsat_dyn_t h) {
     ENTRY(h);
+    { int rc0 = unalias(h); if (rc0) return rc0; }
     int rc = enqueue_rk4(h);
     return rc ? rc : finish(h);
 }
@@ -1011,12 +1086,14 @@ int atsat_dyn_pressure(atsat_dyn_t h, atsat_dyn_pstats* out) {
 
 int atsat_dyn_restore_var(atsat_dyn_t h) {
     ENTRY(h);
+    { int rc0 = unalias(h); if (rc0) return rc0; }
     int rc = enqueue_restore(h);
     return rc ? rc : finish(h);
 }
 
 int atsat_dyn_boundary_conditions(atsat_dyn_t h) {
     ENTRY(h);
+    { int rc0 = unalias(h); if (rc0) return rc0; }
     int rc = enqueue_bc(h);
     return rc ? rc : finish(h);
 }
@@ -1036,9 +1113,9 @@ int atsat_dyn_iterate(atsat_dyn_t h, int32_t iter0, int32_t n) {
             }
             if ((rc = enqueue_pressure(h, h->p.press_sweeps > 0 ? h->p.press_sweeps : 1))) return rc;
         }
-        if ((rc = enqueue_rk4(h))) return rc;
-        if ((rc = enqueue_bc(h))) return rc;
-        if ((rc = enqueue_restore(h))) return rc;
+        if ((rc = enqueue_rk4(h, true))) return rc;
+        if ((rc = enqueue_bc(h, true))) return rc;
+        if ((rc = enqueue_restore(h, true))) return rc;
     }
     return finish(h);
 }

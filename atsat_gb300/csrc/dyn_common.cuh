@@ -156,6 +156,7 @@ struct MixedIO {
 
 struct MixedPrep {
     int write_yn32;
+    int skip_frozen;               // conversions only
     const double* yn64[NPROG];
     const double* live64[NPROG];
     float* yn32[NPROG];
@@ -209,8 +210,9 @@ cudaError_t launch_press_sweep(const KConst& kc, const ColGeo* geo, const double
 cudaError_t launch_press_boundary(const KConst& kc, double* p, cudaStream_t s);
 cudaError_t launch_copy_fields(const KConst& kc, double* const* dst, const double* const* src, int n,
                                cudaStream_t s);
+// s32 (may be null): FP32 copies to keep in step, indexed by field id; wlo: the second FP32 word of w.
 cudaError_t launch_boundary_conditions(const KConst& kc, const atsat_dyn_params& p, double* const* f,
-                                       cudaStream_t s);
+                                       float* const* s32, float* wlo, cudaStream_t s);
 cudaError_t launch_count_nonfinite(const KConst& kc, const double* x, unsigned long long* count,
                                    cudaStream_t s);
 

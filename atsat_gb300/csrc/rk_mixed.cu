@@ -332,6 +332,7 @@ __global__ void __launch_bounds__(256) mixed_prepare_kernel(const KConst K, cons
         }
     }
     for (int q = 0; q < pr.nconv; q++) pr.conv_dst[q][c] = (float)__ldg(pr.conv_src[q] + c);
+    if (pr.skip_frozen) return;
 
     const bool interior = (i >= 1 && i <= K.im - 2 && j >= 2 && j <= K.jm - 3 && k <= K.km - 2);
     if (!interior) return;

@@ -88,3 +88,39 @@ def test_mixed_live_differs_from_n():
     rep = drift(s.arrays, ref.arrays, F.PROG)
     for f in F.PROG:
         assert rep[F.NAMES[f]][0] <= 1e-6, (F.NAMES[f], rep[F.NAMES[f]])
+
+
+def test_mixed_resident_then_dropin_calls():
+    """A resident run (live and n-level fields sharing storage) interleaved with drop-in calls that
+    see them separately: iterate, upload a changed field, single RK4 step, iterate again."""
+    from atsat_gb300 import dyn
+    g, P, st = case((21, 91, 181), seed=53)
+    ref = st.copy()
+    s = st.copy()
+    with dyn.Dycore(g, dict(P, precision=1)) as d:
+        d.load_state(s)
+        d.iterate(1, 3)
+        oracle.steps(ref, P, 3)
+        d.download(ALL)
+        # the host changes the temperature between steps (as the physics block would) and re-uploads
+        s.arrays[F.T][...] *= 1.0 + 1e-4
+        ref.arrays[F.T][...] = s.arrays[F.T]
+        d.upload([F.T])
+        d.RungeKuttaSat()
+        oracle.rk4_step(ref, P)
+        d.download(ALL)
+        rep = drift(s.arrays, ref.arrays, F.PROG)
+        for f in F.PROG:
+            assert rep[F.NAMES[f]][0] <= 1e-6, ("after rk4_step", F.NAMES[f], rep[F.NAMES[f]])
+        assert np.array_equal(s.arrays[F.TN], ref.arrays[F.TN] * 0 + s.arrays[F.TN])
+        # the host's boundary conditions and restoreVar, then more resident iterations
+        oracle.boundary_conditions(ref, P)
+        oracle.restore_var(ref, P)
+        d.boundary_conditions()
+        d.restoreVar()
+        d.iterate(4, 4)
+        oracle.steps(ref, P, 4, iter0=4)
+        d.download(ALL)
+    rep = drift(s.arrays, ref.arrays, F.PROG + F.PROG_N + [F.P_DYN])
+    bad = {k: v[0] for k, v in rep.items() if not v[0] <= TOL_MIXED}
+    assert not bad, bad
