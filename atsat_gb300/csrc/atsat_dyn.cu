@@ -317,6 +317,7 @@ void build_geometry(atsat_dyn* h, const double* vbar0, const double* ubar0) {
             c.p_exp_rm = 1.0;
             c.p_inv_rm = 1.0 / rm;
             c.p_inv_rmsinthe = 1.0 / (rm * sp);
+            c.p_pad_cot_rm = c.cotanthe * c.inv_rm;
         }
     }
 }
@@ -573,6 +574,7 @@ int enqueue_mixed_prepare(atsat_dyn* h, double* const* base, bool with_dl0, bool
     pr.rho_mix = h->f[ATSAT_F_RHO_MIX];
     pr.buoy = h->buoy;
     pr.geo = h->geo;
+    pr.bnum = (h->p.buoy_legacy ? h->p.buoyancy * h->p.g : h->p.g) / (h->kc.rR * h->p.t_ref);
     Timed t(h, ATSAT_K_GLUE);
     CK(h, launch_mixed_prepare(h->kc, pr, h->stream));
     h->launches += 1;
@@ -701,15 +703,20 @@ int unalias(atsat_dyn* h) {
 int enqueue_bc(atsat_dyn* h, bool resident = false) {
     Timed t(h, ATSAT_K_GLUE);
     float* s32[ATSAT_NFIELDS] = {};
-    const bool shadows = resident && h->p.precision == ATSAT_DYN_MIXED;
+    const bool mixed = h->p.precision == ATSAT_DYN_MIXED;
+    const bool shadows = resident && mixed;
     if (shadows)
         for (int q = 0; q < NPROG; q++) s32[q] = h->yo32[q];
-    CK(h, launch_boundary_conditions(h->kc, h->p, h->f, shadows ? s32 : nullptr, shadows ? h->wlo_o : nullptr,
+    // the FP32 copies of the point inputs the boundary passes write are refreshed in the same threads
+    // when they are current; otherwise they are rebuilt before the next step
+    const int bc_inputs[6] = {ATSAT_F_NUE, ATSAT_F_MASSFLUX_H2S, ATSAT_F_MASSFLUX_NH3, ATSAT_F_MASSFLUX_NH4SH,
+                              ATSAT_F_FLUXLIM_NH4SH, ATSAT_F_THERMALMASSFLUX};
+    if (mixed)
+        for (int fid : bc_inputs)
+            if (!h->conv_dirty[conv_slot(fid)]) s32[fid] = h->conv32[conv_slot(fid)];
+    CK(h, launch_boundary_conditions(h->kc, h->p, h->f, mixed ? s32 : nullptr, shadows ? h->wlo_o : nullptr,
                                      h->stream));
     h->launches += 3;
-    for (int fid : {ATSAT_F_NUE, ATSAT_F_MASSFLUX_H2S, ATSAT_F_MASSFLUX_NH3, ATSAT_F_MASSFLUX_NH4SH,
-                    ATSAT_F_FLUXLIM_NH4SH, ATSAT_F_THERMALMASSFLUX})
-        mark_dirty(h, fid);
     return ATSAT_DYN_OK;
 }
 

@@ -28,7 +28,7 @@ struct alignas(16) ColGeo {
     double sinthe_true, cent_rad, cent_the, vbar0;
     double ubar0, p_num1, p_num2, p_num3;            // sweep weights
     double p_den, lc_num1, lc_num2, lc_num3;         // sweep denominator, lc_old weights
-    double p_exp_rm, p_inv_rm, p_inv_rmsinthe, pad0; // divergence-source factors (solver's sine table)
+    double p_exp_rm, p_inv_rm, p_inv_rmsinthe, p_pad_cot_rm; // divergence-source factors; cot / rm
 };
 static_assert(sizeof(ColGeo) == 32 * 8, "ColGeo layout");
 
@@ -174,6 +174,7 @@ struct MixedPrep {
     const double* rho_mix;
     const double* buoy;
     const ColGeo* geo;
+    double bnum;                   // g / (r_mix R_mix t_ref), or buoyancy g / (r_mix R_mix t_ref) legacy
 };
 
 enum StageMode {

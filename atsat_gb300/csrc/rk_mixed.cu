@@ -340,41 +340,52 @@ __global__ void __launch_bounds__(256) mixed_prepare_kernel(const KConst K, cons
     const int ke = (k == K.km - 2) ? 0 : k + 1;
     const int64_t cw = c - k + kw, ce = c - k + ke;
     const ColGeo* g = pr.geo + ((int64_t)i * K.jm + j);
+    // FP64 work is kept to the sums that cancel: every constant product comes from the host, and the
+    // one reciprocal (1/t) is an FP32 estimate refined by one Newton step in FP64 (relative error
+    // ~1e-14, far below what the FP32 storage of the result keeps).
     const double inv_rm = __ldg(&g->inv_rm), inv_rmsinthe = __ldg(&g->inv_rmsinthe);
     const double* p = pr.p_dyn;
     const double dpdr = (__ldg(p + c + P) - __ldg(p + c - P)) * K.inv_2dr;
-    const double dpdthe = (__ldg(p + c + kp) - __ldg(p + c - kp)) * K.inv_2dthe;
-    const double dpdphi = (__ldg(p + ce) - __ldg(p + cw)) * K.inv_2dphi;
+    const double dpdthe = (__ldg(p + c + kp) - __ldg(p + c - kp)) * (K.inv_2dthe * inv_rm);
+    const double dpdphi = (__ldg(p + ce) - __ldg(p + cw)) * (K.inv_2dphi * inv_rmsinthe);
     double dpmdthe = 0.0, dpmdphi = 0.0;
     if (K.metric_split) {
-        dpmdthe = (__ldg(pr.p_metric + c + kp) - __ldg(pr.p_metric + c - kp)) * K.inv_2dthe;
-        dpmdphi = (__ldg(pr.p_metric + ce) - __ldg(pr.p_metric + cw)) * K.inv_2dphi;
+        dpmdthe = (__ldg(pr.p_metric + c + kp) - __ldg(pr.p_metric + c - kp)) * (K.inv_2dthe * inv_rm);
+        dpmdphi = (__ldg(pr.p_metric + ce) - __ldg(pr.p_metric + cw)) * (K.inv_2dphi * inv_rmsinthe);
     }
-    double dps = 0.0;
+    // the adiabatic term only enters rhs_t's small compression work: FP32 after the FP64 difference
+    float dps = 0.0f;
     if (K.adiabatic) {
-        dps = (__ldg(pr.p_stat + c + P) - __ldg(pr.p_stat + c - P)) * K.inv_2dr * K.to_nd;
-        const double rho_l = __ldg(pr.rho_mix + c);
-        if (K.adiabatic_rho && rho_l > 0.0 && isfinite(rho_l)) dps *= K.r_mix / rho_l;
+        dps = (float)(__ldg(pr.p_stat + c + P) - __ldg(pr.p_stat + c - P)) * (float)(K.inv_2dr * K.to_nd);
+        const float rho_l = (float)__ldg(pr.rho_mix + c);
+        if (K.adiabatic_rho && rho_l > 0.0f && isfinite(rho_l)) dps *= (float)K.r_mix / rho_l;
     }
     const double t = __ldg(pr.yn64[ATSAT_F_T] + c);
     const double ps = __ldg(pr.p_stat + c);
     // buoyancy: numerator B p (so that b = B p / t) and the anomaly at t_n
-    double bps, ban = 0.0;
-    if (K.buoy_legacy) bps = K.legacy_buoy * (ps + __ldg(p + c)) / (K.rR * K.t_ref);
-    else bps = K.g * ps / (K.rR * K.t_ref);
-    if (t > 0.0) ban = K.buoy_legacy ? bps / t : (bps / t - __ldg(pr.buoy + i));
+    const double bps = K.buoy_legacy ? (ps + __ldg(p + c)) * pr.bnum : ps * pr.bnum;
+    double ban = 0.0;
+    if (t > 0.0) {
+        double r = (double)(1.0f / (float)t);
+        r = r * (2.0 - t * r);
+        ban = K.buoy_legacy ? bps * r : (bps * r - __ldg(pr.buoy + i));
+    }
     // frozen parts of rhs_u, rhs_v, rhs_w at y_n (RHS_Sat_Turb.cpp:310-350, 388-399, 780-835)
-    const double wn = __ldg(pr.yn64[ATSAT_F_W] + c), vn = __ldg(pr.yn64[ATSAT_F_V] + c);
+    const double wn = __ldg(pr.yn64[ATSAT_F_W] + c);
     double gu = K.centrifugal * __ldg(&g->cent_rad);
-    if (!K.metric_split) gu -= K.metric_on * (vn * vn + wn * wn) * inv_rm;
-    gu -= K.cor_rad_on * K.Coriolis * (__ldg(&g->cor_rad) * wn);
-    const double gv = -dpmdthe * inv_rm + wn * wn * __ldg(&g->cotanthe) * inv_rm
-                    - K.Coriolis * (__ldg(&g->cor_the) * wn) + K.centrifugal * __ldg(&g->cent_the);
-    const double gw = -dpmdphi * inv_rmsinthe;
+    if (!K.metric_split) {
+        const double vn = __ldg(pr.yn64[ATSAT_F_V] + c);
+        gu -= K.metric_on * (vn * vn + wn * wn) * inv_rm;
+    }
+    if (K.cor_rad_on != 0.0) gu -= K.cor_rad_on * K.Coriolis * (__ldg(&g->cor_rad) * wn);
+    // w (w cot / r) - Coriolis cor_the w, the centrifugal and the p_metric gradient
+    const double gv = wn * (wn * __ldg(&g->p_pad_cot_rm) - K.Coriolis * __ldg(&g->cor_the)) - dpmdthe
+                    + K.centrifugal * __ldg(&g->cent_the);
+    const double gw = -dpmdphi;
     pr.fz[FZ_DPR][c] = (float)dpdr;
-    pr.fz[FZ_DPTH][c] = (float)(dpdthe * inv_rm);
-    pr.fz[FZ_DPPH][c] = (float)(dpdphi * inv_rmsinthe);
-    pr.fz[FZ_DPS][c] = (float)dps;
+    pr.fz[FZ_DPTH][c] = (float)dpdthe;
+    pr.fz[FZ_DPPH][c] = (float)dpdphi;
+    pr.fz[FZ_DPS][c] = dps;
     pr.fz[FZ_GU][c] = (float)gu;
     pr.fz[FZ_GV][c] = (float)gv;
     pr.fz[FZ_GW][c] = (float)gw;
