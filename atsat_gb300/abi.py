@@ -15,7 +15,7 @@ FP64, MIXED = 0, 1
 K_RK_STAGE, K_LEVEL_MEAN, K_METRIC_SCAN, K_PRESS_SOURCE, K_PRESS_SWEEP, K_PRESS_BOUNDARY, \
     K_GLUE, K_RHS = range(8)
 K_NAMES = ["rk_stage", "level_mean", "metric_scan", "press_source", "press_sweep",
-           "press_boundary", "glue", "rhs"]
+           "press_boundary", "glue", "rhs", "prepare"]
 
 
 class Grid(C.Structure):

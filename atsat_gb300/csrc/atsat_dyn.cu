@@ -14,6 +14,8 @@
 
 #include <omp.h>
 
+#include <cuda.h>
+
 #include "dyn_common.cuh"
 
 using namespace atsat;
@@ -46,7 +48,7 @@ struct atsat_dyn {
     double* partial = nullptr;
     double* buoy = nullptr;
     double* sin_j = nullptr;
-    double* rm_tab = nullptr;
+    double* rm_tab = nullptr;            // 1 / rm(i)
     double* cor_j = nullptr;
     ColGeo* geo = nullptr;
     double** six = nullptr;              // device array: aux_u, aux_v, aux_w, rhs_u, rhs_v, rhs_w
@@ -81,14 +83,25 @@ struct atsat_dyn {
     bool aliased = false;
     bool shadow_valid = false;
     double* spare_n[NPROG] = {};
+    // stage increments dl_1, dl_2, dl_3 (the stage-0 input live - y_n sits in C until stage 2)
     float* dlA[NPROG] = {};
     float* dlB[NPROG] = {};
-    float* acc32[NPROG - 4] = {};
+    float* dlC[NPROG] = {};
+    bool dl_edges_zero = false;          // the cells no stage writes hold 0 in A, B and C
+    float* acc_turb[2] = {};             // tke, dis: k1 + 2 k2 + 2 k3
     float* fz[NFZ] = {};
     float* conv32[NCONV] = {};
     bool conv_dirty[NCONV] = {};
+    int64_t n32 = 0;                     // FP32 arrays of fsz floats at the head of slab32
     ColGeoF* geof = nullptr;
+    PrepGeo* pgeo = nullptr;
     MixedConstF kf{};
+    // the TMA-tiled stage kernel: tensor maps over slab32; variant 1 = tiled, 0 = direct
+    TileMaps maps{};
+    bool tile_ok = false;
+    int variant = 1;
+    unsigned int* dev_err = nullptr;     // device status word of the bounded waits
+    int timeouts = 0;
     std::string err;
 };
 
@@ -366,9 +379,59 @@ cudaError_t upload_geof(atsat_dyn* h) {
         f.cor_rad_c = (float)(p.Coriolis * c.cor_rad);
         f.vbar0 = (float)c.vbar0; f.ubar0 = (float)c.ubar0;
     }
+    // the prepare kernel's column products, in FP64 (and the two pure scalings in FP32)
+    const KConst& K = h->kc;
+    std::vector<PrepGeo> pg(h->geo_h.size());
+    for (size_t n = 0; n < pg.size(); n++) {
+        const ColGeo& c = h->geo_h[n];
+        PrepGeo& g = pg[n];
+        g.s_the = K.inv_2dthe * c.inv_rm;
+        g.cot_rm = c.p_pad_cot_rm;
+        g.cor_the_c = K.Coriolis * c.cor_the;
+        g.cent_the_c = K.centrifugal * c.cent_the;
+        g.cent_rad_c = K.centrifugal * c.cent_rad;
+        g.cor_rad_c = K.cor_rad_on * K.Coriolis * c.cor_rad;
+        g.metric_inv_rm = K.metric_on * c.inv_rm;
+        g.s_the_f = (float)(K.inv_2dthe * c.inv_rm);
+        g.s_phi_f = (float)(K.inv_2dphi * c.inv_rmsinthe);
+    }
     cudaError_t e = cudaMemcpyAsync(h->geof, gf.data(), sizeof(ColGeoF) * gf.size(), cudaMemcpyHostToDevice, h->stream);
     if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(h->pgeo, pg.data(), sizeof(PrepGeo) * pg.size(), cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return e;
     return cudaStreamSynchronize(h->stream);
+}
+
+// The tiled stage kernel's tensor maps: slab32 as a 4-D FP32 tensor (k, j, i, array) with the strides
+// of the device layout; boxes of TILE_BX x TILE_BY x TILE_BZ (halo box) and TILE_SEAM_X x TILE_J x
+// TILE_I (seam column). Out-of-range parts of a box read as zero. false when the driver offers no
+// encoder or rejects the maps; the direct kernel runs then.
+bool make_tile_maps(atsat_dyn* h) {
+    using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult qr = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr) != cudaSuccess ||
+        qr != cudaDriverEntryPointSuccess || fn == nullptr) {
+        cudaGetLastError();
+        return false;
+    }
+    const KConst& K = h->kc;
+    if ((reinterpret_cast<uintptr_t>(h->slab32) & 15u) != 0) return false;
+    const cuuint64_t dims[4] = {(cuuint64_t)K.kp, (cuuint64_t)K.jm, (cuuint64_t)K.im, (cuuint64_t)h->n32};
+    const cuuint64_t strides[3] = {(cuuint64_t)K.kp * 4, (cuuint64_t)K.plane * 4, (cuuint64_t)K.fsz * 4};
+    const cuuint32_t box_main[4] = {TILE_BX, TILE_BY, TILE_BZ, 1};
+    const cuuint32_t box_seam[4] = {TILE_SEAM_X, TILE_J, TILE_I, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const Encode enc = reinterpret_cast<Encode>(fn);
+    const CUresult r1 = enc(reinterpret_cast<CUtensorMap*>(h->maps.main), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->slab32,
+                            dims, strides, box_main, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    const CUresult r2 = enc(reinterpret_cast<CUtensorMap*>(h->maps.seam), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->slab32,
+                            dims, strides, box_seam, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r1 == CUDA_SUCCESS && r2 == CUDA_SUCCESS;
 }
 
 bool valid_field(int f) { return f >= 0 && f < ATSAT_NFIELDS; }
@@ -430,6 +493,16 @@ int download_one(atsat_dyn* h, int fid) {
 int finish(atsat_dyn* h) {
     CK(h, cudaGetLastError());
     CK(h, cudaStreamSynchronize(h->stream));
+    if (h->dev_err && h->tile_ok) {
+        unsigned int v = 0;
+        CK(h, cudaMemcpy(&v, h->dev_err, sizeof(v), cudaMemcpyDeviceToHost));
+        if (v) {
+            CK(h, cudaMemset(h->dev_err, 0, sizeof(v)));
+            h->timeouts++;
+            return fail(h, ATSAT_DYN_E_TIMEOUT, "tiled stage kernel: device status 0x%x (1 producer wait, 2 consumer "
+                        "wait, 4 plan mismatch, 8 shared-memory alignment)", v);
+        }
+    }
     return ATSAT_DYN_OK;
 }
 
@@ -515,14 +588,16 @@ MixedIO make_mixed_io(atsat_dyn* h, float* const* dl_in, float* const* dl_out, d
         io.yn32[q] = h->yn32[q];
         io.dl_in[q] = dl_in ? dl_in[q] : nullptr;
         io.dl_out[q] = dl_out ? dl_out[q] : nullptr;
+        io.dl1[q] = h->dlA[q];
+        io.dl2[q] = h->dlB[q];
         io.out64[q] = out64 ? out64[q] : nullptr;
         io.out32[q] = nullptr;
         io.rhs[q] = h->f[ATSAT_F_RHS_BASE + q];
     }
     io.wlo = h->wlo;
     io.wlo_out = nullptr;
-    for (int q = 0; q < 4; q++) io.acc64[q] = h->acc[q];
-    for (int q = 0; q < NPROG - 4; q++) io.acc32[q] = h->acc32[q];
+    io.acc_turb[0] = h->acc_turb[0];
+    io.acc_turb[1] = h->acc_turb[1];
     for (int q = 0; q < NFZ; q++) io.fz[q] = h->fz[q];
     io.rho_mix = h->conv32[conv_slot(ATSAT_F_RHO_MIX)];
     io.nue = h->conv32[conv_slot(ATSAT_F_NUE)];
@@ -544,18 +619,23 @@ MixedIO make_mixed_io(atsat_dyn* h, float* const* dl_in, float* const* dl_out, d
     return io;
 }
 
-// Once per RK step: yn32 / wlo <- y_n (`base`), dl_0 <- live - y_n when asked, the dirty FP32 input
-// copies, and the frozen FP64 momentum terms.
+// Once per RK step: yn32 / wlo <- y_n (`base`), dl_0 <- live - y_n into all three increment buffers
+// when asked (the cells no stage writes keep Y_s = live at every stage), the dirty FP32 input copies,
+// and the frozen FP64 momentum terms.
 int enqueue_mixed_prepare(atsat_dyn* h, double* const* base, bool with_dl0, bool resident) {
     MixedPrep pr{};
     pr.write_yn32 = resident ? 0 : 1;
+    const bool dl0 = with_dl0 && !resident;
     for (int q = 0; q < NPROG; q++) {
         pr.yn64[q] = base[q];
         pr.live64[q] = h->f[q];
         pr.yn32[q] = h->yn32[q];
         pr.yn32_b[q] = nullptr;
-        pr.dl0[q] = (with_dl0 && !resident) ? h->dlB[q] : nullptr;
+        pr.dl0[0][q] = dl0 ? h->dlC[q] : nullptr;
+        pr.dl0[1][q] = dl0 ? h->dlA[q] : nullptr;
+        pr.dl0[2][q] = dl0 ? h->dlB[q] : nullptr;
     }
+    if (dl0) h->dl_edges_zero = false;
     pr.wlo = h->wlo;
     pr.wlo_b = nullptr;
     int n = 0;
@@ -573,12 +653,42 @@ int enqueue_mixed_prepare(atsat_dyn* h, double* const* base, bool with_dl0, bool
     pr.p_stat = h->f[ATSAT_F_P_STAT];
     pr.rho_mix = h->f[ATSAT_F_RHO_MIX];
     pr.buoy = h->buoy;
-    pr.geo = h->geo;
+    pr.pgeo = h->pgeo;
     pr.bnum = (h->p.buoy_legacy ? h->p.buoyancy * h->p.g : h->p.g) / (h->kc.rR * h->p.t_ref);
-    Timed t(h, ATSAT_K_GLUE);
+    pr.inv_2dr_f = (float)h->kc.inv_2dr;
+    pr.dps_scale_f = (float)(h->kc.inv_2dr * h->kc.to_nd);
+    pr.r_mix_f = (float)h->kc.r_mix;
+    Timed t(h, ATSAT_K_PREPARE);
     CK(h, launch_mixed_prepare(h->kc, pr, h->stream));
     h->launches += 1;
     return ATSAT_DYN_OK;
+}
+
+int32_t arr_index(const atsat_dyn* h, const float* p) { return (int32_t)((p - h->slab32) / h->kc.fsz); }
+
+// the arrays the tiled kernel streams, in the order it reads them: per field y_n, w's low word, the
+// increment; tke and dis only with turbulence on
+TilePlan make_plan(atsat_dyn* h, const MixedIO& io) {
+    TilePlan pl{};
+    pl.err = h->dev_err;
+    pl.arr_lo = arr_index(h, io.wlo);
+    int n = 0;
+    for (int q = 0; q < NPROG; q++) {
+        pl.arr_yn[q] = arr_index(h, io.yn32[q]);
+        pl.arr_dl[q] = io.dl_in[q] ? arr_index(h, io.dl_in[q]) : -1;
+        if ((q == ATSAT_F_TKE || q == ATSAT_F_DIS) && !h->kc.turb) continue;
+        pl.item[n++] = pl.arr_yn[q];
+        if (q == ATSAT_F_W) pl.item[n++] = pl.arr_lo;
+        if (io.dl_in[q]) pl.item[n++] = pl.arr_dl[q];
+    }
+    pl.n_items = n;
+    return pl;
+}
+
+cudaError_t launch_stage(atsat_dyn* h, const MixedIO& io, const StageParams& sp, int mode) {
+    if (mode != MODE_RHS && h->variant == 1 && h->tile_ok)
+        return launch_rk_tile(h->maps, h->kf, io, sp, make_plan(h, io), mode, h->stream);
+    return launch_rk_stage_mixed(h->kf, io, sp, mode, h->stream);
 }
 
 // resident: called from atsat_dyn_iterate, which keeps the FP32 copies of the next y_n up to date and
@@ -592,6 +702,11 @@ int enqueue_rk4_mixed(atsat_dyn* h, bool resident) {
     for (int q = 0; q < NPROG; q++) { yn[q] = h->f[ATSAT_F_N_BASE + q]; L[q] = h->f[q]; }
     const bool fast = resident && h->aliased && h->shadow_valid;
     if ((rc = enqueue_mixed_prepare(h, yn, true, fast))) return rc;
+    if (fast && !h->dl_edges_zero) {
+        // live == y_n: the cells no stage writes must hold a zero increment in A, B and C (contiguous)
+        CK(h, cudaMemsetAsync(h->dlA[0], 0, (size_t)3 * NPROG * h->kc.fsz * sizeof(float), h->stream));
+        h->dl_edges_zero = true;
+    }
     if (resident && !fast) {
         // the copies of y_{n+1} start as (float) live: cells the step and the BCs leave alone keep them
         MixedPrep pr{};
@@ -599,10 +714,15 @@ int enqueue_rk4_mixed(atsat_dyn* h, bool resident) {
         for (int q = 0; q < NPROG; q++) { pr.yn64[q] = L[q]; pr.live64[q] = L[q]; pr.yn32[q] = h->yo32[q]; }
         pr.wlo = h->wlo_o;
         pr.skip_frozen = 1;
+        Timed t(h, ATSAT_K_PREPARE);
         CK(h, launch_mixed_prepare(h->kc, pr, h->stream));
         h->launches += 1;
     }
     const double dt = h->p.dt;
+    // increments: stage 0 reads dl_0 (C; none when live == y_n) and writes dl_1 to A, stage 1: A -> B,
+    // stage 2: B -> C, the final stage reads C and the point values of A and B
+    float* const* ins[4] = {fast ? nullptr : h->dlC, h->dlA, h->dlB, h->dlC};
+    float* const* outs[4] = {h->dlA, h->dlB, h->dlC, nullptr};
     for (int stage = 0; stage < 4; stage++) {
         StageParams sp{};
         sp.stage = stage;
@@ -610,17 +730,16 @@ int enqueue_rk4_mixed(atsat_dyn* h, bool resident) {
         sp.c_in = (stage == 0 || stage == 1) ? 0.5 * dt : (stage == 2 ? dt : 0.0);
         sp.wgt = (stage == 0 || stage == 3) ? 1.0 : 2.0;
         sp.sixth_dt = dt / 6.0;
-        // dl_0 sits in B; stage 0: B -> A, 1: A -> B, 2: B -> A, 3 reads A
-        float* const* in = (stage == 1 || stage == 3) ? h->dlA : h->dlB;
-        float* const* out = (stage == 1) ? h->dlB : h->dlA;
-        MixedIO io = make_mixed_io(h, (stage == 0 && fast) ? nullptr : in, stage == 3 ? nullptr : out,
-                                   stage == 3 ? L : nullptr);
+        sp.c_in_f = (float)sp.c_in;
+        sp.wgt_f = (float)sp.wgt;
+        sp.sixth_dt_f = (float)sp.sixth_dt;
+        MixedIO io = make_mixed_io(h, ins[stage], outs[stage], stage == 3 ? L : nullptr);
         if (stage == 3 && resident) {
             for (int q = 0; q < NPROG; q++) io.out32[q] = h->yo32[q];
             io.wlo_out = h->wlo_o;
         }
         Timed t(h, ATSAT_K_RK_STAGE);
-        CK(h, launch_rk_stage_mixed(h->kf, io, sp, stage == 3 ? MODE_FINAL : MODE_STAGE, h->stream));
+        CK(h, launch_stage(h, io, sp, stage == 3 ? MODE_FINAL : MODE_STAGE));
         h->launches += 1;
     }
     return ATSAT_DYN_OK;
@@ -648,7 +767,7 @@ int enqueue_pressure(atsat_dyn* h, int sweeps) {
         for (int colour = 0; colour < 2; colour++) {
             Timed t(h, ATSAT_K_PRESS_SWEEP);
             CK(h, launch_press_sweep(K, h->geo, h->src, h->f[ATSAT_F_P_DYN], colour, h->stream));
-            h->launches += 1;
+            h->launches += ((K.km - 1) & 1) ? 2 : 1;     // odd km-1: the seam cells follow their partner
         }
         Timed t(h, ATSAT_K_PRESS_BOUNDARY);
         CK(h, launch_press_boundary(K, h->f[ATSAT_F_P_DYN], h->stream));
@@ -864,13 +983,17 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
     h->sin_j = q; q += K.jm;
     h->rm_tab = q; q += K.im;
     h->cor_j = q; q += K.jm;
-    h->counter = reinterpret_cast<unsigned long long*>(q); q += 8;
+    h->counter = reinterpret_cast<unsigned long long*>(q);
+    h->dev_err = reinterpret_cast<unsigned int*>(q + 1);
+    q += 8;
     h->six = reinterpret_cast<double**>(q); q += 8;
     q = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(q) + 255) & ~uintptr_t(255));
     h->geo = reinterpret_cast<ColGeo*>(q);
     if (p->precision == ATSAT_DYN_MIXED) {
-        const size_t ngeo = ((size_t)K.im * K.jm * sizeof(ColGeoF) + 4095) / 4 + 1024;
-        const size_t n32 = (size_t)(4 * NPROG + 2 + (NPROG - 4) + NFZ + NCONV) * K.fsz + ngeo;
+        // 118 arrays of fsz floats (the tensor maps' fourth dimension), then the two column tables
+        h->n32 = 2 * NPROG + 2 + 3 * NPROG + 2 + NFZ + NCONV;
+        const size_t ngeo = ((size_t)K.im * K.jm * (sizeof(ColGeoF) + sizeof(PrepGeo)) + 4095) / 4 + 1024;
+        const size_t n32 = (size_t)h->n32 * K.fsz + ngeo;
         if ((e = cudaMalloc(&h->slab32, n32 * 4)) != cudaSuccess) return cuda_fail(e, "cudaMalloc (FP32)");
         if ((e = cudaMemsetAsync(h->slab32, 0, n32 * 4, h->stream)) != cudaSuccess) return cuda_fail(e, "cudaMemset");
         float* r = h->slab32;
@@ -880,12 +1003,20 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
         h->wlo_o = r; r += K.fsz;
         for (int s = 0; s < NPROG; s++) { h->dlA[s] = r; r += K.fsz; }
         for (int s = 0; s < NPROG; s++) { h->dlB[s] = r; r += K.fsz; }
-        for (int s = 0; s < NPROG - 4; s++) { h->acc32[s] = r; r += K.fsz; }
+        for (int s = 0; s < NPROG; s++) { h->dlC[s] = r; r += K.fsz; }
+        h->dl_edges_zero = true;
+        for (int s = 0; s < 2; s++) { h->acc_turb[s] = r; r += K.fsz; }
         for (int s = 0; s < NFZ; s++) { h->fz[s] = r; r += K.fsz; }
         for (int s = 0; s < NCONV; s++) { h->conv32[s] = r; r += K.fsz; h->conv_dirty[s] = true; }
+        if (r != h->slab32 + h->n32 * K.fsz) return fail(h, ATSAT_DYN_E_INVALID, "FP32 slab layout");
         r = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(r) + 255) & ~uintptr_t(255));
         h->geof = reinterpret_cast<ColGeoF*>(r);
+        r += (size_t)K.im * K.jm * sizeof(ColGeoF) / 4;
+        r = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(r) + 255) & ~uintptr_t(255));
+        h->pgeo = reinterpret_cast<PrepGeo*>(r);
         if ((e = upload_geof(h)) != cudaSuccess) return cuda_fail(e, "FP32 geometry upload");
+        h->tile_ok = make_tile_maps(h);
+        if (const char* v = std::getenv("ATSAT_DYN_STAGE_VARIANT")) h->variant = std::atoi(v) == 0 ? 0 : 1;
     }
     // small host tables
     std::vector<double> sin_j(K.jm), rm_tab(K.im), cor_j(K.jm);
@@ -894,7 +1025,7 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
         sin_j[j] = std::sin(h->the_z[j]);
         cor_j[j] = p->coriolis_split ? p->Coriolis * nd * 2.0 * p->omega * std::fabs(std::sin(h->the_z[j])) : 0.0;
     }
-    for (int i = 0; i < K.im; i++) rm_tab[i] = metric_radius(*p, h->rad_z[i]);
+    for (int i = 0; i < K.im; i++) rm_tab[i] = 1.0 / metric_radius(*p, h->rad_z[i]);
     double* six_h[6] = {h->f[ATSAT_F_AUX_U], h->f[ATSAT_F_AUX_V], h->f[ATSAT_F_AUX_W],
                         h->f[ATSAT_F_RHS_U], h->f[ATSAT_F_RHS_V], h->f[ATSAT_F_RHS_W]};
     if ((e = cudaMemcpyAsync(h->sin_j, sin_j.data(), 8 * K.jm, cudaMemcpyHostToDevice, h->stream)) ||
@@ -1136,6 +1267,7 @@ int atsat_dyn_status(atsat_dyn_t h, atsat_dyn_diag* out) {
     if (!h || !out) return ATSAT_DYN_E_INVALID;
     memset(out, 0, sizeof(*out));
     out->launches = h->launches;
+    out->timeout = h->timeouts;
     return ATSAT_DYN_OK;
 }
 
@@ -1217,6 +1349,68 @@ int atsat_dyn_set_write_all_rhs(atsat_dyn_t h, int32_t on) {
     if (!h) return ATSAT_DYN_E_INVALID;
     h->write_all_rhs = on != 0;
     return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_set_stage_variant(atsat_dyn_t h, int32_t variant) {
+    if (!h) return ATSAT_DYN_E_INVALID;
+    if (variant != ATSAT_DYN_STAGE_DIRECT && variant != ATSAT_DYN_STAGE_TILED)
+        return fail(h, ATSAT_DYN_E_INVALID, "unknown stage variant %d", variant);
+    if (h->p.precision != ATSAT_DYN_MIXED)
+        return fail(h, ATSAT_DYN_E_UNSUPPORTED, "stage variants are a mixed-precision setting");
+    if (variant == ATSAT_DYN_STAGE_TILED && !h->tile_ok)
+        return fail(h, ATSAT_DYN_E_UNSUPPORTED, "tiled stage kernel unavailable (no tensor-map encoder)");
+    h->variant = variant;
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_get_stage_variant(atsat_dyn_t h, int32_t* variant) {
+    if (!h || !variant) return ATSAT_DYN_E_INVALID;
+    *variant = (h->p.precision == ATSAT_DYN_MIXED && h->variant == 1 && h->tile_ok) ? ATSAT_DYN_STAGE_TILED
+                                                                                  : ATSAT_DYN_STAGE_DIRECT;
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_autotune(atsat_dyn_t h, int32_t reps, int32_t* chosen, double ms[2]) {
+    ENTRY(h);
+    if (!chosen || !ms || reps < 1) return fail(h, ATSAT_DYN_E_INVALID, "autotune: bad arguments");
+    if (h->p.precision != ATSAT_DYN_MIXED)
+        return fail(h, ATSAT_DYN_E_UNSUPPORTED, "autotune applies to the mixed-precision stage kernel");
+    // stage 1 of a step: A -> B, the widest stage input (y_n, w's low word and the increments)
+    StageParams sp{};
+    sp.stage = 1;
+    sp.c_in = 0.5 * h->p.dt;
+    sp.wgt = 2.0;
+    sp.sixth_dt = h->p.dt / 6.0;
+    sp.c_in_f = (float)sp.c_in;
+    sp.wgt_f = (float)sp.wgt;
+    sp.sixth_dt_f = (float)sp.sixth_dt;
+    const MixedIO io = make_mixed_io(h, h->dlA, h->dlB, nullptr);
+    const int keep = h->variant;
+    cudaEvent_t ev[2];
+    CK(h, cudaEventCreate(&ev[0]));
+    CK(h, cudaEventCreate(&ev[1]));
+    int best = -1;
+    for (int v = 0; v < 2; v++) {
+        ms[v] = -1.0;
+        if (v == 1 && !h->tile_ok) continue;
+        h->variant = v;
+        for (int r = 0; r < 2 + reps; r++) {
+            if (r == 2) CK(h, cudaEventRecord(ev[0], h->stream));
+            CK(h, launch_stage(h, io, sp, MODE_STAGE));
+            h->launches += 1;
+        }
+        CK(h, cudaEventRecord(ev[1], h->stream));
+        CK(h, cudaEventSynchronize(ev[1]));
+        float t = 0.0f;
+        CK(h, cudaEventElapsedTime(&t, ev[0], ev[1]));
+        ms[v] = t / reps;
+        if (best < 0 || ms[v] < ms[best]) best = v;
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    h->variant = best >= 0 ? best : keep;
+    *chosen = h->variant;
+    return finish(h);
 }
 
 }  // extern "C"

@@ -16,6 +16,35 @@ namespace atsat {
 
 constexpr int NPROG = ATSAT_NPROG;
 
+// ---- binary32 <-> binary64 conversions on the integer pipe ----
+// GB300 runs F2F (float <-> double) on its FP64 pipe, two operations per SM per cycle like a DADD.
+// These rebuild the IEEE-754 encodings with integer operations for the common cases -- normal
+// numbers and zeros -- and defer to the hardware conversion for subnormals, infinities and NaNs.
+// Both give the hardware's bits (round to nearest even for the narrowing).
+__device__ __forceinline__ double f2d(float f) {
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t a = b & 0x7FFFFFFFu;
+    if (a - 0x00800000u < 0x7F000000u)            // biased exponent 1..254
+        return __longlong_as_double((long long)(((uint64_t)(b & 0x80000000u) << 32) |
+                                                (((uint64_t)a << 29) + (896ull << 52))));
+    if (a == 0u) return __longlong_as_double((long long)((uint64_t)b << 32));
+    return (double)f;
+}
+
+__device__ __forceinline__ float d2f(double d) {
+    const uint64_t b = (uint64_t)__double_as_longlong(d);
+    const uint32_t hi = (uint32_t)(b >> 32);
+    const uint32_t e = (hi >> 20) & 0x7FFu;
+    if (e - 897u < 254u) {                         // result exponent 1..254 before rounding
+        uint32_t q = ((e - 896u) << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu);
+        const uint32_t r = (uint32_t)b & 0x1FFFFFFFu;
+        q += (r > 0x10000000u || (r == 0x10000000u && (q & 1u))) ? 1u : 0u;   // a carry into 255 is inf
+        return __uint_as_float(q | (hi & 0x80000000u));
+    }
+    if ((b << 1) == 0) return __uint_as_float(hi & 0x80000000u);
+    return (float)d;
+}
+
 // Per-(i,j) metric factors of one column. The RK members follow the CellGeometry that
 // RungeKuttaSat builds (RungeKutta_Sat_Turb.cpp:223-243) plus the (i,j)-only products of RHSSat
 // (Coriolis / centrifugal coefficients, RHS_Sat_Turb.cpp:310-350; v_metric :436); the P members are
@@ -124,13 +153,18 @@ struct MixedConstF {
     double tke_max_d, dis_min_d;
 };
 
+// The stage increments are dl_s = c_in k_{s-1} (stage inputs Y_s = y_n + dl_s). Stages 0..2 write
+// dl_1 = dt/2 k1, dl_2 = dt/2 k2, dl_3 = dt k3, so that the final stage forms
+// y_{n+1} = y_n + (dl_1 + 2 dl_2 + dl_3) / 3 + dt/6 k4 without running sums; tke and dis, whose
+// increments are clamped, keep a running k1 + 2 k2 + 2 k3 instead.
 struct MixedIO {
     const float* yn32[NPROG];      // FP32 copy of y_n
     const float* wlo;              // y_n(w) - yn32(w)
     const float* dl_in[NPROG];     // stage increments; null entries: Y_s = y_n
-    float* dl_out[NPROG];
-    double* acc64[4];              // u, v, w, t
-    float* acc32[NPROG - 4];       // the 13 scalars
+    float* dl_out[NPROG];          // stages 0..2
+    const float* dl1[NPROG];       // final stage: dl_1 and dl_2
+    const float* dl2[NPROG];
+    float* acc_turb[2];            // tke, dis
     const double* yn64[NPROG];
     double* out64[NPROG];          // y_{n+1} (final stage)
     float* out32[NPROG];           // optional FP32 copy of y_{n+1}
@@ -154,6 +188,19 @@ struct MixedIO {
     const double* buoy;
 };
 
+// per-column constants of the prepare kernel (products formed on the host)
+struct alignas(16) PrepGeo {
+    double s_the;                  // inv_2dthe / rm
+    double cot_rm;                 // cot(theta) / rm
+    double cor_the_c;              // Coriolis * cor_the
+    double cent_the_c;             // centrifugal * cent_the
+    double cent_rad_c;             // centrifugal * cent_rad
+    double cor_rad_c;              // cor_rad_on * Coriolis * cor_rad
+    double metric_inv_rm;          // metric_on / rm
+    float s_the_f, s_phi_f;        // inv_2dthe / rm, inv_2dphi / (rm sin theta) in FP32
+};
+static_assert(sizeof(PrepGeo) == 64, "PrepGeo layout");
+
 struct MixedPrep {
     int write_yn32;
     int skip_frozen;               // conversions only
@@ -163,7 +210,7 @@ struct MixedPrep {
     float* yn32_b[NPROG];          // optional second copy
     float* wlo;
     float* wlo_b;
-    float* dl0[NPROG];             // null: not written
+    float* dl0[3][NPROG];          // live - y_n into each increment buffer (null: not written)
     const double* conv_src[NCONV];
     float* conv_dst[NCONV];
     int nconv;
@@ -173,8 +220,28 @@ struct MixedPrep {
     const double* p_stat;
     const double* rho_mix;
     const double* buoy;
-    const ColGeo* geo;
+    const PrepGeo* pgeo;
     double bnum;                   // g / (r_mix R_mix t_ref), or buoyancy g / (r_mix R_mix t_ref) legacy
+    float inv_2dr_f, dps_scale_f, r_mix_f;
+};
+
+// The TMA-tiled stage kernel: the FP32 arrays live in one slab at a fixed stride, addressed by a 4-D
+// tensor map (k, j, i, array); `item` lists the arrays the kernel streams, in the order it reads them.
+// A block integrates TILE_K x TILE_J x TILE_I cells (k, j, i); its box carries a halo of one cell in
+// j and i and of four in k (the tensor copy's innermost coordinate must be a multiple of 16 bytes).
+// The seam box fetches the periodic partner column (k = km-2 for k = 0, k = 0 for k = km-2) when the
+// main box does not hold it.
+constexpr int TILE_K = 32, TILE_J = 8, TILE_I = 2;
+constexpr int TILE_BX = TILE_K + 8, TILE_BY = TILE_J + 2, TILE_BZ = TILE_I + 2;
+constexpr int TILE_SEAM_X = 4;
+constexpr int TILE_MAX_ITEMS = 2 * NPROG + 1;
+struct TilePlan {
+    int n_items;
+    int item[TILE_MAX_ITEMS];
+    int arr_yn[NPROG];             // tensor-map array index of each stencil array (-1: absent)
+    int arr_dl[NPROG];
+    int arr_lo;
+    unsigned int* err;             // device status word: bit 0 producer wait, bit 1 consumer wait, bit 2 plan
 };
 
 enum StageMode {
@@ -187,6 +254,7 @@ struct StageParams {
     int stage;
     int write_all_rhs;
     double c_in, wgt, sixth_dt;
+    float c_in_f, wgt_f, sixth_dt_f;
 };
 
 // ---- kernel launchers (each returns cudaGetLastError()) ----
@@ -195,9 +263,14 @@ cudaError_t launch_rk_stage_fp64(const KConst& kc, const StageIO<double>& io, co
 cudaError_t launch_rk_stage_mixed(const MixedConstF& kf, const MixedIO& io, const StageParams& sp, int mode,
                                   cudaStream_t s);
 cudaError_t launch_mixed_prepare(const KConst& kc, const MixedPrep& pr, cudaStream_t s);
+// tensor maps are CUtensorMap objects (128 bytes), passed opaquely
+struct TileMaps { alignas(64) unsigned char main[128]; alignas(64) unsigned char seam[128]; };
+cudaError_t launch_rk_tile(const TileMaps& maps, const MixedConstF& kf, const MixedIO& io, const StageParams& sp,
+                           const TilePlan& plan, int mode, cudaStream_t s);
+size_t rk_tile_smem_bytes();
 cudaError_t launch_level_mean(const KConst& kc, const double* t, const double* p_stat,
                               const double* sin_j, double* partial, double* buoy, cudaStream_t s);
-cudaError_t launch_metric_scan(const KConst& kc, const double* v, const double* w, const double* rm_tab,
+cudaError_t launch_metric_scan(const KConst& kc, const double* v, const double* w, const double* inv_rm,
                                const double* cor_j, const double* p_baro, double* p_metric, cudaStream_t s);
 cudaError_t launch_density(const KConst& kc, const double* t, const double* p_stat, double R_mix,
                            double* rho, cudaStream_t s);

@@ -114,6 +114,22 @@ __global__ void __launch_bounds__(256) press_source_kernel(
 }
 
 // One colour of the red-black sweep (PressureSolver.h:318-495): cells with (i + j + k) & 1 == colour.
+// The reference visits a row's meridians in increasing k. Neighbours of one colour never touch except
+// across the periodic seam when km-1 is odd: then k = 0 and k = km-2 share a colour and km-2 reads
+// the value k = 0 received earlier in the same sweep. That cell waits for press_sweep_seam_kernel.
+__device__ __forceinline__ void sweep_cell(const KConst& K, const ColGeo* __restrict__ geo,
+                                           const double* __restrict__ src, double* __restrict__ p, int i, int j,
+                                           int k) {
+    const int64_t P = K.plane, kp = K.kp;
+    const int64_t c = ((int64_t)i * K.jm + j) * kp + k;
+    const int kw = (k == 0) ? K.km - 2 : k - 1;
+    const int ke = (k == K.km - 2) ? 0 : k + 1;
+    const ColGeo* g = geo + ((int64_t)i * K.jm + j);
+    const double acc = (p[c + P] + p[c - P]) * ldg(&g->p_num1) + (p[c + kp] + p[c - kp]) * ldg(&g->p_num2)
+                     + (p[c - k + ke] + p[c - k + kw]) * ldg(&g->p_num3);
+    p[c] = (acc - ldg(src + c)) / ldg(&g->p_den);
+}
+
 __global__ void __launch_bounds__(256) press_sweep_kernel(const KConst K, const ColGeo* __restrict__ geo,
                                                           const double* __restrict__ src, double* __restrict__ p,
                                                           int colour) {
@@ -123,14 +139,19 @@ __global__ void __launch_bounds__(256) press_sweep_kernel(const KConst K, const 
     if (j < 1 || j > K.jm - 2 || i < 1 || i > K.im - 2) return;
     const int k = 2 * m + ((colour - i - j) & 1);
     if (k > K.km - 2) return;
-    const int64_t P = K.plane, kp = K.kp;
-    const int64_t c = ((int64_t)i * K.jm + j) * kp + k;
-    const int kw = (k == 0) ? K.km - 2 : k - 1;
-    const int ke = (k == K.km - 2) ? 0 : k + 1;
-    const ColGeo* g = geo + ((int64_t)i * K.jm + j);
-    const double acc = (p[c + P] + p[c - P]) * ldg(&g->p_num1) + (p[c + kp] + p[c - kp]) * ldg(&g->p_num2)
-                     + (p[c - k + ke] + p[c - k + kw]) * ldg(&g->p_num3);
-    p[c] = (acc - ldg(src + c)) / ldg(&g->p_den);
+    if (k == K.km - 2 && k > 0 && ((K.km - 1) & 1)) return;      // after its seam partner
+    sweep_cell(K, geo, src, p, i, j, k);
+}
+
+__global__ void __launch_bounds__(256) press_sweep_seam_kernel(const KConst K, const ColGeo* __restrict__ geo,
+                                                               const double* __restrict__ src,
+                                                               double* __restrict__ p, int colour) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = 1 + e / (K.jm - 2), j = 1 + e % (K.jm - 2);
+    if (i > K.im - 2) return;
+    const int k = K.km - 2;
+    if (((i + j + k) & 1) != colour) return;
+    sweep_cell(K, geo, src, p, i, j, k);
 }
 
 // Neumann planes i = 0, im-1 (all j), then j = 0, jm-1 (all i), then the seam copy -- composed per
@@ -214,6 +235,10 @@ cudaError_t launch_press_sweep(const KConst& kc, const ColGeo* geo, const double
     const int nm = (kc.km - 1 + 1) / 2;
     dim3 block(32, 8), grid((nm + 31) / 32, (kc.jm + 7) / 8, kc.im);
     press_sweep_kernel<<<grid, block, 0, s>>>(kc, geo, src, p, colour);
+    if (((kc.km - 1) & 1) && kc.km - 2 > 0 && kc.jm > 2) {
+        const int n = (kc.im - 2) * (kc.jm - 2);
+        press_sweep_seam_kernel<<<(n + 255) / 256, 256, 0, s>>>(kc, geo, src, p, colour);
+    }
     return cudaGetLastError();
 }
 

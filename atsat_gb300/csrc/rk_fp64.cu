@@ -278,8 +278,27 @@ __global__ void __launch_bounds__(256) rk_stage_fp64_kernel(const KConst K, cons
 }
 
 // ---- computeBuoyancyRefLevel (RungeKutta_Sat_Turb.cpp:31-50): two-level deterministic reduction ----
+// One block per (level, chunk of rows); a warp takes whole rows, its lanes the meridians, four at a time
+// so that eight loads are in flight per lane.
 constexpr int LM_CHUNKS = 16;
-constexpr int LM_THREADS = 256;
+constexpr int LM_THREADS = 128;
+
+// 1/x for x in FP32's normal range: the FP32 reciprocal refined by two Newton-Raphson steps
+// r <- r (2 - x r), written as r + r (1 - x r); each step squares the relative error (2^-23 -> 2^-46 ->
+// the FP64 rounding level).
+__device__ __forceinline__ double recip_nr(double x) {
+    double r = (double)__frcp_rn((float)x);
+    r = fma(r, fma(-x, r, 1.0), r);
+    return fma(r, fma(-x, r, 1.0), r);
+}
+
+// the buoyancy g p / (r_mix R_mix T t_ref) of one cell; false where the reference skips the cell
+__device__ __forceinline__ bool cell_buoyancy(const KConst& K, double tc, double pc, double& b) {
+    if (!(tc > 0.0)) return false;
+    const double den = K.rR * tc * K.t_ref;
+    b = (den > 1.0e-30 && den < 1.0e30) ? (K.g * pc) * recip_nr(den) : K.g * pc / den;
+    return isfinite(b);
+}
 
 __global__ void __launch_bounds__(LM_THREADS) level_mean_partial_kernel(const KConst K, const double* __restrict__ t,
                                                                          const double* __restrict__ ps,
@@ -287,25 +306,35 @@ __global__ void __launch_bounds__(LM_THREADS) level_mean_partial_kernel(const KC
                                                                          double* __restrict__ partial) {
     const int i = blockIdx.x, chunk = blockIdx.y;
     const int j0 = (int)((int64_t)K.jm * chunk / LM_CHUNKS), j1 = (int)((int64_t)K.jm * (chunk + 1) / LM_CHUNKS);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double sum = 0.0, wsum = 0.0;
-    const int n = (j1 - j0) * K.km;
-    for (int e = threadIdx.x; e < n; e += LM_THREADS) {
-        const int j = j0 + e / K.km, k = e % K.km;
-        const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
-        const double tc = __ldg(t + c);
-        if (!(tc > 0.0)) continue;
-        const double b = K.g * __ldg(ps + c) / (K.rR * tc * K.t_ref);
-        if (!isfinite(b)) continue;
+    for (int j = j0 + warp; j < j1; j += LM_THREADS / 32) {
+        const int64_t row = ((int64_t)i * K.jm + j) * K.kp;
         const double wgt = __ldg(sin_j + j);
-        sum += wgt * b;
-        wsum += wgt;
+        for (int k0 = 0; k0 < K.km; k0 += 128) {
+            double tv[4], pv[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int k = k0 + q * 32 + lane;
+                tv[q] = (k < K.km) ? __ldg(t + row + k) : 0.0;
+                pv[q] = (k < K.km) ? __ldg(ps + row + k) : 0.0;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                double b;
+                if (cell_buoyancy(K, tv[q], pv[q], b)) {   // tv = 0 past the row end: skipped
+                    sum += wgt * b;
+                    wsum += wgt;
+                }
+            }
+        }
     }
     __shared__ double s_sum[LM_THREADS / 32], s_w[LM_THREADS / 32];
     for (int o = 16; o > 0; o >>= 1) {
         sum += __shfl_down_sync(0xffffffffu, sum, o);
         wsum += __shfl_down_sync(0xffffffffu, wsum, o);
     }
-    if ((threadIdx.x & 31) == 0) { s_sum[threadIdx.x >> 5] = sum; s_w[threadIdx.x >> 5] = wsum; }
+    if (lane == 0) { s_sum[warp] = sum; s_w[warp] = wsum; }
     __syncthreads();
     if (threadIdx.x == 0) {
         double a = 0.0, b = 0.0;
@@ -327,24 +356,41 @@ __global__ void level_mean_final_kernel(const KConst K, const double* __restrict
 }
 
 // ---- computeMetricPressure (RungeKutta_Sat_Turb.cpp:60-108): one radial trapezoid scan per column ----
-__global__ void __launch_bounds__(256) metric_scan_kernel(const KConst K, const double* __restrict__ v,
+// The scan is serial in i; the loads of eight levels are issued ahead of the dependent sums. inv_rm holds
+// 1 / rm(i) (a product instead of the reference's quotient: at most one rounding apart).
+constexpr int MS_BATCH = 8;
+
+__global__ void __launch_bounds__(128) metric_scan_kernel(const KConst K, const double* __restrict__ v,
                                                           const double* __restrict__ w,
-                                                          const double* __restrict__ rm_tab,
+                                                          const double* __restrict__ inv_rm,
                                                           const double* __restrict__ cor_j,
                                                           const double* __restrict__ p_baro,
                                                           double* __restrict__ pm, double dr) {
     const int k = blockIdx.x * 32 + threadIdx.x;
-    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int j = blockIdx.y * 4 + threadIdx.y;
     if (k >= K.km || j >= K.jm) return;
     const double cor = __ldg(cor_j + j);
+    const int64_t c0 = (int64_t)j * K.kp + k;
     double f_prev = 0.0, acc = 0.0;
-    for (int i = 0; i < K.im; i++) {
-        const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
-        const double vv = __ldg(v + c), ww = __ldg(w + c);
-        const double f = (vv * vv + ww * ww) / __ldg(rm_tab + i) + cor * ww;
-        if (i > 0) acc = acc + 0.5 * (f_prev + f) * dr;
-        f_prev = f;
-        pm[c] = p_baro ? acc + __ldg(p_baro + c) : acc;
+    for (int i0 = 0; i0 < K.im; i0 += MS_BATCH) {
+        double vv[MS_BATCH], ww[MS_BATCH], pb[MS_BATCH];
+#pragma unroll
+        for (int q = 0; q < MS_BATCH; q++) {
+            const int64_t c = c0 + (int64_t)(i0 + q) * K.plane;
+            const bool in = i0 + q < K.im;
+            vv[q] = in ? __ldg(v + c) : 0.0;
+            ww[q] = in ? __ldg(w + c) : 0.0;
+            pb[q] = (in && p_baro) ? __ldg(p_baro + c) : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < MS_BATCH; q++) {
+            const int i = i0 + q;
+            if (i >= K.im) break;
+            const double f = (vv[q] * vv[q] + ww[q] * ww[q]) * __ldg(inv_rm + i) + cor * ww[q];
+            if (i > 0) acc = acc + 0.5 * (f_prev + f) * dr;
+            f_prev = f;
+            pm[c0 + (int64_t)i * K.plane] = p_baro ? acc + pb[q] : acc;
+        }
     }
 }
 
@@ -382,10 +428,10 @@ cudaError_t launch_level_mean(const KConst& kc, const double* t, const double* p
     return cudaGetLastError();
 }
 
-cudaError_t launch_metric_scan(const KConst& kc, const double* v, const double* w, const double* rm_tab,
+cudaError_t launch_metric_scan(const KConst& kc, const double* v, const double* w, const double* inv_rm,
                                const double* cor_j, const double* p_baro, double* p_metric, cudaStream_t s) {
-    dim3 block(32, 8), grid((kc.km + 31) / 32, (kc.jm + 7) / 8);
-    metric_scan_kernel<<<grid, block, 0, s>>>(kc, v, w, rm_tab, cor_j, p_baro, p_metric, kc.dr);
+    dim3 block(32, 4), grid((kc.km + 31) / 32, (kc.jm + 3) / 4);
+    metric_scan_kernel<<<grid, block, 0, s>>>(kc, v, w, inv_rm, cor_j, p_baro, p_metric, kc.dr);
     return cudaGetLastError();
 }
 

@@ -78,6 +78,9 @@ def lib():
         L.atsat_dyn_host_free.argtypes = [C.c_void_p]
         L.atsat_dyn_host_free.restype = None
         L.atsat_dyn_set_write_all_rhs.argtypes = [H, C.c_int32]
+        L.atsat_dyn_set_stage_variant.argtypes = [H, C.c_int32]
+        L.atsat_dyn_get_stage_variant.argtypes = [H, C.POINTER(C.c_int32)]
+        L.atsat_dyn_autotune.argtypes = [H, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
         L.atsat_dyn_timer_start.argtypes = [H]
         L.atsat_dyn_timer_stop.argtypes = [H, C.POINTER(C.c_double)]
         _lib = L
@@ -201,6 +204,24 @@ class Dycore:
 
     def set_write_all_rhs(self, on: bool):
         self._ck(lib().atsat_dyn_set_write_all_rhs(self.h, int(bool(on))), "set_write_all_rhs")
+
+    STAGE_DIRECT, STAGE_TILED = 0, 1
+
+    def set_stage_variant(self, variant: int):
+        """Mixed precision: 0 = direct stage kernel, 1 = TMA-tiled stage kernel."""
+        self._ck(lib().atsat_dyn_set_stage_variant(self.h, int(variant)), "set_stage_variant")
+
+    def stage_variant(self) -> int:
+        v = C.c_int32(-1)
+        self._ck(lib().atsat_dyn_get_stage_variant(self.h, C.byref(v)), "get_stage_variant")
+        return v.value
+
+    def autotune(self, reps: int = 10):
+        """Time both stage variants on this grid, keep the faster; returns (chosen, [ms_direct, ms_tiled])."""
+        chosen = C.c_int32(-1)
+        ms = (C.c_double * 2)()
+        self._ck(lib().atsat_dyn_autotune(self.h, int(reps), C.byref(chosen), ms), "autotune")
+        return chosen.value, [ms[0], ms[1]]
 
     # ---- the reference's entry points ----
     def computeMixtureDensity(self):

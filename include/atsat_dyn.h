@@ -262,6 +262,7 @@ enum {
     ATSAT_K_PRESS_BOUNDARY, /* Neumann planes, seam, projection boundary prep */
     ATSAT_K_GLUE,           /* density, restoreVar, boundary conditions */
     ATSAT_K_RHS,            /* standalone RHS pass */
+    ATSAT_K_PREPARE,        /* mixed precision: once-per-step FP32 copies and frozen FP64 terms */
     ATSAT_K_NCLASS
 };
 int atsat_dyn_profile(atsat_dyn_t h, int32_t enable);
@@ -278,6 +279,20 @@ int atsat_dyn_device_field(atsat_dyn_t h, int32_t field, double** dptr, int64_t*
 /* Write every rhs_* at the last RK stage (RHSSat writes all of them at every stage); off by default
  * because only rhs_u/v/w are read outside the step (the projection source and the restart file). */
 int atsat_dyn_set_write_all_rhs(atsat_dyn_t h, int32_t on);
+
+/* Mixed precision: which RK stage kernel runs. ATSAT_DYN_STAGE_DIRECT is one thread per cell with
+ * the stencils read from global memory; ATSAT_DYN_STAGE_TILED streams halo boxes of the FP32 arrays
+ * into shared memory with tensor copies (the default where the driver can encode tensor maps).
+ * No reference counterpart (the reference has one CPU loop nest). Setting TILED where it is
+ * unavailable returns ATSAT_DYN_E_UNSUPPORTED. */
+enum { ATSAT_DYN_STAGE_DIRECT = 0, ATSAT_DYN_STAGE_TILED = 1 };
+int atsat_dyn_set_stage_variant(atsat_dyn_t h, int32_t variant);
+int atsat_dyn_get_stage_variant(atsat_dyn_t h, int32_t* variant);
+/* Time each available stage variant on this handle's grid (`reps` launches of an intermediate RK
+ * stage each, CUDA events, after two untimed launches), keep the fastest and report it with the mean
+ * milliseconds of both (ms[v] < 0: variant unavailable). The stage writes only scratch buffers, so the
+ * model state is unchanged. No reference counterpart. */
+int atsat_dyn_autotune(atsat_dyn_t h, int32_t reps, int32_t* chosen, double ms[2]);
 
 /* Pinned host memory for bound arrays (cudaHostAlloc / cudaFreeHost). */
 void* atsat_dyn_host_alloc(size_t bytes);

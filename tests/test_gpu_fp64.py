@@ -13,7 +13,7 @@ from helpers import TOL_FP64, case, compare
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(9, 13, 17), (21, 91, 181)]
+SHAPES = [(9, 13, 17), (21, 91, 181), (10, 20, 36), (12, 40, 70)]   # the last two: odd km-1 (seam cells share a colour)
 ALL = list(range(F.NFIELDS))
 
 

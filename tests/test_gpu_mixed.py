@@ -29,22 +29,30 @@ def drift(got, ref, fids):
     return out
 
 
-def run_mixed(g, P, st, nsteps):
+TILED, DIRECT = 1, 0
+VARIANTS = [pytest.param(TILED, id="tiled"), pytest.param(DIRECT, id="direct")]
+
+
+def run_mixed(g, P, st, nsteps, variant=TILED):
     from atsat_gb300 import dyn
     s = st.copy()
     with dyn.Dycore(g, dict(P, precision=1)) as d:
+        d.set_stage_variant(variant)
+        assert d.stage_variant() == variant
         d.load_state(s)
         d.iterate(1, nsteps)
         d.download(ALL)
     return s
 
 
-@pytest.mark.parametrize("shape,exercise", [((21, 91, 181), True), ((41, 181, 361), False), ((41, 181, 361), True)])
-def test_mixed_ten_iterations(shape, exercise):
+@pytest.mark.parametrize("variant", VARIANTS)
+@pytest.mark.parametrize("shape,exercise", [((21, 91, 181), True), ((41, 181, 361), False), ((41, 181, 361), True),
+                                            ((9, 13, 17), True), ((12, 40, 70), True), ((10, 20, 36), True)])
+def test_mixed_ten_iterations(shape, exercise, variant):
     g, P, st = case(shape, seed=41, exercise=exercise)
     ref = st.copy()
     oracle.steps(ref, P, 10)
-    got = run_mixed(g, P, st, 10)
+    got = run_mixed(g, P, st, 10, variant)
     rep = drift(got.arrays, ref.arrays, F.PROG + [F.P_DYN])
     print("\nmax / rms relative drift after 10 iterations", shape, "exercise" if exercise else "plain")
     for k, (mx, rms) in rep.items():
@@ -53,7 +61,8 @@ def test_mixed_ten_iterations(shape, exercise):
     assert not bad, bad
 
 
-def test_mixed_one_step_all_fields():
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_mixed_one_step_all_fields(variant):
     """One RK4 step: every prognostic field within 1e-6, rhs_u/v/w and aux within 1e-5 of their max."""
     from atsat_gb300 import dyn
     g, P, st = case((21, 91, 181), seed=43)
@@ -61,6 +70,7 @@ def test_mixed_one_step_all_fields():
     oracle.rk4_step(ref, P)
     s = st.copy()
     with dyn.Dycore(g, dict(P, precision=1)) as d:
+        d.set_stage_variant(variant)
         d.load_state(s)
         d.RungeKuttaSat()
         d.download(ALL)
@@ -72,7 +82,8 @@ def test_mixed_one_step_all_fields():
         assert rep[F.NAMES[f]][0] <= 1e-5, (F.NAMES[f], rep[F.NAMES[f]])
 
 
-def test_mixed_live_differs_from_n():
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_mixed_live_differs_from_n(variant):
     """The drop-in may hand over live fields that differ from y_n: stage 0 must read the live ones."""
     from atsat_gb300 import dyn
     g, P, st = case((9, 13, 17), seed=47)
@@ -82,6 +93,7 @@ def test_mixed_live_differs_from_n():
     oracle.rk4_step(ref, P)
     s = st.copy()
     with dyn.Dycore(g, dict(P, precision=1)) as d:
+        d.set_stage_variant(variant)
         d.load_state(s)
         d.RungeKuttaSat()
         d.download(ALL)
@@ -90,7 +102,8 @@ def test_mixed_live_differs_from_n():
         assert rep[F.NAMES[f]][0] <= 1e-6, (F.NAMES[f], rep[F.NAMES[f]])
 
 
-def test_mixed_resident_then_dropin_calls():
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_mixed_resident_then_dropin_calls(variant):
     """A resident run (live and n-level fields sharing storage) interleaved with drop-in calls that
     see them separately: iterate, upload a changed field, single RK4 step, iterate again."""
     from atsat_gb300 import dyn
@@ -98,6 +111,7 @@ def test_mixed_resident_then_dropin_calls():
     ref = st.copy()
     s = st.copy()
     with dyn.Dycore(g, dict(P, precision=1)) as d:
+        d.set_stage_variant(variant)
         d.load_state(s)
         d.iterate(1, 3)
         oracle.steps(ref, P, 3)
@@ -124,3 +138,39 @@ def test_mixed_resident_then_dropin_calls():
     rep = drift(s.arrays, ref.arrays, F.PROG + F.PROG_N + [F.P_DYN])
     bad = {k: v[0] for k, v in rep.items() if not v[0] <= TOL_MIXED}
     assert not bad, bad
+
+
+def test_stage_variants_agree():
+    """The tiled and the direct stage kernels run the same per-cell arithmetic: after three
+    iterations their states agree far inside the mixed-precision bar."""
+    g, P, st = case((21, 91, 181), seed=59, exercise=True)
+    a = run_mixed(g, P, st, 3, TILED)
+    b = run_mixed(g, P, st, 3, DIRECT)
+    rep = drift(a.arrays, b.arrays, F.PROG + [F.P_DYN])
+    bad = {k: v[0] for k, v in rep.items() if not v[0] <= 1e-7}
+    assert not bad, bad
+
+
+def test_autotune_keeps_state():
+    """The autotuner times the variants on scratch buffers only: every field is bit-identical after it,
+    and the following iterations match a run without it."""
+    from atsat_gb300 import dyn
+    g, P, st = case((21, 91, 181), seed=61, exercise=True)
+    s = st.copy()
+    with dyn.Dycore(g, dict(P, precision=1)) as d:
+        d.load_state(s)
+        d.iterate(1, 2)
+        d.download(ALL)
+        before = {f: s.arrays[f].copy() for f in ALL}
+        chosen, ms = d.autotune(reps=3)
+        print("\nautotune (21, 91, 181):", chosen, ms)
+        assert chosen in (TILED, DIRECT) and ms[DIRECT] > 0
+        d.download(ALL)
+        for f in ALL:
+            assert np.array_equal(before[f], s.arrays[f], equal_nan=True), F.NAMES[f]
+        d.set_stage_variant(TILED)
+        d.iterate(3, 2)
+        d.download(ALL)
+    ref = run_mixed(g, P, st, 4, TILED)
+    for f in F.PROG + [F.P_DYN]:
+        assert np.array_equal(ref.arrays[f], s.arrays[f], equal_nan=True), F.NAMES[f]
