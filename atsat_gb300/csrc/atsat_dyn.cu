@@ -685,10 +685,30 @@ TilePlan make_plan(atsat_dyn* h, const MixedIO& io) {
     return pl;
 }
 
+bool variant_available(const atsat_dyn* h, int v) {
+    if (h->p.precision != ATSAT_DYN_MIXED) return v == ATSAT_DYN_STAGE_DIRECT;
+    switch (v) {
+        case ATSAT_DYN_STAGE_DIRECT: return true;
+        case ATSAT_DYN_STAGE_TILED: return h->tile_ok;
+        case ATSAT_DYN_STAGE_SPLIT:
+        case ATSAT_DYN_STAGE_SPLIT3:
+        case ATSAT_DYN_STAGE_SPLIT13: return !h->kc.divu_on;
+        default: return false;
+    }
+}
+
+int launches_per_stage(const atsat_dyn* h) { return h->variant >= ATSAT_DYN_STAGE_SPLIT ? 2 : 1; }
+
 cudaError_t launch_stage(atsat_dyn* h, const MixedIO& io, const StageParams& sp, int mode) {
-    if (mode != MODE_RHS && h->variant == 1 && h->tile_ok)
-        return launch_rk_tile(h->maps, h->kf, io, sp, make_plan(h, io), mode, h->stream);
-    return launch_rk_stage_mixed(h->kf, io, sp, mode, h->stream);
+    const int v = (mode == MODE_RHS || !variant_available(h, h->variant)) ? ATSAT_DYN_STAGE_DIRECT : h->variant;
+    switch (v) {
+        case ATSAT_DYN_STAGE_TILED:
+            return launch_rk_tile(h->maps, h->kf, io, sp, make_plan(h, io), mode, h->stream);
+        case ATSAT_DYN_STAGE_SPLIT: return launch_rk_split(h->kf, io, sp, mode, 1, h->stream);
+        case ATSAT_DYN_STAGE_SPLIT3: return launch_rk_split(h->kf, io, sp, mode, 3, h->stream);
+        case ATSAT_DYN_STAGE_SPLIT13: return launch_rk_split(h->kf, io, sp, mode, 13, h->stream);
+        default: return launch_rk_stage_mixed(h->kf, io, sp, mode, h->stream);
+    }
 }
 
 // resident: called from atsat_dyn_iterate, which keeps the FP32 copies of the next y_n up to date and
@@ -740,7 +760,7 @@ int enqueue_rk4_mixed(atsat_dyn* h, bool resident) {
         }
         Timed t(h, ATSAT_K_RK_STAGE);
         CK(h, launch_stage(h, io, sp, stage == 3 ? MODE_FINAL : MODE_STAGE));
-        h->launches += 1;
+        h->launches += launches_per_stage(h);
     }
     return ATSAT_DYN_OK;
 }
@@ -1016,7 +1036,7 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
         h->pgeo = reinterpret_cast<PrepGeo*>(r);
         if ((e = upload_geof(h)) != cudaSuccess) return cuda_fail(e, "FP32 geometry upload");
         h->tile_ok = make_tile_maps(h);
-        if (const char* v = std::getenv("ATSAT_DYN_STAGE_VARIANT")) h->variant = std::atoi(v) == 0 ? 0 : 1;
+        if (!h->tile_ok) h->variant = ATSAT_DYN_STAGE_DIRECT;
     }
     // small host tables
     std::vector<double> sin_j(K.jm), rm_tab(K.im), cor_j(K.jm);
@@ -1353,24 +1373,24 @@ int atsat_dyn_set_write_all_rhs(atsat_dyn_t h, int32_t on) {
 
 int atsat_dyn_set_stage_variant(atsat_dyn_t h, int32_t variant) {
     if (!h) return ATSAT_DYN_E_INVALID;
-    if (variant != ATSAT_DYN_STAGE_DIRECT && variant != ATSAT_DYN_STAGE_TILED)
+    if (variant < 0 || variant >= ATSAT_DYN_STAGE_NVARIANT)
         return fail(h, ATSAT_DYN_E_INVALID, "unknown stage variant %d", variant);
     if (h->p.precision != ATSAT_DYN_MIXED)
         return fail(h, ATSAT_DYN_E_UNSUPPORTED, "stage variants are a mixed-precision setting");
-    if (variant == ATSAT_DYN_STAGE_TILED && !h->tile_ok)
-        return fail(h, ATSAT_DYN_E_UNSUPPORTED, "tiled stage kernel unavailable (no tensor-map encoder)");
+    if (!variant_available(h, variant))
+        return fail(h, ATSAT_DYN_E_UNSUPPORTED, "stage variant %d unavailable here (tiled: no tensor-map encoder; "
+                    "split: species_divu on)", variant);
     h->variant = variant;
     return ATSAT_DYN_OK;
 }
 
 int atsat_dyn_get_stage_variant(atsat_dyn_t h, int32_t* variant) {
     if (!h || !variant) return ATSAT_DYN_E_INVALID;
-    *variant = (h->p.precision == ATSAT_DYN_MIXED && h->variant == 1 && h->tile_ok) ? ATSAT_DYN_STAGE_TILED
-                                                                                  : ATSAT_DYN_STAGE_DIRECT;
+    *variant = variant_available(h, h->variant) ? h->variant : ATSAT_DYN_STAGE_DIRECT;
     return ATSAT_DYN_OK;
 }
 
-int atsat_dyn_autotune(atsat_dyn_t h, int32_t reps, int32_t* chosen, double ms[2]) {
+int atsat_dyn_autotune(atsat_dyn_t h, int32_t reps, int32_t* chosen, double* ms) {
     ENTRY(h);
     if (!chosen || !ms || reps < 1) return fail(h, ATSAT_DYN_E_INVALID, "autotune: bad arguments");
     if (h->p.precision != ATSAT_DYN_MIXED)
@@ -1390,14 +1410,14 @@ int atsat_dyn_autotune(atsat_dyn_t h, int32_t reps, int32_t* chosen, double ms[2
     CK(h, cudaEventCreate(&ev[0]));
     CK(h, cudaEventCreate(&ev[1]));
     int best = -1;
-    for (int v = 0; v < 2; v++) {
+    for (int v = 0; v < ATSAT_DYN_STAGE_NVARIANT; v++) {
         ms[v] = -1.0;
-        if (v == 1 && !h->tile_ok) continue;
+        if (!variant_available(h, v)) continue;
         h->variant = v;
         for (int r = 0; r < 2 + reps; r++) {
             if (r == 2) CK(h, cudaEventRecord(ev[0], h->stream));
             CK(h, launch_stage(h, io, sp, MODE_STAGE));
-            h->launches += 1;
+            h->launches += launches_per_stage(h);
         }
         CK(h, cudaEventRecord(ev[1], h->stream));
         CK(h, cudaEventSynchronize(ev[1]));

@@ -263,6 +263,9 @@ cudaError_t launch_rk_stage_fp64(const KConst& kc, const StageIO<double>& io, co
 cudaError_t launch_rk_stage_mixed(const MixedConstF& kf, const MixedIO& io, const StageParams& sp, int mode,
                                   cudaStream_t s);
 cudaError_t launch_mixed_prepare(const KConst& kc, const MixedPrep& pr, cudaStream_t s);
+// momentum / temperature kernel, then the tracer kernel with `groups` (1, 3 or 13) threads per cell
+cudaError_t launch_rk_split(const MixedConstF& kf, const MixedIO& io, const StageParams& sp, int mode, int groups,
+                            cudaStream_t s);
 // tensor maps are CUtensorMap objects (128 bytes), passed opaquely
 struct TileMaps { alignas(64) unsigned char main[128]; alignas(64) unsigned char seam[128]; };
 cudaError_t launch_rk_tile(const TileMaps& maps, const MixedConstF& kf, const MixedIO& io, const StageParams& sp,

@@ -101,6 +101,18 @@ struct CellState {
     float nue_t_s;          // nue_t / Pr_t
 };
 
+// The tracers' view of a cell without the momentum part (species_divu off): stage velocities from the
+// centre values and the eddy viscosity terms, exactly as momentum_t forms them.
+template <class Src>
+__device__ __forceinline__ CellState tracer_state(const MixedConstF& K, const MixedIO& io, const Src& S, int64_t c) {
+    const float u = S.cyn(ATSAT_F_U) + S.cdl(ATSAT_F_U);
+    const float v = S.cyn(ATSAT_F_V) + S.cdl(ATSAT_F_V);
+    const float w = (S.cyn(ATSAT_F_W) + S.clo()) + S.cdl(ATSAT_F_W);
+    const float nue_c = ldf(io.nue + c);
+    const float nue_t = (K.turb_coupling != 0.0f && isfinite(nue_c)) ? K.turb_coupling * smaxf(0.0f, nue_c) : 0.0f;
+    return CellState{u, v, w, 0.0f, nue_c, nue_t * K.inv_pr_t};
+}
+
 // rhs_u, rhs_v, rhs_w (RHS_Sat_Turb.cpp:300-440) and rhs_t (:460-560) of one cell, emitted.
 template <int MODE, class Src>
 __device__ __forceinline__ CellState momentum_t(const MixedConstF& K, const MixedIO& io, const StageParams& sp,

@@ -99,6 +99,54 @@ __global__ void __launch_bounds__(256) rk_stage_mixed_kernel(const MixedConstF K
     }
 }
 
+// Split form of the same stage (species_divu off): the momentum / temperature equations in one kernel
+// and the tracers in another, NG threads per cell each taking a share of the 13 tracer fields. The
+// tracer threads rebuild the stage velocities from the centre values, so the two kernels share no
+// intermediate data. Smaller per-thread programs (fewer registers, more resident warps) hide memory
+// latency better than the fused kernel on some grids; the autotuner decides.
+template <int MODE>
+__global__ void __launch_bounds__(256) rk_mom_kernel(const MixedConstF K, const MixedIO io, const StageParams sp) {
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= K.km || j >= K.jm) return;
+    const bool interior = (i >= 1 && i <= K.im - 2 && j >= 2 && j <= K.jm - 3 && k <= K.km - 2);
+    if (!interior) return;
+    const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
+    const int kw = (k == 0) ? K.km - 2 : k - 1;
+    const int ke = (k == K.km - 2) ? 0 : k + 1;
+    const GlobalSrc S{io, c, K.plane, K.kp, kw - k, ke - k};
+    const ColGeoF g = io.geof[(int64_t)i * K.jm + j];
+    momentum_t<MODE>(K, io, sp, S, i, c, g);
+}
+
+template <int MODE, int NG>
+__global__ void __launch_bounds__(256) rk_tracer_kernel(const MixedConstF K, const MixedIO io, const StageParams sp) {
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i = blockIdx.z / NG, grp = blockIdx.z % NG;
+    if (k >= K.km || j >= K.jm) return;
+    const bool interior = (i >= 1 && i <= K.im - 2 && j >= 2 && j <= K.jm - 3 && k <= K.km - 2);
+    if (!interior) return;
+    const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
+    const int kw = (k == 0) ? K.km - 2 : k - 1;
+    const int ke = (k == K.km - 2) ? 0 : k + 1;
+    const GlobalSrc S{io, c, K.plane, K.kp, kw - k, ke - k};
+    const ColGeoF g = io.geof[(int64_t)i * K.jm + j];
+    const CellState cs = tracer_state(K, io, S, c);
+    constexpr int NT = ATSAT_F_DIS - ATSAT_F_H2O + 1;   // 13 tracer fields
+    const int q0 = ATSAT_F_H2O + grp * NT / NG, q1 = ATSAT_F_H2O + (grp + 1) * NT / NG;
+#pragma unroll
+    for (int q = ATSAT_F_H2O; q <= ATSAT_F_DIS; q++) {
+        if (q < q0 || q >= q1) continue;
+        if (is_turb(q) && !K.turb) {
+            if (MODE == MODE_FINAL && sp.write_all_rhs) io.rhs[q][c] = 0.0;
+            continue;
+        }
+        scalar<MODE>(q, K, io, sp, S, c, g, cs);
+    }
+}
+
 // Once per step: the FP32 copies of y_n (and w's low word), the stage-0 increment live - y_n, the FP32
 // copies of changed point inputs, and the frozen FP64 terms of the momentum equations.
 __global__ void __launch_bounds__(256) mixed_prepare_kernel(const KConst K, const MixedPrep pr) {
@@ -200,6 +248,25 @@ cudaError_t launch_rk_stage_mixed(const MixedConstF& kf, const MixedIO& io, cons
     else if (mode == MODE_STAGE) rk_stage_mixed_kernel<MODE_STAGE><<<grid, block, 0, s>>>(kf, io, sp);
     else rk_stage_mixed_kernel<MODE_FINAL><<<grid, block, 0, s>>>(kf, io, sp);
     return cudaGetLastError();
+}
+
+template <int MODE>
+cudaError_t launch_split_mode(const MixedConstF& kf, const MixedIO& io, const StageParams& sp, int groups,
+                              cudaStream_t s) {
+    const dim3 block(32, 8);
+    const unsigned gx = (kf.km + 31) / 32, gy = (kf.jm + 7) / 8;
+    rk_mom_kernel<MODE><<<dim3(gx, gy, kf.im), block, 0, s>>>(kf, io, sp);
+    if (groups == 1) rk_tracer_kernel<MODE, 1><<<dim3(gx, gy, kf.im), block, 0, s>>>(kf, io, sp);
+    else if (groups == 3) rk_tracer_kernel<MODE, 3><<<dim3(gx, gy, kf.im * 3), block, 0, s>>>(kf, io, sp);
+    else rk_tracer_kernel<MODE, 13><<<dim3(gx, gy, kf.im * 13), block, 0, s>>>(kf, io, sp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rk_split(const MixedConstF& kf, const MixedIO& io, const StageParams& sp, int mode, int groups,
+                            cudaStream_t s) {
+    if (kf.divu_on || (groups != 1 && groups != 3 && groups != 13) || mode == MODE_RHS) return cudaErrorInvalidValue;
+    return mode == MODE_STAGE ? launch_split_mode<MODE_STAGE>(kf, io, sp, groups, s)
+                              : launch_split_mode<MODE_FINAL>(kf, io, sp, groups, s);
 }
 
 cudaError_t launch_mixed_prepare(const KConst& kc, const MixedPrep& pr, cudaStream_t s) {

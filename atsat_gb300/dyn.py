@@ -205,10 +205,11 @@ class Dycore:
     def set_write_all_rhs(self, on: bool):
         self._ck(lib().atsat_dyn_set_write_all_rhs(self.h, int(bool(on))), "set_write_all_rhs")
 
-    STAGE_DIRECT, STAGE_TILED = 0, 1
+    STAGE_DIRECT, STAGE_TILED, STAGE_SPLIT, STAGE_SPLIT3, STAGE_SPLIT13 = range(5)
+    STAGE_NAMES = ["direct", "tiled", "split", "split3", "split13"]
 
     def set_stage_variant(self, variant: int):
-        """Mixed precision: 0 = direct stage kernel, 1 = TMA-tiled stage kernel."""
+        """Mixed precision: the RK stage kernel (STAGE_* constants)."""
         self._ck(lib().atsat_dyn_set_stage_variant(self.h, int(variant)), "set_stage_variant")
 
     def stage_variant(self) -> int:
@@ -217,11 +218,12 @@ class Dycore:
         return v.value
 
     def autotune(self, reps: int = 10):
-        """Time both stage variants on this grid, keep the faster; returns (chosen, [ms_direct, ms_tiled])."""
+        """Time every available stage variant on this grid, keep the fastest; returns (chosen, ms per
+        variant, -1 where unavailable)."""
         chosen = C.c_int32(-1)
-        ms = (C.c_double * 2)()
+        ms = (C.c_double * len(self.STAGE_NAMES))()
         self._ck(lib().atsat_dyn_autotune(self.h, int(reps), C.byref(chosen), ms), "autotune")
-        return chosen.value, [ms[0], ms[1]]
+        return chosen.value, list(ms)
 
     # ---- the reference's entry points ----
     def computeMixtureDensity(self):

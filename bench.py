@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--shape", default="41,181,361")
     ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--stage-variant", default="auto", choices=["auto", "direct", "tiled", "split", "split3", "split13"],
+                    help="mixed precision: the RK stage kernel (auto: the autotuner's choice)")
     ap.add_argument("--precision", default="mixed,fp64",
                     help="comma list; the first is the headline value, the others are reported beside it")
     a = ap.parse_args()
@@ -179,7 +181,10 @@ RK_BYTES_MIXED = ((_MIX_IN + 68 + 8) + 2 * (_MIX_IN + 68 + 68 + 16)
 RK_BYTES = {"fp64": RK_BYTES_FP64, "mixed": RK_BYTES_MIXED}
 KERNEL_NAME = {"fp64": "rk_stage_fp64_kernel (fused RHSSat + RK4 stage, FP64)",
                "mixed": "rk_stage_mixed_kernel (fused RHSSat + RK4 stage, FP32 stencils / FP64 state)",
-               "mixed_tiled": "rk_tile_kernel (TMA-tiled fused RHSSat + RK4 stage, FP32 stencils / FP64 state)"}
+               "mixed_tiled": "rk_tile_kernel (TMA-tiled fused RHSSat + RK4 stage, FP32 stencils / FP64 state)",
+               "mixed_split": "rk_mom_kernel + rk_tracer_kernel<1> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)",
+               "mixed_split3": "rk_mom_kernel + rk_tracer_kernel<3> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)",
+               "mixed_split13": "rk_mom_kernel + rk_tracer_kernel<13> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)"}
 
 
 def cpu_baseline(g, P, seed, target_s=3.0):
@@ -244,10 +249,13 @@ def measure(a, rank, world, g, P, st, pinned, precision):
     # ---- device-resident throughput ----
     d.iterate(1, a.warmup)
     tune = None
-    if precision == "mixed":
+    if precision == "mixed" and a.stage_variant == "auto":
         chosen, tms = d.autotune(reps=5)
-        tune = {"stage_variant": "tiled" if chosen == dyn.Dycore.STAGE_TILED else "direct",
-                "autotune_ms_per_stage": {"direct": tms[0], "tiled": tms[1] if tms[1] > 0 else None}}
+        tune = {"stage_variant": dyn.Dycore.STAGE_NAMES[chosen],
+                "autotune_ms_per_stage": {n: (t if t > 0 else None) for n, t in zip(dyn.Dycore.STAGE_NAMES, tms)}}
+    elif precision == "mixed":
+        d.set_stage_variant(dyn.Dycore.STAGE_NAMES.index(a.stage_variant))
+        tune = {"stage_variant": a.stage_variant}
     it0 = a.warmup + 1
     d.profile(True)
     d.profile_reset()
@@ -295,7 +303,7 @@ def measure(a, rank, world, g, P, st, pinned, precision):
     bytes_per_launch = RK_BYTES[precision] / 4 * interior_rk(g)
     avg_ms = ms_rk / max(n_rk, 1)
     achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9
-    kname = KERNEL_NAME["mixed_tiled" if tune and tune["stage_variant"] == "tiled" else precision]
+    kname = KERNEL_NAME.get("mixed_" + tune["stage_variant"], KERNEL_NAME[precision]) if tune else KERNEL_NAME[precision]
     roof = {"kernel": kname, "bound": "hbm", "achieved": achieved,
             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
             "traffic": traffic_per_launch("rk_stage_" + precision), "algorithmic_bytes_per_launch": bytes_per_launch,

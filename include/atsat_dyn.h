@@ -280,19 +280,29 @@ int atsat_dyn_device_field(atsat_dyn_t h, int32_t field, double** dptr, int64_t*
  * because only rhs_u/v/w are read outside the step (the projection source and the restart file). */
 int atsat_dyn_set_write_all_rhs(atsat_dyn_t h, int32_t on);
 
-/* Mixed precision: which RK stage kernel runs. ATSAT_DYN_STAGE_DIRECT is one thread per cell with
- * the stencils read from global memory; ATSAT_DYN_STAGE_TILED streams halo boxes of the FP32 arrays
- * into shared memory with tensor copies (the default where the driver can encode tensor maps).
- * No reference counterpart (the reference has one CPU loop nest). Setting TILED where it is
- * unavailable returns ATSAT_DYN_E_UNSUPPORTED. */
-enum { ATSAT_DYN_STAGE_DIRECT = 0, ATSAT_DYN_STAGE_TILED = 1 };
+/* Mixed precision: which RK stage kernel runs (all compute the same arithmetic per cell).
+ *   DIRECT   one thread per cell, stencils read from global memory;
+ *   TILED    halo boxes of the FP32 arrays streamed into shared memory with tensor copies (needs a
+ *            driver that can encode tensor maps);
+ *   SPLIT*   a momentum / temperature kernel, then a tracer kernel with 1, 3 or 13 threads per cell
+ *            (not with species_divu on).
+ * The default is TILED where available. No reference counterpart (the reference has one CPU loop
+ * nest). Setting an unavailable variant returns ATSAT_DYN_E_UNSUPPORTED. */
+enum {
+    ATSAT_DYN_STAGE_DIRECT = 0,
+    ATSAT_DYN_STAGE_TILED = 1,
+    ATSAT_DYN_STAGE_SPLIT = 2,
+    ATSAT_DYN_STAGE_SPLIT3 = 3,
+    ATSAT_DYN_STAGE_SPLIT13 = 4,
+    ATSAT_DYN_STAGE_NVARIANT = 5
+};
 int atsat_dyn_set_stage_variant(atsat_dyn_t h, int32_t variant);
 int atsat_dyn_get_stage_variant(atsat_dyn_t h, int32_t* variant);
 /* Time each available stage variant on this handle's grid (`reps` launches of an intermediate RK
  * stage each, CUDA events, after two untimed launches), keep the fastest and report it with the mean
- * milliseconds of both (ms[v] < 0: variant unavailable). The stage writes only scratch buffers, so the
- * model state is unchanged. No reference counterpart. */
-int atsat_dyn_autotune(atsat_dyn_t h, int32_t reps, int32_t* chosen, double ms[2]);
+ * milliseconds of every variant in ms[ATSAT_DYN_STAGE_NVARIANT] (< 0: unavailable). The stage writes
+ * only scratch buffers, so the model state is unchanged. No reference counterpart. */
+int atsat_dyn_autotune(atsat_dyn_t h, int32_t reps, int32_t* chosen, double* ms);
 
 /* Pinned host memory for bound arrays (cudaHostAlloc / cudaFreeHost). */
 void* atsat_dyn_host_alloc(size_t bytes);

@@ -29,8 +29,22 @@ def drift(got, ref, fids):
     return out
 
 
-TILED, DIRECT = 1, 0
-VARIANTS = [pytest.param(TILED, id="tiled"), pytest.param(DIRECT, id="direct")]
+DIRECT, TILED, SPLIT, SPLIT3, SPLIT13 = range(5)
+VARIANTS = [pytest.param(v, id=n) for v, n in
+            [(TILED, "tiled"), (DIRECT, "direct"), (SPLIT, "split"), (SPLIT3, "split3"), (SPLIT13, "split13")]]
+
+_REF = {}
+
+
+def oracle_steps(shape, seed, exercise, n):
+    """The oracle's state after n iterations (cached: every stage variant compares against it)."""
+    key = (shape, seed, exercise, n)
+    if key not in _REF:
+        g, P, st = case(shape, seed=seed, exercise=exercise)
+        ref = st.copy()
+        oracle.steps(ref, P, n)
+        _REF[key] = ref
+    return _REF[key]
 
 
 def run_mixed(g, P, st, nsteps, variant=TILED):
@@ -50,8 +64,7 @@ def run_mixed(g, P, st, nsteps, variant=TILED):
                                             ((9, 13, 17), True), ((12, 40, 70), True), ((10, 20, 36), True)])
 def test_mixed_ten_iterations(shape, exercise, variant):
     g, P, st = case(shape, seed=41, exercise=exercise)
-    ref = st.copy()
-    oracle.steps(ref, P, 10)
+    ref = oracle_steps(shape, 41, exercise, 10)
     got = run_mixed(g, P, st, 10, variant)
     rep = drift(got.arrays, ref.arrays, F.PROG + [F.P_DYN])
     print("\nmax / rms relative drift after 10 iterations", shape, "exercise" if exercise else "plain")
@@ -140,15 +153,28 @@ def test_mixed_resident_then_dropin_calls(variant):
     assert not bad, bad
 
 
-def test_stage_variants_agree():
-    """The tiled and the direct stage kernels run the same per-cell arithmetic: after three
-    iterations their states agree far inside the mixed-precision bar."""
+@pytest.mark.parametrize("variant", VARIANTS[:1] + VARIANTS[2:])
+def test_stage_variants_agree(variant):
+    """Every stage kernel runs the same per-cell arithmetic as the direct one: after three iterations
+    their states agree far inside the mixed-precision bar."""
     g, P, st = case((21, 91, 181), seed=59, exercise=True)
-    a = run_mixed(g, P, st, 3, TILED)
+    a = run_mixed(g, P, st, 3, variant)
     b = run_mixed(g, P, st, 3, DIRECT)
     rep = drift(a.arrays, b.arrays, F.PROG + [F.P_DYN])
     bad = {k: v[0] for k, v in rep.items() if not v[0] <= 1e-7}
     assert not bad, bad
+
+
+def test_split_unavailable_with_species_divu():
+    """The split kernels leave the divergence term to the fused kernels: asking for them with
+    species_divu on is refused, and the default variant still runs."""
+    from atsat_gb300 import dyn
+    g, P, st = case((9, 13, 17), seed=63, exercise=True)
+    with dyn.Dycore(g, dict(P, precision=1, species_divu=0.5)) as d:
+        with pytest.raises(dyn.DycoreError):
+            d.set_stage_variant(SPLIT)
+        chosen, ms = d.autotune(reps=2)
+        assert chosen in (DIRECT, TILED) and ms[SPLIT] < 0 and ms[SPLIT13] < 0
 
 
 def test_autotune_keeps_state():
@@ -164,7 +190,7 @@ def test_autotune_keeps_state():
         before = {f: s.arrays[f].copy() for f in ALL}
         chosen, ms = d.autotune(reps=3)
         print("\nautotune (21, 91, 181):", chosen, ms)
-        assert chosen in (TILED, DIRECT) and ms[DIRECT] > 0
+        assert 0 <= chosen < 5 and ms[chosen] == min(m for m in ms if m > 0)
         d.download(ALL)
         for f in ALL:
             assert np.array_equal(before[f], s.arrays[f], equal_nan=True), F.NAMES[f]
