@@ -200,3 +200,18 @@ def test_autotune_keeps_state():
     ref = run_mixed(g, P, st, 4, TILED)
     for f in F.PROG + [F.P_DYN]:
         assert np.array_equal(ref.arrays[f], s.arrays[f], equal_nan=True), F.NAMES[f]
+
+
+def test_drift_report_and_continuity_residual():
+    """Ten iterations on the default grid with every source term on: the mixed path's drift is inside
+    the bar and its continuity residual max |div u| (the reference's iteration report) matches the FP64
+    path's to 1e-6 relative or stays below it."""
+    import drift_report
+    rep = drift_report.run((41, 181, 361), steps=10, every=10, seed=2)
+    row = rep["rows"][-1]
+    print("\ndrift after 10:", {k: f"{v[0]:.2e}" for k, v in row["mixed"].items()}, row["div_max"])
+    for name in ("u", "v", "w", "p_dyn"):
+        assert row["mixed"][name][0] <= TOL_MIXED, (name, row["mixed"][name])
+        assert row["fp64"][name][0] <= 1e-10, (name, row["fp64"][name])
+    dm, df = row["div_max"]["mixed"], row["div_max"]["fp64"]
+    assert dm <= df * (1 + 1e-6) or abs(dm - df) <= 1e-6 * df, (dm, df)
