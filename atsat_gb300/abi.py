@@ -35,6 +35,14 @@ class PStats(C.Structure):
                 ("src_clamped", C.c_double), ("max_abs_update", C.c_double)]
 
 
+class PoissonStats(C.Structure):
+    _fields_ = [("method", C.c_int32), ("iterations", C.c_int32), ("inner", C.c_int32), ("converged", C.c_int32),
+                ("rel_residual", C.c_double), ("ms", C.c_double), ("reserved", C.c_double * 4)]
+
+
+POISSON_METHODS = ["sor64", "sor32", "refine_sor", "direct64", "direct32", "refine_direct"]
+
+
 class Diag(C.Structure):
     _fields_ = [("launches", C.c_int64), ("nonfinite", C.c_int64), ("timeout", C.c_int32),
                 ("reserved", C.c_int32 * 5)]

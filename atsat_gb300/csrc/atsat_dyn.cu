@@ -102,6 +102,7 @@ struct atsat_dyn {
     int variant = 1;
     unsigned int* dev_err = nullptr;     // device status word of the bounded waits
     int timeouts = 0;
+    PoissonSolver* poisson = nullptr;    // standalone pressure-equation solver, built on first use
     std::string err;
 };
 
@@ -1066,6 +1067,7 @@ void atsat_dyn_destroy(atsat_dyn_t h) {
     for (auto& e : h->pend) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
     for (auto e : h->pool) cudaEventDestroy(e);
     for (auto e : h->timer) if (e) cudaEventDestroy(e);
+    poisson_destroy(h->poisson);
     if (h->slab) cudaFree(h->slab);
     if (h->slab32) cudaFree(h->slab32);
     if (h->pinned) cudaFreeHost(h->pinned);
@@ -1430,6 +1432,89 @@ int atsat_dyn_autotune(atsat_dyn_t h, int32_t reps, int32_t* chosen, double* ms)
     cudaEventDestroy(ev[1]);
     h->variant = best >= 0 ? best : keep;
     *chosen = h->variant;
+    return finish(h);
+}
+
+// ---- standalone pressure-equation solves ----
+
+static int poisson_ready(atsat_dyn* h) {
+    if (h->poisson) return ATSAT_DYN_OK;
+    std::string err;
+    h->poisson = poisson_create(h->kc, h->geo, h->geo_h, h->stream, &err);
+    if (!h->poisson) return fail(h, err.find("cudaMalloc") != std::string::npos ? ATSAT_DYN_E_NOMEM : ATSAT_DYN_E_UNSUPPORTED,
+                                 "%s", err.c_str());
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_poisson_project(atsat_dyn_t h, double* src) {
+    ENTRY(h);
+    if (!src) return fail(h, ATSAT_DYN_E_INVALID, "poisson_project: null source");
+    int rc;
+    if ((rc = poisson_ready(h))) return rc;
+    const KConst& K = h->kc;
+    const std::vector<double>& y = poisson_null_vector(h->poisson);
+    const int NI = K.im - 2, NJ = K.jm - 2, n = K.km - 1;
+    // the phi-mean of the source is its zero-mode part; remove its component along y
+    double yf = 0.0, yy = 0.0;
+    std::vector<double> mean((size_t)NI * NJ);
+    for (int jj = 0; jj < NJ; jj++)
+        for (int ii = 0; ii < NI; ii++) {
+            const double* row = src + ((size_t)(ii + 1) * K.jm + (jj + 1)) * K.km;
+            double a = 0.0;
+            for (int k = 0; k < n; k++) a += row[k];
+            mean[(size_t)jj * NI + ii] = a / n;
+            const double yv = y[(size_t)jj * NI + ii];
+            yf += yv * a / n;
+            yy += yv * yv;
+        }
+    if (!(yy > 0.0)) return fail(h, ATSAT_DYN_E_INVALID, "poisson_project: degenerate null vector");
+    const double alpha = yf / yy;
+    for (int jj = 0; jj < NJ; jj++)
+        for (int ii = 0; ii < NI; ii++) {
+            double* row = src + ((size_t)(ii + 1) * K.jm + (jj + 1)) * K.km;
+            const double d = alpha * y[(size_t)jj * NI + ii];
+            for (int k = 0; k < K.km; k++) row[k] -= d;
+        }
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_poisson_solve(atsat_dyn_t h, int32_t method, const double* src, double* p, double tol,
+                            int32_t max_iter, int32_t inner, double omega, atsat_dyn_poisson_stats* st) {
+    ENTRY(h);
+    if (!src || !p || method < 0 || method >= ATSAT_POISSON_NMETHOD || max_iter < 0 || !(omega > 0.0 && omega < 2.0))
+        return fail(h, ATSAT_DYN_E_INVALID, "poisson_solve: bad arguments");
+    if ((method == ATSAT_POISSON_REFINE_SOR) && inner < 1)
+        return fail(h, ATSAT_DYN_E_INVALID, "poisson_solve: inner sweeps < 1");
+    int rc;
+    if ((rc = poisson_ready(h))) return rc;
+    const KConst& K = h->kc;
+    double* f = poisson_f(h->poisson);
+    CK(h, cudaMemcpy2DAsync(f, (size_t)K.kp * 8, src, (size_t)K.km * 8, (size_t)K.km * 8, (size_t)K.im * K.jm,
+                            cudaMemcpyHostToDevice, h->stream));
+    cudaEvent_t ev[2];
+    CK(h, cudaEventCreate(&ev[0]));
+    CK(h, cudaEventCreate(&ev[1]));
+    CK(h, cudaEventRecord(ev[0], h->stream));
+    int iters = 0, inner_total = 0;
+    double rel = 0.0;
+    CK(h, poisson_run(h->poisson, method, tol, max_iter, inner, omega, &iters, &inner_total, &rel));
+    CK(h, cudaEventRecord(ev[1], h->stream));
+    CK(h, cudaEventSynchronize(ev[1]));
+    float ms = 0.0f;
+    CK(h, cudaEventElapsedTime(&ms, ev[0], ev[1]));
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    CK(h, cudaMemcpy2DAsync(p, (size_t)K.km * 8, poisson_p(h->poisson), (size_t)K.kp * 8, (size_t)K.km * 8,
+                            (size_t)K.im * K.jm, cudaMemcpyDeviceToHost, h->stream));
+    if (st) {
+        memset(st, 0, sizeof(*st));
+        st->method = method;
+        st->iterations = iters;
+        st->inner = inner_total;
+        st->converged = rel <= tol;
+        st->rel_residual = rel;
+        st->ms = ms;
+    }
     return finish(h);
 }
 

@@ -8,6 +8,9 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
+#include <vector>
+
 #include <cuda_runtime.h>
 
 #include "../../include/atsat_dyn.h"
@@ -271,6 +274,17 @@ struct TileMaps { alignas(64) unsigned char main[128]; alignas(64) unsigned char
 cudaError_t launch_rk_tile(const TileMaps& maps, const MixedConstF& kf, const MixedIO& io, const StageParams& sp,
                            const TilePlan& plan, int mode, cudaStream_t s);
 size_t rk_tile_smem_bytes();
+
+// standalone pressure-equation solver (poisson.cu)
+struct PoissonSolver;
+PoissonSolver* poisson_create(const KConst& kc, const ColGeo* geo_dev, const std::vector<ColGeo>& geo_h,
+                              cudaStream_t s, std::string* err);
+void poisson_destroy(PoissonSolver* P);
+double* poisson_f(PoissonSolver* P);          // device source (pitched)
+double* poisson_p(PoissonSolver* P);          // device solution (pitched)
+const std::vector<double>& poisson_null_vector(PoissonSolver* P);   // [(j-1) * (im-2) + (i-1)]
+cudaError_t poisson_run(PoissonSolver* P, int method, double tol, int max_iter, int inner, double omega,
+                        int* iters, int* inner_total, double* rel);
 cudaError_t launch_level_mean(const KConst& kc, const double* t, const double* p_stat,
                               const double* sin_j, double* partial, double* buoy, cudaStream_t s);
 cudaError_t launch_metric_scan(const KConst& kc, const double* v, const double* w, const double* inv_rm,

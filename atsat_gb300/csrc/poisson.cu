@@ -1,0 +1,723 @@
+// Standalone solves of the pressure equation the reference relaxes (PressureSolver.h:318-495, 718-746):
+//
+//   num1 (p[i+1] + p[i-1]) + num2 (p[j+1] + p[j-1]) + num3 (p[k+1] + p[k-1]) - den p = f
+//
+// on the interior P cells (i = 1..im-2, j = 1..jm-2, k = 0..km-2), with the reference's boundary planes
+// p[0] = c43 p[1] - c13 p[2] in r and theta (folded into the rows next to them) and the periodic seam in
+// phi. num1..3 and den are the sweep weights of the column geometry (PressureSolver.h:349-353).
+//
+// The reference only smooths (one red-black Gauss-Seidel sweep per call). This file solves:
+//   * SOR: the reference's red-black update with over-relaxation, FP64 or FP32;
+//   * DIRECT: the coefficients do not depend on phi, so a real DFT over the km-1 meridians decouples
+//     the modes; each mode is a block-tridiagonal system in theta with tridiagonal radial blocks, solved by
+//     block Thomas with the inverse pivot blocks W_j = S_j^-1 factored once on the host (FP64, stored in
+//     FP64 and FP32). The zero mode is singular (constants): one cell is pinned and the result is shifted to
+//     zero interior mean; sources are made compatible by `project` (the component along the zero mode's
+//     left null vector is removed);
+//   * REFINE: FP64 defect correction with FP32 inner solves (direct or SOR sweeps): r = f - L p in FP64,
+//     e = L^-1 r in FP32, p += e, until ||r|| / ||f|| <= tol.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <omp.h>
+
+#include "dyn_common.cuh"
+
+namespace atsat {
+
+namespace {
+
+// ---- stencil helpers over the pitched layout ----
+template <typename T>
+__device__ __forceinline__ T pv_i(const KConst& K, const T* p, int i, int j, int k) {
+    const int64_t row = (int64_t)j * K.kp + k;
+    const T c43 = (T)K.c43, c13 = (T)K.c13;
+    if (i == 0) return c43 * p[K.plane + row] - c13 * p[2 * K.plane + row];
+    if (i == K.im - 1) return c43 * p[(K.im - 2) * K.plane + row] - c13 * p[(K.im - 3) * K.plane + row];
+    return p[(int64_t)i * K.plane + row];
+}
+
+template <typename T>
+__device__ __forceinline__ T pv(const KConst& K, const T* p, int i, int j, int k) {
+    const T c43 = (T)K.c43, c13 = (T)K.c13;
+    if (j == 0) return c43 * pv_i(K, p, i, 1, k) - c13 * pv_i(K, p, i, 2, k);
+    if (j == K.jm - 1) return c43 * pv_i(K, p, i, K.jm - 2, k) - c13 * pv_i(K, p, i, K.jm - 3, k);
+    return pv_i(K, p, i, j, k);
+}
+
+// boundary planes and seam from the interior (the reference's order: radial, polar, seam)
+template <typename T>
+__global__ void fold_kernel(const KConst K, T* __restrict__ p) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int im = K.im, jm = K.jm, km = K.km;
+    const int64_t nA = (int64_t)im * jm, nB = 2LL * jm * (km - 1), nC = 2LL * (im - 2) * (km - 1);
+    int i, j, k;
+    if (e < nA) {
+        i = (int)(e / jm); j = (int)(e % jm); k = km - 1;
+    } else if (e < nA + nB) {
+        const int64_t q = e - nA;
+        k = (int)(q % (km - 1));
+        const int64_t r = q / (km - 1);
+        j = (int)(r % jm);
+        i = (r / jm) ? im - 1 : 0;
+    } else if (e < nA + nB + nC) {
+        const int64_t q = e - nA - nB;
+        k = (int)(q % (km - 1));
+        const int64_t r = q / (km - 1);
+        i = 1 + (int)(r % (im - 2));
+        j = (r / (im - 2)) ? jm - 1 : 0;
+    } else {
+        return;
+    }
+    p[((int64_t)i * jm + j) * K.kp + k] = pv(K, p, i, j, (k == km - 1) ? 0 : k);
+}
+
+// one colour of red-black SOR: p <- (1 - w) p + w (acc - f) / den; the seam partner k = km-2 of an odd
+// ring is done by sor_seam_kernel after k = 0 (the reference's row order)
+template <typename T>
+__device__ __forceinline__ void sor_cell(const KConst& K, const ColGeo* __restrict__ geo, const T* __restrict__ f,
+                                         T* __restrict__ p, int i, int j, int k, T w) {
+    const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
+    const int kw = (k == 0) ? K.km - 2 : k - 1, ke = (k == K.km - 2) ? 0 : k + 1;
+    const ColGeo* g = geo + ((int64_t)i * K.jm + j);
+    const T acc = (p[c + K.plane] + p[c - K.plane]) * (T)__ldg(&g->p_num1) + (p[c + K.kp] + p[c - K.kp]) * (T)__ldg(&g->p_num2)
+                + (p[c - k + ke] + p[c - k + kw]) * (T)__ldg(&g->p_num3);
+    const T nv = (acc - f[c]) / (T)__ldg(&g->p_den);
+    p[c] = p[c] + w * (nv - p[c]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) sor_kernel(const KConst K, const ColGeo* __restrict__ geo,
+                                                  const T* __restrict__ f, T* __restrict__ p, int colour, T w) {
+    const int m = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i = blockIdx.z;
+    if (j < 1 || j > K.jm - 2 || i < 1 || i > K.im - 2) return;
+    const int k = 2 * m + ((colour - i - j) & 1);
+    if (k > K.km - 2) return;
+    if (k == K.km - 2 && k > 0 && ((K.km - 1) & 1)) return;
+    sor_cell(K, geo, f, p, i, j, k, w);
+}
+
+template <typename T>
+__global__ void sor_seam_kernel(const KConst K, const ColGeo* __restrict__ geo, const T* __restrict__ f,
+                                T* __restrict__ p, int colour, T w) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = 1 + e / (K.jm - 2), j = 1 + e % (K.jm - 2);
+    if (i > K.im - 2) return;
+    const int k = K.km - 2;
+    if (((i + j + k) & 1) != colour) return;
+    sor_cell(K, geo, f, p, i, j, k, w);
+}
+
+// r = f - L p on the interior P cells, in FP64 (p FP64), with an FP32 copy of r and the sums
+// sum r^2 and sum f^2 (sq[0], sq[1])
+__global__ void __launch_bounds__(256) residual_kernel(const KConst K, const ColGeo* __restrict__ geo,
+                                                       const double* __restrict__ f, const double* __restrict__ p,
+                                                       double* __restrict__ r, float* __restrict__ r32,
+                                                       double* __restrict__ sq) {
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i = blockIdx.z;
+    double rr = 0.0, ff = 0.0;
+    if (k <= K.km - 2 && j >= 1 && j <= K.jm - 2 && i >= 1 && i <= K.im - 2) {
+        const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
+        const int kw = (k == 0) ? K.km - 2 : k - 1, ke = (k == K.km - 2) ? 0 : k + 1;
+        const ColGeo* g = geo + ((int64_t)i * K.jm + j);
+        const double lp = (p[c + K.plane] + p[c - K.plane]) * __ldg(&g->p_num1)
+                        + (p[c + K.kp] + p[c - K.kp]) * __ldg(&g->p_num2)
+                        + (p[c - k + ke] + p[c - k + kw]) * __ldg(&g->p_num3) - __ldg(&g->p_den) * p[c];
+        const double fc = f[c];
+        const double x = fc - lp;
+        r[c] = x;
+        if (r32) r32[c] = d2f(x);
+        rr = x * x;
+        ff = fc * fc;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        rr += __shfl_down_sync(0xffffffffu, rr, o);
+        ff += __shfl_down_sync(0xffffffffu, ff, o);
+    }
+    __shared__ double s[2][8];
+    if (threadIdx.x == 0) { s[0][threadIdx.y] = rr; s[1][threadIdx.y] = ff; }
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < 8; q++) { a += s[0][q]; b += s[1][q]; }
+        atomicAdd(sq, a);
+        atomicAdd(sq + 1, b);
+    }
+}
+
+// p64 += e32 on the interior P cells
+__global__ void axpy_kernel(const KConst K, double* __restrict__ p, const float* __restrict__ e) {
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k > K.km - 2 || j < 1 || j > K.jm - 2 || i < 1 || i > K.im - 2) return;
+    const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
+    p[c] += f2d(e[c]);
+}
+
+template <typename To, typename Ti>
+__global__ void convert_kernel(const KConst K, To* __restrict__ out, const Ti* __restrict__ in) {
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= K.km || j >= K.jm) return;
+    const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
+    if (sizeof(To) == 8) out[c] = (To)f2d((float)in[c]);
+    else out[c] = (To)d2f((double)in[c]);
+}
+
+// sum of p over the interior P cells (for the zero-mean normalisation)
+template <typename T>
+__global__ void __launch_bounds__(256) sum_kernel(const KConst K, const T* __restrict__ p, double* __restrict__ out) {
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i = blockIdx.z;
+    double v = 0.0;
+    if (k <= K.km - 2 && j >= 1 && j <= K.jm - 2 && i >= 1 && i <= K.im - 2)
+        v = (double)p[((int64_t)i * K.jm + j) * K.kp + k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __shared__ double s[8];
+    if (threadIdx.x == 0) s[threadIdx.y] = v;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        double a = 0.0;
+        for (int q = 0; q < 8; q++) a += s[q];
+        atomicAdd(out, a);
+    }
+}
+
+template <typename T>
+__global__ void shift_kernel(const KConst K, T* __restrict__ p, const double* __restrict__ sum, double inv_n) {
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= K.km || j >= K.jm) return;
+    const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
+    p[c] = (T)((double)p[c] - sum[0] * inv_n);
+}
+
+// ---- spectral solve ----
+// spec layout: [(m * 2 + part) * NJ + jj] * NI + ii, part 0 = cosine, 1 = sine coefficients
+struct Spec {
+    int n, M, NI, NJ;     // ring length km-1, modes n/2+1, radial and polar unknowns
+};
+
+template <typename T>
+__global__ void dft_fwd_kernel(const KConst K, const Spec S, const T* __restrict__ x, const T* __restrict__ tw,
+                               T* __restrict__ spec) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    T* row = reinterpret_cast<T*>(dsm);             // n
+    T* tc = row + S.n;                              // cos table, n
+    T* ts = tc + S.n;                               // sin table, n
+    const int ii = blockIdx.x, jj = blockIdx.y;
+    const int i = ii + 1, j = jj + 1;
+    const int64_t base = ((int64_t)i * K.jm + j) * K.kp;
+    for (int k = threadIdx.x; k < S.n; k += blockDim.x) {
+        row[k] = x[base + k];
+        tc[k] = tw[k];
+        ts[k] = tw[S.n + k];
+    }
+    __syncthreads();
+    for (int m = threadIdx.x; m < S.M; m += blockDim.x) {
+        T a = 0, b = 0;
+        int idx = 0;
+        for (int k = 0; k < S.n; k++) {
+            a += row[k] * tc[idx];
+            b += row[k] * ts[idx];
+            idx += m;
+            if (idx >= S.n) idx -= S.n;
+        }
+        spec[((int64_t)(m * 2 + 0) * S.NJ + jj) * S.NI + ii] = a;
+        spec[((int64_t)(m * 2 + 1) * S.NJ + jj) * S.NI + ii] = b;
+    }
+}
+
+template <typename T>
+__global__ void dft_inv_kernel(const KConst K, const Spec S, const T* __restrict__ spec, const T* __restrict__ tw,
+                               T* __restrict__ x) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    T* a = reinterpret_cast<T*>(dsm);               // M
+    T* b = a + S.M;                                 // M
+    T* tc = b + S.M;                                // n
+    T* ts = tc + S.n;                               // n
+    const int ii = blockIdx.x, jj = blockIdx.y;
+    const int i = ii + 1, j = jj + 1;
+    for (int m = threadIdx.x; m < S.M; m += blockDim.x) {
+        a[m] = spec[((int64_t)(m * 2 + 0) * S.NJ + jj) * S.NI + ii];
+        b[m] = spec[((int64_t)(m * 2 + 1) * S.NJ + jj) * S.NI + ii];
+    }
+    for (int k = threadIdx.x; k < S.n; k += blockDim.x) { tc[k] = tw[k]; ts[k] = tw[S.n + k]; }
+    __syncthreads();
+    const bool even = (S.n & 1) == 0;
+    const int mtop = even ? S.M - 1 : S.M;          // modes with a conjugate partner: 1 .. mtop-1
+    const T inv_n = (T)1 / (T)S.n;
+    const int64_t base = ((int64_t)i * K.jm + j) * K.kp;
+    for (int k = threadIdx.x; k < S.n; k += blockDim.x) {
+        T s = 0;
+        int idx = k;                                  // (m k) mod n for m = 1
+        for (int m = 1; m < mtop; m++) {
+            s += a[m] * tc[idx] + b[m] * ts[idx];
+            idx += k;
+            if (idx >= S.n) idx -= S.n;
+        }
+        T v = a[0] + (T)2 * s;
+        if (even) v += a[S.M - 1] * ((k & 1) ? (T)-1 : (T)1);
+        x[base + k] = v * inv_n;
+    }
+}
+
+// Block Thomas for one (mode, part): g_j = f_j - b_j * (W_{j-1} g_{j-1}); x_NJ = W_NJ g_NJ;
+// x_j = W_j (g_j - c_j * x_{j+1}). W is column-major per block; b, c are the theta couplings (mode
+// independent); the zero mode pins the cell (1, 1) (its row of D_1 is the identity, its c is 0, f = 0).
+template <typename T>
+__global__ void bt_solve_kernel(const Spec S, const T* __restrict__ W, const double* __restrict__ bvec,
+                                const double* __restrict__ cvec, T* __restrict__ spec) {
+    const int m = blockIdx.x >> 1, part = blockIdx.x & 1;
+    const bool even = (S.n & 1) == 0;
+    if (part == 1 && (m == 0 || (even && m == S.M - 1))) return;   // sine part identically zero
+    const int NI = S.NI, NJ = S.NJ;
+    extern __shared__ __align__(16) unsigned char dsm[];
+    T* g = reinterpret_cast<T*>(dsm);   // NI
+    T* t = g + NI;                      // NI
+    T* f = spec + (int64_t)(m * 2 + part) * NJ * NI;
+    const T* Wm = W + (int64_t)m * NJ * NI * NI;
+    const int r = threadIdx.x;
+    const bool pin = (m == 0 && part == 0);
+    // forward
+    if (r < NI) g[r] = (pin && r == 0) ? (T)0 : f[r];
+    __syncthreads();
+    for (int jj = 1; jj < NJ; jj++) {
+        if (r < NI) {
+            const T* Wp = Wm + (int64_t)(jj - 1) * NI * NI;
+            T acc = 0;
+            for (int c = 0; c < NI; c++) acc += Wp[(int64_t)c * NI + r] * g[c];
+            t[r] = f[(int64_t)jj * NI + r] - (T)bvec[jj * NI + r] * acc;
+        }
+        __syncthreads();
+        if (r < NI) {
+            f[(int64_t)(jj - 1) * NI + r] = g[r];     // keep g_{j-1} for the backward pass
+            g[r] = t[r];
+        }
+        __syncthreads();
+    }
+    // backward: x_NJ = W_NJ g_NJ
+    {
+        const T* Wp = Wm + (int64_t)(NJ - 1) * NI * NI;
+        T acc = 0;
+        if (r < NI) for (int c = 0; c < NI; c++) acc += Wp[(int64_t)c * NI + r] * g[c];
+        __syncthreads();
+        if (r < NI) { g[r] = acc; f[(int64_t)(NJ - 1) * NI + r] = acc; }
+        __syncthreads();
+    }
+    for (int jj = NJ - 2; jj >= 0; jj--) {
+        if (r < NI) {
+            T cc = (T)cvec[jj * NI + r];
+            if (pin && jj == 0 && r == 0) cc = 0;
+            t[r] = f[(int64_t)jj * NI + r] - cc * g[r];
+        }
+        __syncthreads();
+        if (r < NI) {
+            const T* Wp = Wm + (int64_t)jj * NI * NI;
+            T acc = 0;
+            for (int c = 0; c < NI; c++) acc += Wp[(int64_t)c * NI + r] * t[c];
+            g[r] = acc;
+            f[(int64_t)jj * NI + r] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+dim3 cell_grid(const KConst& K) { return dim3((K.km + 31) / 32, (K.jm + 7) / 8, K.im); }
+
+// Gauss-Jordan inverse with partial pivoting of an n x n row-major matrix (in place into inv)
+bool invert(int n, std::vector<double>& a, std::vector<double>& inv) {
+    inv.assign((size_t)n * n, 0.0);
+    for (int q = 0; q < n; q++) inv[(size_t)q * n + q] = 1.0;
+    for (int c = 0; c < n; c++) {
+        int piv = c;
+        for (int r = c + 1; r < n; r++)
+            if (std::fabs(a[(size_t)r * n + c]) > std::fabs(a[(size_t)piv * n + c])) piv = r;
+        if (!(std::fabs(a[(size_t)piv * n + c]) > 0.0)) return false;
+        if (piv != c)
+            for (int q = 0; q < n; q++) {
+                std::swap(a[(size_t)c * n + q], a[(size_t)piv * n + q]);
+                std::swap(inv[(size_t)c * n + q], inv[(size_t)piv * n + q]);
+            }
+        const double d = 1.0 / a[(size_t)c * n + c];
+        for (int q = 0; q < n; q++) { a[(size_t)c * n + q] *= d; inv[(size_t)c * n + q] *= d; }
+        for (int r = 0; r < n; r++) {
+            if (r == c) continue;
+            const double fct = a[(size_t)r * n + c];
+            if (fct == 0.0) continue;
+            for (int q = 0; q < n; q++) {
+                a[(size_t)r * n + q] -= fct * a[(size_t)c * n + q];
+                inv[(size_t)r * n + q] -= fct * inv[(size_t)c * n + q];
+            }
+        }
+    }
+    return true;
+}
+
+}  // namespace
+
+struct PoissonSolver {
+    KConst K{};
+    Spec S{};
+    cudaStream_t stream = nullptr;
+    const ColGeo* geo = nullptr;          // device column geometry (owned by the handle)
+    std::vector<double> num1, num2, num3, den;   // host, [jj * NI + ii]
+    std::vector<double> bvec, cvec;       // host theta couplings
+    // device
+    double *f64 = nullptr, *p64 = nullptr, *r64 = nullptr, *sq = nullptr, *W64 = nullptr, *spec64 = nullptr;
+    double *bvec_d = nullptr, *cvec_d = nullptr, *tw64 = nullptr;
+    float *p32 = nullptr, *r32 = nullptr, *e32 = nullptr, *W32 = nullptr, *spec32 = nullptr, *tw32 = nullptr;
+    std::vector<double> ynull;            // left null vector of the zero mode, [jj * NI + ii]
+    void* block = nullptr;
+    int64_t n_interior = 0;
+};
+
+namespace {
+
+// D_j(m) as a dense NI x NI row-major matrix; `pin`: the zero mode's cell (1, 1) becomes x = 0
+void build_D(const PoissonSolver& P, int m, int jj, std::vector<double>& D, bool pin = true) {
+    const int NI = P.S.NI, NJ = P.S.NJ;
+    const double c43 = P.K.c43, c13 = P.K.c13;
+    const double cth = std::cos(2.0 * M_PI * (double)m / (double)P.S.n);
+    D.assign((size_t)NI * NI, 0.0);
+    for (int ii = 0; ii < NI; ii++) {
+        const size_t q = (size_t)jj * NI + ii;
+        double d = -P.den[q] + 2.0 * P.num3[q] * cth;
+        if (jj == 0) d += c43 * P.num2[q];
+        if (jj == NJ - 1) d += c43 * P.num2[q];
+        if (ii == 0) d += c43 * P.num1[q];
+        if (ii == NI - 1) d += c43 * P.num1[q];
+        D[(size_t)ii * NI + ii] = d;
+        if (ii + 1 < NI) D[(size_t)ii * NI + ii + 1] = P.num1[q] * (ii == 0 ? 1.0 - c13 : 1.0);
+        if (ii > 0) D[(size_t)ii * NI + ii - 1] = P.num1[q] * (ii == NI - 1 ? 1.0 - c13 : 1.0);
+    }
+    if (pin && m == 0 && jj == 0) {           // the pinned cell (1, 1)
+        for (int q = 0; q < NI; q++) D[q] = 0.0;
+        D[0] = 1.0;
+    }
+}
+
+}  // namespace
+
+PoissonSolver* poisson_create(const KConst& kc, const ColGeo* geo_dev, const std::vector<ColGeo>& geo_h,
+                              cudaStream_t s, std::string* err) {
+    if (kc.im < 5 || kc.jm < 5 || kc.km < 4) { *err = "poisson: grid too small (im, jm >= 5, km >= 4)"; return nullptr; }
+    auto* P = new PoissonSolver();
+    P->K = kc;
+    P->stream = s;
+    P->geo = geo_dev;
+    Spec& S = P->S;
+    S.n = kc.km - 1;
+    S.M = S.n / 2 + 1;
+    S.NI = kc.im - 2;
+    S.NJ = kc.jm - 2;
+    if (S.NI > 1024) { *err = "poisson: im too large"; delete P; return nullptr; }
+    const int NI = S.NI, NJ = S.NJ;
+    P->n_interior = (int64_t)NI * NJ * S.n;
+    const size_t nc = (size_t)NI * NJ;
+    P->num1.resize(nc); P->num2.resize(nc); P->num3.resize(nc); P->den.resize(nc);
+    for (int jj = 0; jj < NJ; jj++)
+        for (int ii = 0; ii < NI; ii++) {
+            const ColGeo& g = geo_h[(size_t)(ii + 1) * kc.jm + (jj + 1)];
+            const size_t q = (size_t)jj * NI + ii;
+            P->num1[q] = g.p_num1; P->num2[q] = g.p_num2; P->num3[q] = g.p_num3; P->den[q] = g.p_den;
+        }
+    P->bvec.assign(nc, 0.0);
+    P->cvec.assign(nc, 0.0);
+    for (int jj = 0; jj < NJ; jj++)
+        for (int ii = 0; ii < NI; ii++) {
+            const size_t q = (size_t)jj * NI + ii;
+            P->bvec[q] = P->num2[q] * (jj == NJ - 1 ? 1.0 - kc.c13 : 1.0);   // coefficient of x_{j-1}
+            P->cvec[q] = P->num2[q] * (jj == 0 ? 1.0 - kc.c13 : 1.0);        // coefficient of x_{j+1}
+        }
+    // the inverse pivot blocks of every mode (FP64), then an FP32 copy
+    const size_t blk = (size_t)NI * NI;
+    std::vector<double> W((size_t)S.M * NJ * blk);
+    bool ok = true;
+#pragma omp parallel for schedule(dynamic)
+    for (int m = 0; m < S.M; m++) {
+        std::vector<double> D, Sm, inv;
+        double* Wm = W.data() + (size_t)m * NJ * blk;
+        for (int jj = 0; jj < NJ; jj++) {
+            build_D(*P, m, jj, D);
+            Sm = D;
+            if (jj > 0) {
+                const double* Wp = Wm + (size_t)(jj - 1) * blk;     // column-major W_{j-1}
+                for (int r = 0; r < NI; r++) {
+                    const double b = P->bvec[(size_t)jj * NI + r];
+                    for (int c = 0; c < NI; c++) {
+                        double cc = P->cvec[(size_t)(jj - 1) * NI + c];
+                        if (m == 0 && jj - 1 == 0 && c == 0) cc = 0.0;
+                        Sm[(size_t)r * NI + c] -= b * Wp[(size_t)c * NI + r] * cc;
+                    }
+                }
+            }
+            if (!invert(NI, Sm, inv)) {
+#pragma omp atomic write
+                ok = false;
+                break;
+            }
+            double* Wj = Wm + (size_t)jj * blk;
+            for (int r = 0; r < NI; r++)
+                for (int c = 0; c < NI; c++) Wj[(size_t)c * NI + r] = inv[(size_t)r * NI + c];
+        }
+    }
+    if (!ok) { *err = "poisson: singular pivot block"; delete P; return nullptr; }
+    // Left null vector of the unpinned zero-mode operator A0 (host, once): A0^T y = 0 with the transposed
+    // equation of cell (1, 1) replaced by y(1, 1) = 1. A0^T is block tridiagonal: block row j holds
+    // diag(cvec[j-1]) y_{j-1} + D_j^T y_j + diag(bvec[j+1]) y_{j+1}.
+    {
+        std::vector<std::vector<double>> Winv(NJ), g(NJ);
+        std::vector<double> D, Sm(blk), inv;
+        auto upper = [&](int jj, int c) {            // U_jj = diag(bvec[jj+1]), its pinned row zeroed
+            return (jj == 0 && c == 0) ? 0.0 : P->bvec[(size_t)(jj + 1) * NI + c];
+        };
+        for (int jj = 0; jj < NJ; jj++) {
+            build_D(*P, 0, jj, D, false);
+            for (int r = 0; r < NI; r++)
+                for (int c = 0; c < NI; c++) Sm[(size_t)r * NI + c] = D[(size_t)c * NI + r];
+            std::vector<double> rhs(NI, 0.0);
+            if (jj == 0) {
+                for (int c = 0; c < NI; c++) Sm[c] = (c == 0) ? 1.0 : 0.0;
+                rhs[0] = 1.0;
+            } else {
+                std::vector<double> wg(NI, 0.0);
+                for (int r = 0; r < NI; r++) {
+                    const double low = P->cvec[(size_t)(jj - 1) * NI + r];
+                    for (int c = 0; c < NI; c++) {
+                        Sm[(size_t)r * NI + c] -= low * Winv[jj - 1][(size_t)r * NI + c] * upper(jj - 1, c);
+                        wg[r] += Winv[jj - 1][(size_t)r * NI + c] * g[jj - 1][c];
+                    }
+                    rhs[r] -= low * wg[r];
+                }
+            }
+            if (!invert(NI, Sm, inv)) { *err = "poisson: singular block (null vector)"; delete P; return nullptr; }
+            Winv[jj] = inv;
+            g[jj] = rhs;
+        }
+        P->ynull.assign(nc, 0.0);
+        std::vector<double> t(NI), ynext(NI, 0.0);
+        for (int jj = NJ - 1; jj >= 0; jj--) {
+            for (int r = 0; r < NI; r++) t[r] = g[jj][r] - ((jj + 1 < NJ) ? upper(jj, r) * ynext[r] : 0.0);
+            for (int r = 0; r < NI; r++) {
+                double a = 0.0;
+                for (int c = 0; c < NI; c++) a += Winv[jj][(size_t)r * NI + c] * t[c];
+                P->ynull[(size_t)jj * NI + r] = a;
+            }
+            for (int r = 0; r < NI; r++) ynext[r] = P->ynull[(size_t)jj * NI + r];
+        }
+    }
+    // device buffers
+    const size_t fsz = (size_t)kc.fsz;
+    const size_t nspec = (size_t)S.M * 2 * nc;
+    const size_t nW = (size_t)S.M * NJ * blk;
+    size_t bytes = 0;
+    auto take = [&](size_t b) { size_t o = bytes; bytes += (b + 255) & ~size_t(255); return o; };
+    const size_t o_f = take(fsz * 8), o_p = take(fsz * 8), o_r = take(fsz * 8), o_sq = take(64);
+    const size_t o_W64 = take(nW * 8), o_s64 = take(nspec * 8), o_b = take(nc * 8), o_c = take(nc * 8);
+    const size_t o_tw64 = take((size_t)2 * S.n * 8), o_p32 = take(fsz * 4), o_r32 = take(fsz * 4), o_e32 = take(fsz * 4);
+    const size_t o_W32 = take(nW * 4), o_s32 = take(nspec * 4), o_tw32 = take((size_t)2 * S.n * 4);
+    cudaError_t e = cudaMalloc(&P->block, bytes);
+    if (e != cudaSuccess) { *err = std::string("poisson: cudaMalloc: ") + cudaGetErrorString(e); delete P; return nullptr; }
+    char* b0 = static_cast<char*>(P->block);
+    P->f64 = reinterpret_cast<double*>(b0 + o_f);
+    P->p64 = reinterpret_cast<double*>(b0 + o_p);
+    P->r64 = reinterpret_cast<double*>(b0 + o_r);
+    P->sq = reinterpret_cast<double*>(b0 + o_sq);
+    P->W64 = reinterpret_cast<double*>(b0 + o_W64);
+    P->spec64 = reinterpret_cast<double*>(b0 + o_s64);
+    P->bvec_d = reinterpret_cast<double*>(b0 + o_b);
+    P->cvec_d = reinterpret_cast<double*>(b0 + o_c);
+    P->tw64 = reinterpret_cast<double*>(b0 + o_tw64);
+    P->p32 = reinterpret_cast<float*>(b0 + o_p32);
+    P->r32 = reinterpret_cast<float*>(b0 + o_r32);
+    P->e32 = reinterpret_cast<float*>(b0 + o_e32);
+    P->W32 = reinterpret_cast<float*>(b0 + o_W32);
+    P->spec32 = reinterpret_cast<float*>(b0 + o_s32);
+    P->tw32 = reinterpret_cast<float*>(b0 + o_tw32);
+    std::vector<float> W32(nW);
+    for (size_t q = 0; q < nW; q++) W32[q] = (float)W[q];
+    std::vector<double> tw(2 * S.n);
+    std::vector<float> tw32(2 * S.n);
+    for (int k = 0; k < S.n; k++) {
+        tw[k] = std::cos(2.0 * M_PI * k / S.n);
+        tw[S.n + k] = std::sin(2.0 * M_PI * k / S.n);
+    }
+    for (int q = 0; q < 2 * S.n; q++) tw32[q] = (float)tw[q];
+    if ((e = cudaMemsetAsync(P->block, 0, bytes, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(P->W64, W.data(), nW * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(P->W32, W32.data(), nW * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(P->bvec_d, P->bvec.data(), nc * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(P->cvec_d, P->cvec.data(), nc * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(P->tw64, tw.data(), 2 * S.n * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(P->tw32, tw32.data(), 2 * S.n * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+        *err = std::string("poisson: upload: ") + cudaGetErrorString(e);
+        cudaFree(P->block);
+        delete P;
+        return nullptr;
+    }
+    return P;
+}
+
+void poisson_destroy(PoissonSolver* P) {
+    if (!P) return;
+    if (P->block) cudaFree(P->block);
+    delete P;
+}
+
+double* poisson_f(PoissonSolver* P) { return P->f64; }
+double* poisson_p(PoissonSolver* P) { return P->p64; }
+const std::vector<double>& poisson_null_vector(PoissonSolver* P) { return P->ynull; }
+int poisson_modes(PoissonSolver* P) { return P->S.M; }
+
+namespace {
+
+template <typename T>
+cudaError_t fold(PoissonSolver* P, T* p) {
+    const KConst& K = P->K;
+    const int64_t n = (int64_t)K.im * K.jm + 2LL * K.jm * (K.km - 1) + 2LL * (K.im - 2) * (K.km - 1);
+    fold_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, P->stream>>>(K, p);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t sor_sweep(PoissonSolver* P, const T* f, T* p, T w) {
+    const KConst& K = P->K;
+    const int nm = (K.km - 1 + 1) / 2;
+    const dim3 grid((nm + 31) / 32, (K.jm + 7) / 8, K.im), block(32, 8);
+    for (int colour = 0; colour < 2; colour++) {
+        sor_kernel<T><<<grid, block, 0, P->stream>>>(K, P->geo, f, p, colour, w);
+        if (((K.km - 1) & 1) && K.km - 2 > 0) {
+            const int n = (K.im - 2) * (K.jm - 2);
+            sor_seam_kernel<T><<<(n + 255) / 256, 256, 0, P->stream>>>(K, P->geo, f, p, colour, w);
+        }
+    }
+    return fold(P, p);
+}
+
+// x = L^-1 rhs by the spectral block solve in precision T (rhs and x pitched; x may alias rhs)
+template <typename T>
+cudaError_t direct(PoissonSolver* P, const T* rhs, T* x, T* spec, const T* W, const T* tw) {
+    const KConst& K = P->K;
+    const Spec& S = P->S;
+    const dim3 rows(S.NI, S.NJ);
+    dft_fwd_kernel<T><<<rows, 128, (size_t)3 * S.n * sizeof(T), P->stream>>>(K, S, rhs, tw, spec);
+    const int thr = ((S.NI + 31) / 32) * 32;
+    bt_solve_kernel<T><<<2 * S.M, thr, (size_t)2 * S.NI * sizeof(T), P->stream>>>(S, W, P->bvec_d, P->cvec_d, spec);
+    dft_inv_kernel<T><<<rows, 128, (size_t)(2 * S.M + 2 * S.n) * sizeof(T), P->stream>>>(K, S, spec, tw, x);
+    // zero interior mean (the zero mode's pinned constant), then the boundary planes
+    cudaMemsetAsync(P->sq + 2, 0, sizeof(double), P->stream);
+    sum_kernel<T><<<cell_grid(K), dim3(32, 8), 0, P->stream>>>(K, x, P->sq + 2);
+    shift_kernel<T><<<cell_grid(K), dim3(32, 8), 0, P->stream>>>(K, x, P->sq + 2, 1.0 / (double)P->n_interior);
+    return fold(P, x);
+}
+
+// ||f - L p|| / ||f|| with r64 (and r32) written
+cudaError_t residual(PoissonSolver* P, double* rel) {
+    const KConst& K = P->K;
+    cudaError_t e = cudaMemsetAsync(P->sq, 0, 2 * sizeof(double), P->stream);
+    if (e != cudaSuccess) return e;
+    residual_kernel<<<cell_grid(K), dim3(32, 8), 0, P->stream>>>(K, P->geo, P->f64, P->p64, P->r64, P->r32, P->sq);
+    double h[2];
+    if ((e = cudaMemcpyAsync(h, P->sq, sizeof(h), cudaMemcpyDeviceToHost, P->stream)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(P->stream)) != cudaSuccess) return e;
+    *rel = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : std::sqrt(h[0]);
+    return cudaSuccess;
+}
+
+}  // namespace
+
+// Solve L p = f (f in P->f64, result in P->p64, both pitched, boundary planes folded).
+// method: 0 SOR64, 1 SOR32, 2 REFINE with FP32 SOR inner sweeps, 3 DIRECT64, 4 DIRECT32,
+// 5 REFINE with FP32 direct inner solves. Iterations: sweeps (0, 1), outer corrections (2, 5), 1 (3, 4).
+cudaError_t poisson_run_inner(PoissonSolver* P, int method, double tol, int max_iter, int inner, double omega,
+                              int* iters, int* inner_total, double* rel);
+
+// the solve, then the result shifted to zero interior mean (solutions are defined up to a constant)
+cudaError_t poisson_run(PoissonSolver* P, int method, double tol, int max_iter, int inner, double omega,
+                        int* iters, int* inner_total, double* rel) {
+    cudaError_t e = poisson_run_inner(P, method, tol, max_iter, inner, omega, iters, inner_total, rel);
+    if (e != cudaSuccess) return e;
+    const KConst& K = P->K;
+    if ((e = cudaMemsetAsync(P->sq + 2, 0, sizeof(double), P->stream)) != cudaSuccess) return e;
+    sum_kernel<double><<<cell_grid(K), dim3(32, 8), 0, P->stream>>>(K, P->p64, P->sq + 2);
+    shift_kernel<double><<<cell_grid(K), dim3(32, 8), 0, P->stream>>>(K, P->p64, P->sq + 2, 1.0 / (double)P->n_interior);
+    if ((e = fold<double>(P, P->p64)) != cudaSuccess) return e;
+    return cudaStreamSynchronize(P->stream);
+}
+
+cudaError_t poisson_run_inner(PoissonSolver* P, int method, double tol, int max_iter, int inner, double omega,
+                              int* iters, int* inner_total, double* rel) {
+    const KConst& K = P->K;
+    cudaError_t e;
+    *iters = 0;
+    *inner_total = 0;
+    const size_t fsz = (size_t)K.fsz;
+    if (method == 3) {
+        e = direct<double>(P, P->f64, P->p64, P->spec64, P->W64, P->tw64);
+        if (e != cudaSuccess) return e;
+        *iters = 1;
+        return residual(P, rel);
+    }
+    if (method == 4) {
+        convert_kernel<float, double><<<cell_grid(K), dim3(32, 8), 0, P->stream>>>(K, P->r32, P->f64);
+        e = direct<float>(P, P->r32, P->p32, P->spec32, P->W32, P->tw32);
+        if (e != cudaSuccess) return e;
+        convert_kernel<double, float><<<cell_grid(K), dim3(32, 8), 0, P->stream>>>(K, P->p64, P->p32);
+        *iters = 1;
+        return residual(P, rel);
+    }
+    if ((e = cudaMemsetAsync(P->p64, 0, fsz * 8, P->stream)) != cudaSuccess) return e;
+    if (method == 0 || method == 1) {
+        const int check = 50;
+        if (method == 1) {
+            if ((e = cudaMemsetAsync(P->p32, 0, fsz * 4, P->stream)) != cudaSuccess) return e;
+            convert_kernel<float, double><<<cell_grid(K), dim3(32, 8), 0, P->stream>>>(K, P->e32, P->f64);
+        }
+        *rel = 1.0;
+        for (int it = 1; it <= max_iter; it++) {
+            e = (method == 0) ? sor_sweep<double>(P, P->f64, P->p64, omega)
+                              : sor_sweep<float>(P, P->e32, P->p32, (float)omega);
+            if (e != cudaSuccess) return e;
+            *iters = it;
+            if (it % check == 0 || it == max_iter) {
+                if (method == 1) convert_kernel<double, float><<<cell_grid(K), dim3(32, 8), 0, P->stream>>>(K, P->p64, P->p32);
+                if ((e = residual(P, rel)) != cudaSuccess) return e;
+                if (*rel <= tol) break;
+            }
+        }
+        return cudaSuccess;
+    }
+    // defect correction: p64 = 0; r = f - L p; e = L^-1 r (FP32); p += e
+    for (int it = 0; it <= max_iter; it++) {
+        if ((e = residual(P, rel)) != cudaSuccess) return e;
+        if (*rel <= tol || it == max_iter) break;
+        if (method == 5) {
+            e = direct<float>(P, P->r32, P->e32, P->spec32, P->W32, P->tw32);
+            *inner_total += 1;
+        } else {
+            if ((e = cudaMemsetAsync(P->e32, 0, fsz * 4, P->stream)) != cudaSuccess) return e;
+            for (int s = 0; s < inner && e == cudaSuccess; s++) e = sor_sweep<float>(P, P->r32, P->e32, (float)omega);
+            *inner_total += inner;
+        }
+        if (e != cudaSuccess) return e;
+        axpy_kernel<<<cell_grid(K), dim3(32, 8), 0, P->stream>>>(K, P->p64, P->e32);
+        if ((e = fold<double>(P, P->p64)) != cudaSuccess) return e;
+        *iters = it + 1;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace atsat

@@ -81,6 +81,9 @@ def lib():
         L.atsat_dyn_set_stage_variant.argtypes = [H, C.c_int32]
         L.atsat_dyn_get_stage_variant.argtypes = [H, C.POINTER(C.c_int32)]
         L.atsat_dyn_autotune.argtypes = [H, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+        L.atsat_dyn_poisson_project.argtypes = [H, C.POINTER(C.c_double)]
+        L.atsat_dyn_poisson_solve.argtypes = [H, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double,
+                                              C.c_int32, C.c_int32, C.c_double, C.POINTER(abi.PoissonStats)]
         L.atsat_dyn_timer_start.argtypes = [H]
         L.atsat_dyn_timer_stop.argtypes = [H, C.POINTER(C.c_double)]
         _lib = L
@@ -224,6 +227,27 @@ class Dycore:
         ms = (C.c_double * len(self.STAGE_NAMES))()
         self._ck(lib().atsat_dyn_autotune(self.h, int(reps), C.byref(chosen), ms), "autotune")
         return chosen.value, list(ms)
+
+    # ---- standalone pressure-equation solves (no reference counterpart) ----
+    def poisson_project(self, src: np.ndarray) -> np.ndarray:
+        """A copy of `src` (im x jm x km) without its component outside the operator's range."""
+        out = np.ascontiguousarray(src, dtype=np.float64).copy()
+        assert out.shape == self.grid.shape
+        self._ck(lib().atsat_dyn_poisson_project(self.h, abi.dptr(out)), "poisson_project")
+        return out
+
+    def poisson_solve(self, method, src: np.ndarray, tol: float = 1e-10, max_iter: int = 100, inner: int = 0,
+                      omega: float = 1.0):
+        """Solve L p = src with `method` (a name of abi.POISSON_METHODS or its index); returns (p, stats)."""
+        m = abi.POISSON_METHODS.index(method) if isinstance(method, str) else int(method)
+        f = np.ascontiguousarray(src, dtype=np.float64)
+        assert f.shape == self.grid.shape
+        p = np.zeros(self.grid.shape)
+        st = abi.PoissonStats()
+        self._ck(lib().atsat_dyn_poisson_solve(self.h, m, abi.dptr(f), abi.dptr(p), float(tol), int(max_iter),
+                                               int(inner), float(omega), C.byref(st)), "poisson_solve")
+        return p, {"method": abi.POISSON_METHODS[m], "iterations": st.iterations, "inner": st.inner,
+                   "converged": bool(st.converged), "rel_residual": st.rel_residual, "ms": st.ms}
 
     # ---- the reference's entry points ----
     def computeMixtureDensity(self):

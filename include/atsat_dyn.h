@@ -304,6 +304,41 @@ int atsat_dyn_get_stage_variant(atsat_dyn_t h, int32_t* variant);
  * only scratch buffers, so the model state is unchanged. No reference counterpart. */
 int atsat_dyn_autotune(atsat_dyn_t h, int32_t reps, int32_t* chosen, double* ms);
 
+/* ---- standalone solves of the pressure equation ----
+ * The equation the reference relaxes (PressureSolver.h:318-495 with the boundary planes of :718-746):
+ *   num1 (p[i+1] + p[i-1]) + num2 (p[j+1] + p[j-1]) + num3 (p[k+1] + p[k-1]) - den p = src
+ * on i = 1..im-2, j = 1..jm-2, k = 0..km-2, p[0] = c43 p[1] - c13 p[2] in r and theta, periodic in phi.
+ * No reference counterpart: the reference only smooths (one red-black sweep per call). Methods:
+ *   SOR64 / SOR32   red-black SOR (the reference's update, over-relaxed by omega), max_iter sweeps or
+ *                   until ||src - L p|| / ||src|| <= tol (checked every 50 sweeps);
+ *   REFINE_SOR      FP64 defect correction, `inner` FP32 SOR sweeps per correction;
+ *   DIRECT64 / 32   real DFT over phi and a block-tridiagonal solve per mode (exact up to rounding);
+ *   REFINE_DIRECT   FP64 defect correction with FP32 direct inner solves, until tol or max_iter corrections.
+ * Arrays are host, contiguous im x jm x km. The operator is singular (constants): results are shifted to
+ * zero mean over the interior, and a source should first be made compatible by
+ * atsat_dyn_poisson_project (removes its component outside the operator's range, in place). */
+enum {
+    ATSAT_POISSON_SOR64 = 0,
+    ATSAT_POISSON_SOR32 = 1,
+    ATSAT_POISSON_REFINE_SOR = 2,
+    ATSAT_POISSON_DIRECT64 = 3,
+    ATSAT_POISSON_DIRECT32 = 4,
+    ATSAT_POISSON_REFINE_DIRECT = 5,
+    ATSAT_POISSON_NMETHOD = 6
+};
+typedef struct atsat_dyn_poisson_stats {
+    int32_t method;
+    int32_t iterations;        /* sweeps (SOR), corrections (REFINE_*), 1 (DIRECT*) */
+    int32_t inner;             /* inner sweeps or inner solves in total (REFINE_*) */
+    int32_t converged;         /* final relative residual <= tol */
+    double  rel_residual;      /* ||src - L p||_2 / ||src||_2 in FP64 */
+    double  ms;                /* device time of the solve (CUDA events) */
+    double  reserved[4];
+} atsat_dyn_poisson_stats;
+int atsat_dyn_poisson_project(atsat_dyn_t h, double* src);
+int atsat_dyn_poisson_solve(atsat_dyn_t h, int32_t method, const double* src, double* p, double tol,
+                            int32_t max_iter, int32_t inner, double omega, atsat_dyn_poisson_stats* st);
+
 /* Pinned host memory for bound arrays (cudaHostAlloc / cudaFreeHost). */
 void* atsat_dyn_host_alloc(size_t bytes);
 void  atsat_dyn_host_free(void* p);
