@@ -103,6 +103,10 @@ struct atsat_dyn {
     unsigned int* dev_err = nullptr;     // device status word of the bounded waits
     int timeouts = 0;
     PoissonSolver* poisson = nullptr;    // standalone pressure-equation solver, built on first use
+    // a captured CUDA graph of `graph_iters` resident iterations (atsat_dyn_graph_capture)
+    cudaGraphExec_t graph = nullptr;
+    int32_t graph_iters = 0;
+    int64_t graph_kernels = 0;
     std::string err;
 };
 
@@ -987,16 +991,19 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
     if ((e = cudaGetDevice(&h->device)) != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
     if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
         return cuda_fail(e, "cudaStreamCreate");
-    // fields, stage buffers, accumulators, source; then the small tables
-    const int64_t nbig = ATSAT_NFIELDS + 2 * NPROG + 2;
+    // fields, FP64 stage buffers and accumulators (FP64 path only), source; then the small tables
+    const bool fp64_stage = p->precision != ATSAT_DYN_MIXED;
+    const int64_t nbig = ATSAT_NFIELDS + (fp64_stage ? 2 * NPROG : 0) + 2;
     const int64_t nsmall = 2LL * K.im * 16 + K.im + K.jm + K.im + K.jm + 64;
     const size_t bytes = (size_t)(nbig * K.fsz + nsmall) * 8 + sizeof(ColGeo) * (size_t)K.im * K.jm + 4096;
     if ((e = cudaMalloc(&h->slab, bytes)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
     if ((e = cudaMemsetAsync(h->slab, 0, bytes, h->stream)) != cudaSuccess) return cuda_fail(e, "cudaMemset");
     double* q = h->slab;
     for (int f = 0; f < ATSAT_NFIELDS; f++) { h->f[f] = q; q += K.fsz; }
-    for (int s = 0; s < NPROG; s++) { h->stage[s] = q; q += K.fsz; }
-    for (int s = 0; s < NPROG; s++) { h->acc[s] = q; q += K.fsz; }
+    if (fp64_stage) {
+        for (int s = 0; s < NPROG; s++) { h->stage[s] = q; q += K.fsz; }
+        for (int s = 0; s < NPROG; s++) { h->acc[s] = q; q += K.fsz; }
+    }
     h->src = q; q += K.fsz;
     h->p_baro = q; q += K.fsz;
     h->partial = q; q += 2LL * K.im * 16;
@@ -1068,6 +1075,7 @@ void atsat_dyn_destroy(atsat_dyn_t h) {
     for (auto e : h->pool) cudaEventDestroy(e);
     for (auto e : h->timer) if (e) cudaEventDestroy(e);
     poisson_destroy(h->poisson);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
     if (h->slab) cudaFree(h->slab);
     if (h->slab32) cudaFree(h->slab32);
     if (h->pinned) cudaFreeHost(h->pinned);
@@ -1258,26 +1266,130 @@ int atsat_dyn_boundary_conditions(atsat_dyn_t h) {
     return rc ? rc : finish(h);
 }
 
+}  // extern "C"
+
+namespace {
+
+// one resident dycore iteration (cSaturnModel.cpp:864-1111 restricted to the dycore), enqueued
+int enqueue_iteration(atsat_dyn* h, int32_t it) {
+    int rc;
+    if (it % 2 == 0) {
+        {
+            Timed t(h, ATSAT_K_GLUE);
+            CK(h, launch_density(h->kc, h->f[ATSAT_F_T], h->f[ATSAT_F_P_STAT], h->p.R_mix, h->f[ATSAT_F_RHO_MIX],
+                                 h->stream));
+            h->launches += 1;
+            mark_dirty(h, ATSAT_F_RHO_MIX);
+        }
+        if ((rc = enqueue_pressure(h, h->p.press_sweeps > 0 ? h->p.press_sweeps : 1))) return rc;
+    }
+    if ((rc = enqueue_rk4(h, true))) return rc;
+    if ((rc = enqueue_bc(h, true))) return rc;
+    return enqueue_restore(h, true);
+}
+
+bool resident_steady(const atsat_dyn* h) {
+    if (h->p.precision != ATSAT_DYN_MIXED) return true;
+    if (!(h->aliased && h->shadow_valid && h->dl_edges_zero)) return false;
+    for (int s = 0; s < NCONV; s++)
+        if (h->conv_dirty[s]) return false;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
 int atsat_dyn_iterate(atsat_dyn_t h, int32_t iter0, int32_t n) {
     ENTRY(h);
     if (n < 0) return fail(h, ATSAT_DYN_E_INVALID, "negative iteration count");
     for (int32_t it = iter0; it < iter0 + n; it++) {
-        int rc;
-        if (it % 2 == 0) {
-            {
-                Timed t(h, ATSAT_K_GLUE);
-                CK(h, launch_density(h->kc, h->f[ATSAT_F_T], h->f[ATSAT_F_P_STAT], h->p.R_mix, h->f[ATSAT_F_RHO_MIX],
-                                     h->stream));
-                h->launches += 1;
-                mark_dirty(h, ATSAT_F_RHO_MIX);
-            }
-            if ((rc = enqueue_pressure(h, h->p.press_sweeps > 0 ? h->p.press_sweeps : 1))) return rc;
-        }
-        if ((rc = enqueue_rk4(h, true))) return rc;
-        if ((rc = enqueue_bc(h, true))) return rc;
-        if ((rc = enqueue_restore(h, true))) return rc;
+        const int rc = enqueue_iteration(h, it);
+        if (rc) return rc;
     }
     return finish(h);
+}
+
+int atsat_dyn_graph_capture(atsat_dyn_t h, int32_t iter0, int32_t n) {
+    ENTRY(h);
+    if (n < 2 || (n & 1)) return fail(h, ATSAT_DYN_E_INVALID, "graph_capture: n must be even and >= 2");
+    if (!resident_steady(h))
+        return fail(h, ATSAT_DYN_E_INVALID, "graph_capture: run two resident iterations first (the mixed path's "
+                    "resident buffers are not established yet)");
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    const bool prof = h->profiling;
+    h->profiling = false;
+    const int64_t l0 = h->launches;
+    cudaGraph_t g = nullptr;
+    CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = ATSAT_DYN_OK;
+    for (int32_t it = iter0; it < iter0 + n && rc == ATSAT_DYN_OK; it++) rc = enqueue_iteration(h, it);
+    const cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    h->profiling = prof;
+    h->graph_kernels = h->launches - l0;
+    h->launches = l0;                                  // captured, not run
+    if (rc != ATSAT_DYN_OK) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return fail(h, ATSAT_DYN_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    // n is even: the FP32 copies swapped back to where they were; the steady flags still hold
+    if (!resident_steady(h)) { cudaGraphDestroy(g); return fail(h, ATSAT_DYN_E_INVALID, "graph_capture: state moved"); }
+    const cudaError_t ei = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) { h->graph = nullptr; return fail(h, ATSAT_DYN_E_CUDA, "graph instantiate: %s", cudaGetErrorString(ei)); }
+    h->graph_iters = n;
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_graph_launch(atsat_dyn_t h, int32_t reps) {
+    ENTRY(h);
+    if (!h->graph || reps < 0) return fail(h, ATSAT_DYN_E_INVALID, "graph_launch: no captured graph");
+    for (int32_t r = 0; r < reps; r++) CK(h, cudaGraphLaunch(h->graph, h->stream));
+    h->launches += (int64_t)reps * h->graph_kernels;
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_ensemble_run(const atsat_dyn_t* members, int32_t n, int32_t reps, int32_t concurrent, double* ms) {
+    if (!members || n < 1 || reps < 0 || !ms) return ATSAT_DYN_E_INVALID;
+    for (int32_t m = 0; m < n; m++)
+        if (!members[m] || !members[m]->graph) return ATSAT_DYN_E_INVALID;
+    atsat_dyn* h0 = members[0];
+    std::vector<cudaEvent_t> done(n);
+    cudaEvent_t start, stop;
+    CK(h0, cudaEventCreate(&start));
+    CK(h0, cudaEventCreate(&stop));
+    for (int32_t m = 0; m < n; m++) CK(h0, cudaEventCreateWithFlags(&done[m], cudaEventDisableTiming));
+    CK(h0, cudaEventRecord(start, h0->stream));
+    for (int32_t m = 0; m < n; m++) {
+        atsat_dyn* h = members[m];
+        // every member starts after `start`; one after another: also after the previous member
+        CK(h0, cudaStreamWaitEvent(h->stream, (concurrent || m == 0) ? start : done[m - 1], 0));
+        if (concurrent) continue;
+        for (int32_t r = 0; r < reps; r++) CK(h0, cudaGraphLaunch(h->graph, h->stream));
+        h->launches += (int64_t)reps * h->graph_kernels;
+        CK(h0, cudaEventRecord(done[m], h->stream));
+    }
+    if (concurrent) {
+        // round-robin over the members so that every stream has work queued early
+        for (int32_t r = 0; r < reps; r++)
+            for (int32_t m = 0; m < n; m++) CK(h0, cudaGraphLaunch(members[m]->graph, members[m]->stream));
+        for (int32_t m = 0; m < n; m++) {
+            members[m]->launches += (int64_t)reps * members[m]->graph_kernels;
+            CK(h0, cudaEventRecord(done[m], members[m]->stream));
+        }
+    }
+    for (int32_t m = 0; m < n; m++) CK(h0, cudaStreamWaitEvent(h0->stream, done[m], 0));
+    CK(h0, cudaEventRecord(stop, h0->stream));
+    CK(h0, cudaEventSynchronize(stop));
+    float t = 0.0f;
+    CK(h0, cudaEventElapsedTime(&t, start, stop));
+    *ms = t;
+    cudaEventDestroy(start);
+    cudaEventDestroy(stop);
+    for (auto e : done) cudaEventDestroy(e);
+    for (int32_t m = 0; m < n; m++) {
+        const int rc = finish(members[m]);
+        if (rc) return rc;
+    }
+    return ATSAT_DYN_OK;
 }
 
 int atsat_dyn_sync(atsat_dyn_t h) {

@@ -81,6 +81,9 @@ def lib():
         L.atsat_dyn_set_stage_variant.argtypes = [H, C.c_int32]
         L.atsat_dyn_get_stage_variant.argtypes = [H, C.POINTER(C.c_int32)]
         L.atsat_dyn_autotune.argtypes = [H, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+        L.atsat_dyn_graph_capture.argtypes = [H, C.c_int32, C.c_int32]
+        L.atsat_dyn_graph_launch.argtypes = [H, C.c_int32]
+        L.atsat_dyn_ensemble_run.argtypes = [C.POINTER(H), C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_double)]
         L.atsat_dyn_poisson_project.argtypes = [H, C.POINTER(C.c_double)]
         L.atsat_dyn_poisson_solve.argtypes = [H, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double,
                                               C.c_int32, C.c_int32, C.c_double, C.POINTER(abi.PoissonStats)]
@@ -228,6 +231,15 @@ class Dycore:
         self._ck(lib().atsat_dyn_autotune(self.h, int(reps), C.byref(chosen), ms), "autotune")
         return chosen.value, list(ms)
 
+    # ---- CUDA graphs of the resident loop (no reference counterpart) ----
+    def graph_capture(self, iter0: int, n: int = 2):
+        """Record n resident iterations from iter0 into a CUDA graph (needs two resident iterations first)."""
+        self._ck(lib().atsat_dyn_graph_capture(self.h, int(iter0), int(n)), "graph_capture")
+
+    def graph_launch(self, reps: int = 1):
+        """Enqueue `reps` replays of the captured graph (asynchronous; sync() waits)."""
+        self._ck(lib().atsat_dyn_graph_launch(self.h, int(reps)), "graph_launch")
+
     # ---- standalone pressure-equation solves (no reference counterpart) ----
     def poisson_project(self, src: np.ndarray) -> np.ndarray:
         """A copy of `src` (im x jm x km) without its component outside the operator's range."""
@@ -315,3 +327,15 @@ class Dycore:
         n, ms = C.c_int64(), C.c_double()
         self._ck(lib().atsat_dyn_profile_read(self.h, kclass, C.byref(n), C.byref(ms)), "profile_read")
         return int(n.value), float(ms.value)
+
+
+def ensemble_run(members, reps: int, concurrent: bool = True) -> float:
+    """Replay every member's captured graph `reps` times, concurrently (one stream per member) or one
+    member after another; returns the device milliseconds of the whole set."""
+    H = C.c_void_p
+    arr = (H * len(members))(*[m.h for m in members])
+    ms = C.c_double(0.0)
+    rc = lib().atsat_dyn_ensemble_run(arr, len(members), int(reps), int(bool(concurrent)), C.byref(ms))
+    if rc != 0:
+        raise DycoreError(rc, "ensemble_run", lib().atsat_dyn_last_error(members[0].h).decode())
+    return ms.value

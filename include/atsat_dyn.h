@@ -304,6 +304,18 @@ int atsat_dyn_get_stage_variant(atsat_dyn_t h, int32_t* variant);
  * only scratch buffers, so the model state is unchanged. No reference counterpart. */
 int atsat_dyn_autotune(atsat_dyn_t h, int32_t reps, int32_t* chosen, double* ms);
 
+/* ---- CUDA graphs and ensembles (no reference counterpart) ----
+ * graph_capture records n (even, >= 2) resident iterations starting at iter0 (the parity of iter0 fixes
+ * which of them carry the pressure call) into a CUDA graph, without running them; it needs two resident
+ * iterations done first (atsat_dyn_iterate) so that the mixed path's buffers are established. A replay
+ * advances the state by n iterations: graph_launch enqueues `reps` replays on the handle's stream (no sync;
+ * atsat_dyn_sync waits). ensemble_run replays every member's graph `reps` times, either concurrently (each
+ * member on its own stream) or one member after another, and returns the device time of the whole set
+ * from CUDA events (members must live on one device). */
+int atsat_dyn_graph_capture(atsat_dyn_t h, int32_t iter0, int32_t n);
+int atsat_dyn_graph_launch(atsat_dyn_t h, int32_t reps);
+int atsat_dyn_ensemble_run(const atsat_dyn_t* members, int32_t n, int32_t reps, int32_t concurrent, double* ms);
+
 /* ---- standalone solves of the pressure equation ----
  * The equation the reference relaxes (PressureSolver.h:318-495 with the boundary planes of :718-746):
  *   num1 (p[i+1] + p[i-1]) + num2 (p[j+1] + p[j-1]) + num3 (p[k+1] + p[k-1]) - den p = src

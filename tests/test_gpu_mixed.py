@@ -215,3 +215,60 @@ def test_drift_report_and_continuity_residual():
         assert row["fp64"][name][0] <= 1e-10, (name, row["fp64"][name])
     dm, df = row["div_max"]["mixed"], row["div_max"]["fp64"]
     assert dm <= df * (1 + 1e-6) or abs(dm - df) <= 1e-6 * df, (dm, df)
+
+
+@pytest.mark.parametrize("precision", [1, 0], ids=["mixed", "fp64"])
+def test_graph_replay_equals_iterate(precision):
+    """Two iterations captured as a CUDA graph and replayed twice give the state of six plain
+    iterations bit for bit; the host can go on with plain iterations afterwards."""
+    from atsat_gb300 import dyn
+    g, P, st = case((21, 91, 181), seed=67, exercise=True)
+    a, b = st.copy(), st.copy()
+    with dyn.Dycore(g, dict(P, precision=precision)) as d:
+        d.load_state(a)
+        d.iterate(1, 2)
+        d.graph_capture(3, 2)
+        d.graph_launch(2)
+        d.iterate(7, 1)
+        d.download(ALL)
+    with dyn.Dycore(g, dict(P, precision=precision)) as d:
+        d.load_state(b)
+        d.iterate(1, 7)
+        d.download(ALL)
+    for f in F.PROG + F.PROG_N + [F.P_DYN, F.RHS_U, F.AUX_W]:
+        assert np.array_equal(a.arrays[f], b.arrays[f], equal_nan=True), F.NAMES[f]
+
+
+def test_ensemble_concurrent_equals_sequential():
+    """Members of two sizes replayed concurrently and one after another end in identical states, equal
+    to plain iterations."""
+    from atsat_gb300 import dyn
+    shapes = [(9, 13, 17), (21, 91, 181), (9, 13, 17)]
+    runs = []
+    for concurrent in (True, False):
+        states, members = [], []
+        for m, shp in enumerate(shapes):
+            g, P, st = case(shp, seed=70 + m, exercise=True)
+            d = dyn.Dycore(g, dict(P, precision=1))
+            s = st.copy()
+            d.load_state(s)
+            d.iterate(1, 2)
+            d.graph_capture(3, 2)
+            members.append(d)
+            states.append(s)
+        ms = dyn.ensemble_run(members, reps=2, concurrent=concurrent)
+        assert ms > 0
+        for d in members:
+            d.download(ALL)
+            d.close()
+        runs.append(states)
+    for m, shp in enumerate(shapes):
+        g, P, st = case(shp, seed=70 + m, exercise=True)
+        s = st.copy()
+        with dyn.Dycore(g, dict(P, precision=1)) as d:
+            d.load_state(s)
+            d.iterate(1, 6)
+            d.download(ALL)
+        for f in F.PROG + [F.P_DYN]:
+            assert np.array_equal(runs[0][m].arrays[f], runs[1][m].arrays[f]), (shp, F.NAMES[f])
+            assert np.array_equal(runs[0][m].arrays[f], s.arrays[f]), (shp, F.NAMES[f])
