@@ -348,6 +348,7 @@ void build_mixed_constants(atsat_dyn* h) {
     F.im = K.im; F.jm = K.jm; F.km = K.km; F.kp = K.kp; F.plane = K.plane;
     F.metric_split = K.metric_split; F.hydro_buoy = K.hydro_buoy; F.turb = K.turb; F.rad_on = K.rad_on;
     F.precip_on = K.precip_on; F.tmf_on = K.tmf_on; F.divu_on = K.divu_on;
+    F.fsz_over_int = K.fsz >= (int64_t)0x7FFFFFFF ? 1 : 0;
     F.inv_2dr = (float)K.inv_2dr; F.inv_2dthe = (float)K.inv_2dthe; F.inv_2dphi = (float)K.inv_2dphi;
     F.inv_dr2 = (float)K.inv_dr2; F.inv_dthe2 = (float)K.inv_dthe2; F.inv_dphi2 = (float)K.inv_dphi2;
     F.coeff_energy_p = (float)K.coeff_energy_p; F.inv_re = (float)K.inv_re; F.inv_re_pr = (float)K.inv_re_pr;
@@ -436,7 +437,19 @@ bool make_tile_maps(atsat_dyn* h) {
     const CUresult r2 = enc(reinterpret_cast<CUtensorMap*>(h->maps.seam), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->slab32,
                             dims, strides, box_seam, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r1 == CUDA_SUCCESS && r2 == CUDA_SUCCESS;
+    const cuuint32_t box_main4[4] = {TILE_BX, TILE_BY, TTILE_BZ, 1};
+    const cuuint32_t box_seam4[4] = {TILE_SEAM_X, TILE_J, TTILE_I, 1};
+    const CUresult r3 = enc(reinterpret_cast<CUtensorMap*>(h->maps.main4), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->slab32,
+                            dims, strides, box_main4, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    const CUresult r4 = enc(reinterpret_cast<CUtensorMap*>(h->maps.seam4), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->slab32,
+                            dims, strides, box_seam4, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    const cuuint32_t box_pt4[4] = {TILE_K, TILE_J, TTILE_I, 1};
+    const CUresult r5 = enc(reinterpret_cast<CUtensorMap*>(h->maps.pt4), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->slab32,
+                            dims, strides, box_pt4, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r1 == CUDA_SUCCESS && r2 == CUDA_SUCCESS && r3 == CUDA_SUCCESS && r4 == CUDA_SUCCESS && r5 == CUDA_SUCCESS;
 }
 
 bool valid_field(int f) { return f >= 0 && f < ATSAT_NFIELDS; }
@@ -698,11 +711,55 @@ bool variant_available(const atsat_dyn* h, int v) {
         case ATSAT_DYN_STAGE_SPLIT:
         case ATSAT_DYN_STAGE_SPLIT3:
         case ATSAT_DYN_STAGE_SPLIT13: return !h->kc.divu_on;
+        case ATSAT_DYN_STAGE_SPLIT_TILED: return !h->kc.divu_on && h->tile_ok && !h->kf.fsz_over_int;
         default: return false;
     }
 }
 
 int launches_per_stage(const atsat_dyn* h) { return h->variant >= ATSAT_DYN_STAGE_SPLIT ? 2 : 1; }
+
+// The tracer kernel's stream, in the order its consumers read it: the winds' point values (u, [du], v,
+// [dv], w, w's low word, [dw]) and nue; then per tracer field its y_n and increment halo boxes, its
+// sources, the tke/dis running sum, and at the final stage dl_1 and dl_2.
+TracerPlan make_plan_tracer(atsat_dyn* h, const MixedIO& io, int mode) {
+    TracerPlan pl{};
+    pl.err = h->dev_err;
+    int n = 0;
+    auto add = [&](const float* p, int kind) {
+        if (n < TRACER_MAX_ITEMS) { pl.arr[n] = arr_index(h, p); pl.kind[n] = (unsigned char)kind; }
+        n++;
+    };
+    const bool dl = io.dl_in[0] != nullptr;
+    add(io.yn32[ATSAT_F_U], 1); if (dl) add(io.dl_in[ATSAT_F_U], 1);
+    add(io.yn32[ATSAT_F_V], 1); if (dl) add(io.dl_in[ATSAT_F_V], 1);
+    add(io.yn32[ATSAT_F_W], 1); add(io.wlo, 1); if (dl) add(io.dl_in[ATSAT_F_W], 1);
+    add(io.nue, 1);
+    for (int q = ATSAT_F_H2O; q < NPROG; q++) {
+        const bool turb = q == ATSAT_F_TKE || q == ATSAT_F_DIS;
+        if (turb && !h->kc.turb) continue;
+        add(io.yn32[q], 0);
+        if (dl) add(io.dl_in[q], 0);
+        switch (q) {
+            case ATSAT_F_H2O: add(io.s_precip[0], 1); break;
+            case ATSAT_F_H2O_CLOUD: add(io.s_precip[1], 1); break;
+            case ATSAT_F_H2O_ICE: add(io.s_precip[2], 1); break;
+            case ATSAT_F_H2S: add(io.massflux_h2s, 1); break;
+            case ATSAT_F_NH3: add(io.massflux_nh3, 1); add(io.s_precip[3], 1); break;
+            case ATSAT_F_NH3_CLOUD: add(io.s_precip[4], 1); break;
+            case ATSAT_F_NH3_ICE: add(io.s_precip[5], 1); break;
+            case ATSAT_F_CH4: add(io.s_precip[6], 1); break;
+            case ATSAT_F_CH4_CLOUD: add(io.s_precip[7], 1); break;
+            case ATSAT_F_CH4_ICE: add(io.s_precip[8], 1); break;
+            case ATSAT_F_NH4SH: add(io.fluxlim_nh4sh, 1); add(io.massflux_nh4sh, 1); break;
+            case ATSAT_F_TKE: add(io.tke_source, 1); break;
+            default: add(io.dis_source, 1); break;
+        }
+        if (turb) add(io.acc_turb[q - ATSAT_F_TKE], 1);
+        else if (mode == MODE_FINAL) { add(io.dl1[q], 1); add(io.dl2[q], 1); }
+    }
+    pl.n_items = n;
+    return pl;
+}
 
 cudaError_t launch_stage(atsat_dyn* h, const MixedIO& io, const StageParams& sp, int mode) {
     const int v = (mode == MODE_RHS || !variant_available(h, h->variant)) ? ATSAT_DYN_STAGE_DIRECT : h->variant;
@@ -712,6 +769,14 @@ cudaError_t launch_stage(atsat_dyn* h, const MixedIO& io, const StageParams& sp,
         case ATSAT_DYN_STAGE_SPLIT: return launch_rk_split(h->kf, io, sp, mode, 1, h->stream);
         case ATSAT_DYN_STAGE_SPLIT3: return launch_rk_split(h->kf, io, sp, mode, 3, h->stream);
         case ATSAT_DYN_STAGE_SPLIT13: return launch_rk_split(h->kf, io, sp, mode, 13, h->stream);
+        case ATSAT_DYN_STAGE_SPLIT_TILED: {
+            const cudaError_t e = launch_rk_mom(h->kf, io, sp, mode, h->stream);
+            if (e != cudaSuccess) return e;
+            const TracerPlan pl = make_plan_tracer(h, io, mode);
+            if (pl.n_items != tracer_plan_items(mode, io.dl_in[0] != nullptr, h->kc.turb != 0))
+                return cudaErrorInvalidValue;   // the plan and the kernel disagree: never expected
+            return launch_rk_tracer_tile(h->maps, h->kf, io, sp, pl, mode, h->stream);
+        }
         default: return launch_rk_stage_mixed(h->kf, io, sp, mode, h->stream);
     }
 }

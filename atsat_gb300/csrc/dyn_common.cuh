@@ -145,7 +145,7 @@ struct MixedConstF {
     int im, jm, km, kp;
     int64_t plane;
     int metric_split, hydro_buoy, turb, rad_on;
-    int precip_on, tmf_on, divu_on, pad0;
+    int precip_on, tmf_on, divu_on, fsz_over_int;   // fsz_over_int: cell offsets need 64 bits
     float inv_2dr, inv_2dthe, inv_2dphi, inv_dr2, inv_dthe2, inv_dphi2;
     float coeff_energy_p, inv_re, inv_re_pr;
     float inv_sc_re_ch4, inv_sc_re_h2o, inv_sc_re_h2s, inv_sc_re_nh3, inv_sc_re_nh4sh;
@@ -238,6 +238,8 @@ constexpr int TILE_K = 32, TILE_J = 8, TILE_I = 2;
 constexpr int TILE_BX = TILE_K + 8, TILE_BY = TILE_J + 2, TILE_BZ = TILE_I + 2;
 constexpr int TILE_SEAM_X = 4;
 constexpr int TILE_MAX_ITEMS = 2 * NPROG + 1;
+// the tracer kernel's taller tile: four radial levels per thread
+constexpr int TTILE_I = 4, TTILE_BZ = TTILE_I + 2;
 struct TilePlan {
     int n_items;
     int item[TILE_MAX_ITEMS];
@@ -270,10 +272,31 @@ cudaError_t launch_mixed_prepare(const KConst& kc, const MixedPrep& pr, cudaStre
 cudaError_t launch_rk_split(const MixedConstF& kf, const MixedIO& io, const StageParams& sp, int mode, int groups,
                             cudaStream_t s);
 // tensor maps are CUtensorMap objects (128 bytes), passed opaquely
-struct TileMaps { alignas(64) unsigned char main[128]; alignas(64) unsigned char seam[128]; };
+struct TileMaps {
+    alignas(64) unsigned char main[128];    // box TILE_BX x TILE_BY x TILE_BZ
+    alignas(64) unsigned char seam[128];    // box TILE_SEAM_X x TILE_J x TILE_I
+    alignas(64) unsigned char main4[128];   // box TILE_BX x TILE_BY x TTILE_BZ
+    alignas(64) unsigned char seam4[128];   // box TILE_SEAM_X x TILE_J x TTILE_I
+    alignas(64) unsigned char pt4[128];     // box TILE_K x TILE_J x TTILE_I (point values, no halo)
+};
+
+// The tracer kernel's stream: every array it reads, in consumption order, each either a halo box
+// (kind 0) or a point box (kind 1).
+constexpr int TRACER_MAX_ITEMS = 96;
+struct TracerPlan {
+    int n_items;
+    int arr[TRACER_MAX_ITEMS];
+    unsigned char kind[TRACER_MAX_ITEMS];
+    unsigned int* err;
+};
 cudaError_t launch_rk_tile(const TileMaps& maps, const MixedConstF& kf, const MixedIO& io, const StageParams& sp,
                            const TilePlan& plan, int mode, cudaStream_t s);
 size_t rk_tile_smem_bytes();
+// the 13 tracer fields alone, TMA-tiled (after rk_mom_kernel; species_divu off)
+cudaError_t launch_rk_tracer_tile(const TileMaps& maps, const MixedConstF& kf, const MixedIO& io,
+                                  const StageParams& sp, const TracerPlan& plan, int mode, cudaStream_t s);
+cudaError_t launch_rk_mom(const MixedConstF& kf, const MixedIO& io, const StageParams& sp, int mode, cudaStream_t s);
+int tracer_plan_items(int mode, bool has_dl, bool turb);
 
 // standalone pressure-equation solver (poisson.cu)
 struct PoissonSolver;

@@ -262,6 +262,14 @@ cudaError_t launch_split_mode(const MixedConstF& kf, const MixedIO& io, const St
     return cudaGetLastError();
 }
 
+cudaError_t launch_rk_mom(const MixedConstF& kf, const MixedIO& io, const StageParams& sp, int mode, cudaStream_t s) {
+    if (kf.divu_on || mode == MODE_RHS) return cudaErrorInvalidValue;
+    const dim3 block(32, 8), grid((kf.km + 31) / 32, (kf.jm + 7) / 8, kf.im);
+    if (mode == MODE_STAGE) rk_mom_kernel<MODE_STAGE><<<grid, block, 0, s>>>(kf, io, sp);
+    else rk_mom_kernel<MODE_FINAL><<<grid, block, 0, s>>>(kf, io, sp);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_rk_split(const MixedConstF& kf, const MixedIO& io, const StageParams& sp, int mode, int groups,
                             cudaStream_t s) {
     if (kf.divu_on || (groups != 1 && groups != 3 && groups != 13) || mode == MODE_RHS) return cudaErrorInvalidValue;

@@ -14,12 +14,14 @@
 #include <cuda.h>
 
 #include "mixed_physics.cuh"
+#include "tma_pipe.cuh"
 
 namespace atsat {
 
 namespace {
 
 using namespace mixed;
+using namespace tma;
 
 constexpr int PL = TILE_BX * TILE_BY;                     // floats per plane of a box (400)
 constexpr int BOX_F = PL * TILE_BZ;                       // 1600
@@ -32,52 +34,9 @@ constexpr int NCW = TILE_J;                               // consumer warps
 constexpr int THREADS = (NCW + 1) * 32;
 constexpr int GEO_F = TILE_I * TILE_J * 16;               // ColGeoF of the block's columns
 constexpr size_t SMEM_BYTES = (size_t)NSLOT * SLOT_F * 4 + (size_t)GEO_F * 4 + 2 * NSLOT * 8;
-constexpr long long WAIT_LIMIT = 1LL << 31;               // SM clocks, about a second
 
 static_assert((SLOT_F * 4) % 128 == 0, "slots stay 128-byte aligned");
 static_assert((BOX_F * 4) % 128 == 0, "the seam box starts 128-byte aligned");
-
-enum : unsigned int { ERR_PRODUCER = 1u, ERR_CONSUMER = 2u, ERR_PLAN = 4u, ERR_ALIGN = 8u };
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// wait for the phase of parity `parity` to complete; false after WAIT_LIMIT clocks
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    if (mbar_try(bar, parity)) return true;
-    const long long t0 = clock64();
-    do {
-        if (mbar_try(bar, parity)) return true;
-    } while (clock64() - t0 < WAIT_LIMIT);
-    return false;
-}
-__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, int w,
-                                            uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(bar)
-        : "memory");
-}
 
 // position of the items of field q in the stream (compile-time once q is): per field y_n, then w's low
 // word, then the increment
@@ -127,33 +86,6 @@ struct TileSrc {
     }
 };
 
-struct Ring {
-    uint32_t full0, empty0;     // shared addresses of full[0], empty[0]
-    __device__ __forceinline__ uint32_t full(int s) const { return full0 + 8u * (uint32_t)s; }
-    __device__ __forceinline__ uint32_t empty(int s) const { return empty0 + 8u * (uint32_t)s; }
-};
-
-// consumer side: wait for items [n0, n1); false (warp-uniform) when a wait gave up
-__device__ __forceinline__ bool acquire(const Ring& rg, int n0, int n1, const TilePlan& plan, const int* expect) {
-    bool ok = true;
-#pragma unroll
-    for (int n = n0; n < n1; n++) ok = ok && mbar_wait(rg.full(n % NSLOT), (uint32_t)((n / NSLOT) & 1));
-    if (threadIdx.x == 0) {
-        bool same = true;
-#pragma unroll
-        for (int n = n0; n < n1; n++) same = same && plan.item[n] == expect[n - n0];
-        if (!same) atomicOr(plan.err, ERR_PLAN);
-    }
-    return !__any_sync(0xffffffffu, !ok);
-}
-__device__ __forceinline__ void release(const Ring& rg, int n0, int n1) {
-    __syncwarp();
-    if ((threadIdx.x & 31) == 0) {
-#pragma unroll
-        for (int n = n0; n < n1; n++) mbar_arrive(rg.empty(n % NSLOT));
-    }
-}
-
 template <int MODE, bool HAS_DL>
 __global__ void __launch_bounds__(THREADS, 2)
 rk_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_constant__ CUtensorMap map_seam,
@@ -187,23 +119,9 @@ rk_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_consta
 
     if (warp == NCW) {
         // ---- producer ----
-        if (lane == 0) {
-            const uint32_t bytes = BOX_BYTES + (seam ? SEAM_BYTES : 0u);
-            int n = 0;
-            bool ok = true;
-            for (; n < plan.n_items; n++) {
-                const int s = n % NSLOT;
-                if (n >= NSLOT && !mbar_wait(rg.empty(s), (uint32_t)(((n / NSLOT) - 1) & 1))) { ok = false; break; }
-                const uint32_t dst = smem_u32(smem + s * SLOT_F);
-                mbar_expect_tx(rg.full(s), bytes);
-                tma_load_4d(dst, &map_main, k0 - 4, j0 - 1, i0 - 1, plan.item[n], rg.full(s));
-                if (seam) tma_load_4d(dst + BOX_BYTES, &map_seam, xs, j0, i0, plan.item[n], rg.full(s));
-            }
-            if (!ok) atomicOr(plan.err, ERR_PRODUCER);
-            // no copy may land after the block is gone: wait for the last copy of every slot
-            for (int m = (n > NSLOT ? n - NSLOT : 0); m < n; m++)
-                if (!mbar_wait(rg.full(m % NSLOT), (uint32_t)((m / NSLOT) & 1))) break;
-        }
+        if (lane == 0)
+            produce<NSLOT>(rg, smem, SLOT_F, BOX_BYTES, SEAM_BYTES, &map_main, &map_seam, k0 - 4, j0 - 1, i0 - 1, seam,
+                           xs, j0, i0, plan);
         return;
     }
 
@@ -248,7 +166,7 @@ rk_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_consta
             if (q == ATSAT_F_W) expect[item_lo<HAS_DL>()] = plan.arr_lo;
             if (HAS_DL) expect[item_dl<HAS_DL>(q)] = plan.arr_dl[q];
         }
-        if (!acquire(rg, 0, N_MOM, plan, expect)) {
+        if (!acquire<NSLOT>(rg, 0, N_MOM, plan, expect)) {
             if (lane == 0) atomicOr(plan.err, ERR_CONSUMER);
             return;
         }
@@ -261,7 +179,7 @@ rk_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_consta
             cs[ii] = momentum_t<MODE>(K, io, sp, S[ii], i0 + ii, c[ii], g);
         }
     }
-    release(rg, 0, N_MOM);
+    release<NSLOT>(rg, 0, N_MOM);
 
     // the tracers, one field (one or two arrays) at a time
     const int q_last = K.turb ? ATSAT_F_DIS : ATSAT_F_NH4SH;
@@ -270,7 +188,7 @@ rk_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_consta
         if (q > q_last) break;
         const int n0 = item_yn<HAS_DL>(q), n1 = n0 + (HAS_DL ? 2 : 1);
         int expect[2] = {plan.arr_yn[q], plan.arr_dl[q]};
-        if (!acquire(rg, n0, n1, plan, expect)) {
+        if (!acquire<NSLOT>(rg, n0, n1, plan, expect)) {
             if (lane == 0) atomicOr(plan.err, ERR_CONSUMER);
             return;
         }
@@ -281,7 +199,7 @@ rk_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_consta
                 scalar<MODE>(q, K, io, sp, S[ii], c[ii], g, cs[ii]);
             }
         }
-        release(rg, n0, n1);
+        release<NSLOT>(rg, n0, n1);
     }
     if (!K.turb && MODE == MODE_FINAL && sp.write_all_rhs) {
 #pragma unroll

@@ -48,7 +48,8 @@ def parse():
     ap.add_argument("--shape", default="41,181,361")
     ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--stage-variant", default="auto", choices=["auto", "direct", "tiled", "split", "split3", "split13"],
+    ap.add_argument("--stage-variant", default="auto",
+                    choices=["auto", "direct", "tiled", "split", "split3", "split13", "split_tiled"],
                     help="mixed precision: the RK stage kernel (auto: the autotuner's choice)")
     ap.add_argument("--poisson", action="store_true",
                     help="the standalone pressure-equation solves instead of the dycore iteration")
@@ -189,7 +190,8 @@ KERNEL_NAME = {"fp64": "rk_stage_fp64_kernel (fused RHSSat + RK4 stage, FP64)",
                "mixed_tiled": "rk_tile_kernel (TMA-tiled fused RHSSat + RK4 stage, FP32 stencils / FP64 state)",
                "mixed_split": "rk_mom_kernel + rk_tracer_kernel<1> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)",
                "mixed_split3": "rk_mom_kernel + rk_tracer_kernel<3> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)",
-               "mixed_split13": "rk_mom_kernel + rk_tracer_kernel<13> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)"}
+               "mixed_split13": "rk_mom_kernel + rk_tracer_kernel<13> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)",
+               "mixed_split_tiled": "rk_mom_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, TMA-tiled tracers)"}
 
 
 def cpu_baseline(g, P, seed, target_s=3.0):

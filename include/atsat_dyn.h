@@ -285,7 +285,8 @@ int atsat_dyn_set_write_all_rhs(atsat_dyn_t h, int32_t on);
  *   TILED    halo boxes of the FP32 arrays streamed into shared memory with tensor copies (needs a
  *            driver that can encode tensor maps);
  *   SPLIT*   a momentum / temperature kernel, then a tracer kernel with 1, 3 or 13 threads per cell
- *            (not with species_divu on).
+ *            (not with species_divu on);
+ *   SPLIT_TILED  the same momentum kernel, then the tracers TMA-tiled (4 radial levels per thread).
  * The default is TILED where available. No reference counterpart (the reference has one CPU loop
  * nest). Setting an unavailable variant returns ATSAT_DYN_E_UNSUPPORTED. */
 enum {
@@ -294,7 +295,8 @@ enum {
     ATSAT_DYN_STAGE_SPLIT = 2,
     ATSAT_DYN_STAGE_SPLIT3 = 3,
     ATSAT_DYN_STAGE_SPLIT13 = 4,
-    ATSAT_DYN_STAGE_NVARIANT = 5
+    ATSAT_DYN_STAGE_SPLIT_TILED = 5,
+    ATSAT_DYN_STAGE_NVARIANT = 6
 };
 int atsat_dyn_set_stage_variant(atsat_dyn_t h, int32_t variant);
 int atsat_dyn_get_stage_variant(atsat_dyn_t h, int32_t* variant);
