@@ -24,6 +24,11 @@ constexpr int NPROG = ATSAT_NPROG;
 // These rebuild the IEEE-754 encodings with integer operations for the common cases -- normal
 // numbers and zeros -- and defer to the hardware conversion for subnormals, infinities and NaNs.
 // Both give the hardware's bits (round to nearest even for the narrowing).
+// The rare cases go through calls that the compiler cannot if-convert: an inlined fallback would be
+// evaluated (and its F2F issued) on every call.
+static __device__ __noinline__ double f2d_rare(float f) { return (double)f; }
+static __device__ __noinline__ float d2f_rare(double d) { return (float)d; }
+
 __device__ __forceinline__ double f2d(float f) {
     const uint32_t b = __float_as_uint(f);
     const uint32_t a = b & 0x7FFFFFFFu;
@@ -31,7 +36,7 @@ __device__ __forceinline__ double f2d(float f) {
         return __longlong_as_double((long long)(((uint64_t)(b & 0x80000000u) << 32) |
                                                 (((uint64_t)a << 29) + (896ull << 52))));
     if (a == 0u) return __longlong_as_double((long long)((uint64_t)b << 32));
-    return (double)f;
+    return f2d_rare(f);
 }
 
 __device__ __forceinline__ float d2f(double d) {
@@ -45,7 +50,7 @@ __device__ __forceinline__ float d2f(double d) {
         return __uint_as_float(q | (hi & 0x80000000u));
     }
     if ((b << 1) == 0) return __uint_as_float(hi & 0x80000000u);
-    return (float)d;
+    return d2f_rare(d);
 }
 
 // Per-(i,j) metric factors of one column. The RK members follow the CellGeometry that

@@ -244,10 +244,24 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
 
     const int q_last = K.turb ? ATSAT_F_DIS : ATSAT_F_NH4SH;
     const float pc = K.precip_coupling, chem = K.chem;
+    // final stage: y_n in FP64 of the next field, loaded one field ahead
+    double y64n[TI];
+    if (MODE == MODE_FINAL) {
+#pragma unroll
+        for (int ii = 0; ii < TI; ii++) y64n[ii] = valid[ii] ? ldd(io.yn64[ATSAT_F_H2O] + c[ii]) : 0.0;
+    }
 #pragma unroll
     for (int q = ATSAT_F_H2O; q <= ATSAT_F_DIS; q++) {
         if (q > q_last) break;
         const int hb = h0<HAS_DL>(q), pb = pt0<MODE, HAS_DL>(q), npq = n_pt<MODE>(q);
+        double y64[TI];
+        if (MODE == MODE_FINAL) {
+#pragma unroll
+            for (int ii = 0; ii < TI; ii++) {
+                y64[ii] = y64n[ii];
+                if (q < q_last && valid[ii]) y64n[ii] = ldd(io.yn64[q + 1] + c[ii]);
+            }
+        }
         if (!wait_items<NHS>(rh, hb, hb + (HAS_DL ? 2 : 1)) || !wait_items<NPS>(rp, pb, pb + npq)) { fail(); return; }
         const float* Y = hs + (hb % NHS) * HSLOT_F;
         const float* D = hs + ((hb + 1) % NHS) * HSLOT_F;
@@ -307,7 +321,7 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
                     const float dl1 = (n_src(q) == 2 ? P2 : P1)[x], dl2 = (n_src(q) == 2 ? P3 : P2)[x];
                     inc = THIRD * (dl1 + 2.0f * dl2 + dl_c) + sp.sixth_dt_f * r;
                 }
-                double y = ldd(io.yn64[q] + cc) + f2d(inc);
+                double y = y64[ii] + f2d(inc);
                 if (q == ATSAT_F_TKE) y = smin(smax(y, 0.0), K.tke_max_d);
                 else if (q == ATSAT_F_DIS) y = smax(y, K.dis_min_d);
                 io.out64[q][cc] = y;
