@@ -449,7 +449,12 @@ bool make_tile_maps(atsat_dyn* h) {
     const CUresult r5 = enc(reinterpret_cast<CUtensorMap*>(h->maps.pt4), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->slab32,
                             dims, strides, box_pt4, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r1 == CUDA_SUCCESS && r2 == CUDA_SUCCESS && r3 == CUDA_SUCCESS && r4 == CUDA_SUCCESS && r5 == CUDA_SUCCESS;
+    const cuuint32_t box_pt2[4] = {TILE_K, TILE_J, TILE_I, 1};
+    const CUresult r6 = enc(reinterpret_cast<CUtensorMap*>(h->maps.pt2), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->slab32,
+                            dims, strides, box_pt2, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r1 == CUDA_SUCCESS && r2 == CUDA_SUCCESS && r3 == CUDA_SUCCESS && r4 == CUDA_SUCCESS && r5 == CUDA_SUCCESS &&
+           r6 == CUDA_SUCCESS;
 }
 
 bool valid_field(int f) { return f >= 0 && f < ATSAT_NFIELDS; }
@@ -711,7 +716,8 @@ bool variant_available(const atsat_dyn* h, int v) {
         case ATSAT_DYN_STAGE_SPLIT:
         case ATSAT_DYN_STAGE_SPLIT3:
         case ATSAT_DYN_STAGE_SPLIT13: return !h->kc.divu_on;
-        case ATSAT_DYN_STAGE_SPLIT_TILED: return !h->kc.divu_on && h->tile_ok && !h->kf.fsz_over_int;
+        case ATSAT_DYN_STAGE_SPLIT_TILED:
+        case ATSAT_DYN_STAGE_TILED2: return !h->kc.divu_on && h->tile_ok && !h->kf.fsz_over_int;
         default: return false;
     }
 }
@@ -761,6 +767,30 @@ TracerPlan make_plan_tracer(atsat_dyn* h, const MixedIO& io, int mode) {
     return pl;
 }
 
+// The momentum kernel's stream: nue; the halo boxes of u, v, w (with its low word) and t, y_n then the
+// increment; then the frozen terms and inputs in the groups rhs_u, rhs_v, rhs_w and rhs_t use them.
+TracerPlan make_plan_mom(atsat_dyn* h, const MixedIO& io) {
+    TracerPlan pl{};
+    pl.err = h->dev_err;
+    int n = 0;
+    auto add = [&](const float* p, int kind) {
+        if (n < TRACER_MAX_ITEMS) { pl.arr[n] = arr_index(h, p); pl.kind[n] = (unsigned char)kind; }
+        n++;
+    };
+    const bool dl = io.dl_in[0] != nullptr;
+    add(io.nue, 1);
+    add(io.yn32[ATSAT_F_U], 0); if (dl) add(io.dl_in[ATSAT_F_U], 0);
+    add(io.yn32[ATSAT_F_V], 0); if (dl) add(io.dl_in[ATSAT_F_V], 0);
+    add(io.yn32[ATSAT_F_W], 0); add(io.wlo, 0); if (dl) add(io.dl_in[ATSAT_F_W], 0);
+    add(io.yn32[ATSAT_F_T], 0); if (dl) add(io.dl_in[ATSAT_F_T], 0);
+    add(io.fz[FZ_DPR], 1); add(io.fz[FZ_GU], 1); add(io.fz[FZ_BAN], 1); add(io.fz[FZ_BPS], 1);
+    add(io.fz[FZ_DPTH], 1); add(io.fz[FZ_GV], 1);
+    add(io.fz[FZ_DPPH], 1); add(io.fz[FZ_GW], 1);
+    add(io.fz[FZ_DPS], 1); add(io.rho_mix, 1); add(io.q_rad, 1); add(io.q_precip, 1); add(io.thermalmassflux, 1);
+    pl.n_items = n;
+    return pl;
+}
+
 cudaError_t launch_stage(atsat_dyn* h, const MixedIO& io, const StageParams& sp, int mode) {
     const int v = (mode == MODE_RHS || !variant_available(h, h->variant)) ? ATSAT_DYN_STAGE_DIRECT : h->variant;
     switch (v) {
@@ -776,6 +806,16 @@ cudaError_t launch_stage(atsat_dyn* h, const MixedIO& io, const StageParams& sp,
             if (pl.n_items != tracer_plan_items(mode, io.dl_in[0] != nullptr, h->kc.turb != 0))
                 return cudaErrorInvalidValue;   // the plan and the kernel disagree: never expected
             return launch_rk_tracer_tile(h->maps, h->kf, io, sp, pl, mode, h->stream);
+        }
+        case ATSAT_DYN_STAGE_TILED2: {
+            const TracerPlan pm = make_plan_mom(h, io);
+            const TracerPlan pt = make_plan_tracer(h, io, mode);
+            const bool dl = io.dl_in[0] != nullptr;
+            if (pm.n_items != mom_plan_items(dl) || pt.n_items != tracer_plan_items(mode, dl, h->kc.turb != 0))
+                return cudaErrorInvalidValue;   // the plans and the kernels disagree: never expected
+            const cudaError_t e = launch_rk_mom_tile(h->maps, h->kf, io, sp, pm, mode, h->stream);
+            if (e != cudaSuccess) return e;
+            return launch_rk_tracer_tile(h->maps, h->kf, io, sp, pt, mode, h->stream);
         }
         default: return launch_rk_stage_mixed(h->kf, io, sp, mode, h->stream);
     }

@@ -283,6 +283,7 @@ struct TileMaps {
     alignas(64) unsigned char main4[128];   // box TILE_BX x TILE_BY x TTILE_BZ
     alignas(64) unsigned char seam4[128];   // box TILE_SEAM_X x TILE_J x TTILE_I
     alignas(64) unsigned char pt4[128];     // box TILE_K x TILE_J x TTILE_I (point values, no halo)
+    alignas(64) unsigned char pt2[128];     // box TILE_K x TILE_J x TILE_I (point values, no halo)
 };
 
 // The tracer kernel's stream: every array it reads, in consumption order, each either a halo box
@@ -302,6 +303,10 @@ cudaError_t launch_rk_tracer_tile(const TileMaps& maps, const MixedConstF& kf, c
                                   const StageParams& sp, const TracerPlan& plan, int mode, cudaStream_t s);
 cudaError_t launch_rk_mom(const MixedConstF& kf, const MixedIO& io, const StageParams& sp, int mode, cudaStream_t s);
 int tracer_plan_items(int mode, bool has_dl, bool turb);
+// the momentum / temperature equations alone, TMA-tiled (species_divu off)
+cudaError_t launch_rk_mom_tile(const TileMaps& maps, const MixedConstF& kf, const MixedIO& io, const StageParams& sp,
+                               const TracerPlan& plan, int mode, cudaStream_t s);
+int mom_plan_items(bool has_dl);
 
 // standalone pressure-equation solver (poisson.cu)
 struct PoissonSolver;

@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--stage-variant", default="auto",
-                    choices=["auto", "direct", "tiled", "split", "split3", "split13", "split_tiled"],
+                    choices=["auto", "direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2"],
                     help="mixed precision: the RK stage kernel (auto: the autotuner's choice)")
     ap.add_argument("--poisson", action="store_true",
                     help="the standalone pressure-equation solves instead of the dycore iteration")
@@ -191,7 +191,8 @@ KERNEL_NAME = {"fp64": "rk_stage_fp64_kernel (fused RHSSat + RK4 stage, FP64)",
                "mixed_split": "rk_mom_kernel + rk_tracer_kernel<1> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)",
                "mixed_split3": "rk_mom_kernel + rk_tracer_kernel<3> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)",
                "mixed_split13": "rk_mom_kernel + rk_tracer_kernel<13> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)",
-               "mixed_split_tiled": "rk_mom_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, TMA-tiled tracers)"}
+               "mixed_split_tiled": "rk_mom_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, TMA-tiled tracers)",
+               "mixed_tiled2": "rk_mom_tile_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, all inputs TMA-streamed)"}
 
 
 def cpu_baseline(g, P, seed, target_s=3.0):

@@ -29,10 +29,10 @@ def drift(got, ref, fids):
     return out
 
 
-DIRECT, TILED, SPLIT, SPLIT3, SPLIT13, SPLIT_TILED = range(6)
+DIRECT, TILED, SPLIT, SPLIT3, SPLIT13, SPLIT_TILED, TILED2 = range(7)
 VARIANTS = [pytest.param(v, id=n) for v, n in
             [(TILED, "tiled"), (DIRECT, "direct"), (SPLIT, "split"), (SPLIT3, "split3"), (SPLIT13, "split13"),
-             (SPLIT_TILED, "split_tiled")]]
+             (SPLIT_TILED, "split_tiled"), (TILED2, "tiled2")]]
 
 _REF = {}
 
@@ -175,7 +175,7 @@ def test_split_unavailable_with_species_divu():
         with pytest.raises(dyn.DycoreError):
             d.set_stage_variant(SPLIT)
         chosen, ms = d.autotune(reps=2)
-        assert chosen in (DIRECT, TILED) and ms[SPLIT] < 0 and ms[SPLIT13] < 0 and ms[SPLIT_TILED] < 0
+        assert chosen in (DIRECT, TILED) and ms[SPLIT] < 0 and ms[SPLIT13] < 0 and ms[SPLIT_TILED] < 0 and ms[TILED2] < 0
 
 
 def test_autotune_keeps_state():
@@ -191,7 +191,7 @@ def test_autotune_keeps_state():
         before = {f: s.arrays[f].copy() for f in ALL}
         chosen, ms = d.autotune(reps=3)
         print("\nautotune (21, 91, 181):", chosen, ms)
-        assert 0 <= chosen < 6 and ms[chosen] == min(m for m in ms if m > 0)
+        assert 0 <= chosen < 7 and ms[chosen] == min(m for m in ms if m > 0)
         d.download(ALL)
         for f in ALL:
             assert np.array_equal(before[f], s.arrays[f], equal_nan=True), F.NAMES[f]
