@@ -238,6 +238,7 @@ void build_constants(atsat_dyn* h) {
     K.to_nd = 1.0 / (p.r_mix * p.u_0 * p.u_0 * 1.0e-5);
     K.r_mix = p.r_mix;
     K.rR = p.r_mix * p.R_mix;
+    K.buoy_c = p.g / (K.rR * p.t_ref);
     K.t_ref = p.t_ref;
     K.g = p.g;
     const double L_m = p.L_atm * 1.0e3;

@@ -85,6 +85,7 @@ struct KConst {
     double to_nd;                  // 1 / (r_mix u_0 u_0 1e-5)
     double r_mix;
     double rR, t_ref, g;           // r_mix R_mix, for the buoyancy b = g p / (rR t t_ref)
+    double buoy_c;                 // g / (rR t_ref)
     double kbuoy;                  // -nd_buoy * buoy_scale * buoyancy
     double legacy_buoy;            // buoyancy * g
     double inv_re, inv_re_pr;

@@ -2,9 +2,9 @@
 // RK4 steps (planet/BoundaryConditions.h:150-518 with BC_Sat.cpp:61-179), on the fields of the dycore.
 //
 // Each of the three routines only moves data along one grid direction, so each is one kernel whose
-// threads own disjoint lines: bcTheta works along j for every (i, k), bcPhi along k for every (i, j),
-// bcRadius (with the rigid-wall u, the top taper and the species lid / wall copies) along i for
-// every (j, k). They run in the order cSaturnModel::Run calls them (cSaturnModel.cpp:1091-1093).
+// threads own disjoint (line, field) pairs: bcTheta works along j for every (i, k), bcPhi along k for
+// every (i, j), bcRadius (with the rigid-wall u, the top taper and the species lid / wall copies) along i
+// for every (j, k). They run in the order cSaturnModel::Run calls them (cSaturnModel.cpp:1091-1093).
 //
 // In a resident mixed-precision run the prognostic fields also have FP32 copies (and w a second FP32
 // word) that the next step's stencils read; every value written here is written to them too.
@@ -49,106 +49,107 @@ __device__ __forceinline__ void put(const BCArgs& A, int id, int64_t c, double x
     }
 }
 
+// Each kernel runs one thread per (line, field): a field's boundary steps depend only on that field (and
+// rho_mix for the wall copy), so the fields of a line are independent and go to separate threads.
+// blockIdx.z is the field's task: an index into the kernel's field lists.
+
 __global__ void bc_theta_kernel(const KConst K, const BCArgs A) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = 1 + blockIdx.y;
+    const int task = blockIdx.z;                      // 0..16 extrapolated, 17..19 zeroed, 20..22 turbulence
     if (k > K.km - 2 || i > K.im - 2) return;
+    if (task >= 20 && !A.turb_on) return;
     const int64_t kp = K.kp, jm = K.jm;
     const int64_t base = (int64_t)i * K.plane + k;     // (i, 0, k)
     auto at = [&](int j) { return base + (int64_t)j * kp; };
-    if (A.pole_fill) {
-        const int jf = 2;
-        const double ramp = 1.0 / 2.0;
-        for (int q = 0; q < 17; q++) {
-            const int F = A.theta_extrap[q];
+    const int jf = 2;
+    if (task < 17) {
+        const int F = A.theta_extrap[task];
+        if (A.pole_fill) {
             put(A, F, at(1), get(A, F, at(jf)));
             put(A, F, at(jm - 2), get(A, F, at(jm - 1 - jf)));
         }
-        for (int q = 0; q < 3; q++) {
-            const int F = A.theta_zero[q];
-            put(A, F, at(1), ramp * get(A, F, at(jf)));
-            put(A, F, at(jm - 2), ramp * get(A, F, at(jm - 1 - jf)));
-        }
-        if (A.turb_on)
-            for (int q = 0; q < 3; q++) {
-                const int F = A.turb[q];
-                put(A, F, at(1), smax(A.turb_floor[q], get(A, F, at(jf))));
-                put(A, F, at(jm - 2), smax(A.turb_floor[q], get(A, F, at(jm - 1 - jf))));
-            }
-    }
-    for (int q = 0; q < 3; q++) {
-        put(A, A.theta_zero[q], at(0), 0.0);
-        put(A, A.theta_zero[q], at(jm - 1), 0.0);
-    }
-    for (int q = 0; q < 17; q++) {
-        const int F = A.theta_extrap[q];
         put(A, F, at(0), form3(A.pole_form, get(A, F, at(1)), get(A, F, at(2)), get(A, F, at(3)), K.c43, K.c13));
         put(A, F, at(jm - 1), form3(A.pole_form, get(A, F, at(jm - 2)), get(A, F, at(jm - 3)), get(A, F, at(jm - 4)),
                                     K.c43, K.c13));
-    }
-    if (A.turb_on)
-        for (int q = 0; q < 3; q++) {
-            const int F = A.turb[q];
-            put(A, F, at(0), smax(A.turb_floor[q], K.c43 * get(A, F, at(1)) - K.c13 * get(A, F, at(2))));
-            put(A, F, at(jm - 1), smax(A.turb_floor[q], K.c43 * get(A, F, at(jm - 2)) - K.c13 * get(A, F, at(jm - 3))));
+    } else if (task < 20) {
+        const int F = A.theta_zero[task - 17];
+        if (A.pole_fill) {
+            const double ramp = 1.0 / 2.0;
+            put(A, F, at(1), ramp * get(A, F, at(jf)));
+            put(A, F, at(jm - 2), ramp * get(A, F, at(jm - 1 - jf)));
         }
+        put(A, F, at(0), 0.0);
+        put(A, F, at(jm - 1), 0.0);
+    } else {
+        const int q = task - 20;
+        const int F = A.turb[q];
+        if (A.pole_fill) {
+            put(A, F, at(1), smax(A.turb_floor[q], get(A, F, at(jf))));
+            put(A, F, at(jm - 2), smax(A.turb_floor[q], get(A, F, at(jm - 1 - jf))));
+        }
+        put(A, F, at(0), smax(A.turb_floor[q], K.c43 * get(A, F, at(1)) - K.c13 * get(A, F, at(2))));
+        put(A, F, at(jm - 1), smax(A.turb_floor[q], K.c43 * get(A, F, at(jm - 2)) - K.c13 * get(A, F, at(jm - 3))));
+    }
 }
 
 __global__ void bc_phi_kernel(const KConst K, const BCArgs A) {
     const int row = blockIdx.x * blockDim.x + threadIdx.x;     // i * jm + j
+    const int task = blockIdx.z;                                // 0..19 copied, 20..22 turbulence
     if (row >= K.im * K.jm) return;
     const int64_t c0 = (int64_t)row * K.kp, c1 = c0 + K.km - 1;
-    for (int q = 0; q < 20; q++) put(A, A.radius[q], c1, get(A, A.radius[q], c0));
-    if (A.turb_on)
-        for (int q = 0; q < 3; q++) {
-            const int F = A.turb[q];
-            const double x = smax(A.turb_floor[q], get(A, F, c0));
-            put(A, F, c0, x);
-            put(A, F, c1, x);
-        }
+    if (task < 20) {
+        put(A, A.radius[task], c1, get(A, A.radius[task], c0));
+    } else if (A.turb_on) {
+        const int q = task - 20;
+        const int F = A.turb[q];
+        const double x = smax(A.turb_floor[q], get(A, F, c0));
+        put(A, F, c0, x);
+        put(A, F, c1, x);
+    }
 }
 
 __global__ void bc_radius_kernel(const KConst K, const BCArgs A) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y;
+    const int task = blockIdx.z;                                // 0..19 radius fields, 20..22 turbulence
     if (k >= K.km || j >= K.jm) return;
     const int64_t P = K.plane;
     const int64_t c0 = (int64_t)j * K.kp + k;                  // (0, j, k)
     const int im = K.im;
     auto at = [&](int i) { return c0 + (int64_t)i * P; };
-    if (j >= 1 && j <= K.jm - 2 && k <= K.km - 2) {
-        for (int q = 0; q < 20; q++) {
-            const int F = A.radius[q];
-            const int fb = (A.bottom_form != 0 && F != ATSAT_F_U) ? A.bottom_form : A.radius_form;
-            put(A, F, at(0), form3(fb, get(A, F, at(1)), get(A, F, at(2)), get(A, F, at(3)), K.c43, K.c13));
-            put(A, F, at(im - 1), form3(A.radius_form, get(A, F, at(im - 2)), get(A, F, at(im - 3)),
-                                        get(A, F, at(im - 4)), K.c43, K.c13));
-        }
-        if (A.turb_on)
-            for (int q = 0; q < 3; q++) {
-                const int F = A.turb[q];
-                put(A, F, at(0), smax(A.turb_floor[q], K.c43 * get(A, F, at(1)) - K.c13 * get(A, F, at(2))));
-                put(A, F, at(im - 1), smax(A.turb_floor[q], K.c43 * get(A, F, at(im - 2)) - K.c13 * get(A, F, at(im - 3))));
-            }
+    const bool inner = j >= 1 && j <= K.jm - 2 && k <= K.km - 2;
+    if (task >= 20) {
+        if (!A.turb_on || !inner) return;
+        const int q = task - 20;
+        const int F = A.turb[q];
+        put(A, F, at(0), smax(A.turb_floor[q], K.c43 * get(A, F, at(1)) - K.c13 * get(A, F, at(2))));
+        put(A, F, at(im - 1), smax(A.turb_floor[q], K.c43 * get(A, F, at(im - 2)) - K.c13 * get(A, F, at(im - 3))));
+        return;
     }
-    if (A.lid_u) { put(A, ATSAT_F_U, at(0), 0.0); put(A, ATSAT_F_U, at(im - 1), 0.0); }
-    if (A.top_taper) {
+    const int F = A.radius[task];
+    if (inner) {
+        const int fb = (A.bottom_form != 0 && F != ATSAT_F_U) ? A.bottom_form : A.radius_form;
+        put(A, F, at(0), form3(fb, get(A, F, at(1)), get(A, F, at(2)), get(A, F, at(3)), K.c43, K.c13));
+        put(A, F, at(im - 1), form3(A.radius_form, get(A, F, at(im - 2)), get(A, F, at(im - 3)),
+                                    get(A, F, at(im - 4)), K.c43, K.c13));
+    }
+    if (F == ATSAT_F_U && A.lid_u) { put(A, ATSAT_F_U, at(0), 0.0); put(A, ATSAT_F_U, at(im - 1), 0.0); }
+    if ((F == ATSAT_F_V || F == ATSAT_F_W) && A.top_taper) {
         const int iml = im - 1;
-        put(A, ATSAT_F_V, at(iml), 0.0);
-        put(A, ATSAT_F_W, at(iml), 0.0);
+        put(A, F, at(iml), 0.0);
         if (A.top_taper == 2) {
-            put(A, ATSAT_F_V, at(iml - 1), (1.0 / 3.0) * get(A, ATSAT_F_V, at(iml - 3)));
-            put(A, ATSAT_F_W, at(iml - 1), (1.0 / 3.0) * get(A, ATSAT_F_W, at(iml - 3)));
-            put(A, ATSAT_F_V, at(iml - 2), (2.0 / 3.0) * get(A, ATSAT_F_V, at(iml - 3)));
-            put(A, ATSAT_F_W, at(iml - 2), (2.0 / 3.0) * get(A, ATSAT_F_W, at(iml - 3)));
+            put(A, F, at(iml - 1), (1.0 / 3.0) * get(A, F, at(iml - 3)));
+            put(A, F, at(iml - 2), (2.0 / 3.0) * get(A, F, at(iml - 3)));
         } else {
-            put(A, ATSAT_F_V, at(iml - 1), get(A, ATSAT_F_V, at(iml - 1)) * (1.0 / 3.0));
-            put(A, ATSAT_F_W, at(iml - 1), get(A, ATSAT_F_W, at(iml - 1)) * (1.0 / 3.0));
-            put(A, ATSAT_F_V, at(iml - 2), get(A, ATSAT_F_V, at(iml - 2)) * (2.0 / 3.0));
-            put(A, ATSAT_F_W, at(iml - 2), get(A, ATSAT_F_W, at(iml - 2)) * (2.0 / 3.0));
+            put(A, F, at(iml - 1), get(A, F, at(iml - 1)) * (1.0 / 3.0));
+            put(A, F, at(iml - 2), get(A, F, at(iml - 2)) * (2.0 / 3.0));
         }
     }
     if (A.lid_copy == 0 && A.wall_copy == 0) return;
+    bool species = false;
+    for (int q = 0; q < 11; q++) species = species || (A.species[q] == F);
+    if (!species) return;
     double fr = 1.0;
     if (A.wall_copy == 2) {
         double r0 = A.r_mix, r1 = A.r_mix;
@@ -159,11 +160,8 @@ __global__ void bc_radius_kernel(const KConst K, const BCArgs A) {
         }
         fr = r0 / r1;
     }
-    for (int q = 0; q < 11; q++) {
-        const int F = A.species[q];
-        if (A.lid_copy != 0) put(A, F, at(im - 1), get(A, F, at(im - 2)));
-        if (A.wall_copy != 0) put(A, F, at(0), get(A, F, at(1)) * fr);
-    }
+    if (A.lid_copy != 0) put(A, F, at(im - 1), get(A, F, at(im - 2)));
+    if (A.wall_copy != 0) put(A, F, at(0), get(A, F, at(1)) * fr);
 }
 
 }  // namespace
@@ -208,9 +206,9 @@ cudaError_t launch_boundary_conditions(const KConst& kc, const atsat_dyn_params&
     A.lid_copy = p.bc_species_lid_copy;
     A.wall_copy = p.bc_species_wall_copy;
     A.local_rho = p.local_rho;
-    bc_theta_kernel<<<dim3((kc.km - 1 + 127) / 128, kc.im - 2), 128, 0, s>>>(kc, A);
-    bc_phi_kernel<<<(kc.im * kc.jm + 127) / 128, 128, 0, s>>>(kc, A);
-    bc_radius_kernel<<<dim3((kc.km + 127) / 128, kc.jm), 128, 0, s>>>(kc, A);
+    bc_theta_kernel<<<dim3((kc.km - 1 + 127) / 128, kc.im - 2, 23), 128, 0, s>>>(kc, A);
+    bc_phi_kernel<<<dim3((kc.im * kc.jm + 127) / 128, 1, 23), 128, 0, s>>>(kc, A);
+    bc_radius_kernel<<<dim3((kc.km + 127) / 128, kc.jm, 23), 128, 0, s>>>(kc, A);
     return cudaGetLastError();
 }
 

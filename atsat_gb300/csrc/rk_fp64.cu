@@ -283,20 +283,27 @@ __global__ void __launch_bounds__(256) rk_stage_fp64_kernel(const KConst K, cons
 constexpr int LM_CHUNKS = 16;
 constexpr int LM_THREADS = 128;
 
-// 1/x for x in FP32's normal range: the FP32 reciprocal refined by two Newton-Raphson steps
-// r <- r (2 - x r), written as r + r (1 - x r); each step squares the relative error (2^-23 -> 2^-46 ->
-// the FP64 rounding level).
+// 1/x for x > 0 in FP32's normal range: the FP32 reciprocal refined by one Newton-Raphson step
+// r <- r + r (1 - x r) (relative error 2^-23 -> ~2^-46, always from below). in_range tests the range on
+// the integer pipe (exponent field of x); x's FP32 copy and the result's widening are integer too.
+__device__ __forceinline__ bool in_rcp_range(double x) {
+    const uint32_t hi = (uint32_t)((uint64_t)__double_as_longlong(x) >> 32);
+    return (hi >> 31) == 0u && ((hi >> 20) & 0x7FFu) - 897u < 250u;   // 0 < x, float-normal with margin
+}
 __device__ __forceinline__ double recip_nr(double x) {
-    double r = (double)__frcp_rn((float)x);
-    r = fma(r, fma(-x, r, 1.0), r);
+    const double r = f2d(__frcp_rn(d2f(x)));
     return fma(r, fma(-x, r, 1.0), r);
 }
 
-// the buoyancy g p / (r_mix R_mix T t_ref) of one cell; false where the reference skips the cell
+// the buoyancy g p / (r_mix R_mix T t_ref) = bc p / t of one cell (bc formed on the host); false where
+// the reference skips the cell (!(t > 0), non-finite b)
 __device__ __forceinline__ bool cell_buoyancy(const KConst& K, double tc, double pc, double& b) {
-    if (!(tc > 0.0)) return false;
-    const double den = K.rR * tc * K.t_ref;
-    b = (den > 1.0e-30 && den < 1.0e30) ? (K.g * pc) * recip_nr(den) : K.g * pc / den;
+    if (in_rcp_range(tc)) {
+        b = (K.buoy_c * pc) * recip_nr(tc);
+    } else {
+        if (!(tc > 0.0)) return false;
+        b = K.g * pc / (K.rR * tc * K.t_ref);
+    }
     return isfinite(b);
 }
 
@@ -405,7 +412,8 @@ __global__ void __launch_bounds__(256) density_kernel(const KConst K, const doub
     const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
     const double T = __ldg(t + c) * K.t_ref;
     if (!(T > 0.0) || !(R_mix > 0.0)) { rho[c] = 0.0; return; }
-    const double r = (__ldg(ps + c) * 1.0e5) / (R_mix * T);
+    const double den = R_mix * T;
+    const double r = in_rcp_range(den) ? (__ldg(ps + c) * 1.0e5) * recip_nr(den) : (__ldg(ps + c) * 1.0e5) / den;
     rho[c] = isfinite(r) ? r : 0.0;
 }
 
