@@ -60,6 +60,7 @@ struct atsat_dyn {
     double* bind_base[ATSAT_NFIELDS] = {};
     std::vector<double*> bind_rows[ATSAT_NFIELDS];
     double* pinned = nullptr;            // staging for ragged rows, fsz doubles
+    double* dstage = nullptr;            // device staging for contiguous host arrays, im*jm*km doubles
 
     int64_t launches = 0;
     bool profiling = false;
@@ -478,8 +479,16 @@ int upload_one(atsat_dyn* h, int fid) {
     mark_dirty(h, fid);
     const int im = K.im, jm = K.jm, km = K.km, kp = K.kp;
     if (h->bind_kind[fid] == BIND_ARRAY) {
-        CK(h, cudaMemcpy2DAsync(h->f[fid], (size_t)kp * 8, h->bind_base[fid], (size_t)km * 8, (size_t)km * 8,
-                                (size_t)im * jm, cudaMemcpyHostToDevice, h->stream));
+        // one contiguous copy at full link bandwidth, then the padding on the device (a 2-D copy of
+        // km-double rows runs far below it)
+        const size_t n = (size_t)im * jm * km;
+        if (kp == km) {
+            CK(h, cudaMemcpyAsync(h->f[fid], h->bind_base[fid], n * 8, cudaMemcpyHostToDevice, h->stream));
+        } else {
+            CK(h, cudaMemcpyAsync(h->dstage, h->bind_base[fid], n * 8, cudaMemcpyHostToDevice, h->stream));
+            CK(h, launch_repitch(h->f[fid], kp, h->dstage, km, km, (int64_t)im * jm, h->stream));
+            h->launches += 1;
+        }
     } else if (h->bind_kind[fid] == BIND_ROWS) {
         CK(h, cudaStreamSynchronize(h->stream));     // the staging buffer is free again
         double* const* rows = h->bind_rows[fid].data();
@@ -498,8 +507,14 @@ int download_one(atsat_dyn* h, int fid) {
     const KConst& K = h->kc;
     const int im = K.im, jm = K.jm, km = K.km, kp = K.kp;
     if (h->bind_kind[fid] == BIND_ARRAY) {
-        CK(h, cudaMemcpy2DAsync(h->bind_base[fid], (size_t)km * 8, h->f[fid], (size_t)kp * 8, (size_t)km * 8,
-                                (size_t)im * jm, cudaMemcpyDeviceToHost, h->stream));
+        const size_t n = (size_t)im * jm * km;
+        if (kp == km) {
+            CK(h, cudaMemcpyAsync(h->bind_base[fid], h->f[fid], n * 8, cudaMemcpyDeviceToHost, h->stream));
+        } else {
+            CK(h, launch_repitch(h->dstage, km, h->f[fid], kp, km, (int64_t)im * jm, h->stream));
+            h->launches += 1;
+            CK(h, cudaMemcpyAsync(h->bind_base[fid], h->dstage, n * 8, cudaMemcpyDeviceToHost, h->stream));
+        }
     } else if (h->bind_kind[fid] == BIND_ROWS) {
         CK(h, cudaMemcpyAsync(h->pinned, h->f[fid], (size_t)K.fsz * 8, cudaMemcpyDeviceToHost, h->stream));
         CK(h, cudaStreamSynchronize(h->stream));
@@ -1185,6 +1200,7 @@ void atsat_dyn_destroy(atsat_dyn_t h) {
     if (h->slab) cudaFree(h->slab);
     if (h->slab32) cudaFree(h->slab32);
     if (h->pinned) cudaFreeHost(h->pinned);
+    if (h->dstage) cudaFree(h->dstage);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -1210,6 +1226,14 @@ int atsat_dyn_bind_host_rows(atsat_dyn_t h, int32_t field, double* const* rows) 
 int atsat_dyn_bind_host_array(atsat_dyn_t h, int32_t field, double* base) {
     if (!h || !h->slab) return ATSAT_DYN_E_INVALID;
     if (!valid_field(field)) return fail(h, ATSAT_DYN_E_INVALID, "bad field %d", field);
+    if (base && !h->dstage && h->kc.kp != h->kc.km) {
+        CK(h, cudaSetDevice(h->device));
+        const cudaError_t e = cudaMalloc(&h->dstage, (size_t)h->kc.im * h->kc.jm * h->kc.km * 8);
+        if (e != cudaSuccess) {
+            h->dstage = nullptr;
+            return fail(h, ATSAT_DYN_E_NOMEM, "device staging: %s", cudaGetErrorString(e));
+        }
+    }
     h->bind_kind[field] = base ? BIND_ARRAY : BIND_NONE;
     h->bind_base[field] = base;
     h->bind_rows[field].clear();

@@ -338,6 +338,8 @@ cudaError_t launch_copy_fields(const KConst& kc, double* const* dst, const doubl
 // s32 (may be null): FP32 copies to keep in step, indexed by field id; wlo: the second FP32 word of w.
 cudaError_t launch_boundary_conditions(const KConst& kc, const atsat_dyn_params& p, double* const* f,
                                        float* const* s32, float* wlo, cudaStream_t s);
+cudaError_t launch_repitch(double* dst, int dst_pitch, const double* src, int src_pitch, int width, int64_t rows,
+                           cudaStream_t s);
 cudaError_t launch_count_nonfinite(const KConst& kc, const double* x, unsigned long long* count,
                                    cudaStream_t s);
 

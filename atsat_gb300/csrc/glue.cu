@@ -164,7 +164,27 @@ __global__ void bc_radius_kernel(const KConst K, const BCArgs A) {
     if (A.wall_copy != 0) put(A, F, at(0), get(A, F, at(1)) * fr);
 }
 
+// dst[r * dst_pitch + k] = src[r * src_pitch + k] for k < width: host arrays are contiguous rows of km
+// values, the device layout pads them to kp, so host copies go through a contiguous staging field
+__global__ void repitch_kernel(double* __restrict__ dst, int dst_pitch, const double* __restrict__ src, int src_pitch,
+                               int width, int64_t rows) {
+    const int64_t r = (int64_t)blockIdx.y * gridDim.z + blockIdx.z;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows || k >= width) return;
+    dst[r * dst_pitch + k] = src[r * src_pitch + k];
+}
+
 }  // namespace
+
+cudaError_t launch_repitch(double* dst, int dst_pitch, const double* src, int src_pitch, int width, int64_t rows,
+                           cudaStream_t s) {
+    // rows split over grid y and z (each below 65536)
+    const int64_t gz = rows < 1024 ? rows : 1024;
+    const int64_t gy = (rows + gz - 1) / gz;
+    repitch_kernel<<<dim3((width + 127) / 128, (unsigned)gy, (unsigned)gz), 128, 0, s>>>(dst, dst_pitch, src, src_pitch,
+                                                                                        width, rows);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_boundary_conditions(const KConst& kc, const atsat_dyn_params& p, double* const* f,
                                        float* const* s32, float* wlo, cudaStream_t s) {
