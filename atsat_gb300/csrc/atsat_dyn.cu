@@ -60,7 +60,12 @@ struct atsat_dyn {
     double* bind_base[ATSAT_NFIELDS] = {};
     std::vector<double*> bind_rows[ATSAT_NFIELDS];
     double* pinned = nullptr;            // staging for ragged rows, fsz doubles
-    double* dstage = nullptr;            // device staging for contiguous host arrays, im*jm*km doubles
+    // copy pipeline for contiguous host arrays: two device staging buffers of im*jm*km doubles, a copy
+    // stream, and per buffer an event for "copy landed / re-pitched out" and one for "free again"
+    double* dstage[2] = {};
+    cudaStream_t cstream = nullptr;
+    cudaEvent_t ev_ready[2] = {}, ev_free[2] = {}, ev_join = nullptr;
+    int stage_next = 0;
 
     int64_t launches = 0;
     bool profiling = false;
@@ -474,20 +479,95 @@ void mark_dirty(atsat_dyn* h, int fid) {
     if (s >= 0) h->conv_dirty[s] = true;
 }
 
+// Contiguous host arrays hold im*jm*km doubles per field while the device rows are kp doubles long. A
+// pitched 2-D copy of 2.9 KB rows runs far below the link, so every field goes as one contiguous copy into a
+// device staging buffer and a kernel moves it to (or from) the pitched layout. Two buffers alternate: the
+// copy stream carries the transfers, the handle stream the re-pitch kernels, and events order each buffer's
+// producer before its consumer and its consumer before the buffer's next producer, so the transfer of one
+// field overlaps the re-pitch of the one before.
+void stage_pipe_free(atsat_dyn* h) {
+    if (h->cstream) cudaStreamSynchronize(h->cstream);
+    for (int b = 0; b < 2; b++) {
+        if (h->dstage[b]) cudaFree(h->dstage[b]);
+        if (h->ev_ready[b]) cudaEventDestroy(h->ev_ready[b]);
+        if (h->ev_free[b]) cudaEventDestroy(h->ev_free[b]);
+        h->dstage[b] = nullptr;
+        h->ev_ready[b] = h->ev_free[b] = nullptr;
+    }
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->cstream) cudaStreamDestroy(h->cstream);
+    h->ev_join = nullptr;
+    h->cstream = nullptr;
+}
+
+// All or nothing: the copy stream exists only when both buffers and all events do.
+int stage_pipe_create(atsat_dyn* h) {
+    CK(h, cudaSetDevice(h->device));
+    const size_t bytes = (size_t)h->kc.im * h->kc.jm * h->kc.km * 8;
+    cudaError_t e = cudaSuccess;
+    for (int b = 0; b < 2 && e == cudaSuccess; b++) {
+        e = cudaMalloc(&h->dstage[b], bytes);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_ready[b], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_free[b], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->cstream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        stage_pipe_free(h);
+        cudaGetLastError();
+        return fail(h, ATSAT_DYN_E_NOMEM, "device staging: %s", cudaGetErrorString(e));
+    }
+    h->stage_next = 0;
+    return ATSAT_DYN_OK;
+}
+
+int stage_in(atsat_dyn* h, double* dst, const double* host) {
+    const KConst& K = h->kc;
+    const int b = h->stage_next;
+    h->stage_next ^= 1;
+    CK(h, cudaStreamWaitEvent(h->cstream, h->ev_free[b], 0));
+    CK(h, cudaMemcpyAsync(h->dstage[b], host, (size_t)K.im * K.jm * K.km * 8, cudaMemcpyHostToDevice, h->cstream));
+    CK(h, cudaEventRecord(h->ev_ready[b], h->cstream));
+    CK(h, cudaStreamWaitEvent(h->stream, h->ev_ready[b], 0));
+    CK(h, launch_repitch(dst, K.kp, h->dstage[b], K.km, K.km, (int64_t)K.im * K.jm, h->stream));
+    h->launches += 1;
+    CK(h, cudaEventRecord(h->ev_free[b], h->stream));
+    return ATSAT_DYN_OK;
+}
+
+int stage_out(atsat_dyn* h, double* host, const double* src) {
+    const KConst& K = h->kc;
+    const int b = h->stage_next;
+    h->stage_next ^= 1;
+    CK(h, cudaStreamWaitEvent(h->stream, h->ev_free[b], 0));
+    CK(h, launch_repitch(h->dstage[b], K.km, src, K.kp, K.km, (int64_t)K.im * K.jm, h->stream));
+    h->launches += 1;
+    CK(h, cudaEventRecord(h->ev_ready[b], h->stream));
+    CK(h, cudaStreamWaitEvent(h->cstream, h->ev_ready[b], 0));
+    CK(h, cudaMemcpyAsync(host, h->dstage[b], (size_t)K.im * K.jm * K.km * 8, cudaMemcpyDeviceToHost, h->cstream));
+    CK(h, cudaEventRecord(h->ev_free[b], h->cstream));
+    return ATSAT_DYN_OK;
+}
+
+// The handle stream waits for everything queued on the copy stream, so one synchronisation of it covers both.
+int stage_join(atsat_dyn* h) {
+    if (!h->cstream) return ATSAT_DYN_OK;
+    CK(h, cudaEventRecord(h->ev_join, h->cstream));
+    CK(h, cudaStreamWaitEvent(h->stream, h->ev_join, 0));
+    return ATSAT_DYN_OK;
+}
+
 int upload_one(atsat_dyn* h, int fid) {
     const KConst& K = h->kc;
     mark_dirty(h, fid);
     const int im = K.im, jm = K.jm, km = K.km, kp = K.kp;
     if (h->bind_kind[fid] == BIND_ARRAY) {
-        // one contiguous copy at full link bandwidth, then the padding on the device (a 2-D copy of
-        // km-double rows runs far below it)
         const size_t n = (size_t)im * jm * km;
         if (kp == km) {
             CK(h, cudaMemcpyAsync(h->f[fid], h->bind_base[fid], n * 8, cudaMemcpyHostToDevice, h->stream));
         } else {
-            CK(h, cudaMemcpyAsync(h->dstage, h->bind_base[fid], n * 8, cudaMemcpyHostToDevice, h->stream));
-            CK(h, launch_repitch(h->f[fid], kp, h->dstage, km, km, (int64_t)im * jm, h->stream));
-            h->launches += 1;
+            int rc = stage_in(h, h->f[fid], h->bind_base[fid]);
+            if (rc) return rc;
         }
     } else if (h->bind_kind[fid] == BIND_ROWS) {
         CK(h, cudaStreamSynchronize(h->stream));     // the staging buffer is free again
@@ -511,9 +591,8 @@ int download_one(atsat_dyn* h, int fid) {
         if (kp == km) {
             CK(h, cudaMemcpyAsync(h->bind_base[fid], h->f[fid], n * 8, cudaMemcpyDeviceToHost, h->stream));
         } else {
-            CK(h, launch_repitch(h->dstage, km, h->f[fid], kp, km, (int64_t)im * jm, h->stream));
-            h->launches += 1;
-            CK(h, cudaMemcpyAsync(h->bind_base[fid], h->dstage, n * 8, cudaMemcpyDeviceToHost, h->stream));
+            int rc = stage_out(h, h->bind_base[fid], h->f[fid]);
+            if (rc) return rc;
         }
     } else if (h->bind_kind[fid] == BIND_ROWS) {
         CK(h, cudaMemcpyAsync(h->pinned, h->f[fid], (size_t)K.fsz * 8, cudaMemcpyDeviceToHost, h->stream));
@@ -1200,7 +1279,7 @@ void atsat_dyn_destroy(atsat_dyn_t h) {
     if (h->slab) cudaFree(h->slab);
     if (h->slab32) cudaFree(h->slab32);
     if (h->pinned) cudaFreeHost(h->pinned);
-    if (h->dstage) cudaFree(h->dstage);
+    stage_pipe_free(h);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -1226,13 +1305,9 @@ int atsat_dyn_bind_host_rows(atsat_dyn_t h, int32_t field, double* const* rows) 
 int atsat_dyn_bind_host_array(atsat_dyn_t h, int32_t field, double* base) {
     if (!h || !h->slab) return ATSAT_DYN_E_INVALID;
     if (!valid_field(field)) return fail(h, ATSAT_DYN_E_INVALID, "bad field %d", field);
-    if (base && !h->dstage && h->kc.kp != h->kc.km) {
-        CK(h, cudaSetDevice(h->device));
-        const cudaError_t e = cudaMalloc(&h->dstage, (size_t)h->kc.im * h->kc.jm * h->kc.km * 8);
-        if (e != cudaSuccess) {
-            h->dstage = nullptr;
-            return fail(h, ATSAT_DYN_E_NOMEM, "device staging: %s", cudaGetErrorString(e));
-        }
+    if (base && !h->cstream && h->kc.kp != h->kc.km) {
+        int rc = stage_pipe_create(h);
+        if (rc) return rc;
     }
     h->bind_kind[field] = base ? BIND_ARRAY : BIND_NONE;
     h->bind_base[field] = base;
@@ -1254,7 +1329,8 @@ int atsat_dyn_upload(atsat_dyn_t h, const int32_t* fields, int32_t n) {
         int rc = upload_one(h, fields[q]);
         if (rc) return rc;
     }
-    return finish(h);
+    int rc = stage_join(h);
+    return rc ? rc : finish(h);
 }
 
 int atsat_dyn_download(atsat_dyn_t h, const int32_t* fields, int32_t n) {
@@ -1265,7 +1341,8 @@ int atsat_dyn_download(atsat_dyn_t h, const int32_t* fields, int32_t n) {
         int rc = download_one(h, fields[q]);
         if (rc) return rc;
     }
-    return finish(h);
+    int rc = stage_join(h);
+    return rc ? rc : finish(h);
 }
 
 int atsat_dyn_set_tables(atsat_dyn_t h, const double* cell_vbar0, const double* cell_ubar0, const double* p_baro) {

@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--shape", default="41,181,361")
-    ap.add_argument("--e2e-steps", type=int, default=6)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--stage-variant", default="auto",
                     choices=["auto", "direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2"],
@@ -286,21 +286,30 @@ def measure(a, rank, world, g, P, st, pinned, precision):
     # ---- end to end through the C ABI with host buffers ----
     ins = F.STEP_INPUTS
     outs = F.STEP_OUTPUTS
-    h2d = d2h = 0
-    it = it0 + a.steps
-    barrier(world)
-    t0 = time.perf_counter()
-    for s in range(a.e2e_steps):
+
+    def e2e_step(it):
+        """One drop-in step: upload the inputs, pressure call on even steps, RK4, download; bytes moved."""
+        up, down = len(ins) * g.cells * 8, len(outs) * g.cells * 8
         d.upload(ins)
-        h2d += len(ins) * g.cells * 8
         if it % 2 == 0:
             d.computeMixtureDensity()
             d.PressureSolver_run()
             d.download([F.P_DYN])
-            d2h += g.cells * 8
+            down += g.cells * 8
         d.RungeKuttaSat()
         d.download(outs)
-        d2h += len(outs) * g.cells * 8
+        return up, down
+
+    it = it0 + a.steps
+    e2e_step(it)                 # untimed: the first host-fed step leaves the resident (aliased) state
+    it += 1
+    h2d = d2h = 0
+    barrier(world)
+    t0 = time.perf_counter()
+    for s in range(a.e2e_steps):
+        up, down = e2e_step(it)
+        h2d += up
+        d2h += down
         it += 1
     e2e_s = reduce_max(world, time.perf_counter() - t0)
     e2e = {"value": world * a.e2e_steps * g.cells / e2e_s / 1e6, "unit": UNIT,
