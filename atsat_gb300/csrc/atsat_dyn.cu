@@ -59,7 +59,12 @@ struct atsat_dyn {
     int bind_kind[ATSAT_NFIELDS] = {};
     double* bind_base[ATSAT_NFIELDS] = {};
     std::vector<double*> bind_rows[ATSAT_NFIELDS];
-    double* pinned = nullptr;            // staging for ragged rows, fsz doubles
+    // ragged-row bindings: two pinned staging buffers of fsz doubles, each with the event of its last copy,
+    // so that packing (unpacking) one field on the host overlaps the transfer of the one before (after)
+    double* pinned[2] = {};
+    cudaEvent_t ev_pin[2] = {};
+    int pin_next = 0;
+    int rows_pending = -1, rows_pending_buf = 0;
     // copy pipeline for contiguous host arrays: two device staging buffers of im*jm*km doubles, a copy
     // stream, and per buffer an event for "copy landed / re-pitched out" and one for "free again"
     double* dstage[2] = {};
@@ -570,16 +575,35 @@ int upload_one(atsat_dyn* h, int fid) {
             if (rc) return rc;
         }
     } else if (h->bind_kind[fid] == BIND_ROWS) {
-        CK(h, cudaStreamSynchronize(h->stream));     // the staging buffer is free again
+        const int b = h->pin_next;
+        h->pin_next ^= 1;
+        CK(h, cudaEventSynchronize(h->ev_pin[b]));  // the previous copy out of this buffer has finished
         double* const* rows = h->bind_rows[fid].data();
-        double* st = h->pinned;
+        double* st = h->pinned[b];
         const int nrows = im * jm;
 #pragma omp parallel for schedule(static)
         for (int r = 0; r < nrows; r++) memcpy(st + (size_t)r * kp, rows[r], (size_t)km * 8);
         CK(h, cudaMemcpyAsync(h->f[fid], st, (size_t)K.fsz * 8, cudaMemcpyHostToDevice, h->stream));
+        CK(h, cudaEventRecord(h->ev_pin[b], h->stream));
     } else {
         return fail(h, ATSAT_DYN_E_UNBOUND, "field %d has no host binding", fid);
     }
+    return ATSAT_DYN_OK;
+}
+
+// Unpacks the field whose device->host copy was queued last, once that copy has landed.
+int rows_flush(atsat_dyn* h) {
+    const int fid = h->rows_pending;
+    if (fid < 0) return ATSAT_DYN_OK;
+    h->rows_pending = -1;
+    const KConst& K = h->kc;
+    const int b = h->rows_pending_buf;
+    CK(h, cudaEventSynchronize(h->ev_pin[b]));
+    double* const* rows = h->bind_rows[fid].data();
+    const double* st = h->pinned[b];
+    const int nrows = K.im * K.jm, km = K.km, kp = K.kp;
+#pragma omp parallel for schedule(static)
+    for (int r = 0; r < nrows; r++) memcpy(rows[r], st + (size_t)r * kp, (size_t)km * 8);
     return ATSAT_DYN_OK;
 }
 
@@ -595,13 +619,15 @@ int download_one(atsat_dyn* h, int fid) {
             if (rc) return rc;
         }
     } else if (h->bind_kind[fid] == BIND_ROWS) {
-        CK(h, cudaMemcpyAsync(h->pinned, h->f[fid], (size_t)K.fsz * 8, cudaMemcpyDeviceToHost, h->stream));
-        CK(h, cudaStreamSynchronize(h->stream));
-        double* const* rows = h->bind_rows[fid].data();
-        const double* st = h->pinned;
-        const int nrows = im * jm;
-#pragma omp parallel for schedule(static)
-        for (int r = 0; r < nrows; r++) memcpy(rows[r], st + (size_t)r * kp, (size_t)km * 8);
+        // the buffer was last read by the unpack two fields ago, which the flush below has completed
+        const int b = h->pin_next;
+        h->pin_next ^= 1;
+        CK(h, cudaMemcpyAsync(h->pinned[b], h->f[fid], (size_t)K.fsz * 8, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaEventRecord(h->ev_pin[b], h->stream));
+        int rc = rows_flush(h);
+        if (rc) return rc;
+        h->rows_pending = fid;
+        h->rows_pending_buf = b;
     } else {
         return fail(h, ATSAT_DYN_E_UNBOUND, "field %d has no host binding", fid);
     }
@@ -1278,7 +1304,10 @@ void atsat_dyn_destroy(atsat_dyn_t h) {
     if (h->graph) cudaGraphExecDestroy(h->graph);
     if (h->slab) cudaFree(h->slab);
     if (h->slab32) cudaFree(h->slab32);
-    if (h->pinned) cudaFreeHost(h->pinned);
+    for (int b = 0; b < 2; b++) {
+        if (h->pinned[b]) cudaFreeHost(h->pinned[b]);
+        if (h->ev_pin[b]) cudaEventDestroy(h->ev_pin[b]);
+    }
     stage_pipe_free(h);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -1292,9 +1321,17 @@ int atsat_dyn_bind_host_rows(atsat_dyn_t h, int32_t field, double* const* rows) 
     const size_t n = (size_t)h->kc.im * h->kc.jm;
     for (size_t r = 0; r < n; r++)
         if (!rows[r]) return fail(h, ATSAT_DYN_E_INVALID, "row %zu of field %d is null", r, field);
-    if (!h->pinned) {
-        cudaError_t e = cudaHostAlloc(&h->pinned, (size_t)h->kc.fsz * 8, cudaHostAllocDefault);
-        if (e != cudaSuccess) { h->pinned = nullptr; return fail(h, ATSAT_DYN_E_NOMEM, "pinned staging: %s", cudaGetErrorString(e)); }
+    if (!h->ev_pin[1]) {
+        CK(h, cudaSetDevice(h->device));
+        cudaError_t e = cudaSuccess;
+        for (int b = 0; b < 2 && e == cudaSuccess; b++) {
+            if (!h->pinned[b]) e = cudaHostAlloc(&h->pinned[b], (size_t)h->kc.fsz * 8, cudaHostAllocDefault);
+            if (e == cudaSuccess && !h->ev_pin[b]) e = cudaEventCreateWithFlags(&h->ev_pin[b], cudaEventDisableTiming);
+        }
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(h, ATSAT_DYN_E_NOMEM, "pinned staging: %s", cudaGetErrorString(e));
+        }
     }
     h->bind_rows[field].assign(rows, rows + n);
     h->bind_kind[field] = BIND_ROWS;
@@ -1339,9 +1376,10 @@ int atsat_dyn_download(atsat_dyn_t h, const int32_t* fields, int32_t n) {
     for (int32_t q = 0; q < n; q++) {
         if (!valid_field(fields[q])) return fail(h, ATSAT_DYN_E_INVALID, "bad field %d", fields[q]);
         int rc = download_one(h, fields[q]);
-        if (rc) return rc;
+        if (rc) { h->rows_pending = -1; return rc; }
     }
-    int rc = stage_join(h);
+    int rc = rows_flush(h);
+    if (!rc) rc = stage_join(h);
     return rc ? rc : finish(h);
 }
 

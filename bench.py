@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--shape", default="41,181,361")
     ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-rows-steps", type=int, default=4,
+                    help="steps of the e2e loop over ragged pageable rows (0 skips it)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--stage-variant", default="auto",
                     choices=["auto", "direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2"],
@@ -244,8 +246,15 @@ def config(g, precision):
             "parallelism": "replicas"}
 
 
+def omp_threads():
+    """Threads the library's OpenMP host loops use (OMP_NUM_THREADS, else every core)."""
+    v = os.environ.get("OMP_NUM_THREADS", "")
+    return int(v) if v.isdigit() and int(v) > 0 else os.cpu_count()
+
+
 def measure(a, rank, world, g, P, st, pinned, precision):
     """Resident throughput, e2e throughput and the stage kernel's roofline of one precision."""
+    import numpy as np
     from atsat_gb300 import abi, dyn, fields as F
     d = dyn.Dycore(g, dict(P, precision=1 if precision == "mixed" else 0))
     for fid in range(F.NFIELDS):
@@ -314,7 +323,30 @@ def measure(a, rank, world, g, P, st, pinned, precision):
     e2e_s = reduce_max(world, time.perf_counter() - t0)
     e2e = {"value": world * a.e2e_steps * g.cells / e2e_s / 1e6, "unit": UNIT,
            "h2d_bytes_per_step": h2d // a.e2e_steps, "d2h_bytes_per_step": d2h // a.e2e_steps,
-           "steps": a.e2e_steps, "ms_per_step": e2e_s * 1e3 / a.e2e_steps}
+           "steps": a.e2e_steps, "ms_per_step": e2e_s * 1e3 / a.e2e_steps,
+           "binding": "contiguous pinned arrays (bind_host_array)"}
+
+    # the same loop over the reference's own storage: one pageable row of km doubles per (i, j), as
+    # lib/Array.cpp allocates it, bound through bind_host_rows (packed on the host into pinned staging)
+    if a.e2e_rows_steps > 0:
+        keep = {}
+        for fid in sorted(set(ins) | set(outs) | {F.P_DYN}):
+            base = np.array(pinned[fid].array, copy=True)
+            rows = [base[i, j] for i in range(g.im) for j in range(g.jm)]
+            keep[fid] = base
+            d.bind_rows(fid, rows)
+        e2e_step(it)
+        it += 1
+        barrier(world)
+        t0 = time.perf_counter()
+        for s in range(a.e2e_rows_steps):
+            e2e_step(it)
+            it += 1
+        rows_s = reduce_max(world, time.perf_counter() - t0)
+        e2e["rows"] = {"value": world * a.e2e_rows_steps * g.cells / rows_s / 1e6, "unit": UNIT,
+                       "steps": a.e2e_rows_steps, "ms_per_step": rows_s * 1e3 / a.e2e_rows_steps,
+                       "binding": "ragged pageable rows (bind_host_rows)", "host_threads": omp_threads()}
+        del keep
 
     peak, peak_kind = peaks()
     bytes_per_launch = RK_BYTES[precision] / 4 * interior_rk(g)
