@@ -29,27 +29,38 @@ constexpr int NPROG = ATSAT_NPROG;
 static __device__ __noinline__ double f2d_rare(float f) { return (double)f; }
 static __device__ __noinline__ float d2f_rare(double d) { return (float)d; }
 
+// The double's two words pass through a register move in inline PTX: tests on its bits then stay
+// integer tests (the compiler would otherwise fold a test such as "all bits but the sign are zero"
+// back into an FP64 comparison, a DSETP on the FP64 pipe).
+__device__ __forceinline__ void split_f64(double d, uint32_t& lo, uint32_t& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(d));
+}
+__device__ __forceinline__ double join_f64(uint32_t lo, uint32_t hi) {
+    double d;
+    asm("mov.b64 %0, {%1, %2};" : "=d"(d) : "r"(lo), "r"(hi));
+    return d;
+}
+
 __device__ __forceinline__ double f2d(float f) {
     const uint32_t b = __float_as_uint(f);
     const uint32_t a = b & 0x7FFFFFFFu;
     if (a - 0x00800000u < 0x7F000000u)            // biased exponent 1..254
-        return __longlong_as_double((long long)(((uint64_t)(b & 0x80000000u) << 32) |
-                                                (((uint64_t)a << 29) + (896ull << 52))));
-    if (a == 0u) return __longlong_as_double((long long)((uint64_t)b << 32));
+        return join_f64(a << 29, (b & 0x80000000u) | ((a >> 3) + (896u << 20)));
+    if (a == 0u) return join_f64(0u, b);
     return f2d_rare(f);
 }
 
 __device__ __forceinline__ float d2f(double d) {
-    const uint64_t b = (uint64_t)__double_as_longlong(d);
-    const uint32_t hi = (uint32_t)(b >> 32);
+    uint32_t lo, hi;
+    split_f64(d, lo, hi);
     const uint32_t e = (hi >> 20) & 0x7FFu;
     if (e - 897u < 254u) {                         // result exponent 1..254 before rounding
-        uint32_t q = ((e - 896u) << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu);
-        const uint32_t r = (uint32_t)b & 0x1FFFFFFFu;
+        uint32_t q = ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+        const uint32_t r = lo & 0x1FFFFFFFu;
         q += (r > 0x10000000u || (r == 0x10000000u && (q & 1u))) ? 1u : 0u;   // a carry into 255 is inf
         return __uint_as_float(q | (hi & 0x80000000u));
     }
-    if ((b << 1) == 0) return __uint_as_float(hi & 0x80000000u);
+    if (((hi << 1) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
     return d2f_rare(d);
 }
 

@@ -287,7 +287,8 @@ constexpr int LM_THREADS = 128;
 // r <- r + r (1 - x r) (relative error 2^-23 -> ~2^-46, always from below). in_range tests the range on
 // the integer pipe (exponent field of x); x's FP32 copy and the result's widening are integer too.
 __device__ __forceinline__ bool in_rcp_range(double x) {
-    const uint32_t hi = (uint32_t)((uint64_t)__double_as_longlong(x) >> 32);
+    uint32_t lo, hi;
+    split_f64(x, lo, hi);
     return (hi >> 31) == 0u && ((hi >> 20) & 0x7FFu) - 897u < 250u;   // 0 < x, float-normal with margin
 }
 __device__ __forceinline__ double recip_nr(double x) {

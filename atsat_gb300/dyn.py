@@ -89,8 +89,19 @@ def lib():
                                               C.c_int32, C.c_int32, C.c_double, C.POINTER(abi.PoissonStats)]
         L.atsat_dyn_timer_start.argtypes = [H]
         L.atsat_dyn_timer_stop.argtypes = [H, C.POINTER(C.c_double)]
+        L.atsat_dyn_conv_selftest.argtypes = [C.c_int32, C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         _lib = L
     return _lib
+
+
+def conv_selftest(n_doubles: int = 1 << 32, device: int = 0) -> tuple[int, int]:
+    """Mismatches of the integer-pipe float<->double conversions against the hardware's (widening over
+    all 2^32 floats, narrowing over those and n_doubles hashed doubles); (0, 0) means bit-identical."""
+    w, n = C.c_uint64(0), C.c_uint64(0)
+    rc = lib().atsat_dyn_conv_selftest(device, n_doubles, C.byref(w), C.byref(n))
+    if rc != 0:
+        raise DycoreError(rc, "atsat_dyn_conv_selftest", "CUDA error")
+    return w.value, n.value
 
 
 def params_from_env(base: dict | None = None) -> dict:

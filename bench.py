@@ -42,11 +42,11 @@ UNIT = "Mcell-steps/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--shape", default="41,181,361")
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=10, help="timed host-fed steps (0 skips the e2e loops)")
     ap.add_argument("--e2e-rows-steps", type=int, default=4,
                     help="steps of the e2e loop over ragged pageable rows (0 skips it)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -310,25 +310,27 @@ def measure(a, rank, world, g, P, st, pinned, precision):
         return up, down
 
     it = it0 + a.steps
-    e2e_step(it)                 # untimed: the first host-fed step leaves the resident (aliased) state
-    it += 1
-    h2d = d2h = 0
-    barrier(world)
-    t0 = time.perf_counter()
-    for s in range(a.e2e_steps):
-        up, down = e2e_step(it)
-        h2d += up
-        d2h += down
+    e2e = None
+    if a.e2e_steps > 0:
+        e2e_step(it)             # untimed: the first host-fed step leaves the resident (aliased) state
         it += 1
-    e2e_s = reduce_max(world, time.perf_counter() - t0)
-    e2e = {"value": world * a.e2e_steps * g.cells / e2e_s / 1e6, "unit": UNIT,
-           "h2d_bytes_per_step": h2d // a.e2e_steps, "d2h_bytes_per_step": d2h // a.e2e_steps,
-           "steps": a.e2e_steps, "ms_per_step": e2e_s * 1e3 / a.e2e_steps,
-           "binding": "contiguous pinned arrays (bind_host_array)"}
+        h2d = d2h = 0
+        barrier(world)
+        t0 = time.perf_counter()
+        for s in range(a.e2e_steps):
+            up, down = e2e_step(it)
+            h2d += up
+            d2h += down
+            it += 1
+        e2e_s = reduce_max(world, time.perf_counter() - t0)
+        e2e = {"value": world * a.e2e_steps * g.cells / e2e_s / 1e6, "unit": UNIT,
+               "h2d_bytes_per_step": h2d // a.e2e_steps, "d2h_bytes_per_step": d2h // a.e2e_steps,
+               "steps": a.e2e_steps, "ms_per_step": e2e_s * 1e3 / a.e2e_steps,
+               "binding": "contiguous pinned arrays (bind_host_array)"}
 
     # the same loop over the reference's own storage: one pageable row of km doubles per (i, j), as
     # lib/Array.cpp allocates it, bound through bind_host_rows (packed on the host into pinned staging)
-    if a.e2e_rows_steps > 0:
+    if e2e is not None and a.e2e_rows_steps > 0:
         keep = {}
         for fid in sorted(set(ins) | set(outs) | {F.P_DYN}):
             base = np.array(pinned[fid].array, copy=True)
@@ -355,7 +357,8 @@ def measure(a, rank, world, g, P, st, pinned, precision):
     kname = KERNEL_NAME.get("mixed_" + tune["stage_variant"], KERNEL_NAME[precision]) if tune else KERNEL_NAME[precision]
     roof = {"kernel": kname, "bound": "hbm", "achieved": achieved,
             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-            "traffic": traffic_per_launch("rk_stage_" + precision), "algorithmic_bytes_per_launch": bytes_per_launch,
+            "traffic": traffic_per_launch("rk_stage_" + precision + ("_" + tune["stage_variant"] if tune else "")),
+            "algorithmic_bytes_per_launch": bytes_per_launch,
             "launches": n_rk, "mean_launch_ms": avg_ms}
     if precision == "fp64":
         roof["note"] = "bound by GB300's FP64 pipe (2 DFMA per SM per cycle), not by HBM"

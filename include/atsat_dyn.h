@@ -387,6 +387,14 @@ int atsat_dyn_buoyancy_ref_level_noalloc(const double* t, const double* p_stat, 
                                          double g, double r_mix, double R_mix, double t_ref,
                                          double* buoy_out, void* stream);
 
+/* Self-test of the library's integer-pipe float <-> double conversions (no reference counterpart): on
+ * `device`, compares them bit for bit with the hardware conversions over every one of the 2^32 binary32
+ * encodings (widening, and narrowing of the widened value) and over n_doubles hashed binary64 encodings
+ * (narrowing; a quarter raw bit patterns, the rest with exponents around binary32's range, a third of
+ * those exact rounding ties and a third one unit either side of a tie). Writes the mismatch counts;
+ * both 0 means the conversions equal the hardware's on everything tested. */
+int atsat_dyn_conv_selftest(int32_t device, uint64_t n_doubles, uint64_t* bad_widen, uint64_t* bad_narrow);
+
 #ifdef __cplusplus
 }
 #endif
