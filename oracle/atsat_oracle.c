@@ -14,7 +14,8 @@
  *   cSaturnModel::RungeKuttaSat             planet/RungeKutta_Sat_Turb.cpp:110-387
  *   cSaturnModel::computeMixtureDensity     planet/Pressure_Sat.cpp:49-62
  *   cSaturnModel::prepareProjectionBoundaries planet/Pressure_Sat.cpp:78-194
- *   PressureSolver<cSaturnModel>::run       planet/PressureSolver.h:145-766 (pointwise sweep)
+ *   PressureSolver<cSaturnModel>::run       planet/PressureSolver.h:145-766 (pointwise sweep, and the
+ *                                           PRESS_LINE / PRESS_BAROTROPIC passes of :300-316, 502-708, 750-755)
  *   cSaturnModel::restoreVar(1.0)           planet/cSaturnModel.cpp:1551-1600
  * Parity of this file with the reference is pinned by tests/test_oracle_golden.py against
  * fixtures produced by the reference itself (oracle/ref_harness.cpp).
@@ -28,6 +29,10 @@
 #include <string.h>
 
 #include "../include/atsat_dyn.h"
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846   /* the value of glibc's <math.h>, which the reference uses */
+#endif
 
 typedef struct {
     int im, jm, km;
@@ -544,6 +549,207 @@ static void prepare_projection_boundaries(M* m, int rigid_lid) {
     }
 }
 
+/* ---------------- PressureSolver.h:300-316, 502-708: the PRESS_LINE and PRESS_BAROTROPIC passes ----------------
+ * Sequential sums in the reference's loop order (its OpenMP reductions agree with these at one thread). */
+static double interior_mean(const M* m, int k_first) {
+    double s = 0.0;
+    long cnt = 0;
+    for (int i = 1; i < m->im - 1; i++)
+        for (int j = 1; j < m->jm - 1; j++)
+            for (int k = k_first; k < m->km - 1; k++) { s += X(m, ATSAT_F_P_DYN, i, j, k); cnt++; }
+    return cnt ? s / cnt : 0.0;
+}
+
+/* PressureSolver.h:502-570: per colour ((j + k) & 1), every (j, k) column relaxed exactly in r by a
+ * Thomas solve with the theta / phi neighbours lagged and both radial ends folded (p0 = c43 p1 - c13 p2).
+ * The columns of one colour read only the other colour's cells except across an odd periodic seam,
+ * where k = 0 and k = km-2 share a colour; rows are solved in increasing k, as one thread of the
+ * reference visits them. */
+static void line_pass(M* m, const double* sinthe_table, const double* line_rhs, int k_first, double inv_dr2,
+                      double inv_dthe2, double inv_dphi2) {
+    const atsat_dyn_params* p = m->p;
+    const int im = m->im, jm = m->jm, km = m->km, per = p->phi_periodic;
+    const double c43 = 4.0 / 3.0, c13 = 1.0 / 3.0;
+    const int P = ATSAT_F_P_DYN;
+    for (int colour = 0; colour < 2; colour++) {
+        #pragma omp parallel
+        {
+            double* aa = (double*)malloc(sizeof(double) * 6 * (size_t)im);
+            double *bb = aa + im, *cc = bb + im, *dd = cc + im, *cp = dd + im, *dp = cp + im;
+            #pragma omp for schedule(static)
+            for (int j = 1; j < jm - 1; j++) {
+                for (int k = k_first; k < km - 1; k++) {
+                    if (((j + k) & 1) != colour) continue;
+                    const int kw = phi_wrap(per, k - 1, km), ke = phi_wrap(per, k + 1, km);
+                    for (int i = 1; i < im - 1; i++) {
+                        const double rm = metric_radius(m, m->rad_z[i]);
+                        const double erm = p->coord_stretching ? 1.0 / (rm + 1.0) : 1.0;
+                        const double num1 = erm * erm * inv_dr2;
+                        const double num2 = inv_dthe2 / (rm * rm);
+                        const double num3 = inv_dphi2 / (rm * rm * sinthe_table[j] * sinthe_table[j]);
+                        const double acc_h = num2 * (X(m, P, i, j + 1, k) + X(m, P, i, j - 1, k))
+                                           + num3 * (X(m, P, i, j, ke) + X(m, P, i, j, kw));
+                        aa[i] = -num1;
+                        bb[i] = 2.0 * (num1 + num2 + num3);
+                        cc[i] = -num1;
+                        dd[i] = acc_h - line_rhs[IDX(m, i, j, k)];
+                    }
+                    const int lo = 1, hi = im - 2;
+                    if (hi > lo) { bb[lo] += aa[lo] * c43; cc[lo] -= aa[lo] * c13; }
+                    else dd[lo] -= aa[lo] * X(m, P, lo - 1, j, k);
+                    if (hi > lo) { bb[hi] += cc[hi] * c43; aa[hi] -= cc[hi] * c13; }
+                    else dd[hi] -= cc[hi] * X(m, P, hi + 1, j, k);
+                    cp[lo] = cc[lo] / bb[lo];
+                    dp[lo] = dd[lo] / bb[lo];
+                    for (int q = lo + 1; q <= hi; q++) {
+                        const double dn = bb[q] - aa[q] * cp[q - 1];
+                        cp[q] = cc[q] / dn;
+                        dp[q] = (dd[q] - aa[q] * dp[q - 1]) / dn;
+                    }
+                    double x = dp[hi];
+                    if (isfinite(x)) X(m, P, hi, j, k) = x;
+                    for (int q = hi - 1; q >= lo; q--) {
+                        x = dp[q] - cp[q] * x;
+                        if (isfinite(x)) X(m, P, q, j, k) = x;
+                    }
+                }
+            }
+            free(aa);
+        }
+    }
+}
+
+/* PressureSolver.h:573-708: the column residual R(j, k) = sum_i (src - Lc(p)) / sum_i 1/rm^2 (the end
+ * rows read as the boundary pass sets them), its real DFT over the N = km-1 meridians, per mode a
+ * tridiagonal in theta (mode 0 made consistent, pinned at j = 1 and shifted to zero sin-weighted mean),
+ * and the correction q(j, k) added to every level of the column. */
+static double col_resid(const M* m, const double* sinthe_table, const double* line_rhs, int j, int k,
+                        double A2, double inv_dr2, double inv_dthe2, double inv_dphi2) {
+    const atsat_dyn_params* p = m->p;
+    const int im = m->im, jm = m->jm, km = m->km;
+    const double c43 = 4.0 / 3.0, c13 = 1.0 / 3.0;
+    const int P = ATSAT_F_P_DYN;
+    const int kw = phi_wrap(1, k - 1, km), ke = phi_wrap(1, k + 1, km);
+    double s = 0.0;
+    for (int i = 1; i < im - 1; i++) {
+        const double rm = metric_radius(m, m->rad_z[i]);
+        const double erm = p->coord_stretching ? 1.0 / (rm + 1.0) : 1.0;
+        const double num1 = erm * erm * inv_dr2;
+        const double num2 = inv_dthe2 / (rm * rm);
+        const double num3 = inv_dphi2 / (rm * rm * sinthe_table[j] * sinthe_table[j]);
+        const double pjp = (j + 1 == jm - 1) ? c43 * X(m, P, i, jm - 2, k) - c13 * X(m, P, i, jm - 3, k) : X(m, P, i, j + 1, k);
+        const double pjm = (j - 1 == 0) ? c43 * X(m, P, i, 1, k) - c13 * X(m, P, i, 2, k) : X(m, P, i, j - 1, k);
+        const double pip = (i + 1 == im - 1) ? c43 * X(m, P, im - 2, j, k) - c13 * X(m, P, im - 3, j, k) : X(m, P, i + 1, j, k);
+        const double pim = (i - 1 == 0) ? c43 * X(m, P, 1, j, k) - c13 * X(m, P, 2, j, k) : X(m, P, i - 1, j, k);
+        const double p0 = X(m, P, i, j, k);
+        const double lc = num1 * (pip + pim - 2.0 * p0)
+                        + num2 * (pjp + pjm - 2.0 * p0)
+                        + num3 * (X(m, P, i, j, ke) + X(m, P, i, j, kw) - 2.0 * p0);
+        s += line_rhs[IDX(m, i, j, k)] - lc;
+    }
+    return s / A2;
+}
+
+static void barotropic_pass(M* m, const double* sinthe_table, const double* line_rhs, double inv_dr2,
+                            double inv_dthe2, double inv_dphi2) {
+    const int im = m->im, jm = m->jm, km = m->km;
+    const double c43 = 4.0 / 3.0, c13 = 1.0 / 3.0;
+    const int N = km - 1, J = jm - 2, NM = N / 2;
+    double A2 = 0.0;
+    for (int i = 1; i < im - 1; i++) { const double rm = metric_radius(m, m->rad_z[i]); A2 += 1.0 / (rm * rm); }
+    double* R = (double*)malloc(sizeof(double) * (size_t)J * N);
+    #pragma omp parallel for schedule(static)
+    for (int j = 1; j < jm - 1; j++)
+        for (int k = 0; k < N; k++)
+            R[(size_t)(j - 1) * N + k] = col_resid(m, sinthe_table, line_rhs, j, k, A2, inv_dr2, inv_dthe2, inv_dphi2);
+    double* ct = (double*)malloc(sizeof(double) * (size_t)(NM + 1) * N);
+    double* stb = (double*)malloc(sizeof(double) * (size_t)(NM + 1) * N);
+    for (int mm = 0; mm <= NM; mm++)
+        for (int k = 0; k < N; k++) {
+            const double a = 2.0 * M_PI * (double)((long)mm * k % N) / N;
+            ct[(size_t)mm * N + k] = cos(a);
+            stb[(size_t)mm * N + k] = sin(a);
+        }
+    double* Ac = (double*)calloc((size_t)(NM + 1) * J, sizeof(double));
+    double* As = (double*)calloc((size_t)(NM + 1) * J, sizeof(double));
+    #pragma omp parallel for collapse(2) schedule(static)
+    for (int mm = 0; mm <= NM; mm++)
+        for (int jj = 0; jj < J; jj++) {
+            double sc = 0.0, ss = 0.0;
+            const double* r_ = &R[(size_t)jj * N];
+            for (int k = 0; k < N; k++) { sc += r_[k] * ct[(size_t)mm * N + k]; ss += r_[k] * stb[(size_t)mm * N + k]; }
+            if (mm > 0) {
+                double ra = 0.0;
+                for (int k = 0; k < N; k++) ra += fabs(r_[k]);
+                const double tol = 1.0e-12 * ra;
+                if (fabs(sc) < tol) sc = 0.0;
+                if (fabs(ss) < tol) ss = 0.0;
+            }
+            Ac[(size_t)mm * J + jj] = sc;
+            As[(size_t)mm * J + jj] = ss;
+        }
+    const double e = inv_dthe2;
+    #pragma omp parallel
+    {
+        double* a = (double*)malloc(sizeof(double) * 5 * (size_t)J);
+        double *b = a + J, *c = b + J, *cp = c + J, *dp = cp + J;
+        #pragma omp for schedule(static)
+        for (int mm = 0; mm <= NM; mm++) {
+            const double sl = sin(M_PI * mm / N);
+            const double lam = 4.0 * sl * sl * inv_dphi2;
+            for (int jj = 0; jj < J; jj++) {
+                const double s_ = sinthe_table[jj + 1];
+                a[jj] = e; c[jj] = e; b[jj] = -2.0 * e - lam / (s_ * s_);
+            }
+            a[0] = 0.0;     b[0] += c43 * e;     c[0] -= c13 * e;
+            c[J - 1] = 0.0; b[J - 1] += c43 * e; a[J - 1] -= c13 * e;
+            for (int part = 0; part < 2; part++) {
+                if (mm == 0 && part == 1) continue;
+                if (2 * mm == N && part == 1) continue;
+                double* d = (part == 0 ? &Ac[(size_t)mm * J] : &As[(size_t)mm * J]);
+                double b0 = b[0], c0 = c[0];
+                if (mm == 0) {
+                    double yr = 0.0, ys = 0.0;
+                    for (int jj = 0; jj < J; jj++) {
+                        const double y = (jj == 0 || jj == J - 1) ? 1.5 : 1.0;
+                        const double s_ = fabs(sin(m->the_z[jj + 1]));
+                        yr += y * d[jj]; ys += y * s_;
+                    }
+                    for (int jj = 0; jj < J; jj++) d[jj] -= yr / ys * fabs(sin(m->the_z[jj + 1]));
+                    b0 = 1.0; c0 = 0.0; d[0] = 0.0;
+                }
+                cp[0] = c0 / b0; dp[0] = d[0] / b0;
+                for (int jj = 1; jj < J; jj++) {
+                    const double dn = b[jj] - a[jj] * cp[jj - 1];
+                    cp[jj] = c[jj] / dn; dp[jj] = (d[jj] - a[jj] * dp[jj - 1]) / dn;
+                }
+                d[J - 1] = dp[J - 1];
+                for (int jj = J - 2; jj >= 0; jj--) d[jj] = dp[jj] - cp[jj] * d[jj + 1];
+                if (mm == 0) {
+                    double sq = 0.0, sw = 0.0;
+                    for (int jj = 0; jj < J; jj++) { const double s_ = fabs(sin(m->the_z[jj + 1])); sq += s_ * d[jj]; sw += s_; }
+                    for (int jj = 0; jj < J; jj++) d[jj] -= sq / sw;
+                }
+            }
+        }
+        free(a);
+    }
+    #pragma omp parallel for schedule(static)
+    for (int jj = 0; jj < J; jj++) {
+        for (int k = 0; k < N; k++) {
+            double q = 0.0;
+            for (int mm = 0; mm <= NM; mm++) {
+                const double w_ = (mm == 0 || 2 * mm == N) ? 1.0 : 2.0;
+                q += w_ * (Ac[(size_t)mm * J + jj] * ct[(size_t)mm * N + k]
+                         + ((mm == 0 || 2 * mm == N) ? 0.0 : As[(size_t)mm * J + jj] * stb[(size_t)mm * N + k]));
+            }
+            q /= N;
+            for (int i = 0; i < im; i++) X(m, ATSAT_F_P_DYN, i, jj + 1, k) += q;
+        }
+    }
+    free(R); free(ct); free(stb); free(Ac); free(As);
+}
+
 /* ---------------- PressureSolver.h:145-766 (pointwise red-black sweeps) ---------------- */
 static void pressure(M* m, atsat_dyn_pstats* st) {
     const atsat_dyn_params* p = m->p;
@@ -573,6 +779,11 @@ static void pressure(M* m, atsat_dyn_pstats* st) {
     const size_t n = (size_t)im * jm * km;
     double* lc_old = NULL;
     const int P = ATSAT_F_P_DYN;
+    /* the variants of PressureSolver.h:300-308: the radial line pass, and the column-mean correction,
+     * which needs the periodic seam and no solid body */
+    const int press_line = p->press_line != 0;
+    const int press_baro = p->press_baro != 0 && per && !press_wall;
+    double* line_rhs = (press_line || press_baro) ? (double*)calloc(n, sizeof(double)) : NULL;
 
     if (press_incr) {
         lc_old = (double*)calloc(n, sizeof(double));
@@ -607,6 +818,7 @@ static void pressure(M* m, atsat_dyn_pstats* st) {
         }
     }
 
+    const double p_mean0 = press_line ? interior_mean(m, k_first) : 0.0;
     double clamped = 0.0, maxupd = 0.0;
     for (int sweep = 0; sweep < n_sweeps; sweep++) {
         double mu = 0.0;
@@ -659,6 +871,7 @@ static void pressure(M* m, atsat_dyn_pstats* st) {
                         else if (div_src > src_max) { div_src = src_max; clamped += 1.0; }
                         else if (div_src < -src_max) { div_src = -src_max; clamped += 1.0; }
                         if (press_incr) div_src += lc_old[IDX(m, i, j, k)];
+                        if (line_rhs) line_rhs[IDX(m, i, j, k)] = div_src;
                         const double old = X(m, P, i, j, k);
                         const double nv = (acc - div_src) / den;
                         X(m, P, i, j, k) = nv;
@@ -669,6 +882,8 @@ static void pressure(M* m, atsat_dyn_pstats* st) {
             }
         }
         maxupd = mu;
+        if (press_line) line_pass(m, sinthe_table, line_rhs, k_first, inv_dr2, inv_dthe2, inv_dphi2);
+        if (press_baro) barotropic_pass(m, sinthe_table, line_rhs, inv_dr2, inv_dthe2, inv_dphi2);
         /* outer boundary of the relaxation, PressureSolver.h:718-746 */
         #pragma omp parallel for collapse(2)
         for (int k = 0; k < km; k++) {
@@ -693,8 +908,15 @@ static void pressure(M* m, atsat_dyn_pstats* st) {
                 X(m, P, i, j, 0) = X(m, P, i, j, km - 1) = (X(m, P, i, j, 0) + X(m, P, i, j, km - 1)) / 2.0;
             }
         }
+        /* PRESS_LINE holds the all-Neumann constant: one shift of every cell (PressureSolver.h:750-755) */
+        if (press_line) {
+            const double shift = interior_mean(m, k_first) - p_mean0;
+            double* pd = m->f[P];
+            for (size_t c = 0; c < n; c++) pd[c] -= shift;
+        }
     }
     if (st) { st->sweeps = n_sweeps; st->src_clamped = clamped; st->max_abs_update = maxupd; }
+    free(line_rhs);
     free(lc_old);
     free(sinthe_table);
 }
@@ -891,7 +1113,7 @@ static void bc_radius(M* m) {
 static int setup(M* m, const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields,
                  const double* vbar0, const double* ubar0, const double* p_baro, double* buoy) {
     if (!g || !p || !fields || g->im < 4 || g->jm < 5 || g->km < 4) return ATSAT_DYN_E_INVALID;
-    if (p->chrom || p->cp_h2_dyn || p->print_diag || p->press_line || p->press_baro) return ATSAT_DYN_E_UNSUPPORTED;
+    if (p->chrom || p->cp_h2_dyn || p->print_diag) return ATSAT_DYN_E_UNSUPPORTED;
     memset(m, 0, sizeof(*m));
     m->im = g->im; m->jm = g->jm; m->km = g->km;
     m->rad_z = g->rad_z; m->the_z = g->the_z;

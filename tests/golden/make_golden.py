@@ -33,7 +33,20 @@ CASES = {
     "density_s1": ("density", 1, 1, True, {}),
     "steps4_s2": ("steps", 4, 2, True, {}),
     "rk_plain_s0": ("rk", 1, 0, False, {}),
+    # the pressure variants of PressureSolver.h:300-308, 502-708 (knobs set in the reference's environment)
+    "pressure_line_s1": ("pressure", 1, 1, True, {"press_line": 1}),
+    "pressure_baro_s1": ("pressure", 1, 1, True, {"press_baro": 1}),
+    "pressure_lb3_s1": ("pressure", 1, 1, True, {"press_line": 1, "press_baro": 1, "press_sweeps": 3}),
+    "steps4_lb_s2": ("steps", 4, 2, True, {"press_line": 1, "press_baro": 1}),
 }
+
+# the reference reads these knobs from its environment (PressureSolver.h:174-175, 300-303)
+KNOB_ENV = {"press_line": "ATSAT_PRESS_LINE", "press_baro": "ATSAT_PRESS_BAROTROPIC",
+            "press_sweeps": "ATSAT_PRESS_SWEEPS"}
+
+
+def reference_env(over):
+    return {KNOB_ENV[k]: str(v) for k, v in over.items()}
 
 OUTPUTS = {
     "rhs": F.RHS_FIELDS + F.AUX_FIELDS + [F.P_METRIC],
@@ -61,13 +74,16 @@ def input_sums(st):
     return np.array([float(np.sum(st.arrays[f])) for f in range(F.NFIELDS)])
 
 
-def main():
+def main(names=None):
     from oracle import refrun
     if not refrun.available():
         sys.exit("the reference harness is not built: python oracle/build_ref.py")
     for name, (op, nsteps, seed, exercise, over) in CASES.items():
+        if names and name not in names:
+            continue
         g, P, st = make_state(name)
-        out = refrun.run(st, op, nsteps=nsteps)
+        # one thread: the interior-mean reduction of PRESS_LINE then sums in loop order, as the oracle does
+        out = refrun.run(st, op, nsteps=nsteps, env=reference_env(over), threads=1 if over else None)
         idx = sample_index(name, g.cells)
         rec = {"input_sums": input_sums(st), "index": idx}
         for fid in OUTPUTS[op]:
@@ -82,4 +98,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

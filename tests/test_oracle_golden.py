@@ -59,3 +59,23 @@ def test_oracle_matches_reference_bitwise():
     oracle.rk4_step(s, P)
     for fid in range(F.NFIELDS):
         assert np.array_equal(s.arrays[fid], ref[fid]), F.NAMES[fid]
+
+
+@pytest.mark.parametrize("name", ["pressure_line_s1", "pressure_baro_s1", "pressure_lb3_s1"])
+def test_oracle_pressure_variants_match_reference_bitwise(name):
+    """PRESS_LINE / PRESS_BAROTROPIC: the restatement against the reference run here, bit for bit
+    (one reference thread: its interior-mean reduction then sums in the oracle's loop order)."""
+    from oracle import refrun
+    from golden.make_golden import reference_env
+    if not refrun.available():
+        pytest.skip("reference harness not built here")
+    import platform
+    if platform.machine() not in ("x86_64", "AMD64"):
+        pytest.skip("bitwise equality is established on x86-64 (no FMA contraction at -O2)")
+    op, nsteps, seed, exercise, over = CASES[name]
+    g, P, st = make_state(name)
+    ref = refrun.run(st, op, env=reference_env(over), threads=1)
+    s = st.copy()
+    oracle.pressure(s, P)
+    for fid in range(F.NFIELDS):
+        assert np.array_equal(s.arrays[fid], ref[fid]), F.NAMES[fid]
