@@ -44,6 +44,11 @@ struct atsat_dyn {
     double* stage[NPROG] = {};
     double* acc[NPROG] = {};
     double* src = nullptr;
+    // PRESS_LINE / PRESS_BAROTROPIC: forward-sweep scratch of the line pass, interior-mean partials and
+    // the means on entry and after a sweep, the barotropic tables and scratch (one allocation)
+    double* pv_buf = nullptr;
+    double *line_cp = nullptr, *line_dp = nullptr, *imean_partial = nullptr, *pmean = nullptr;
+    BaroTables baro{};
     double* p_baro = nullptr;            // null unless set
     double* partial = nullptr;
     double* buoy = nullptr;
@@ -203,8 +208,6 @@ int check_supported(atsat_dyn* h, const atsat_dyn_params& p) {
         {p.hydro_buoy != 0, "ATSAT_HYDRO_BUOY"},
         {p.t_limiter != 0, "ATSAT_T_LIMITER (reads tn at k-1 = -1 on the periodic seam in the reference)"},
         {p.press_wall != 0, "ATSAT_PRESS_WALL (no solid body exists in ATSAT)"},
-        {p.press_line != 0, "ATSAT_PRESS_LINE"},
-        {p.press_baro != 0, "ATSAT_PRESS_BAROTROPIC"},
         {p.precision != ATSAT_DYN_FP64 && p.precision != ATSAT_DYN_MIXED, "unknown precision"},
     };
     for (auto& r : rules)
@@ -1014,15 +1017,43 @@ int enqueue_pressure(atsat_dyn* h, int sweeps) {
                                   h->f[ATSAT_F_RHS_W], h->f[ATSAT_F_P_DYN], h->src, h->counter, h->stream));
         h->launches += 1;
     }
+    const bool line = h->p.press_line != 0, baro = h->p.press_baro != 0;
+    double* pd = h->f[ATSAT_F_P_DYN];
+    if (line) {                 // the interior mean on entry, held after every sweep
+        Timed t(h, ATSAT_K_PRESS_BOUNDARY);
+        int n = 0;
+        CK(h, launch_interior_mean(K, pd, h->imean_partial, h->pmean, h->stream, &n));
+        h->launches += n;
+    }
     for (int s = 0; s < sweeps; s++) {
         for (int colour = 0; colour < 2; colour++) {
             Timed t(h, ATSAT_K_PRESS_SWEEP);
-            CK(h, launch_press_sweep(K, h->geo, h->src, h->f[ATSAT_F_P_DYN], colour, h->stream));
+            CK(h, launch_press_sweep(K, h->geo, h->src, pd, colour, h->stream));
             h->launches += ((K.km - 1) & 1) ? 2 : 1;     // odd km-1: the seam cells follow their partner
         }
+        if (line) {
+            for (int colour = 0; colour < 2; colour++) {
+                Timed t(h, ATSAT_K_PRESS_SWEEP);
+                int n = 0;
+                CK(h, launch_line_pass(K, h->geo, h->src, pd, h->line_cp, h->line_dp, colour, h->stream, &n));
+                h->launches += n;
+            }
+        }
+        if (baro) {
+            Timed t(h, ATSAT_K_PRESS_SWEEP);
+            int n = 0;
+            CK(h, launch_barotropic(K, h->geo, h->src, pd, h->baro, h->stream, &n));
+            h->launches += n;
+        }
         Timed t(h, ATSAT_K_PRESS_BOUNDARY);
-        CK(h, launch_press_boundary(K, h->f[ATSAT_F_P_DYN], h->stream));
+        CK(h, launch_press_boundary(K, pd, h->stream));
         h->launches += 1;
+        if (line) {
+            int n = 0;
+            CK(h, launch_interior_mean(K, pd, h->imean_partial, h->pmean + 1, h->stream, &n));
+            CK(h, launch_mean_shift(K, pd, h->pmean, h->stream));
+            h->launches += n + 1;
+        }
     }
     return ATSAT_DYN_OK;
 }
@@ -1189,6 +1220,77 @@ int atsat_dyn_params_from_env(atsat_dyn_params* p) {
     return ATSAT_DYN_OK;
 }
 
+// Device tables of the pressure variants, built with the reference's own expressions
+// (PressureSolver.h:150-162, 310-316, 578-580, 613-616, 640-644).
+int setup_press_variants(atsat_dyn* h) {
+    const KConst& K = h->kc;
+    const atsat_dyn_params& p = h->p;
+    const bool line = p.press_line != 0, baro = p.press_baro != 0;
+    if (!line && !baro) return ATSAT_DYN_OK;
+    constexpr double PI = 3.14159265358979323846;
+    const int N = K.km - 1, J = K.jm - 2, NM = N / 2;
+    const int64_t n_line = line ? 2 * K.fsz : 0;
+    const int64_t n_mean = line ? interior_mean_partials(K) + 2 : 0;
+    const int64_t n_tab = baro ? 2LL * (NM + 1) * N + (NM + 1) + K.jm + J : 0;
+    const int64_t n_scr = baro ? (int64_t)J * N + J + 4LL * (NM + 1) * J : 0;
+    const int64_t total = n_line + n_mean + n_tab + n_scr + 64;
+    cudaError_t e = cudaMalloc(&h->pv_buf, (size_t)total * 8);
+    if (e != cudaSuccess) { h->pv_buf = nullptr; return fail(h, ATSAT_DYN_E_NOMEM, "pressure variants: %s", cudaGetErrorString(e)); }
+    double* q = h->pv_buf;
+    if (line) {
+        h->line_cp = q; q += K.fsz;
+        h->line_dp = q; q += K.fsz;
+        h->pmean = q; q += 2;
+        h->imean_partial = q; q += interior_mean_partials(K);
+    }
+    if (baro) {
+        std::vector<double> tab((size_t)n_tab);
+        double* ct = tab.data();
+        double* st = ct + (size_t)(NM + 1) * N;
+        double* lam = st + (size_t)(NM + 1) * N;
+        double* sinthe = lam + (NM + 1);
+        double* abs_sin = sinthe + K.jm;
+        for (int mm = 0; mm <= NM; mm++) {
+            for (int k = 0; k < N; k++) {
+                const double a = 2.0 * PI * (double)((long)mm * k % N) / N;
+                ct[(size_t)mm * N + k] = std::cos(a);
+                st[(size_t)mm * N + k] = std::sin(a);
+            }
+            const double sl = std::sin(PI * mm / N);
+            lam[mm] = 4.0 * sl * sl * K.inv_dphi2;
+        }
+        for (int j = 0; j < K.jm; j++) {
+            double sv = std::sin(h->the_z[j]);
+            if (sv < p.sinthe_min) sv = p.sinthe_min;
+            if (sv == 0.0) sv = 1.0e-5;
+            sinthe[j] = sv;
+        }
+        for (int jj = 0; jj < J; jj++) abs_sin[jj] = std::fabs(std::sin(h->the_z[jj + 1]));
+        double A2 = 0.0;
+        for (int i = 1; i < K.im - 1; i++) {
+            const double rm = metric_radius(p, h->rad_z[i]);
+            A2 += 1.0 / (rm * rm);
+        }
+        double* dtab = q; q += n_tab;
+        e = cudaMemcpy(dtab, tab.data(), (size_t)n_tab * 8, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail(h, ATSAT_DYN_E_CUDA, "pressure variant tables: %s", cudaGetErrorString(e));
+        BaroTables& T = h->baro;
+        T.A2 = A2;
+        T.ct = dtab;
+        T.st = dtab + (size_t)(NM + 1) * N;
+        T.lam = T.st + (size_t)(NM + 1) * N;
+        T.sinthe = T.lam + (NM + 1);
+        T.abs_sin = T.sinthe + K.jm;
+        T.R = q; q += (int64_t)J * N;
+        T.ra = q; q += J;
+        T.Ac = q; q += (int64_t)(NM + 1) * J;
+        T.As = q; q += (int64_t)(NM + 1) * J;
+        T.cp = q; q += (int64_t)(NM + 1) * J;
+        T.dp = q; q += (int64_t)(NM + 1) * J;
+    }
+    return ATSAT_DYN_OK;
+}
+
 int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_dyn_t* out) {
     if (!g || !p || !out || !g->rad_z || !g->the_z) return ATSAT_DYN_E_INVALID;
     *out = nullptr;
@@ -1291,7 +1393,7 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
         (e = cudaStreamSynchronize(h->stream)))
         return cuda_fail(e, "table upload");
     *out = h;
-    return ATSAT_DYN_OK;
+    return setup_press_variants(h);
 }
 
 void atsat_dyn_destroy(atsat_dyn_t h) {
@@ -1301,6 +1403,7 @@ void atsat_dyn_destroy(atsat_dyn_t h) {
     for (auto e : h->pool) cudaEventDestroy(e);
     for (auto e : h->timer) if (e) cudaEventDestroy(e);
     poisson_destroy(h->poisson);
+    if (h->pv_buf) cudaFree(h->pv_buf);
     if (h->graph) cudaGraphExecDestroy(h->graph);
     if (h->slab) cudaFree(h->slab);
     if (h->slab32) cudaFree(h->slab32);

@@ -344,6 +344,22 @@ cudaError_t launch_press_source(const KConst& kc, const ColGeo* geo, const doubl
 cudaError_t launch_press_sweep(const KConst& kc, const ColGeo* geo, const double* src, double* p, int colour,
                                cudaStream_t s);
 cudaError_t launch_press_boundary(const KConst& kc, double* p, cudaStream_t s);
+
+// PRESS_LINE / PRESS_BAROTROPIC (press_variants.cu)
+struct BaroTables {
+    double A2;                                    // sum over i = 1..im-2 of 1 / rm^2
+    const double *ct, *st;                        // (N/2 + 1) x N: cos, sin(2 pi (m k mod N) / N)
+    const double *lam, *sinthe, *abs_sin;         // per mode; the solver's sine table (jm); |sin(theta_j+1)|
+    double *R, *ra, *Ac, *As, *cp, *dp;           // scratch
+};
+cudaError_t launch_line_pass(const KConst& kc, const ColGeo* geo, const double* src, double* p, double* cpb,
+                             double* dpb, int colour, cudaStream_t s, int* launches);
+cudaError_t launch_interior_mean(const KConst& kc, const double* p, double* partial, double* out, cudaStream_t s,
+                                 int* launches);
+int interior_mean_partials(const KConst& kc);
+cudaError_t launch_mean_shift(const KConst& kc, double* p, const double* mean, cudaStream_t s);
+cudaError_t launch_barotropic(const KConst& kc, const ColGeo* geo, const double* src, double* p, const BaroTables& T,
+                              cudaStream_t s, int* launches);
 cudaError_t launch_copy_fields(const KConst& kc, double* const* dst, const double* const* src, int n,
                                cudaStream_t s);
 // s32 (may be null): FP32 copies to keep in step, indexed by field id; wlo: the second FP32 word of w.

@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--poisson", action="store_true",
                     help="the standalone pressure-equation solves instead of the dycore iteration")
     ap.add_argument("--sor-sweeps", type=int, default=4000)
+    ap.add_argument("--press-variants", action="store_true",
+                    help="time one pressure call with and without PRESS_LINE / PRESS_BAROTROPIC")
     ap.add_argument("--ensemble", action="store_true",
                     help="the 32-member mixed-size ensemble: concurrent graph replays vs one after another")
     ap.add_argument("--precision", default="mixed,fp64",
@@ -435,6 +437,48 @@ def run_poisson(a, rank, world):
             "methods": out}
 
 
+def run_press_variants(a, rank, world):
+    """One pressure call (PressureSolver<cSaturnModel>::run with prepareProjectionBoundaries) at the
+    workload grid in its four forms: the default pointwise red-black sweep, + PRESS_LINE (a radial
+    Thomas solve per column, held interior mean), + PRESS_BAROTROPIC (DFT in phi and a theta tridiagonal
+    per mode), and both. FP64 on the device (CUDA events around K calls after W warm-up calls) beside the
+    oracle's FP64 OpenMP restatement of the same call on the host cores (one call)."""
+    if rank != 0:
+        return None
+    from atsat_gb300 import abi, dyn, fields as F, synth
+    from oracle import oracle
+    g = synth.make_grid(*a.shape)
+    out = {}
+    for name, over in (("default", {}), ("line", {"press_line": 1}), ("barotropic", {"press_baro": 1}),
+                       ("line+barotropic", {"press_line": 1, "press_baro": 1})):
+        P = abi.default_params(**over)
+        st = synth.saturn_state(g, P, seed=11, exercise=True)
+        t0 = time.perf_counter()
+        oracle.pressure(st.copy(), P)
+        cpu_s = time.perf_counter() - t0
+        with dyn.Dycore(g, P) as d:
+            d.load_state(st)
+            for _ in range(a.warmup):
+                d.PressureSolver_run()
+            d.profile(True)
+            d.profile_reset()
+            d.timer_start()
+            for _ in range(a.steps):
+                d.PressureSolver_run()
+            ms = d.timer_stop() / a.steps
+            kern = {abi.K_NAMES[c]: d.profile_read(c)[1] / a.steps for c in range(len(abi.K_NAMES))
+                    if d.profile_read(c)[0] > 0}
+            d.profile(False)
+        out[name] = {"ms_per_call": ms, "kernel_ms_per_call": kern, "cpu_oracle_s_per_call": cpu_s,
+                     "cpu_cores": os.cpu_count()}
+    return {"metric": "pressure call (PressureSolver::run) device time, 1 GB300, FP64, per variant",
+            "value": out["line+barotropic"]["ms_per_call"], "unit": "ms per call (PRESS_LINE + PRESS_BAROTROPIC)",
+            "higher_is_better": False, "n_gpus": 1, "data": "synthetic", "steps": a.steps, "warmup": a.warmup,
+            "config": {"workload": f"pressure call on {g.im}x{g.jm}x{g.km}, interior {g.interior_p} cells, "
+                                   "seeded synthetic state with stale tendencies (exercise)"},
+            "variants": out}
+
+
 def run_ensemble(a, rank, world):
     """32 independent members, 16 at 21x91x181, 12 at 41x181x361 and 4 at 61x271x541, each from the seeded
     generator with its own seed and noise amplitude U[0.5, 2], mixed precision, stage kernels autotuned per
@@ -496,6 +540,8 @@ def main():
         res = run_ensemble(a, rank, world)
     elif a.poisson:
         res = run_poisson(a, rank, world)
+    elif a.press_variants:
+        res = run_press_variants(a, rank, world)
     else:
         res = run_reference(a, rank, world) if a.impl == "reference" else run_ours(a, rank, world)
     if rank == 0 and res is not None:

@@ -117,6 +117,37 @@ def test_pressure_knob_variants(over):
     compare(got.arrays, ref.arrays, ALL, TOL_FP64, f"pressure {over}")
 
 
+LINE_BARO = [dict(press_line=1), dict(press_baro=1), dict(press_line=1, press_baro=1),
+             dict(press_line=1, press_baro=1, press_sweeps=3)]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("over", LINE_BARO, ids=lambda d: ",".join(f"{k}={v}" for k, v in d.items()))
+def test_pressure_line_barotropic(shape, over):
+    """PRESS_LINE (radial Thomas per column, held interior mean) and PRESS_BAROTROPIC (DFT in phi +
+    tridiagonal in theta per mode) against the oracle, which equals the reference bit for bit; the odd
+    km-1 grids exercise the seam column solved after its partner."""
+    g, P, st = case(shape, seed=21, **over)
+    got, _ = run_gpu("pressure", g, P, st)
+    ref, _ = run_oracle("pressure", P, st)
+    compare(got.arrays, ref.arrays, ALL, TOL_FP64, f"pressure {over} {shape}")
+
+
+def test_pressure_line_holds_interior_mean():
+    """After a PRESS_LINE call the interior mean of p_dyn equals its value on entry (the all-Neumann
+    constant, PressureSolver.h:750-755), whatever the source."""
+    from atsat_gb300 import dyn
+    g, P, st = case((12, 40, 70), seed=23, press_line=1, press_sweeps=2)
+    p0 = st.arrays[F.P_DYN][1:-1, 1:-1, : g.km - 1].mean()
+    s = st.copy()
+    with dyn.Dycore(g, P) as d:
+        d.load_state(s)
+        d.PressureSolver_run()
+        d.download([F.P_DYN])
+    p1 = s.arrays[F.P_DYN][1:-1, 1:-1, : g.km - 1].mean()
+    assert abs(p1 - p0) <= 1e-12 * max(1.0, float(np.max(np.abs(s.arrays[F.P_DYN]))))
+
+
 def test_pressure_clamp_count():
     from atsat_gb300 import dyn
     g, P, st = case((9, 13, 17), seed=9, pdyn_cap=1e-9)

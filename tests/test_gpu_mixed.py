@@ -75,6 +75,19 @@ def test_mixed_ten_iterations(shape, exercise, variant):
     assert not bad, bad
 
 
+@pytest.mark.parametrize("shape", [(21, 91, 181), (12, 40, 70)])
+def test_mixed_ten_iterations_line_barotropic(shape):
+    """The mixed path with the PRESS_LINE and PRESS_BAROTROPIC pressure passes (FP64 in both paths)."""
+    over = dict(press_line=1, press_baro=1)
+    g, P, st = case(shape, seed=43, exercise=True, **over)
+    ref = st.copy()
+    oracle.steps(ref, P, 10)
+    got = run_mixed(g, P, st, 10, TILED2)
+    rep = drift(got.arrays, ref.arrays, F.PROG + [F.P_DYN])
+    bad = {F.NAMES[f]: rep[F.NAMES[f]][0] for f in CRITERION if not rep[F.NAMES[f]][0] <= TOL_MIXED}
+    assert not bad, bad
+
+
 @pytest.mark.parametrize("variant", VARIANTS)
 def test_mixed_one_step_all_fields(variant):
     """One RK4 step: every prognostic field within 1e-6, rhs_u/v/w and aux within 1e-5 of their max."""
