@@ -47,6 +47,9 @@ struct atsat_dyn {
     // PRESS_LINE / PRESS_BAROTROPIC: forward-sweep scratch of the line pass, interior-mean partials and
     // the means on entry and after a sweep, the barotropic tables and scratch (one allocation)
     double* pv_buf = nullptr;
+    // clampNegativeSpecies' budget: added[11], added_bnd[11] (doubles), cells[11], cells_bnd[11] (counts)
+    double* clamp_added = nullptr;
+    unsigned long long* clamp_cells = nullptr;
     double *line_cp = nullptr, *line_dp = nullptr, *imean_partial = nullptr, *pmean = nullptr;
     BaroTables baro{};
     double* p_baro = nullptr;            // null unless set
@@ -1121,6 +1124,58 @@ int enqueue_bc(atsat_dyn* h, bool resident = false) {
     return ATSAT_DYN_OK;
 }
 
+// AtomUtils::damp_wiggles (lib/Utils.cpp:229-322) on a device field, the pressure source as the copy
+int enqueue_damp(atsat_dyn* h, int fid, bool ai, bool aj, bool ak, double strength, int passes) {
+    Timed t(h, ATSAT_K_GLUE);
+    const KConst& K = h->kc;
+    const size_t bytes = (size_t)K.fsz * 8;
+    const double coeff = strength * 0.25;
+    const int seam = (h->p.phi_periodic && K.km > 2) ? 1 : 0;
+    double* f = h->f[fid];
+    for (int pass = 0; pass < passes; pass++) {
+        const bool axes[3] = {ak, aj, ai};
+        for (int a = 0; a < 3; a++) {
+            if (!axes[a]) continue;
+            CK(h, cudaMemcpyAsync(h->src, f, bytes, cudaMemcpyDeviceToDevice, h->stream));
+            CK(h, launch_damp_axis(K, h->src, f, coeff, a, seam, h->stream));
+            h->launches += 1;
+        }
+    }
+    mark_dirty(h, fid);
+    return ATSAT_DYN_OK;
+}
+
+// the p_dyn filter of cSaturnModel::Run after the pressure call (cSaturnModel.cpp:894-897)
+int enqueue_damp_pdyn(atsat_dyn* h) {
+    switch (h->p.damp_pdyn) {
+        case 1: return enqueue_damp(h, ATSAT_F_P_DYN, true, true, true, 1.0, 1);
+        case 2: return enqueue_damp(h, ATSAT_F_P_DYN, true, false, false, 1.0, 1);
+        case 3: return enqueue_damp(h, ATSAT_F_P_DYN, true, false, true, 1.0, 1);
+        default: return ATSAT_DYN_OK;
+    }
+}
+
+const int CLAMP_SPECIES[11] = {ATSAT_F_H2O, ATSAT_F_H2O_CLOUD, ATSAT_F_H2O_ICE, ATSAT_F_H2S, ATSAT_F_NH3,
+                               ATSAT_F_NH3_CLOUD, ATSAT_F_NH3_ICE, ATSAT_F_CH4, ATSAT_F_CH4_CLOUD,
+                               ATSAT_F_CH4_ICE, ATSAT_F_NH4SH};
+
+// cSaturnModel::clampNegativeSpecies (FileIO_Sat.cpp:716-772); resident mixed runs also floor the FP32
+// copies of y_{n+1} that the next step starts from
+int enqueue_clamp(atsat_dyn* h, bool resident = false) {
+    if (!h->p.clamp_species) return ATSAT_DYN_OK;
+    Timed t(h, ATSAT_K_GLUE);
+    double* f[11];
+    float* s32[11];
+    const bool shadows = resident && h->p.precision == ATSAT_DYN_MIXED;
+    for (int q = 0; q < 11; q++) {
+        f[q] = h->f[CLAMP_SPECIES[q]];
+        s32[q] = shadows ? h->yo32[CLAMP_SPECIES[q]] : nullptr;
+    }
+    CK(h, launch_clamp_species(h->kc, f, shadows ? s32 : nullptr, h->clamp_added, h->clamp_cells, h->stream));
+    h->launches += 1;
+    return ATSAT_DYN_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1151,6 +1206,7 @@ int atsat_dyn_params_default(atsat_dyn_params* p) {
     p->press_line = 0; p->press_baro = 0; p->precision = ATSAT_DYN_FP64;
     p->bc_radius_form = 2; p->bc_bottom_form = 3; p->bc_pole_form = 1; p->bc_pole_fill = 1; p->bc_lid_u = 1;
     p->bc_top_taper = 2; p->bc_species_lid_copy = 1; p->bc_species_wall_copy = 2; p->local_rho = 1;
+    p->damp_pdyn = 3; p->clamp_species = 1; p->driver_glue = 0;
     return ATSAT_DYN_OK;
 }
 
@@ -1216,6 +1272,9 @@ int atsat_dyn_params_from_env(atsat_dyn_params* p) {
     p->bc_species_lid_copy = env_i("ATSAT_BC_SPECIES_LID_COPY", 1);
     p->bc_species_wall_copy = env_i("ATSAT_BC_SPECIES_WALL_COPY", 2);
     p->local_rho = envs("ATSAT_LOCAL_RHO") ? (env_i("ATSAT_LOCAL_RHO", 1) != 0) : 1;
+    // the driver's glue (cSaturnModel.cpp:894; FileIO_Sat.cpp:717)
+    p->damp_pdyn = envs("ATSAT_DAMP_PDYN") ? env_i("ATSAT_DAMP_PDYN", 0) : (geo ? 3 : 1);
+    p->clamp_species = env_i("ATSAT_NO_CLAMP", 0) ? 0 : 1;
     if (env_i("ATSAT_BC_SEAM_DAMP", 0) != 0 || env_i("ATSAT_BC_T_LID_PIN", 0) != 0) return ATSAT_DYN_E_UNSUPPORTED;
     return ATSAT_DYN_OK;
 }
@@ -1392,6 +1451,9 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
                              h->stream)) ||
         (e = cudaStreamSynchronize(h->stream)))
         return cuda_fail(e, "table upload");
+    if ((e = cudaMalloc(&h->clamp_added, 22 * 8 + 22 * 8)) != cudaSuccess) return cuda_fail(e, "cudaMalloc (budget)");
+    h->clamp_cells = reinterpret_cast<unsigned long long*>(h->clamp_added + 22);
+    if ((e = cudaMemset(h->clamp_added, 0, 44 * 8)) != cudaSuccess) return cuda_fail(e, "cudaMemset (budget)");
     *out = h;
     return setup_press_variants(h);
 }
@@ -1404,6 +1466,7 @@ void atsat_dyn_destroy(atsat_dyn_t h) {
     for (auto e : h->timer) if (e) cudaEventDestroy(e);
     poisson_destroy(h->poisson);
     if (h->pv_buf) cudaFree(h->pv_buf);
+    if (h->clamp_added) cudaFree(h->clamp_added);
     if (h->graph) cudaGraphExecDestroy(h->graph);
     if (h->slab) cudaFree(h->slab);
     if (h->slab32) cudaFree(h->slab32);
@@ -1614,6 +1677,45 @@ int atsat_dyn_boundary_conditions(atsat_dyn_t h) {
     return rc ? rc : finish(h);
 }
 
+int atsat_dyn_damp_wiggles(atsat_dyn_t h, int32_t field, int32_t along_i, int32_t along_j, int32_t along_k,
+                           double strength, int32_t passes) {
+    ENTRY(h);
+    if (!valid_field(field) || passes < 0) return fail(h, ATSAT_DYN_E_INVALID, "damp_wiggles: bad field or passes");
+    { int rc0 = unalias(h); if (rc0) return rc0; }
+    int rc = enqueue_damp(h, field, along_i != 0, along_j != 0, along_k != 0, strength, passes);
+    return rc ? rc : finish(h);
+}
+
+int atsat_dyn_damp_pdyn(atsat_dyn_t h) {
+    ENTRY(h);
+    int rc = enqueue_damp_pdyn(h);
+    return rc ? rc : finish(h);
+}
+
+int atsat_dyn_clamp_negative_species(atsat_dyn_t h) {
+    ENTRY(h);
+    { int rc0 = unalias(h); if (rc0) return rc0; }
+    int rc = enqueue_clamp(h);
+    return rc ? rc : finish(h);
+}
+
+int atsat_dyn_clamp_budget(atsat_dyn_t h, double* added, int64_t* cells, double* added_bnd, int64_t* cells_bnd) {
+    ENTRY(h);
+    if (!added || !cells || !added_bnd || !cells_bnd) return fail(h, ATSAT_DYN_E_INVALID, "clamp_budget: null output");
+    double a[22];
+    unsigned long long c[22];
+    CK(h, cudaStreamSynchronize(h->stream));
+    CK(h, cudaMemcpy(a, h->clamp_added, sizeof(a), cudaMemcpyDeviceToHost));
+    CK(h, cudaMemcpy(c, h->clamp_cells, sizeof(c), cudaMemcpyDeviceToHost));
+    for (int q = 0; q < 11; q++) {
+        added[q] = a[q];
+        added_bnd[q] = a[11 + q];
+        cells[q] = (int64_t)c[q];
+        cells_bnd[q] = (int64_t)c[11 + q];
+    }
+    return ATSAT_DYN_OK;
+}
+
 }  // extern "C"
 
 namespace {
@@ -1630,9 +1732,11 @@ int enqueue_iteration(atsat_dyn* h, int32_t it) {
             mark_dirty(h, ATSAT_F_RHO_MIX);
         }
         if ((rc = enqueue_pressure(h, h->p.press_sweeps > 0 ? h->p.press_sweeps : 1))) return rc;
+        if (h->p.driver_glue && (rc = enqueue_damp_pdyn(h))) return rc;
     }
     if ((rc = enqueue_rk4(h, true))) return rc;
     if ((rc = enqueue_bc(h, true))) return rc;
+    if (h->p.driver_glue && (rc = enqueue_clamp(h, true))) return rc;
     return enqueue_restore(h, true);
 }
 

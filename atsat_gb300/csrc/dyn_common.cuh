@@ -345,6 +345,12 @@ cudaError_t launch_press_sweep(const KConst& kc, const ColGeo* geo, const double
                                cudaStream_t s);
 cudaError_t launch_press_boundary(const KConst& kc, double* p, cudaStream_t s);
 
+// the driver's glue (glue.cu): one axis of AtomUtils::damp_wiggles; cSaturnModel::clampNegativeSpecies
+cudaError_t launch_damp_axis(const KConst& kc, const double* tmp, double* f, double coeff, int axis, int seam,
+                             cudaStream_t s);
+cudaError_t launch_clamp_species(const KConst& kc, double* const f[11], float* const s32[11], double* added,
+                                 unsigned long long* cells, cudaStream_t s);
+
 // PRESS_LINE / PRESS_BAROTROPIC (press_variants.cu)
 struct BaroTables {
     double A2;                                    // sum over i = 1..im-2 of 1 / rm^2

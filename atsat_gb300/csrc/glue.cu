@@ -174,7 +174,103 @@ __global__ void repitch_kernel(double* __restrict__ dst, int dst_pitch, const do
     dst[r * dst_pitch + k] = src[r * src_pitch + k];
 }
 
+// ---- AtomUtils::damp_wiggles (lib/Utils.cpp:229-322), no surface mask: one axis of the 1-2-1 filter,
+// f = t + coeff (t[-1] - 2 t + t[+1]) with t the field's copy. axis 0: k, periodic over the km-1 distinct
+// meridians with k = km-1 their copy (seam), else over all km; axis 1: j, clamped at the poles; axis 2: i,
+// clamped at the walls.
+__global__ void __launch_bounds__(256) damp_axis_kernel(const KConst K, const double* __restrict__ t,
+                                                        double* __restrict__ f, double coeff, int axis, int seam) {
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= K.km || j >= K.jm) return;
+    const int64_t row = ((int64_t)i * K.jm + j) * K.kp;
+    const int64_t c = row + k;
+    const double t0 = t[c];
+    double a, b;
+    if (axis == 0) {
+        if (seam) {
+            if (k == K.km - 1) return;                      // the copy, written with k = 0
+            a = t[row + ((k == 0) ? K.km - 2 : k - 1)];
+            b = t[row + ((k == K.km - 2) ? 0 : k + 1)];
+        } else {
+            a = t[row + (k - 1 + K.km) % K.km];
+            b = t[row + (k + 1) % K.km];
+        }
+    } else if (axis == 1) {
+        a = t[c + (int64_t)((j > 0 ? j - 1 : 0) - j) * K.kp];
+        b = t[c + (int64_t)((j < K.jm - 1 ? j + 1 : K.jm - 1) - j) * K.kp];
+    } else {
+        a = t[c + (int64_t)((i > 0 ? i - 1 : 0) - i) * K.plane];
+        b = t[c + (int64_t)((i < K.im - 1 ? i + 1 : K.im - 1) - i) * K.plane];
+    }
+    const double v = t0 + coeff * (a - 2.0 * t0 + b);
+    f[c] = v;
+    if (axis == 0 && seam && k == 0) f[row + K.km - 1] = v;
+}
+
+// ---- cSaturnModel::clampNegativeSpecies (FileIO_Sat.cpp:716-772) ----
+// blockIdx.z = species * im + i. !(v >= 0) (NaN included) becomes 0 in the FP64 field and, when given,
+// its FP32 copy; the finite amounts clipped and the cells are summed per warp and added to the budget:
+// added[11], added_bnd[11] (doubles), then cells[11], cells_bnd[11] (64-bit counts).
+struct ClampArgs {
+    double* f[11];
+    float* s32[11];
+    double* added;
+    unsigned long long* cells;
+};
+
+__global__ void __launch_bounds__(256) clamp_species_kernel(const KConst K, const ClampArgs A) {
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int q = blockIdx.z / K.im, i = blockIdx.z % K.im;
+    double add = 0.0;
+    unsigned cnt = 0;
+    if (k < K.km && j < K.jm) {
+        const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
+        const double v = A.f[q][c];
+        if (!(v >= 0.0)) {
+            if (isfinite(v)) { add = -v; cnt = 1; }
+            A.f[q][c] = 0.0;
+            if (A.s32[q]) A.s32[q][c] = 0.0f;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        add += __shfl_down_sync(0xffffffffu, add, o);
+        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    }
+    if ((threadIdx.x & 31) == 0 && cnt) {
+        const bool bnd = (i == 0 || i == K.im - 1);
+        atomicAdd(A.added + q, add);
+        atomicAdd(A.cells + q, (unsigned long long)cnt);
+        if (bnd) {
+            atomicAdd(A.added + 11 + q, add);
+            atomicAdd(A.cells + 11 + q, (unsigned long long)cnt);
+        }
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_damp_axis(const KConst& kc, const double* tmp, double* f, double coeff, int axis, int seam,
+                             cudaStream_t s) {
+    damp_axis_kernel<<<dim3((kc.km + 31) / 32, (kc.jm + 7) / 8, kc.im), dim3(32, 8), 0, s>>>(kc, tmp, f, coeff, axis,
+                                                                                           seam);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_clamp_species(const KConst& kc, double* const f[11], float* const s32[11], double* added,
+                                 unsigned long long* cells, cudaStream_t s) {
+    ClampArgs A{};
+    for (int q = 0; q < 11; q++) {
+        A.f[q] = f[q];
+        A.s32[q] = s32 ? s32[q] : nullptr;
+    }
+    A.added = added;
+    A.cells = cells;
+    clamp_species_kernel<<<dim3((kc.km + 31) / 32, (kc.jm + 7) / 8, kc.im * 11), dim3(32, 8), 0, s>>>(kc, A);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_repitch(double* dst, int dst_pitch, const double* src, int src_pitch, int width, int64_t rows,
                            cudaStream_t s) {

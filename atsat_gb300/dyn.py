@@ -90,6 +90,11 @@ def lib():
         L.atsat_dyn_timer_start.argtypes = [H]
         L.atsat_dyn_timer_stop.argtypes = [H, C.POINTER(C.c_double)]
         L.atsat_dyn_conv_selftest.argtypes = [C.c_int32, C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.atsat_dyn_damp_wiggles.argtypes = [H, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_int32]
+        L.atsat_dyn_damp_pdyn.argtypes = [H]
+        L.atsat_dyn_clamp_negative_species.argtypes = [H]
+        L.atsat_dyn_clamp_budget.argtypes = [H, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_double),
+                                             C.POINTER(C.c_int64)]
         _lib = L
     return _lib
 
@@ -295,6 +300,27 @@ class Dycore:
         st = abi.PStats()
         self._ck(lib().atsat_dyn_pressure(self.h, C.byref(st)), "pressure")
         return st
+
+    def damp_wiggles(self, fid: int, along_i: bool, along_j: bool, along_k: bool, strength: float = 1.0,
+                     passes: int = 1):
+        """AtomUtils::damp_wiggles on a device field (lib/Utils.cpp:229-322), no surface mask."""
+        self._ck(lib().atsat_dyn_damp_wiggles(self.h, int(fid), int(along_i), int(along_j), int(along_k),
+                                              float(strength), int(passes)), "damp_wiggles")
+
+    def damp_pdyn(self):
+        """The p_dyn filter of cSaturnModel::Run after the pressure call (cSaturnModel.cpp:894-897)."""
+        self._ck(lib().atsat_dyn_damp_pdyn(self.h), "damp_pdyn")
+
+    def clampNegativeSpecies(self):
+        self._ck(lib().atsat_dyn_clamp_negative_species(self.h), "clamp_negative_species")
+
+    def clamp_budget(self) -> np.ndarray:
+        """44 values: clipped amount, cells, clipped amount on the radial planes, cells there (11 species each)."""
+        a, c = (C.c_double * 11)(), (C.c_int64 * 11)()
+        ab, cb = (C.c_double * 11)(), (C.c_int64 * 11)()
+        self._ck(lib().atsat_dyn_clamp_budget(self.h, a, c, ab, cb), "clamp_budget")
+        return np.concatenate([np.array(a[:]), np.array(c[:], dtype=np.float64), np.array(ab[:]),
+                               np.array(cb[:], dtype=np.float64)])
 
     def restoreVar(self):
         self._ck(lib().atsat_dyn_restore_var(self.h), "restore_var")

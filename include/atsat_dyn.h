@@ -171,7 +171,12 @@ typedef struct atsat_dyn_params {
     int32_t bc_species_lid_copy;  /* ATSAT_BC_SPECIES_LID_COPY, 1 */
     int32_t bc_species_wall_copy; /* ATSAT_BC_SPECIES_WALL_COPY, 2 (mass-fraction copy) */
     int32_t local_rho;         /* ATSAT_LOCAL_RHO, 1 (rho_at reads rho_mix) */
-    int32_t reserved[7];
+    /* the driver's glue around the dycore (cSaturnModel.cpp:894-897, 1101), used by atsat_dyn_damp_pdyn,
+     * atsat_dyn_clamp_negative_species and, when driver_glue is 1, by atsat_dyn_iterate */
+    int32_t damp_pdyn;         /* ATSAT_DAMP_PDYN, 3 under GEO_BALANCE, else 1 */
+    int32_t clamp_species;     /* 1; 0 with ATSAT_NO_CLAMP */
+    int32_t driver_glue;       /* 0: atsat_dyn_iterate runs the dycore sequence only; 1: also the two above */
+    int32_t reserved[4];
 } atsat_dyn_params;
 
 /* statistics of one pressure call */
@@ -245,6 +250,29 @@ int atsat_dyn_boundary_conditions(atsat_dyn_t h);
  * the device (cSaturnModel.cpp:864-1111): on even iterations computeMixtureDensity and the pressure
  * call; then RungeKuttaSat, the boundary conditions and restoreVar. */
 int atsat_dyn_iterate(atsat_dyn_t h, int32_t iter0, int32_t n);
+
+/* The driver's glue around the dycore (cSaturnModel::Run), for runs that keep the state on the device.
+ * With params.driver_glue = 1, atsat_dyn_iterate runs atsat_dyn_damp_pdyn after each pressure call and
+ * atsat_dyn_clamp_negative_species after the boundary conditions, as Run does (cSaturnModel.cpp:894-897,
+ * 1101). */
+/* AtomUtils::damp_wiggles (lib/Utils.cpp:229-322) on one field, no surface mask: the 1-2-1 filter
+ * f += strength/4 (f[-1] - 2 f + f[+1]) along k (periodic over the km-1 distinct meridians with
+ * k = km-1 their copy when ATSAT_BC_PHI_PERIODIC is on), then j (clamped at the poles), then i (clamped
+ * at the walls), each axis from a copy of the field, `passes` times. Uses the handle's pressure-source
+ * buffer as the copy. */
+int atsat_dyn_damp_wiggles(atsat_dyn_t h, int32_t field, int32_t along_i, int32_t along_j, int32_t along_k,
+                           double strength, int32_t passes);
+/* the p_dyn filter Run applies after each pressure call (cSaturnModel.cpp:894-897), by params.damp_pdyn:
+ * 1 along i, j and k; 2 along i; 3 along i and k (the default under GEO_BALANCE); other values nothing */
+int atsat_dyn_damp_pdyn(atsat_dyn_t h);
+/* cSaturnModel::clampNegativeSpecies (FileIO_Sat.cpp:716-772): the 11 condensable species floored at 0
+ * where !(v >= 0), NaN included; the finite amount clipped and the cells are accumulated per species,
+ * and separately for the radial planes i = 0, im-1. Nothing when params.clamp_species is 0. */
+int atsat_dyn_clamp_negative_species(atsat_dyn_t h);
+/* the accumulated budget of the species floor since create, 11 entries each, in the order h2o,
+ * h2o_cloud, h2o_ice, h2s, nh3, nh3_cloud, nh3_ice, ch4, ch4_cloud, ch4_ice, nh4sh (the reference's
+ * clamp_added, clamp_cells, clamp_added_bnd, clamp_cells_bnd) */
+int atsat_dyn_clamp_budget(atsat_dyn_t h, double* added, int64_t* cells, double* added_bnd, int64_t* cells_bnd);
 
 /* ---- diagnostics and timing ---- */
 int atsat_dyn_sync(atsat_dyn_t h);

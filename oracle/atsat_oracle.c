@@ -17,6 +17,8 @@
  *   PressureSolver<cSaturnModel>::run       planet/PressureSolver.h:145-766 (pointwise sweep, and the
  *                                           PRESS_LINE / PRESS_BAROTROPIC passes of :300-316, 502-708, 750-755)
  *   cSaturnModel::restoreVar(1.0)           planet/cSaturnModel.cpp:1551-1600
+ *   AtomUtils::damp_wiggles (p_dyn filter)  lib/Utils.cpp:229-322, cSaturnModel.cpp:894-897
+ *   cSaturnModel::clampNegativeSpecies      planet/FileIO_Sat.cpp:716-772
  * Parity of this file with the reference is pinned by tests/test_oracle_golden.py against
  * fixtures produced by the reference itself (oracle/ref_harness.cpp).
  *
@@ -921,6 +923,104 @@ static void pressure(M* m, atsat_dyn_pstats* st) {
     free(sinthe_table);
 }
 
+/* ---------------- AtomUtils::damp_wiggles, lib/Utils.cpp:229-322 (no surface mask) ----------------
+ * The 1-2-1 filter f += strength/4 (f[-1] - 2 f + f[+1]) along k (periodic over the km-1 distinct
+ * meridians with k = km-1 their copy when the seam is periodic, else over all km), then j (clamped at
+ * the poles), then i (clamped at the walls); each pass reads a copy of the field. */
+static void damp_wiggles(M* m, int fid, int along_i, int along_j, int along_k, double strength, int passes) {
+    const int im = m->im, jm = m->jm, km = m->km;
+    const size_t n = (size_t)im * jm * km;
+    const double coeff = strength * 0.25;
+    double* f = m->f[fid];
+    double* tmp = (double*)malloc(n * sizeof(double));
+    for (int pass = 0; pass < passes; ++pass) {
+        if (along_k) {
+            memcpy(tmp, f, n * sizeof(double));
+            const int seam = m->p->phi_periodic && km > 2;
+            const int k_end = seam ? km - 1 : km;
+            #pragma omp parallel for collapse(2) schedule(static)
+            for (int i = 0; i < im; ++i)
+                for (int j = 0; j < jm; ++j) {
+                    for (int k = 0; k < k_end; ++k) {
+                        const int km1 = seam ? (k == 0 ? km - 2 : k - 1) : (k - 1 + km) % km;
+                        const int kp1 = seam ? (k == km - 2 ? 0 : k + 1) : (k + 1) % km;
+                        const double t0 = tmp[IDX(m, i, j, k)];
+                        f[IDX(m, i, j, k)] = t0 + coeff * (tmp[IDX(m, i, j, km1)] - 2.0 * t0 + tmp[IDX(m, i, j, kp1)]);
+                    }
+                    if (seam) f[IDX(m, i, j, km - 1)] = f[IDX(m, i, j, 0)];
+                }
+        }
+        if (along_j) {
+            memcpy(tmp, f, n * sizeof(double));
+            #pragma omp parallel for collapse(2) schedule(static)
+            for (int i = 0; i < im; ++i)
+                for (int j = 0; j < jm; ++j) {
+                    const int jm1 = j - 1 < 0 ? 0 : j - 1, jp1 = j + 1 > jm - 1 ? jm - 1 : j + 1;
+                    for (int k = 0; k < km; ++k) {
+                        const double t0 = tmp[IDX(m, i, j, k)];
+                        f[IDX(m, i, j, k)] = t0 + coeff * (tmp[IDX(m, i, jm1, k)] - 2.0 * t0 + tmp[IDX(m, i, jp1, k)]);
+                    }
+                }
+        }
+        if (along_i) {
+            memcpy(tmp, f, n * sizeof(double));
+            #pragma omp parallel for collapse(2) schedule(static)
+            for (int j = 0; j < jm; ++j)
+                for (int k = 0; k < km; ++k)
+                    for (int i = 0; i < im; ++i) {
+                        const int im1 = i - 1 < 0 ? 0 : i - 1, ip1 = i + 1 > im - 1 ? im - 1 : i + 1;
+                        const double t0 = tmp[IDX(m, i, j, k)];
+                        f[IDX(m, i, j, k)] = t0 + coeff * (tmp[IDX(m, im1, j, k)] - 2.0 * t0 + tmp[IDX(m, ip1, j, k)]);
+                    }
+        }
+    }
+    free(tmp);
+}
+
+/* the p_dyn filter of cSaturnModel::Run after the pressure call (cSaturnModel.cpp:894-897) */
+static void damp_pdyn(M* m) {
+    const int mode = m->p->damp_pdyn;
+    if (mode == 1) damp_wiggles(m, ATSAT_F_P_DYN, 1, 1, 1, 1.0, 1);
+    else if (mode == 2) damp_wiggles(m, ATSAT_F_P_DYN, 1, 0, 0, 1.0, 1);
+    else if (mode == 3) damp_wiggles(m, ATSAT_F_P_DYN, 1, 0, 1, 1.0, 1);
+}
+
+/* ---------------- cSaturnModel::clampNegativeSpecies, FileIO_Sat.cpp:716-772 ----------------
+ * budget (optional): 4 x 11 doubles, the finite amount clipped, the cells, and both again for the radial
+ * planes i = 0, im-1, per species in the reference's order, added to what they hold. */
+static const int CLAMP_SPECIES[11] = { ATSAT_F_H2O, ATSAT_F_H2O_CLOUD, ATSAT_F_H2O_ICE, ATSAT_F_H2S, ATSAT_F_NH3,
+                                       ATSAT_F_NH3_CLOUD, ATSAT_F_NH3_ICE, ATSAT_F_CH4, ATSAT_F_CH4_CLOUD,
+                                       ATSAT_F_CH4_ICE, ATSAT_F_NH4SH };
+
+static void clamp_negative_species(M* m, double* budget) {
+    if (!m->p->clamp_species) return;
+    const int im = m->im, jm = m->jm, km = m->km;
+    for (int q = 0; q < 11; q++) {
+        double* F = m->f[CLAMP_SPECIES[q]];
+        double added = 0.0, added_bnd = 0.0;
+        long cells = 0, cells_bnd = 0;
+        #pragma omp parallel for collapse(2) schedule(static) reduction(+:added, cells, added_bnd, cells_bnd)
+        for (int i = 0; i < im; i++)
+            for (int j = 0; j < jm; j++)
+                for (int k = 0; k < km; k++) {
+                    const double v = F[IDX(m, i, j, k)];
+                    if (!(v >= 0.0)) {
+                        if (isfinite(v)) {
+                            added -= v; cells++;
+                            if (i == 0 || i == im - 1) { added_bnd -= v; cells_bnd++; }
+                        }
+                        F[IDX(m, i, j, k)] = 0.0;
+                    }
+                }
+        if (budget) {
+            budget[q] += added;
+            budget[11 + q] += (double)cells;
+            budget[22 + q] += added_bnd;
+            budget[33 + q] += (double)cells_bnd;
+        }
+    }
+}
+
 /* ---------------- cSaturnModel.cpp:1551-1600 ---------------- */
 static void restore_var(M* m) {
     const size_t n = (size_t)m->im * m->jm * m->km;
@@ -1182,6 +1282,29 @@ int orc_pressure(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fi
     if (rc) return rc;
     pressure(&m, st);
     return 0;
+}
+
+int orc_damp_wiggles(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields, int fid, int along_i,
+                     int along_j, int along_k, double strength, int passes) {
+    M m; int rc = setup(&m, g, p, fields, NULL, NULL, NULL, NULL);
+    if (rc) return rc;
+    if (fid < 0 || fid >= ATSAT_NFIELDS) return ATSAT_DYN_E_INVALID;
+    damp_wiggles(&m, fid, along_i, along_j, along_k, strength, passes);
+    return ATSAT_DYN_OK;
+}
+
+int orc_damp_pdyn(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields) {
+    M m; int rc = setup(&m, g, p, fields, NULL, NULL, NULL, NULL);
+    if (rc) return rc;
+    damp_pdyn(&m);
+    return ATSAT_DYN_OK;
+}
+
+int orc_clamp_negative_species(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields, double* budget) {
+    M m; int rc = setup(&m, g, p, fields, NULL, NULL, NULL, NULL);
+    if (rc) return rc;
+    clamp_negative_species(&m, budget);
+    return ATSAT_DYN_OK;
 }
 
 int orc_restore_var(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields) {

@@ -110,13 +110,41 @@ def boundary_conditions(state, params):
     _check(lib().orc_boundary_conditions(C.byref(c.gh.s), C.byref(c.p), c.ptrs), "bc")
 
 
-def steps(state, params, nsteps: int, iter0: int = 1):
+def damp_wiggles(state, params, fid: int, along_i: bool, along_j: bool, along_k: bool, strength: float = 1.0,
+                 passes: int = 1):
+    """AtomUtils::damp_wiggles (lib/Utils.cpp:229-322) on one field, no surface mask."""
+    c = _Call(state, params)
+    _check(lib().orc_damp_wiggles(C.byref(c.gh.s), C.byref(c.p), c.ptrs, int(fid), int(along_i), int(along_j),
+                                  int(along_k), C.c_double(strength), int(passes)), "damp_wiggles")
+
+
+def damp_pdyn(state, params):
+    """The p_dyn filter of cSaturnModel::Run after the pressure call (cSaturnModel.cpp:894-897)."""
+    c = _Call(state, params)
+    _check(lib().orc_damp_pdyn(C.byref(c.gh.s), C.byref(c.p), c.ptrs), "damp_pdyn")
+
+
+def clamp_negative_species(state, params, budget=None):
+    """cSaturnModel::clampNegativeSpecies (FileIO_Sat.cpp:716-772). budget: a float64 array of 44 (the
+    clipped amount, the cells, and both for the radial planes, 11 species each) that is added to."""
+    c = _Call(state, params)
+    b = budget if budget is not None else np.zeros(44)
+    _check(lib().orc_clamp_negative_species(C.byref(c.gh.s), C.byref(c.p), c.ptrs, abi.dptr(b)), "clamp")
+    return b
+
+
+def steps(state, params, nsteps: int, iter0: int = 1, glue: bool = False, budget=None):
     """The dycore sequence of cSaturnModel::Run (cSaturnModel.cpp:864-1111 restricted to the dycore):
-    density + pressure on even iterations, RK4, boundary conditions, restoreVar."""
+    density + pressure on even iterations, RK4, boundary conditions, restoreVar. glue: also the driver's
+    p_dyn filter after the pressure call and the species floor after the boundary conditions."""
     for it in range(iter0, iter0 + nsteps):
         if it % 2 == 0:
             mixture_density(state, params)
             pressure(state, params)
+            if glue:
+                damp_pdyn(state, params)
         rk4_step(state, params)
         boundary_conditions(state, params)
+        if glue:
+            clamp_negative_species(state, params, budget)
         restore_var(state, params)

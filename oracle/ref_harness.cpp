@@ -16,12 +16,17 @@
 //                  (cSaturnModel.cpp:864-1111 restricted to the dycore): on even iterations
 //                  computeMixtureDensity + pressure; then RungeKuttaSat; bcTheta, bcPhi, bcRadius;
 //                  restoreVar(1.0). Iterations run iter0 .. iter0+nsteps-1 (iter0 defaults to 1).
+//        damp      the p_dyn filter Run applies after the pressure call (cSaturnModel.cpp:894-897)
+//        clamp     cSaturnModel::clampNegativeSpecies() (FileIO_Sat.cpp:716-772); writes its budget
+//        driver    as steps, with damp after the pressure call and clamp after the boundary conditions
 // Record format of both files: char name[48]; int64 count; double data[count].
 
 #include "cSaturnModel.h"
 #include "ProcessDiag.h"
 #include "PressureSolverSat.h"
 #include "BC_Sat.h"
+#include "Utils.h"
+#include "ATPhys.h"
 
 #include <cstdio>
 #include <cstdlib>
@@ -96,6 +101,16 @@ public:
         for(int i = 0; i < im; i++) for(int j = 0; j < jm; j++) for(int k = 0; k < km; k++)
             d[((size_t)i * jm + j) * km + k] = a.x[i][j][k];
         write_record(f, name, d.data(), (int64_t)d.size());
+    }
+
+    // The p_dyn filter of cSaturnModel::Run after the pressure call (cSaturnModel.cpp:894-897), with its
+    // mode chosen as Run chooses it.
+    static void damp_pdyn(cSaturnModel& m){
+        const char* e = getenv("ATSAT_DAMP_PDYN");
+        const int mode = e ? atoi(e) : (cSaturnModel::geo_balance() ? 3 : 1);
+        if(mode == 1)      AtomUtils::damp_wiggles(m.p_dyn, nullptr, true, true, true);
+        else if(mode == 2) AtomUtils::damp_wiggles(m.p_dyn, nullptr, true, false, false);
+        else if(mode == 3) AtomUtils::damp_wiggles(m.p_dyn, nullptr, true, false, true);
     }
 
     // One RHSSat pass with the per-column geometry RungeKuttaSat builds
@@ -197,6 +212,28 @@ public:
                 BC_Sat(m).bcRadius();
                 m.restoreVar(1.0);
             }
+        } else if(op == "damp"){
+            AtomUtils::set_phi_seam_periodic(ATPhys::phi_periodic<cSaturnModel>());   // as Run() does
+            damp_pdyn(m);
+        } else if(op == "clamp"){
+            m.clampNegativeSpecies();
+        } else if(op == "driver"){
+            // the dycore sequence with the driver's glue around it: the p_dyn filter after the pressure
+            // call (cSaturnModel.cpp:894-897) and the species floor after the boundary conditions (:1101)
+            AtomUtils::set_phi_seam_periodic(ATPhys::phi_periodic<cSaturnModel>());
+            for(int it = iter0; it < iter0 + nsteps; it++){
+                if(it % 2 == 0){
+                    m.computeMixtureDensity();
+                    m.getPressureSolver().run();
+                    damp_pdyn(m);
+                }
+                m.RungeKuttaSat();
+                BC_Sat(m).bcTheta();
+                BC_Sat(m).bcPhi();
+                BC_Sat(m).bcRadius();
+                m.clampNegativeSpecies();
+                m.restoreVar(1.0);
+            }
         } else { fprintf(stderr, "unknown op %s\n", op.c_str()); return 2; }
 
         FILE* f = fopen(argv[2], "wb");
@@ -213,6 +250,15 @@ public:
                                  "dr", "dthe", "dphi" };
         for(size_t c = 0; c < sizeof(consts) / sizeof(consts[0]); c++)
             write_record(f, std::string("const:") + cnames[c], &consts[c], 1);
+        if(!m.clamp_added.empty()){
+            const size_t nf = m.clamp_added.size();
+            std::vector<double> cells(nf), cells_bnd(nf);
+            for(size_t q = 0; q < nf; q++){ cells[q] = (double)m.clamp_cells[q]; cells_bnd[q] = (double)m.clamp_cells_bnd[q]; }
+            write_record(f, "clamp_added", m.clamp_added.data(), (int64_t)nf);
+            write_record(f, "clamp_cells", cells.data(), (int64_t)nf);
+            write_record(f, "clamp_added_bnd", m.clamp_added_bnd.data(), (int64_t)nf);
+            write_record(f, "clamp_cells_bnd", cells_bnd.data(), (int64_t)nf);
+        }
         write_record(f, "rad_z", m.rad.z, m.im);
         write_record(f, "the_z", m.the.z, m.jm);
         fclose(f);

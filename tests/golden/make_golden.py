@@ -38,11 +38,19 @@ CASES = {
     "pressure_baro_s1": ("pressure", 1, 1, True, {"press_baro": 1}),
     "pressure_lb3_s1": ("pressure", 1, 1, True, {"press_line": 1, "press_baro": 1, "press_sweeps": 3}),
     "steps4_lb_s2": ("steps", 4, 2, True, {"press_line": 1, "press_baro": 1}),
+    # the driver's glue: the p_dyn filter (cSaturnModel.cpp:894-897) and the species floor (FileIO_Sat.cpp:716-772)
+    "damp_s1": ("damp", 1, 1, True, {}),
+    "damp_m1_s1": ("damp", 1, 1, True, {"damp_pdyn": 1}),
+    "clamp_s3": ("clamp", 1, 3, True, {}),
+    "driver4_s3": ("driver", 4, 3, True, {}),
 }
+
+# cases whose state carries planted undershoots (negative and NaN species cells) for the species floor
+PLANTED = {"clamp_s3", "driver4_s3"}
 
 # the reference reads these knobs from its environment (PressureSolver.h:174-175, 300-303)
 KNOB_ENV = {"press_line": "ATSAT_PRESS_LINE", "press_baro": "ATSAT_PRESS_BAROTROPIC",
-            "press_sweeps": "ATSAT_PRESS_SWEEPS"}
+            "press_sweeps": "ATSAT_PRESS_SWEEPS", "damp_pdyn": "ATSAT_DAMP_PDYN"}
 
 
 def reference_env(over):
@@ -55,14 +63,40 @@ OUTPUTS = {
     "density": [F.RHO_MIX],
     "steps": F.PROG + F.PROG_N + [F.P_DYN, F.P_DYNN, F.RHO_MIX, F.P_METRIC, F.NUE] + F.AUX_FIELDS
              + [F.RHS_U, F.RHS_V, F.RHS_W],
+    "damp": [F.P_DYN],
+    "clamp": [F.H2O, F.H2O_CLOUD, F.H2O_ICE, F.H2S, F.NH3, F.NH3_CLOUD, F.NH3_ICE, F.CH4, F.CH4_CLOUD, F.CH4_ICE,
+              F.NH4SH],
 }
+OUTPUTS["driver"] = OUTPUTS["steps"]
+
+
+def plant_undershoots(st, seed):
+    """Negative cells (scattered, and patches on both radial planes) in five species, one NaN in a sixth:
+    what the species floor exists for. Seeded with the package's own generator."""
+    g = st.grid
+    n = g.cells
+    for q, f in enumerate((F.H2O, F.NH3, F.NH4SH, F.CH4_ICE, F.H2S)):
+        a = st.arrays[f]
+        u = synth.uniform(seed, 500 + q, n)
+        pick = u < 2000.0 / n
+        flat = a.reshape(-1)
+        flat[pick] = -np.abs(flat[pick]) * 0.3 - 1e-9
+        a[0, 5:9, 10:20] = -1e-8
+        a[-1, 7, 30] = -2e-8
+    st.arrays[F.NH3_CLOUD][3, 4, 5] = np.nan
+    for f in range(F.NPROG):
+        st.arrays[F.N_BASE + f] = st.arrays[f].copy()
+    return st
 
 
 def make_state(name):
     op, nsteps, seed, exercise, over = CASES[name]
     g = synth.make_grid()
     P = abi.default_params(**over)
-    return g, P, synth.saturn_state(g, P, seed=seed, exercise=exercise)
+    st = synth.saturn_state(g, P, seed=seed, exercise=exercise)
+    if name in PLANTED:
+        plant_undershoots(st, seed)
+    return g, P, st
 
 
 def sample_index(name, n_cells):
@@ -71,7 +105,7 @@ def sample_index(name, n_cells):
 
 
 def input_sums(st):
-    return np.array([float(np.sum(st.arrays[f])) for f in range(F.NFIELDS)])
+    return np.array([float(np.nansum(st.arrays[f])) for f in range(F.NFIELDS)])
 
 
 def main(names=None):
@@ -92,6 +126,9 @@ def main(names=None):
             rec[f"sum_{fid}"] = np.array([np.sum(a), np.sum(np.abs(a)), np.max(np.abs(a))])
         if "buoy_ref_level" in out and op in ("rhs", "rk"):
             rec["buoy_ref_level"] = out["buoy_ref_level"]
+        if "clamp_added" in out:
+            rec["clamp_budget"] = np.concatenate([out["clamp_added"], out["clamp_cells"], out["clamp_added_bnd"],
+                                                  out["clamp_cells_bnd"]])
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **rec)
         print(name, os.path.getsize(path), "bytes")

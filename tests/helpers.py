@@ -35,3 +35,21 @@ def compare(got: dict, ref: dict, fids, tol: float, label: str = ""):
             bad.append(f"{F.NAMES[fid]}: {e:.3e}")
     assert not bad, f"{label} fields above {tol:g}: " + ", ".join(bad)
     return worst
+
+
+def plant_negatives(st, seed=0):
+    """Negative cells in five species (scattered and on both radial planes) and one NaN: the undershoots
+    cSaturnModel::clampNegativeSpecies floors. Any grid of at least 5 x 7 x 5."""
+    g = st.grid
+    rng = np.random.default_rng(seed)
+    for f in (F.H2O, F.NH3, F.NH4SH, F.CH4_ICE, F.H2S):
+        a = st.arrays[f]
+        flat = a.reshape(-1)
+        idx = rng.choice(flat.size, max(1, flat.size // 50), replace=False)
+        flat[idx] = -np.abs(flat[idx]) * 0.3 - 1e-9
+        a[0, 1:4, 1:4] = -1e-8
+        a[-1, 2, 3] = -2e-8
+    st.arrays[F.NH3_CLOUD][2, 3, 1] = np.nan
+    for f in range(F.NPROG):
+        st.arrays[F.N_BASE + f] = st.arrays[f].copy()
+    return st

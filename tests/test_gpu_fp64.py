@@ -148,6 +148,95 @@ def test_pressure_line_holds_interior_mean():
     assert abs(p1 - p0) <= 1e-12 * max(1.0, float(np.max(np.abs(s.arrays[F.P_DYN]))))
 
 
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("mode", [3, 1, 2, 0])
+def test_damp_pdyn_modes(shape, mode):
+    """The p_dyn filter of cSaturnModel::Run (AtomUtils::damp_wiggles along the mode's axes)."""
+    from atsat_gb300 import dyn
+    g, P, st = case(shape, seed=25, damp_pdyn=mode)
+    ref = st.copy()
+    oracle.damp_pdyn(ref, P)
+    s = st.copy()
+    with dyn.Dycore(g, P) as d:
+        d.load_state(s)
+        d.damp_pdyn()
+        d.download(ALL)
+    compare(s.arrays, ref.arrays, ALL, 1e-13, f"damp mode {mode} {shape}")
+
+
+@pytest.mark.parametrize("axes,strength,passes", [((1, 1, 1), 1.0, 1), ((0, 1, 0), 0.5, 3), ((1, 0, 1), 2.0, 2)])
+def test_damp_wiggles_generic(axes, strength, passes):
+    from atsat_gb300 import dyn
+    g, P, st = case((12, 40, 70), seed=27)
+    ref = st.copy()
+    oracle.damp_wiggles(ref, P, F.T, *axes, strength, passes)
+    s = st.copy()
+    with dyn.Dycore(g, P) as d:
+        d.load_state(s)
+        d.damp_wiggles(F.T, *axes, strength, passes)
+        d.download(ALL)
+    compare(s.arrays, ref.arrays, ALL, 1e-13, f"damp {axes} {strength} {passes}")
+
+
+@pytest.mark.parametrize("shape", SHAPES[:2])
+def test_clamp_negative_species(shape):
+    from atsat_gb300 import dyn
+    from helpers import plant_negatives
+    g, P, st = case(shape, seed=29)
+    plant_negatives(st, seed=3)
+    ref = st.copy()
+    rb = oracle.clamp_negative_species(ref, P)
+    s = st.copy()
+    with dyn.Dycore(g, P) as d:
+        d.load_state(s)
+        d.clampNegativeSpecies()
+        d.download(ALL)
+        budget = d.clamp_budget()
+    for fid in ALL:
+        assert np.array_equal(s.arrays[fid], ref.arrays[fid], equal_nan=True), F.NAMES[fid]
+    assert np.array_equal(budget[11:22], rb[11:22]) and np.array_equal(budget[33:], rb[33:])
+    assert np.allclose(budget, rb, rtol=1e-13, atol=0.0)
+    assert rb[11:22].sum() > 0 and rb[33:].sum() > 0
+
+
+def test_clamp_off_with_no_clamp():
+    from atsat_gb300 import dyn
+    from helpers import plant_negatives
+    g, P, st = case((9, 13, 17), seed=31, clamp_species=0)
+    plant_negatives(st, seed=4)
+    s = st.copy()
+    with dyn.Dycore(g, P) as d:
+        d.load_state(s)
+        d.clampNegativeSpecies()
+        d.download(ALL)
+        assert not d.clamp_budget().any()
+    for fid in ALL:
+        assert np.array_equal(s.arrays[fid], st.arrays[fid], equal_nan=True)
+
+
+@pytest.mark.parametrize("shape", [(9, 13, 17), (10, 20, 36)])
+def test_iterate_with_driver_glue(shape):
+    """Four resident iterations with the driver's glue (p_dyn filter after the pressure call, species
+    floor after the boundary conditions) against the oracle's same sequence."""
+    from atsat_gb300 import dyn
+    from helpers import plant_negatives
+    g, P, st = case(shape, seed=33, driver_glue=1)
+    plant_negatives(st, seed=5)
+    ref = st.copy()
+    rb = np.zeros(44)
+    oracle.steps(ref, P, 4, glue=True, budget=rb)
+    s = st.copy()
+    with dyn.Dycore(g, P) as d:
+        d.load_state(s)
+        d.set_write_all_rhs(True)
+        d.iterate(1, 4)
+        d.download(ALL)
+        budget = d.clamp_budget()
+    compare(s.arrays, ref.arrays, ALL, TOL_FP64, f"driver glue {shape}")
+    assert np.array_equal(budget[11:22], rb[11:22])
+    assert np.allclose(budget, rb, rtol=1e-9, atol=0.0)
+
+
 def test_pressure_clamp_count():
     from atsat_gb300 import dyn
     g, P, st = case((9, 13, 17), seed=9, pdyn_cap=1e-9)

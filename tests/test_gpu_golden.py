@@ -19,10 +19,17 @@ def test_gpu_against_reference_fixture(name):
     rec = load(name)
     check_inputs(rec, st)
     s = st.copy()
-    with dyn.Dycore(g, P) as d:
+    budget = None
+    with dyn.Dycore(g, dict(P, driver_glue=1) if op == "driver" else P) as d:
         d.load_state(s)
         d.set_write_all_rhs(True)
-        if op == "rhs":
+        if op in ("driver", "steps"):
+            d.iterate(1, nsteps)
+        elif op == "damp":
+            d.damp_pdyn()
+        elif op == "clamp":
+            d.clampNegativeSpecies()
+        elif op == "rhs":
             d.computeBuoyancyRefLevel()
             d.computeMetricPressure()
             d.RHSSat_pass()
@@ -32,10 +39,16 @@ def test_gpu_against_reference_fixture(name):
             d.PressureSolver_run()
         elif op == "density":
             d.computeMixtureDensity()
-        elif op == "steps":
-            d.iterate(1, nsteps)
         d.download(list(range(F.NFIELDS)))
         buoy = d.buoy_ref_level()
+        if op in ("clamp", "driver"):
+            budget = d.clamp_budget()
     check_outputs(rec, s.arrays, TOL_FP64, name)
+    if budget is not None:
+        rb = rec["clamp_budget"]
+        n = len(rb) // 4
+        # counts exactly (the cells a floor touches), amounts to the FP64 bar
+        assert np.array_equal(budget[n:2 * n], rb[n:2 * n]) and np.array_equal(budget[3 * n:], rb[3 * n:])
+        assert np.all(np.abs(budget - rb) <= TOL_FP64 * np.maximum(np.abs(rb), 1e-300)), (budget, rb)
     if "buoy_ref_level" in rec:
         assert np.max(np.abs(buoy - rec["buoy_ref_level"])) <= TOL_FP64 * np.max(np.abs(rec["buoy_ref_level"]))

@@ -88,6 +88,22 @@ def test_mixed_ten_iterations_line_barotropic(shape):
     assert not bad, bad
 
 
+def test_mixed_ten_iterations_driver_glue():
+    """The mixed path with the driver's glue: the species floor must also reach the FP32 copies the next
+    step starts from."""
+    from helpers import plant_negatives
+    g, P, st = case((21, 91, 181), seed=45, exercise=True, driver_glue=1)
+    plant_negatives(st, seed=6)
+    ref = st.copy()
+    oracle.steps(ref, P, 10, glue=True)
+    got = run_mixed(g, P, st, 10, TILED2)
+    rep = drift(got.arrays, ref.arrays, F.PROG + [F.P_DYN])
+    bad = {F.NAMES[f]: rep[F.NAMES[f]][0] for f in CRITERION if not rep[F.NAMES[f]][0] <= TOL_MIXED}
+    assert not bad, bad
+    for f in (F.H2O, F.NH3, F.NH4SH, F.CH4_ICE, F.H2S, F.NH3_CLOUD):
+        assert np.all(got.arrays[f] >= 0.0), F.NAMES[f]
+
+
 @pytest.mark.parametrize("variant", VARIANTS)
 def test_mixed_one_step_all_fields(variant):
     """One RK4 step: every prognostic field within 1e-6, rhs_u/v/w and aux within 1e-5 of their max."""
