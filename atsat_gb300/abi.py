@@ -30,6 +30,41 @@ class Params(C.Structure):
                 + [("reserved", C.c_int32 * 4)])
 
 
+class TurbParams(C.Structure):
+    """atsat_dyn_turb_params: the knobs and constants of Turbulence<cSaturnModel>::run."""
+    _fields_ = [("model", C.c_int32), ("turb_free", C.c_int32), ("clamp_pass", C.c_int32), ("abl_taper", C.c_int32),
+                ("curv", C.c_int32), ("buoy", C.c_int32), ("k_bg", C.c_double), ("l_bg", C.c_double),
+                ("nue_max_phys", C.c_double), ("vel_star_max", C.c_double), ("vel_star_ref", C.c_double),
+                ("z_0", C.c_double), ("nue_gas", C.c_double), ("abl_height", C.c_double),
+                ("ep", C.c_double * 3), ("lv", C.c_double * 3), ("ls", C.c_double * 3), ("t_0", C.c_double * 3),
+                ("reserved", C.c_double * 4)]
+
+
+TURB_K_EPSILON, TURB_K_OMEGA, TURB_K_OMEGA_SST = 0, 1, 2
+
+# the reference's defaults (Turbulence.h:119-187, 348-352, 712-713, 812-813; the moist gases' constants of
+# cSaturnModel.h read back from its build: H2O, NH3, CH4)
+TURB_DEFAULTS = dict(model=TURB_K_OMEGA_SST, turb_free=1, clamp_pass=1, abl_taper=0, curv=1, buoy=3, k_bg=1.0,
+                     l_bg=0.0, nue_max_phys=1.0e5, vel_star_max=0.002 ** 0.5 * 200.0, vel_star_ref=0.4, z_0=0.1,
+                     nue_gas=1.8e-5, abl_height=20000.0, ep=(8.1253, 7.6752, 7.6752),
+                     lv=(2.5009e6, 1.372e6, 5.11e5), ls=(2.8339e6, 1.832e6, 5.11e5), t_0=(273.15, 195.5, 90.69))
+
+
+def make_turb_params(**over) -> TurbParams:
+    d = dict(TURB_DEFAULTS)
+    for k, v in over.items():
+        if k not in d:
+            raise KeyError(k)
+        d[k] = v
+    tp = TurbParams()
+    for k, v in d.items():
+        if isinstance(v, tuple):
+            getattr(tp, k)[:] = v
+        else:
+            setattr(tp, k, v)
+    return tp
+
+
 class PStats(C.Structure):
     _fields_ = [("sweeps", C.c_int32), ("reserved0", C.c_int32),
                 ("src_clamped", C.c_double), ("max_abs_update", C.c_double)]

@@ -274,6 +274,41 @@ int atsat_dyn_clamp_negative_species(atsat_dyn_t h);
  * clamp_added, clamp_cells, clamp_added_bnd, clamp_cells_bnd) */
 int atsat_dyn_clamp_budget(atsat_dyn_t h, double* added, int64_t* cells, double* added_bnd, int64_t* cells_bnd);
 
+/* ---- the turbulence closure (Turbulence<cSaturnModel>::run, planet/Turbulence.h:306-329) ----
+ * Its knobs are the ATSAT_TURB_* / NUE_MAX / VEL_STAR_MAX / ABL_TAPER environment of the reference
+ * (Turbulence.h:119-187, 348-352, 712-713, 812-813) and the model's constants it reads. */
+enum { ATSAT_TURB_K_EPSILON = 0, ATSAT_TURB_K_OMEGA = 1, ATSAT_TURB_K_OMEGA_SST = 2 };
+typedef struct atsat_dyn_turb_params {
+    int32_t model;             /* ATSAT_TURB_MODEL, else the configuration's turb_model: ATSAT_TURB_K_OMEGA_SST */
+    int32_t turb_free;         /* ATSAT_TURB_FREE, 1 (no wall law; uniform background k) */
+    int32_t clamp_pass;        /* ATSAT_TURB_CLAMP_PASS, 1 (the floors as passes around the source loop) */
+    int32_t abl_taper;         /* ATSAT_ABL_TAPER, 0 */
+    int32_t curv;              /* ATSAT_TURB_CURV, 1 (curvature terms of the velocity-gradient tensor) */
+    int32_t buoy;              /* ATSAT_TURB_BUOY, 3 (moist N^2 buoyancy sink of k) */
+    double  k_bg;              /* ATSAT_TURB_K_BG [m2/s2], 1.0 */
+    double  l_bg;              /* ATSAT_TURB_L_BG [m]; <= 0: one mean layer, L_atm / (im - 1) */
+    double  nue_max_phys;      /* ATSAT_NUE_MAX [m2/s], 1e5 */
+    double  vel_star_max;      /* ATSAT_VEL_STAR_MAX [m/s], sqrt(0.002) * 200 */
+    double  vel_star_ref;      /* reference friction velocity [m/s], 0.4 */
+    double  z_0;               /* roughness length [m], 0.1 */
+    double  nue_gas;           /* kinematic viscosity of H2/He [m2/s], 1.8e-5 */
+    double  abl_height;        /* boundary-layer height [m], 20000 */
+    /* the condensable gases of the moist N^2 (cSaturnModel.cpp:259-266): H2O, NH3, CH4 */
+    double  ep[3], lv[3], ls[3], t_0[3];
+    double  reserved[4];
+} atsat_dyn_turb_params;
+
+int atsat_dyn_turb_params_default(atsat_dyn_turb_params* tp);
+int atsat_dyn_turb_params_from_env(atsat_dyn_turb_params* tp);   /* the knobs above, as the reference reads them */
+int atsat_dyn_set_turb_params(atsat_dyn_t h, const atsat_dyn_turb_params* tp);   /* the handle starts with the defaults */
+/* Turbulence<cSaturnModel>::run on the device fields: friction velocity, the sources of the chosen closure
+ * (tke_source, dis_source, nue, the production P_k), the wall condition at i = 0, the nue cap, the seam and
+ * lid-corner copies; tke and dis are floored as the reference floors them. */
+int atsat_dyn_turbulence(atsat_dyn_t h);
+/* the closure's own arrays after the last atsat_dyn_turbulence: the production P_k (im*jm*km, contiguous,
+ * k fastest) and the friction velocity u_tau (jm*km); either may be null */
+int atsat_dyn_turbulence_diag(atsat_dyn_t h, double* prod, double* vel_star);
+
 /* ---- diagnostics and timing ---- */
 int atsat_dyn_sync(atsat_dyn_t h);
 int atsat_dyn_status(atsat_dyn_t h, atsat_dyn_diag* out);

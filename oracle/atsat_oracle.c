@@ -19,6 +19,7 @@
  *   cSaturnModel::restoreVar(1.0)           planet/cSaturnModel.cpp:1551-1600
  *   AtomUtils::damp_wiggles (p_dyn filter)  lib/Utils.cpp:229-322, cSaturnModel.cpp:894-897
  *   cSaturnModel::clampNegativeSpecies      planet/FileIO_Sat.cpp:716-772
+ *   Turbulence<cSaturnModel>::run           planet/Turbulence.h:306-329, 335-1115
  * Parity of this file with the reference is pinned by tests/test_oracle_golden.py against
  * fixtures produced by the reference itself (oracle/ref_harness.cpp).
  *
@@ -1021,6 +1022,383 @@ static void clamp_negative_species(M* m, double* budget) {
     }
 }
 
+/* ---------------- Turbulence<cSaturnModel>::run, planet/Turbulence.h:306-329 ----------------
+ * ATSAT has no solid body (cSaturnModel.h:254-255: surface_index 0, is_solid false), so the land branches
+ * are constant. Layer heights are the model's float table (cSaturnModel.h:1062-1074): h = (float)(L_atm dr),
+ * height(i) = (float)i * h km. cp for the lapse rate is cp_mix (CpH2.h:129-131, ATSAT keeps it in the
+ * dynamics). prod is the closure's production array (im*jm*km), vel_star its u_tau (jm*km). */
+typedef struct {
+    const M* m;
+    const atsat_dyn_turb_params* tp;
+    float h;                     /* the layer spacing in km, as the model's float table holds it */
+    double L_m, nue_air, re_turb;
+} TurbCtx;
+
+static inline double t_height_m(const TurbCtx* c, int i) {
+    if (0 > i || i > c->m->im - 1) return (double)(-1.0f) * 1.0e3;
+    return (double)((float)i * c->h) * 1.0e3;
+}
+static inline double t_layer_thickness_m(const TurbCtx* c, int i) {
+    if (i < 0 || i > c->m->im - 2) return 0.0;
+    return (double)((float)(i + 1) * c->h - (float)i * c->h) * 1.0e3;
+}
+static inline double clamp3(double x, double lo, double hi) { return (x < lo) ? lo : ((x > hi) ? hi : x); }
+
+#define TK(i, j, k) X(m, ATSAT_F_TKE, i, j, k)
+#define DS(i, j, k) X(m, ATSAT_F_DIS, i, j, k)
+
+static void turb_sst(const TurbCtx* c, double* prod, int i, int j, int k, double y_mount, double rm, double sinthe,
+                     double dtkedr, double ddisdr, double Omega) {
+    M* m = (M*)c->m;
+    const double a1 = 0.31, bet_star = 0.09, bet1 = 0.0333, bet2 = 0.0368, gam1 = 0.413, gam2 = 0.2, sig_w2 = 1.168;
+    const double L_m = c->L_m;
+    const double nue_air_nd = c->nue_air / (m->p->u_0 * L_m);
+    const double dz_layer = smax(1.0, t_layer_thickness_m(c, (i - 1 > 0) ? i - 1 : 0));
+    const double y_phys = c->tp->turb_free ? 1.0e20 : smax(t_height_m(c, i) - y_mount, dz_layer);
+    const double y_star = y_phys / L_m;
+    const double rmsinthe = rm * sinthe;
+    const int per = m->p->phi_periodic;
+    const int kw = phi_wrap(per, k - 1, m->km), ke = phi_wrap(per, k + 1, m->km);
+    const double dtkedthe = (TK(i, j + 1, k) - TK(i, j - 1, k)) / (rm * 2.0 * m->dthe);
+    const double ddisdthe = (DS(i, j + 1, k) - DS(i, j - 1, k)) / (rm * 2.0 * m->dthe);
+    const double dtkedphi = (TK(i, j, ke) - TK(i, j, kw)) / (rmsinthe * 2.0 * m->dphi);
+    const double ddisdphi = (DS(i, j, ke) - DS(i, j, kw)) / (rmsinthe * 2.0 * m->dphi);
+    const double grad_dot = dtkedr * ddisdr + dtkedthe * ddisdthe + dtkedphi * ddisdphi;
+    const double CD_kw = smax(2.0 * sig_w2 / smax(DS(i, j, k), 1.0e-20) * grad_dot, 1.0e-20);
+    const double dis_safe = smax(DS(i, j, k), 1.0e-20);
+    const double arg1 = smin(smax(sqrt(TK(i, j, k)) / (bet_star * dis_safe * y_star),
+                                  500.0 * nue_air_nd / (y_star * y_star * dis_safe)),
+                             4.0 * sig_w2 * TK(i, j, k) / (CD_kw * y_star * y_star));
+    const double arg2 = smax(2.0 * sqrt(TK(i, j, k)) / (bet_star * dis_safe * y_star),
+                             500.0 * nue_air_nd / (y_star * y_star * dis_safe));
+    const double F1 = tanh(pow(arg1, 4));
+    const double F2 = tanh(pow(arg2, 2));
+    X(m, ATSAT_F_NUE, i, j, k) = a1 * TK(i, j, k) / smax(a1 * dis_safe, Omega * F2);
+    const double tke_safe = smax(TK(i, j, k), 1.0e-20);
+    const double P_k = smin(prod[IDX(m, i, j, k)], 20.0 * bet_star * tke_safe * dis_safe);
+    const double Y_k = bet_star * tke_safe * dis_safe;
+    const double P_w = (F1 * gam1 + (1.0 - F1) * gam2) * P_k * dis_safe / tke_safe;
+    const double Y_w = (F1 * bet1 + (1.0 - F1) * bet2) * dis_safe * dis_safe;
+    const double D_w = 2.0 * (1.0 - F1) * sig_w2 / dis_safe * grad_dot;
+    X(m, ATSAT_F_TKE_SOURCE, i, j, k) = P_k - Y_k;
+    X(m, ATSAT_F_DIS_SOURCE, i, j, k) = P_w - Y_w + D_w;
+}
+
+static void turb_k_omega(const TurbCtx* c, double* prod, int i, int j, int k, double dtkedr, double ddisdr,
+                         double Omega_mag) {
+    M* m = (M*)c->m;
+    const double bet_star = 0.09, gam = 0.52, C_lim = 0.875, bet_0 = 0.0708;
+    const double rm = metric_radius(m, m->rad_z[i]);
+    double sinthe = sin(m->the_z[j]);
+    if (sinthe == 0.0) sinthe = 1.0e-5;
+    const double rmsinthe = rm * sinthe;
+    const int per = m->p->phi_periodic;
+    const int kw = phi_wrap(per, k - 1, m->km), ke = phi_wrap(per, k + 1, m->km);
+    const double dtkedthe_neu = (TK(i, j + 1, k) - TK(i, j - 1, k)) / (rm * 2.0 * m->dthe);
+    const double ddisdthe_neu = (DS(i, j + 1, k) - DS(i, j - 1, k)) / (rm * 2.0 * m->dthe);
+    const double dtkedphi_neu = (TK(i, j, ke) - TK(i, j, kw)) / (rmsinthe * 2.0 * m->dphi);
+    const double ddisdphi_neu = (DS(i, j, ke) - DS(i, j, kw)) / (rmsinthe * 2.0 * m->dphi);
+    const double dudr = (X(m, ATSAT_F_U, i + 1, j, k) - X(m, ATSAT_F_U, i - 1, j, k)) / (2.0 * m->dr) / (rm + 1.0);
+    const double dvdthe = (X(m, ATSAT_F_V, i, j + 1, k) - X(m, ATSAT_F_V, i, j - 1, k)) / (rm * 2.0 * m->dthe);
+    const double dwdphi = (X(m, ATSAT_F_W, i, j, ke) - X(m, ATSAT_F_W, i, j, kw)) / (rmsinthe * 2.0 * m->dphi);
+    const double dudthe_u = (X(m, ATSAT_F_U, i, j + 1, k) - X(m, ATSAT_F_U, i, j - 1, k)) / (rm * 2.0 * m->dthe);
+    const double dudphi_u = (X(m, ATSAT_F_U, i, j, ke) - X(m, ATSAT_F_U, i, j, kw)) / (rmsinthe * 2.0 * m->dphi);
+    const double dvdr_u = (X(m, ATSAT_F_V, i + 1, j, k) - X(m, ATSAT_F_V, i - 1, j, k)) / (2.0 * m->dr) / (rm + 1.0);
+    const double dwdr_u = (X(m, ATSAT_F_W, i + 1, j, k) - X(m, ATSAT_F_W, i - 1, j, k)) / (2.0 * m->dr) / (rm + 1.0);
+    const double dvdphi_u = (X(m, ATSAT_F_V, i, j, ke) - X(m, ATSAT_F_V, i, j, kw)) / (rmsinthe * 2.0 * m->dphi);
+    const double dwdthe_u = (X(m, ATSAT_F_W, i, j + 1, k) - X(m, ATSAT_F_W, i, j - 1, k)) / (rm * 2.0 * m->dthe);
+    const double S11 = dudr, S22 = dvdthe, S33 = dwdphi;
+    const double S12 = 0.5 * (dudthe_u + dvdr_u);
+    const double S13 = 0.5 * (dudphi_u + dwdr_u);
+    const double S23 = 0.5 * (dvdphi_u + dwdthe_u);
+    const double S_mag = sqrt(2.0 * (S11 * S11 + S22 * S22 + S33 * S33 + 2.0 * (S12 * S12 + S13 * S13 + S23 * S23)));
+    const double w_hat = smax(DS(i, j, k), C_lim * S_mag / sqrt(bet_star));
+    const double gd = dtkedr * ddisdr + dtkedthe_neu * ddisdthe_neu + dtkedphi_neu * ddisdphi_neu;
+    const double sig_d = (gd <= 0.0) ? 0.0 : 0.125;
+    const double chi_w = fabs(Omega_mag * Omega_mag * S_mag / pow(bet_star * smax(DS(i, j, k), 1.0e-20), 3));
+    const double f_bet = (1.0 + 85.0 * chi_w) / (1.0 + 100.0 * chi_w);
+    const double bet_wc = bet_0 * f_bet;
+    X(m, ATSAT_F_NUE, i, j, k) = TK(i, j, k) / smax(w_hat, 1.0e-20);
+    const double P_k = smin(prod[IDX(m, i, j, k)], 20.0 * bet_star * TK(i, j, k) * DS(i, j, k));
+    const double Y_k = bet_star * TK(i, j, k) * DS(i, j, k);
+    const double P_w = gam * DS(i, j, k) / smax(TK(i, j, k), 1.0e-20) * P_k;
+    const double Y_w = bet_wc * DS(i, j, k) * DS(i, j, k);
+    const double D_w = sig_d / smax(DS(i, j, k), 1.0e-20)
+                     * (dtkedr * ddisdr + dtkedthe_neu * ddisdthe_neu + dtkedphi_neu * ddisdphi_neu);
+    X(m, ATSAT_F_TKE_SOURCE, i, j, k) = P_k - Y_k;
+    X(m, ATSAT_F_DIS_SOURCE, i, j, k) = P_w - Y_w + D_w;
+}
+
+static void turb_k_epsilon(const TurbCtx* c, double* prod, const double* vel_star, int i, int j, int k, double y_mount) {
+    M* m = (M*)c->m;
+    const double C_eps_1 = 1.35, C_eps_2 = 1.80, C_nue = 0.028, dis_min = 1.0e-10;
+    const double L_m = c->L_m;
+    const double y_phys = c->tp->turb_free ? 1.0e20 : smax(t_height_m(c, i) - y_mount, L_m);
+    const double y_star = y_phys / L_m;
+    X(m, ATSAT_F_NUE, i, j, k) = C_nue * TK(i, j, k) * TK(i, j, k) / smax(DS(i, j, k), dis_min);
+    const double d_plus = y_phys * vel_star[(size_t)j * m->km + k] / c->nue_air;
+    const double f_nue = 1.0 - exp(-0.0115 * d_plus);
+    const double Re_T = TK(i, j, k) * TK(i, j, k) * m->p->u_0 * L_m / smax(DS(i, j, k) * c->nue_air, dis_min * c->nue_air);
+    const double f_2 = 1.0 - 0.4 / 1.8 * exp(-Re_T * Re_T / 36.0);
+    X(m, ATSAT_F_NUE, i, j, k) *= f_nue;
+    const double y_star2 = y_star * y_star;
+    const double L_k = -2.0 * TK(i, j, k) / y_star2;
+    const double L_w = -2.0 * DS(i, j, k) / y_star2 * exp(-d_plus / 2.0);
+    const double P_k = prod[IDX(m, i, j, k)];
+    const double Y_k = DS(i, j, k);
+    const double tke_safe = smax(TK(i, j, k), dis_min);
+    const double P_w = C_eps_1 * DS(i, j, k) / tke_safe * P_k;
+    const double Y_w = C_eps_2 * f_2 * DS(i, j, k) * DS(i, j, k) / tke_safe;
+    X(m, ATSAT_F_TKE_SOURCE, i, j, k) = P_k - Y_k + L_k / c->re_turb;
+    X(m, ATSAT_F_DIS_SOURCE, i, j, k) = P_w - Y_w + L_w / c->re_turb;
+}
+
+static void turbulence_run(M* m, const atsat_dyn_turb_params* tp, double* prod, double* vel_star) {
+    const atsat_dyn_params* p = m->p;
+    const int im = m->im, jm = m->jm, km = m->km;
+    const double C_nue = 0.028, Karman = 0.42, dis_min = 1.0e-10;
+    (void)Karman;
+    TurbCtx c;
+    c.m = m;
+    c.tp = tp;
+    c.h = (float)(p->L_atm * m->dr);
+    c.L_m = p->L_atm * 1.0e3;
+    c.nue_air = tp->nue_gas;
+    c.re_turb = tp->vel_star_ref * tp->z_0 / tp->nue_gas;
+    const double u_0 = p->u_0;
+    const int per = p->phi_periodic;
+    const int k_first = per ? 0 : 1;
+    const double nue_max = tp->nue_max_phys / (u_0 * c.L_m);
+
+    /* compute_vel_star (Turbulence.h:335-378) */
+    for (int j = 0; j < jm; j++)
+        for (int k = 0; k < km; k++) {
+            double vs;
+            if (tp->turb_free) vs = 0.05;
+            else {
+                const int i_surf = (0 + 1 < im - 1) ? 0 + 1 : im - 1;
+                const double v_s = X(m, ATSAT_F_V, i_surf, j, k), w_s = X(m, ATSAT_F_W, i_surf, j, k);
+                const double vw2 = v_s * v_s + w_s * w_s;
+                vs = !isfinite(vw2) ? 0.05 : clamp3(sqrt(0.002) * (u_0 * sqrt(vw2)), 0.05, tp->vel_star_max);
+            }
+            vel_star[(size_t)j * km + k] = vs;
+        }
+
+    /* compute_sources (Turbulence.h:613-882) */
+    const double k_bg_free = tp->k_bg / (u_0 * u_0);
+    #define K_BG_OF(j, k) (tp->turb_free ? k_bg_free \
+        : 0.01 * vel_star[(size_t)(j) * km + (k)] * vel_star[(size_t)(j) * km + (k)] / (sqrt(C_nue) * u_0 * u_0))
+    if (tp->clamp_pass) {
+        for (int j = 1; j < jm - 1; j++)
+            for (int k = k_first; k < km - 1; k++)
+                for (int i = 1; i < im - 1; i++) {
+                    TK(i, j, k) = smax(0.0, TK(i, j, k));
+                    DS(i, j, k) = smax(dis_min, DS(i, j, k));
+                }
+    }
+    #pragma omp parallel for collapse(2) schedule(static)
+    for (int j = 1; j < jm - 1; j++) {
+        for (int k = k_first; k < km - 1; k++) {
+            const int kw = phi_wrap(per, k - 1, km), ke = phi_wrap(per, k + 1, km);
+            const double y_mount = t_height_m(&c, 0);
+            const double k_bg_nd = K_BG_OF(j, k);
+            for (int i = 1; i < im - 1; i++) {
+                const double rm = metric_radius(m, m->rad_z[i]);
+                const double exp_rm = p->coord_stretching ? 1.0 / (rm + 1.0) : 1.0;
+                double sinthe = sin(m->the_z[j]);
+                if (sinthe == 0.0) sinthe = 1.0e-5;
+                const double costhe = cos(m->the_z[j]);
+                const double cotanthe = costhe / sinthe;
+                const double inv_rm = 1.0 / rm;
+                const double rmsinthe = rm * sinthe;
+                const double inv_2dr = 1.0 / (2.0 * m->dr);
+                const double inv_2dthe = 1.0 / (2.0 * m->dthe);
+                const double inv_2dphi = 1.0 / (2.0 * m->dphi);
+                const double inv_rm2dthe = inv_2dthe / rm;
+                const double inv_rmsinthe2dphi = inv_2dphi / rmsinthe;
+                if (!tp->clamp_pass) { TK(i, j, k) = smax(0.0, TK(i, j, k)); DS(i, j, k) = smax(dis_min, DS(i, j, k)); }
+                const double dudr = (X(m, ATSAT_F_U, i + 1, j, k) - X(m, ATSAT_F_U, i - 1, j, k)) * inv_2dr * exp_rm;
+                const double dvdr = (X(m, ATSAT_F_V, i + 1, j, k) - X(m, ATSAT_F_V, i - 1, j, k)) * inv_2dr * exp_rm;
+                const double dwdr = (X(m, ATSAT_F_W, i + 1, j, k) - X(m, ATSAT_F_W, i - 1, j, k)) * inv_2dr * exp_rm;
+                const double dudthe = (X(m, ATSAT_F_U, i, j + 1, k) - X(m, ATSAT_F_U, i, j - 1, k)) * inv_rm2dthe;
+                const double dvdthe = (X(m, ATSAT_F_V, i, j + 1, k) - X(m, ATSAT_F_V, i, j - 1, k)) * inv_rm2dthe;
+                const double dwdthe = (X(m, ATSAT_F_W, i, j + 1, k) - X(m, ATSAT_F_W, i, j - 1, k)) * inv_rm2dthe;
+                const double dudphi = (X(m, ATSAT_F_U, i, j, ke) - X(m, ATSAT_F_U, i, j, kw)) * inv_rmsinthe2dphi;
+                const double dvdphi = (X(m, ATSAT_F_V, i, j, ke) - X(m, ATSAT_F_V, i, j, kw)) * inv_rmsinthe2dphi;
+                const double dwdphi = (X(m, ATSAT_F_W, i, j, ke) - X(m, ATSAT_F_W, i, j, kw)) * inv_rmsinthe2dphi;
+                const double dtkedr = (TK(i + 1, j, k) - TK(i - 1, j, k)) * inv_2dr * exp_rm;
+                const double ddisdr = (DS(i + 1, j, k) - DS(i - 1, j, k)) * inv_2dr * exp_rm;
+                double cnue;
+                {
+                    const double dis_here = smax(DS(i, j, k), dis_min);
+                    const double tke_here = smax(TK(i, j, k), 0.0);
+                    cnue = (tp->model == ATSAT_TURB_K_EPSILON) ? C_nue * tke_here * tke_here / dis_here
+                                                               : tke_here / dis_here;
+                    cnue = smin(cnue, nue_max);
+                }
+                const double u_r = tp->curv ? X(m, ATSAT_F_U, i, j, k) * inv_rm : 0.0;
+                const double v_r = tp->curv ? X(m, ATSAT_F_V, i, j, k) * inv_rm : 0.0;
+                const double w_r = tp->curv ? X(m, ATSAT_F_W, i, j, k) * inv_rm : 0.0;
+                const double v_cot_r = v_r * cotanthe;
+                const double w_cot_r = w_r * cotanthe;
+                const double g_rr = dudr, g_rt = dudthe - v_r, g_rp = dudphi - w_r;
+                const double g_tr = dvdr, g_tt = dvdthe + u_r, g_tp = dvdphi - w_cot_r;
+                const double g_pr = dwdr, g_pt = dwdthe, g_pp = dwdphi + u_r + v_cot_r;
+                const double der = 0.66667 * (g_rr + g_tt + g_pp);
+                const double tk = TK(i, j, k);
+                prod[IDX(m, i, j, k)] = smax(0.0,
+                      (cnue * (2.0 * g_rr - der) - 0.66667 * tk) * g_rr
+                    + (cnue * (g_rt + g_tr))                     * g_rt
+                    + (cnue * (g_rp + g_pr))                     * g_rp
+                    + (cnue * (2.0 * g_tt - der) - 0.66667 * tk) * g_tt
+                    + (cnue * (g_tr + g_rt))                     * g_tr
+                    + (cnue * (g_tp + g_pt))                     * g_tp
+                    + (cnue * (2.0 * g_pp - der) - 0.66667 * tk) * g_pp
+                    + (cnue * (g_pr + g_rp))                     * g_pr
+                    + (cnue * (g_pt + g_tp))                     * g_pt);
+                const double W12 = g_rt - g_tr, W13 = g_rp - g_pr, W23 = g_tp - g_pt;
+                const double Omega = sqrt(W12 * W12 + W13 * W13 + W23 * W23);
+                if (tp->model == ATSAT_TURB_K_EPSILON) turb_k_epsilon(&c, prod, vel_star, i, j, k, y_mount);
+                else if (tp->model == ATSAT_TURB_K_OMEGA) turb_k_omega(&c, prod, i, j, k, dtkedr, ddisdr, Omega);
+                else turb_sst(&c, prod, i, j, k, y_mount, rm, sinthe, dtkedr, ddisdr, Omega);
+                if (tp->buoy != 0) {
+                    const double Pr_t = 0.9;
+                    const double T = X(m, ATSAT_F_T, i, j, k) * p->t_ref;
+                    const double dz = t_height_m(&c, i + 1) - t_height_m(&c, i - 1);
+                    const double dTdz = (X(m, ATSAT_F_T, i + 1, j, k) - X(m, ATSAT_F_T, i - 1, j, k)) * p->t_ref / dz;
+                    const double cp = p->cp_mix;
+                    double Gam = p->g / cp, fac = 1.0;
+                    if (tp->buoy == 3 && T > 0.0) {
+                        double rho = p->r_mix;
+                        if (p->local_rho) {
+                            const double r_ = X(m, ATSAT_F_RHO_MIX, i, j, k);
+                            rho = (r_ > 0.0 && isfinite(r_)) ? r_ : p->r_mix;
+                        }
+                        double A = 0.0, B = 0.0;
+                        static const int gv_[3] = { ATSAT_F_H2O, ATSAT_F_NH3, ATSAT_F_CH4 };
+                        static const int gc_[3] = { ATSAT_F_H2O_CLOUD, ATSAT_F_NH3_CLOUD, ATSAT_F_CH4_CLOUD };
+                        static const int gi_[3] = { ATSAT_F_H2O_ICE, ATSAT_F_NH3_ICE, ATSAT_F_CH4_ICE };
+                        for (int n = 0; rho > 0.0 && n < 3; n++) {
+                            const double qc = (smax(0.0, X(m, gc_[n], i, j, k)) + smax(0.0, X(m, gi_[n], i, j, k))) / rho;
+                            if (!(qc > 1.0e-9)) continue;
+                            const double qv = smax(0.0, X(m, gv_[n], i, j, k)) / rho;
+                            const double L = T >= tp->t_0[n] ? tp->lv[n] : tp->ls[n];
+                            A += L * qv / (p->R_mix * T);
+                            B += tp->ep[n] * L * L * qv / (cp * p->R_mix * T * T);
+                        }
+                        if (isfinite(A + B)) { Gam *= (1.0 + A) / (1.0 + B); fac = 1.0 + A; }
+                    }
+                    const double N2 = (T > 0.0 && dz > 0.0) ? p->g / T * (dTdz + Gam) * fac : 0.0;
+                    if (isfinite(N2) && (N2 > 0.0 || tp->buoy == 2)) {
+                        const double tL = c.L_m / u_0;
+                        X(m, ATSAT_F_TKE_SOURCE, i, j, k) -= smax(0.0, X(m, ATSAT_F_NUE, i, j, k)) * N2 * tL * tL / Pr_t;
+                    }
+                }
+                if (!tp->clamp_pass) {
+                    TK(i, j, k) = smax(k_bg_nd, TK(i, j, k));
+                    DS(i, j, k) = smax(dis_min, DS(i, j, k));
+                    X(m, ATSAT_F_NUE, i, j, k) = clamp3(X(m, ATSAT_F_NUE, i, j, k), 0.0, nue_max);
+                    const double dsm = 20.0 * DS(i, j, k) * DS(i, j, k);
+                    X(m, ATSAT_F_DIS_SOURCE, i, j, k) = clamp3(X(m, ATSAT_F_DIS_SOURCE, i, j, k), -dsm, dsm);
+                    const double tsm = 20.0 * TK(i, j, k) * DS(i, j, k);
+                    X(m, ATSAT_F_TKE_SOURCE, i, j, k) = clamp3(X(m, ATSAT_F_TKE_SOURCE, i, j, k), -tsm, tsm);
+                }
+            }
+        }
+    }
+    if (tp->clamp_pass) {
+        for (int j = 1; j < jm - 1; j++)
+            for (int k = k_first; k < km - 1; k++) {
+                const double k_bg_nd = K_BG_OF(j, k);
+                for (int i = 1; i < im - 1; i++) {
+                    TK(i, j, k) = smax(k_bg_nd, TK(i, j, k));
+                    DS(i, j, k) = smax(dis_min, DS(i, j, k));
+                    X(m, ATSAT_F_NUE, i, j, k) = clamp3(X(m, ATSAT_F_NUE, i, j, k), 0.0, nue_max);
+                    const double dsm = 20.0 * DS(i, j, k) * DS(i, j, k);
+                    X(m, ATSAT_F_DIS_SOURCE, i, j, k) = clamp3(X(m, ATSAT_F_DIS_SOURCE, i, j, k), -dsm, dsm);
+                    const double tsm = 20.0 * TK(i, j, k) * DS(i, j, k);
+                    X(m, ATSAT_F_TKE_SOURCE, i, j, k) = clamp3(X(m, ATSAT_F_TKE_SOURCE, i, j, k), -tsm, tsm);
+                }
+            }
+    }
+    #undef K_BG_OF
+
+    /* apply_wall_bc (Turbulence.h:382-423): no obstacle, so the zero-gradient copy at i = 0 everywhere */
+    for (int j = 0; j < jm; j++)
+        for (int k = 0; k < km; k++) {
+            TK(0, j, k) = TK(1, j, k);
+            DS(0, j, k) = DS(1, j, k);
+            X(m, ATSAT_F_NUE, 0, j, k) = X(m, ATSAT_F_NUE, 1, j, k);
+        }
+
+    /* clamp_nue (Turbulence.h:564-589) */
+    {
+        int i_abl = 0;
+        while (i_abl < im - 1 && t_height_m(&c, i_abl) <= tp->abl_height) i_abl++;
+        const double taper_dz = smax(1.0, t_height_m(&c, i_abl < im - 1 ? i_abl : im - 1)
+                                        - t_height_m(&c, i_abl - 1 > 0 ? i_abl - 1 : 0));
+        for (int i = 0; i < im; i++)
+            for (int j = 0; j < jm; j++)
+                for (int k = 0; k < km; k++) {
+                    double f = 1.0;
+                    if (tp->abl_taper) {
+                        const double z_agl = t_height_m(&c, i) - t_height_m(&c, 0);
+                        f = clamp3((tp->abl_height + taper_dz - z_agl) / taper_dz, 0.0, 1.0);
+                    }
+                    X(m, ATSAT_F_NUE, i, j, k) = clamp3(X(m, ATSAT_F_NUE, i, j, k), 0.0, nue_max) * f;
+                }
+    }
+
+    /* seam_copy (Turbulence.h:542-561) */
+    if (per) {
+        const int fl[7] = { ATSAT_F_TKE, ATSAT_F_DIS, ATSAT_F_TKEN, ATSAT_F_DISN, ATSAT_F_NUE,
+                            ATSAT_F_TKE_SOURCE, ATSAT_F_DIS_SOURCE };
+        for (int i = 0; i < im; i++)
+            for (int j = 0; j < jm; j++) {
+                for (int q = 0; q < 7; q++) X(m, fl[q], i, j, km - 1) = X(m, fl[q], i, j, 0);
+                prod[IDX(m, i, j, km - 1)] = prod[IDX(m, i, j, 0)];
+            }
+    }
+
+    /* fill_lid_corners (Turbulence.h:510-540); ATSAT treats the closure's arrays in its own boundary
+     * conditions (bc_turb_active = turb_active), so only the two lid corners get the mean */
+    if (tp->turb_free) {
+        const int il = im - 1;
+        if (!p->turb_active) {
+            /* bc_turb_active false: the whole lid and both pole rows by the zero-gradient copy */
+            const int fl[7] = { ATSAT_F_TKE, ATSAT_F_DIS, ATSAT_F_TKEN, ATSAT_F_DISN, ATSAT_F_NUE,
+                                ATSAT_F_TKE_SOURCE, ATSAT_F_DIS_SOURCE };
+            for (int j = 1; j < jm - 1; j++)
+                for (int k = 0; k < km; k++) {
+                    for (int q = 0; q < 7; q++) X(m, fl[q], il, j, k) = X(m, fl[q], il - 1, j, k);
+                    prod[IDX(m, il, j, k)] = prod[IDX(m, il - 1, j, k)];
+                }
+            for (int i = 0; i < im; i++)
+                for (int k = 0; k < km; k++) {
+                    for (int q = 0; q < 7; q++) {
+                        X(m, fl[q], i, 0, k) = X(m, fl[q], i, 1, k);
+                        X(m, fl[q], i, jm - 1, k) = X(m, fl[q], i, jm - 2, k);
+                    }
+                    prod[IDX(m, i, 0, k)] = prod[IDX(m, i, 1, k)];
+                    prod[IDX(m, i, jm - 1, k)] = prod[IDX(m, i, jm - 2, k)];
+                }
+        } else {
+            /* the reference's array order: tke, dis, tken, disn, nue, prod, tke_source, dis_source */
+            for (int k = 0; k < km; k++) {
+                for (int q = 0; q < 8; q++) {
+                    double* a = (q == 5) ? prod : m->f[q < 5 ? (int[]){ ATSAT_F_TKE, ATSAT_F_DIS, ATSAT_F_TKEN,
+                                                                        ATSAT_F_DISN, ATSAT_F_NUE }[q]
+                                                             : (q == 6 ? ATSAT_F_TKE_SOURCE : ATSAT_F_DIS_SOURCE)];
+                    a[IDX(m, il, 0, k)] = 0.5 * (a[IDX(m, il, 1, k)] + a[IDX(m, il - 1, 0, k)]);
+                    a[IDX(m, il, jm - 1, k)] = 0.5 * (a[IDX(m, il, jm - 2, k)] + a[IDX(m, il - 1, jm - 1, k)]);
+                }
+            }
+        }
+    }
+}
+#undef TK
+#undef DS
+
 /* ---------------- cSaturnModel.cpp:1551-1600 ---------------- */
 static void restore_var(M* m) {
     const size_t n = (size_t)m->im * m->jm * m->km;
@@ -1304,6 +1682,15 @@ int orc_clamp_negative_species(const atsat_dyn_grid* g, const atsat_dyn_params* 
     M m; int rc = setup(&m, g, p, fields, NULL, NULL, NULL, NULL);
     if (rc) return rc;
     clamp_negative_species(&m, budget);
+    return ATSAT_DYN_OK;
+}
+
+int orc_turbulence(const atsat_dyn_grid* g, const atsat_dyn_params* p, double** fields,
+                   const atsat_dyn_turb_params* tp, double* prod, double* vel_star) {
+    M m; int rc = setup(&m, g, p, fields, NULL, NULL, NULL, NULL);
+    if (rc) return rc;
+    if (!tp || !prod || !vel_star || tp->model < 0 || tp->model > 2) return ATSAT_DYN_E_INVALID;
+    turbulence_run(&m, tp, prod, vel_star);
     return ATSAT_DYN_OK;
 }
 

@@ -133,10 +133,23 @@ def clamp_negative_species(state, params, budget=None):
     return b
 
 
-def steps(state, params, nsteps: int, iter0: int = 1, glue: bool = False, budget=None):
+def turbulence(state, params, tparams=None):
+    """Turbulence<cSaturnModel>::run (Turbulence.h:306-329). Returns (prod, vel_star)."""
+    c = _Call(state, params)
+    tp = tparams if tparams is not None else abi.make_turb_params()
+    g = state.grid
+    prod = np.zeros(g.shape)
+    vs = np.zeros((g.jm, g.km))
+    _check(lib().orc_turbulence(C.byref(c.gh.s), C.byref(c.p), c.ptrs, C.byref(tp), abi.dptr(prod), abi.dptr(vs)),
+           "turbulence")
+    return prod, vs
+
+
+def steps(state, params, nsteps: int, iter0: int = 1, glue: bool = False, budget=None, tparams=None):
     """The dycore sequence of cSaturnModel::Run (cSaturnModel.cpp:864-1111 restricted to the dycore):
     density + pressure on even iterations, RK4, boundary conditions, restoreVar. glue: also the driver's
-    p_dyn filter after the pressure call and the species floor after the boundary conditions."""
+    p_dyn filter after the pressure call, the species floor after the boundary conditions and the
+    turbulence closure after restoreVar (cSaturnModel.cpp:894-897, 1101, 1116)."""
     for it in range(iter0, iter0 + nsteps):
         if it % 2 == 0:
             mixture_density(state, params)
@@ -148,3 +161,5 @@ def steps(state, params, nsteps: int, iter0: int = 1, glue: bool = False, budget
         if glue:
             clamp_negative_species(state, params, budget)
         restore_var(state, params)
+        if glue and params.get("turb_active", 1):
+            turbulence(state, params, tparams)

@@ -18,13 +18,16 @@
 //                  restoreVar(1.0). Iterations run iter0 .. iter0+nsteps-1 (iter0 defaults to 1).
 //        damp      the p_dyn filter Run applies after the pressure call (cSaturnModel.cpp:894-897)
 //        clamp     cSaturnModel::clampNegativeSpecies() (FileIO_Sat.cpp:716-772); writes its budget
-//        driver    as steps, with damp after the pressure call and clamp after the boundary conditions
+//        driver    as steps, with damp after the pressure call, clamp after the boundary conditions and
+//                  the turbulence closure after restoreVar (cSaturnModel.cpp:894-897, 1101, 1116)
+//        turb      TurbulenceSat(m).run() (Turbulence.h:306-329); writes prod, vel_star and the constants
 // Record format of both files: char name[48]; int64 count; double data[count].
 
 #include "cSaturnModel.h"
 #include "ProcessDiag.h"
 #include "PressureSolverSat.h"
 #include "BC_Sat.h"
+#include "TurbulenceSat.h"
 #include "Utils.h"
 #include "ATPhys.h"
 
@@ -217,6 +220,8 @@ public:
             damp_pdyn(m);
         } else if(op == "clamp"){
             m.clampNegativeSpecies();
+        } else if(op == "turb"){
+            TurbulenceSat(m).run();
         } else if(op == "driver"){
             // the dycore sequence with the driver's glue around it: the p_dyn filter after the pressure
             // call (cSaturnModel.cpp:894-897) and the species floor after the boundary conditions (:1101)
@@ -233,6 +238,7 @@ public:
                 BC_Sat(m).bcRadius();
                 m.clampNegativeSpecies();
                 m.restoreVar(1.0);
+                if(m.turb_active) TurbulenceSat(m).run();
             }
         } else { fprintf(stderr, "unknown op %s\n", op.c_str()); return 2; }
 
@@ -258,6 +264,15 @@ public:
             write_record(f, "clamp_cells", cells.data(), (int64_t)nf);
             write_record(f, "clamp_added_bnd", m.clamp_added_bnd.data(), (int64_t)nf);
             write_record(f, "clamp_cells_bnd", cells_bnd.data(), (int64_t)nf);
+        }
+        {
+            std::vector<double> vs((size_t)m.jm * m.km);
+            for(int j = 0; j < m.jm; j++) for(int k = 0; k < m.km; k++) vs[(size_t)j * m.km + k] = m.vel_star.y[j][k];
+            write_record(f, "vel_star", vs.data(), (int64_t)vs.size());
+            dump_array(m, f, "prod", m.prod);
+            const double tc[] = { m.ep_h2o, m.ep_nh3, m.ep_ch4, m.lv_h2o, m.lv_nh3, m.lv_ch4, m.ls_h2o, m.ls_nh3,
+                                  m.ls_ch4, m.t_0_h2o, m.t_0_nh3, m.t_0_ch4, m.abl_height };
+            write_record(f, "turb_consts", tc, (int64_t)(sizeof(tc) / sizeof(tc[0])));
         }
         write_record(f, "rad_z", m.rad.z, m.im);
         write_record(f, "the_z", m.the.z, m.jm);

@@ -43,6 +43,10 @@ CASES = {
     "damp_m1_s1": ("damp", 1, 1, True, {"damp_pdyn": 1}),
     "clamp_s3": ("clamp", 1, 3, True, {}),
     "driver4_s3": ("driver", 4, 3, True, {}),
+    # Turbulence<cSaturnModel>::run (Turbulence.h:306-329); "turb:" keys are the closure's own knobs
+    "turb_s1": ("turb", 1, 1, True, {}),
+    "turb_kw_s1": ("turb", 1, 1, True, {"turb:model": 1}),
+    "turb_ke_nf_s1": ("turb", 1, 1, True, {"turb:model": 0, "turb:turb_free": 0}),
 }
 
 # cases whose state carries planted undershoots (negative and NaN species cells) for the species floor
@@ -53,8 +57,27 @@ KNOB_ENV = {"press_line": "ATSAT_PRESS_LINE", "press_baro": "ATSAT_PRESS_BAROTRO
             "press_sweeps": "ATSAT_PRESS_SWEEPS", "damp_pdyn": "ATSAT_DAMP_PDYN"}
 
 
+TURB_ENV = {"turb:turb_free": "ATSAT_TURB_FREE", "turb:buoy": "ATSAT_TURB_BUOY", "turb:curv": "ATSAT_TURB_CURV",
+            "turb:clamp_pass": "ATSAT_TURB_CLAMP_PASS", "turb:abl_taper": "ATSAT_ABL_TAPER"}
+TURB_MODEL_NAMES = {0: "k_epsilon", 1: "k_omega", 2: "k_omega_SST"}
+
+
+def split_over(over):
+    """(the main parameters' overrides, the closure's overrides)"""
+    return ({k: v for k, v in over.items() if not k.startswith("turb:")},
+            {k[5:]: v for k, v in over.items() if k.startswith("turb:")})
+
+
 def reference_env(over):
-    return {KNOB_ENV[k]: str(v) for k, v in over.items()}
+    env = {}
+    for k, v in over.items():
+        if k == "turb:model":
+            env["ATSAT_TURB_MODEL"] = TURB_MODEL_NAMES[v]
+        elif k in TURB_ENV:
+            env[TURB_ENV[k]] = str(v)
+        else:
+            env[KNOB_ENV[k]] = str(v)
+    return env
 
 OUTPUTS = {
     "rhs": F.RHS_FIELDS + F.AUX_FIELDS + [F.P_METRIC],
@@ -67,7 +90,8 @@ OUTPUTS = {
     "clamp": [F.H2O, F.H2O_CLOUD, F.H2O_ICE, F.H2S, F.NH3, F.NH3_CLOUD, F.NH3_ICE, F.CH4, F.CH4_CLOUD, F.CH4_ICE,
               F.NH4SH],
 }
-OUTPUTS["driver"] = OUTPUTS["steps"]
+OUTPUTS["driver"] = OUTPUTS["steps"] + [F.TKE_SOURCE, F.DIS_SOURCE]
+OUTPUTS["turb"] = [F.TKE, F.DIS, F.TKEN, F.DISN, F.NUE, F.TKE_SOURCE, F.DIS_SOURCE]
 
 
 def plant_undershoots(st, seed):
@@ -92,7 +116,7 @@ def plant_undershoots(st, seed):
 def make_state(name):
     op, nsteps, seed, exercise, over = CASES[name]
     g = synth.make_grid()
-    P = abi.default_params(**over)
+    P = abi.default_params(**split_over(over)[0])
     st = synth.saturn_state(g, P, seed=seed, exercise=exercise)
     if name in PLANTED:
         plant_undershoots(st, seed)
@@ -126,6 +150,15 @@ def main(names=None):
             rec[f"sum_{fid}"] = np.array([np.sum(a), np.sum(np.abs(a)), np.max(np.abs(a))])
         if "buoy_ref_level" in out and op in ("rhs", "rk"):
             rec["buoy_ref_level"] = out["buoy_ref_level"]
+        if op == "turb":
+            a = out["prod"].ravel()
+            rec["prod_s"] = a[idx]
+            rec["prod_sum"] = np.array([np.sum(a), np.sum(np.abs(a)), np.max(np.abs(a))])
+            vs = out["vel_star"]
+            vidx = sample_index(name + "/vel_star", vs.size)
+            rec["vel_star_index"] = vidx
+            rec["vel_star_s"] = vs[vidx]
+            rec["vel_star_sum"] = np.array([np.sum(vs), np.sum(np.abs(vs)), np.max(np.abs(vs))])
         if "clamp_added" in out:
             rec["clamp_budget"] = np.concatenate([out["clamp_added"], out["clamp_cells"], out["clamp_added_bnd"],
                                                   out["clamp_cells_bnd"]])

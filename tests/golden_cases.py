@@ -42,3 +42,14 @@ def check_outputs(rec, got: dict, tol: float, label: str):
         if not (e <= tol and es <= tol and em <= tol):
             bad.append(f"{F.NAMES[fid]}: sample {e:.2e} sum {es:.2e} max {em:.2e}")
     assert not bad, f"{label}: " + "; ".join(bad)
+
+
+def check_closure_arrays(rec, prod, vel_star, tol: float):
+    """The turbulence closure's own arrays (production P_k, friction velocity) against a fixture."""
+    for got, key, idx in ((np.asarray(prod).ravel(), "prod", rec["index"]),
+                          (np.asarray(vel_star).ravel(), "vel_star", rec["vel_star_index"])):
+        ref_s, sums = rec[key + "_s"], rec[key + "_sum"]
+        scale = sums[2] if sums[2] > 0 else 1.0
+        e = float(np.max(np.abs(got[idx] - ref_s))) / scale
+        es = abs(float(np.sum(got)) - sums[0]) / max(sums[1], 1e-300)
+        assert e <= tol and es <= tol, f"{key}: sample {e:.2e} sum {es:.2e}"

@@ -12,7 +12,7 @@ from atsat_gb300 import fields as F
 from oracle import oracle
 from golden.make_golden import CASES, make_state
 
-from golden_cases import check_inputs, check_outputs, load
+from golden_cases import check_closure_arrays, check_inputs, check_outputs, load
 
 TOL_GOLDEN = 1e-12
 
@@ -32,6 +32,11 @@ def run_case(name):
     if op == "damp":
         oracle.damp_pdyn(s, P)
         return st, s, None
+    if op == "turb":
+        from atsat_gb300 import abi
+        from golden.make_golden import split_over
+        prod, vs = oracle.turbulence(s, P, abi.make_turb_params(**split_over(over)[1]))
+        return st, s, {"prod": prod, "vel_star": vs}
     if op == "rhs":
         buoy = oracle.rhs(s, P)
     elif op == "rk":
@@ -51,7 +56,9 @@ def test_oracle_against_reference_fixture(name):
     st, out, buoy = run_case(name)
     check_inputs(rec, st)
     check_outputs(rec, out.arrays, TOL_GOLDEN, name)
-    if "clamp_budget" in rec:
+    if "prod_s" in rec:
+        check_closure_arrays(rec, buoy["prod"], buoy["vel_star"], TOL_GOLDEN)
+    elif "clamp_budget" in rec:
         # reductions in another order: the clipped amounts to 1e-12, the cell counts exactly
         rb = rec["clamp_budget"]
         assert np.all(np.abs(buoy - rb) <= 1e-12 * np.maximum(np.abs(rb), 1e-300)), (buoy, rb)
