@@ -47,6 +47,11 @@ struct atsat_dyn {
     // PRESS_LINE / PRESS_BAROTROPIC: forward-sweep scratch of the line pass, interior-mean partials and
     // the means on entry and after a sweep, the barotropic tables and scratch (one allocation)
     double* pv_buf = nullptr;
+    // the turbulence closure: its knobs, one allocation for P_k (fsz), u_tau (jm x kp) and the tables
+    atsat_dyn_turb_params tp{};
+    double* turb_buf = nullptr;
+    double *turb_prod = nullptr, *turb_vs = nullptr;
+    TurbTables ttab{};
     // clampNegativeSpecies' budget: added[11], added_bnd[11] (doubles), cells[11], cells_bnd[11] (counts)
     double* clamp_added = nullptr;
     unsigned long long* clamp_cells = nullptr;
@@ -1350,6 +1355,93 @@ int setup_press_variants(atsat_dyn* h) {
     return ATSAT_DYN_OK;
 }
 
+// The closure's buffers and tables (Turbulence.h:243-269 geometry, cSaturnModel.h:1062-1074, 686-692).
+int setup_turbulence(atsat_dyn* h) {
+    const KConst& K = h->kc;
+    const atsat_dyn_params& p = h->p;
+    const atsat_dyn_grid& g = h->g;
+    const int im = K.im, jm = K.jm;
+    const int64_t n_tab = 5LL * im + 2LL * jm + (int64_t)im * jm;
+    const int64_t total = K.fsz + (int64_t)jm * K.kp + n_tab + 16;
+    cudaError_t e = cudaMalloc(&h->turb_buf, (size_t)total * 8);
+    if (e != cudaSuccess) { h->turb_buf = nullptr; return fail(h, ATSAT_DYN_E_NOMEM, "turbulence: %s", cudaGetErrorString(e)); }
+    e = cudaMemset(h->turb_buf, 0, (size_t)total * 8);
+    if (e != cudaSuccess) return fail(h, ATSAT_DYN_E_CUDA, "turbulence: %s", cudaGetErrorString(e));
+    double* q = h->turb_buf;
+    h->turb_prod = q; q += K.fsz;
+    h->turb_vs = q; q += (int64_t)jm * K.kp;
+    std::vector<double> t((size_t)n_tab);
+    double* rm = t.data();
+    double* inv_rm = rm + im;
+    double* inv_rm2dthe = inv_rm + im;
+    double* height = inv_rm2dthe + im;
+    double* thick = height + im;
+    double* sinthe = thick + im;
+    double* cot = sinthe + jm;
+    double* irs = cot + jm;
+    const float hl = (float)(p.L_atm * g.dr);           // the model's float layer spacing, km
+    const double inv_2dthe = 1.0 / (2.0 * g.dthe), inv_2dphi = 1.0 / (2.0 * g.dphi);
+    for (int i = 0; i < im; i++) {
+        rm[i] = metric_radius(p, h->rad_z[i]);
+        inv_rm[i] = 1.0 / rm[i];
+        inv_rm2dthe[i] = inv_2dthe / rm[i];
+        height[i] = (double)((float)i * hl) * 1.0e3;
+        thick[i] = (i > im - 2) ? 0.0 : (double)((float)(i + 1) * hl - (float)i * hl) * 1.0e3;
+    }
+    for (int j = 0; j < jm; j++) {
+        double sv = std::sin(h->the_z[j]);
+        if (sv == 0.0) sv = 1.0e-5;
+        sinthe[j] = sv;
+        cot[j] = std::cos(h->the_z[j]) / sv;
+    }
+    for (int i = 0; i < im; i++)
+        for (int j = 0; j < jm; j++) irs[(size_t)i * jm + j] = inv_2dphi / (rm[i] * sinthe[j]);
+    double* d = q;
+    e = cudaMemcpy(d, t.data(), (size_t)n_tab * 8, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(h, ATSAT_DYN_E_CUDA, "turbulence tables: %s", cudaGetErrorString(e));
+    TurbTables& T = h->ttab;
+    T.rm = d; T.inv_rm = d + im; T.inv_rm2dthe = d + 2 * im; T.height_m = d + 3 * im; T.thick_m = d + 4 * im;
+    T.sinthe = d + 5 * im; T.cotanthe = d + 5 * im + jm; T.inv_rmsinthe2dphi = d + 5 * im + 2 * jm;
+    T.dr = g.dr; T.dthe = g.dthe; T.dphi = g.dphi;
+    return ATSAT_DYN_OK;
+}
+
+// the ABL taper's layer step (Turbulence.h:569-574), from the model's float layer table
+double turb_taper_dz(const atsat_dyn* h) {
+    const int im = h->kc.im;
+    const float hl = (float)(h->p.L_atm * h->g.dr);
+    auto height = [&](int i) { return (double)((float)i * hl) * 1.0e3; };
+    int i_abl = 0;
+    while (i_abl < im - 1 && height(i_abl) <= h->tp.abl_height) i_abl++;
+    const double a = height(i_abl < im - 1 ? i_abl : im - 1), b = height(i_abl - 1 > 0 ? i_abl - 1 : 0);
+    return std::max(1.0, a - b);
+}
+
+// Turbulence<cSaturnModel>::run on the device fields. It runs after restoreVar and changes the live k* and
+// omega* only, so the next step starts from the n-level values restoreVar saved (its y_n) with the live
+// ones as its stage-0 input (RungeKutta_Sat_Turb.cpp:250-320). A resident mixed run shares the live and
+// n-level storage after restoreVar, so it gives the n-level fields their own copies first; the next step
+// then rebuilds its FP32 copies of y_n and the stage-0 increment live - y_n.
+int enqueue_turbulence(atsat_dyn* h, bool resident = false) {
+    if (!h->turb_buf) {
+        int rc = setup_turbulence(h);
+        if (rc) return rc;
+    }
+    if (resident && h->p.precision == ATSAT_DYN_MIXED) {
+        int rc = unalias(h);
+        if (rc) return rc;
+    }
+    h->ttab.taper_dz = turb_taper_dz(h);
+    {
+        Timed t(h, ATSAT_K_GLUE);
+        int n = 0;
+        CK(h, launch_turbulence(h->kc, h->p, h->tp, h->ttab, h->f, h->turb_prod, h->turb_vs, h->stream, &n));
+        h->launches += n;
+    }
+    for (int fid : {ATSAT_F_NUE, ATSAT_F_TKE_SOURCE, ATSAT_F_DIS_SOURCE}) mark_dirty(h, fid);
+    return ATSAT_DYN_OK;
+}
+
 int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_dyn_t* out) {
     if (!g || !p || !out || !g->rad_z || !g->the_z) return ATSAT_DYN_E_INVALID;
     *out = nullptr;
@@ -1451,6 +1543,12 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
                              h->stream)) ||
         (e = cudaStreamSynchronize(h->stream)))
         return cuda_fail(e, "table upload");
+    atsat_dyn_turb_params_default(&h->tp);
+    if (p->turb_active) {
+        *out = h;
+        const int trc = setup_turbulence(h);
+        if (trc) return trc;
+    }
     if ((e = cudaMalloc(&h->clamp_added, 22 * 8 + 22 * 8)) != cudaSuccess) return cuda_fail(e, "cudaMalloc (budget)");
     h->clamp_cells = reinterpret_cast<unsigned long long*>(h->clamp_added + 22);
     if ((e = cudaMemset(h->clamp_added, 0, 44 * 8)) != cudaSuccess) return cuda_fail(e, "cudaMemset (budget)");
@@ -1467,6 +1565,7 @@ void atsat_dyn_destroy(atsat_dyn_t h) {
     poisson_destroy(h->poisson);
     if (h->pv_buf) cudaFree(h->pv_buf);
     if (h->clamp_added) cudaFree(h->clamp_added);
+    if (h->turb_buf) cudaFree(h->turb_buf);
     if (h->graph) cudaGraphExecDestroy(h->graph);
     if (h->slab) cudaFree(h->slab);
     if (h->slab32) cudaFree(h->slab32);
@@ -1699,6 +1798,72 @@ int atsat_dyn_clamp_negative_species(atsat_dyn_t h) {
     return rc ? rc : finish(h);
 }
 
+int atsat_dyn_turb_params_default(atsat_dyn_turb_params* tp) {
+    if (!tp) return ATSAT_DYN_E_INVALID;
+    *tp = atsat_dyn_turb_params{};
+    tp->model = ATSAT_TURB_K_OMEGA_SST; tp->turb_free = 1; tp->clamp_pass = 1; tp->abl_taper = 0; tp->curv = 1;
+    tp->buoy = 3;                                  // cSaturnModel::turb_default_buoy() (cSaturnModel.h:299)
+    tp->k_bg = 1.0; tp->l_bg = 0.0; tp->nue_max_phys = 1.0e5; tp->vel_star_max = std::sqrt(0.002) * 200.0;
+    tp->vel_star_ref = 0.4; tp->z_0 = 0.1; tp->nue_gas = 1.8e-5;       // TurbulenceSat's constructor defaults
+    tp->abl_height = 20000.0;                                          // cSaturnModel.h:1281
+    // H2O, NH3, CH4: the moist gases of cSaturnModel::moist_gas_for_turb (cSaturnModel.cpp:259-266), values
+    // read back from the reference's build
+    const double ep[3] = {8.1253, 7.6752, 7.6752}, lv[3] = {2.5009e6, 1.372e6, 5.11e5};
+    const double ls[3] = {2.8339e6, 1.832e6, 5.11e5}, t0[3] = {273.15, 195.5, 90.69};
+    for (int n = 0; n < 3; n++) { tp->ep[n] = ep[n]; tp->lv[n] = lv[n]; tp->ls[n] = ls[n]; tp->t_0[n] = t0[n]; }
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_turb_params_from_env(atsat_dyn_turb_params* tp) {
+    if (!tp) return ATSAT_DYN_E_INVALID;
+    if (const char* e = getenv("ATSAT_TURB_MODEL")) {
+        const std::string m(e);
+        tp->model = m == "k_epsilon" ? ATSAT_TURB_K_EPSILON : (m == "k_omega" ? ATSAT_TURB_K_OMEGA : ATSAT_TURB_K_OMEGA_SST);
+    }
+    if (const char* e = getenv("ATSAT_TURB_FREE")) tp->turb_free = atoi(e);
+    if (const char* e = getenv("ATSAT_TURB_CLAMP_PASS")) tp->clamp_pass = atoi(e);
+    if (const char* e = getenv("ATSAT_ABL_TAPER")) tp->abl_taper = atoi(e);
+    if (const char* e = getenv("ATSAT_TURB_CURV")) tp->curv = atoi(e) != 0;
+    if (const char* e = getenv("ATSAT_TURB_BUOY")) tp->buoy = atoi(e);
+    if (const char* e = getenv("ATSAT_TURB_K_BG")) tp->k_bg = atof(e);
+    if (const char* e = getenv("ATSAT_TURB_L_BG")) tp->l_bg = atof(e);
+    if (const char* e = getenv("ATSAT_NUE_MAX")) tp->nue_max_phys = atof(e);
+    if (const char* e = getenv("ATSAT_VEL_STAR_MAX")) tp->vel_star_max = atof(e);
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_set_turb_params(atsat_dyn_t h, const atsat_dyn_turb_params* tp) {
+    if (!h || !h->slab || !tp) return ATSAT_DYN_E_INVALID;
+    if (tp->model < ATSAT_TURB_K_EPSILON || tp->model > ATSAT_TURB_K_OMEGA_SST)
+        return fail(h, ATSAT_DYN_E_INVALID, "turbulence: unknown model %d", tp->model);
+    if (!tp->clamp_pass)
+        return fail(h, ATSAT_DYN_E_UNSUPPORTED, "ATSAT_TURB_CLAMP_PASS=0: the reference's sources then read neighbours "
+                    "other threads are flooring, so its result depends on the thread count (Turbulence.h:165-173)");
+    h->tp = *tp;
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_turbulence(atsat_dyn_t h) {
+    ENTRY(h);
+    { int rc0 = unalias(h); if (rc0) return rc0; }
+    int rc = enqueue_turbulence(h);
+    return rc ? rc : finish(h);
+}
+
+int atsat_dyn_turbulence_diag(atsat_dyn_t h, double* prod, double* vel_star) {
+    ENTRY(h);
+    if (!h->turb_buf) return fail(h, ATSAT_DYN_E_INVALID, "turbulence_diag: the closure has not run");
+    const KConst& K = h->kc;
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (prod)
+        CK(h, cudaMemcpy2D(prod, (size_t)K.km * 8, h->turb_prod, (size_t)K.kp * 8, (size_t)K.km * 8,
+                           (size_t)K.im * K.jm, cudaMemcpyDeviceToHost));
+    if (vel_star)
+        CK(h, cudaMemcpy2D(vel_star, (size_t)K.km * 8, h->turb_vs, (size_t)K.kp * 8, (size_t)K.km * 8, (size_t)K.jm,
+                           cudaMemcpyDeviceToHost));
+    return ATSAT_DYN_OK;
+}
+
 int atsat_dyn_clamp_budget(atsat_dyn_t h, double* added, int64_t* cells, double* added_bnd, int64_t* cells_bnd) {
     ENTRY(h);
     if (!added || !cells || !added_bnd || !cells_bnd) return fail(h, ATSAT_DYN_E_INVALID, "clamp_budget: null output");
@@ -1737,7 +1902,9 @@ int enqueue_iteration(atsat_dyn* h, int32_t it) {
     if ((rc = enqueue_rk4(h, true))) return rc;
     if ((rc = enqueue_bc(h, true))) return rc;
     if (h->p.driver_glue && (rc = enqueue_clamp(h, true))) return rc;
-    return enqueue_restore(h, true);
+    if ((rc = enqueue_restore(h, true))) return rc;
+    if (h->p.driver_glue && h->p.turb_active && (rc = enqueue_turbulence(h, true))) return rc;
+    return ATSAT_DYN_OK;
 }
 
 bool resident_steady(const atsat_dyn* h) {

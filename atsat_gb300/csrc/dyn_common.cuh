@@ -351,6 +351,18 @@ cudaError_t launch_damp_axis(const KConst& kc, const double* tmp, double* f, dou
 cudaError_t launch_clamp_species(const KConst& kc, double* const f[11], float* const s32[11], double* added,
                                  unsigned long long* cells, cudaStream_t s);
 
+// Turbulence<cSaturnModel>::run (turbulence.cu). Device tables per level i and row j, formed on the host with
+// the reference's expressions; height_m / thick_m from the model's float layer table.
+struct TurbTables {
+    const double *rm, *inv_rm, *inv_rm2dthe, *height_m, *thick_m;   // im
+    const double *sinthe, *cotanthe;                                // jm: exact-zero guard, no floor
+    const double* inv_rmsinthe2dphi;                                // im x jm
+    double dr, dthe, dphi, taper_dz;
+};
+cudaError_t launch_turbulence(const KConst& K, const atsat_dyn_params& p, const atsat_dyn_turb_params& tp,
+                              const TurbTables& tab, double* const* f, double* prod, double* vel_star, cudaStream_t s,
+                              int* launches);
+
 // PRESS_LINE / PRESS_BAROTROPIC (press_variants.cu)
 struct BaroTables {
     double A2;                                    // sum over i = 1..im-2 of 1 / rm^2

@@ -92,6 +92,11 @@ def lib():
         L.atsat_dyn_conv_selftest.argtypes = [C.c_int32, C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.atsat_dyn_damp_wiggles.argtypes = [H, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_int32]
         L.atsat_dyn_damp_pdyn.argtypes = [H]
+        L.atsat_dyn_turb_params_default.argtypes = [C.POINTER(abi.TurbParams)]
+        L.atsat_dyn_turb_params_from_env.argtypes = [C.POINTER(abi.TurbParams)]
+        L.atsat_dyn_set_turb_params.argtypes = [H, C.POINTER(abi.TurbParams)]
+        L.atsat_dyn_turbulence.argtypes = [H]
+        L.atsat_dyn_turbulence_diag.argtypes = [H, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.atsat_dyn_clamp_negative_species.argtypes = [H]
         L.atsat_dyn_clamp_budget.argtypes = [H, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                              C.POINTER(C.c_int64)]
@@ -310,6 +315,22 @@ class Dycore:
     def damp_pdyn(self):
         """The p_dyn filter of cSaturnModel::Run after the pressure call (cSaturnModel.cpp:894-897)."""
         self._ck(lib().atsat_dyn_damp_pdyn(self.h), "damp_pdyn")
+
+    def set_turb_params(self, tp):
+        """The closure's knobs (abi.TurbParams, e.g. abi.make_turb_params(model=1))."""
+        self._ck(lib().atsat_dyn_set_turb_params(self.h, C.byref(tp)), "set_turb_params")
+
+    def TurbulenceSat_run(self):
+        """Turbulence<cSaturnModel>::run on the device fields (Turbulence.h:306-329)."""
+        self._ck(lib().atsat_dyn_turbulence(self.h), "turbulence")
+
+    def turbulence_diag(self):
+        """(P_k over the grid, u_tau per (j, k)) after the last closure run."""
+        g = self.grid
+        prod = np.zeros(g.shape)
+        vs = np.zeros((g.jm, g.km))
+        self._ck(lib().atsat_dyn_turbulence_diag(self.h, abi.dptr(prod), abi.dptr(vs)), "turbulence_diag")
+        return prod, vs
 
     def clampNegativeSpecies(self):
         self._ck(lib().atsat_dyn_clamp_negative_species(self.h), "clamp_negative_species")

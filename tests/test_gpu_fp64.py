@@ -237,6 +237,47 @@ def test_iterate_with_driver_glue(shape):
     assert np.allclose(budget, rb, rtol=1e-9, atol=0.0)
 
 
+TURB_VARIANTS = [dict(), dict(model=1), dict(model=0), dict(turb_free=0), dict(buoy=1), dict(buoy=2, curv=0),
+                 dict(abl_taper=1, nue_max_phys=1e-3), dict(buoy=0, model=0, turb_free=0)]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_turbulence_default(shape):
+    """Turbulence<cSaturnModel>::run (SST, moist buoyancy sink) against the oracle, which equals the reference."""
+    _turbulence_case(shape, {})
+
+
+@pytest.mark.parametrize("over", TURB_VARIANTS[1:], ids=lambda d: ",".join(f"{k}={v}" for k, v in d.items()))
+def test_turbulence_variants(over):
+    _turbulence_case((12, 40, 70), over)
+
+
+def _turbulence_case(shape, over):
+    from atsat_gb300 import abi, dyn
+    g, P, st = case(shape, seed=35)
+    tp = abi.make_turb_params(**over)
+    ref = st.copy()
+    rprod, rvs = oracle.turbulence(ref, P, tp)
+    s = st.copy()
+    with dyn.Dycore(g, P) as d:
+        d.load_state(s)
+        d.set_turb_params(tp)
+        d.TurbulenceSat_run()
+        d.download(ALL)
+        prod, vs = d.turbulence_diag()
+    compare(s.arrays, ref.arrays, ALL, TOL_FP64, f"turbulence {over} {shape}")
+    assert np.max(np.abs(prod - rprod)) <= TOL_FP64 * max(np.max(np.abs(rprod)), 1e-300)
+    assert np.max(np.abs(vs - rvs)) <= TOL_FP64 * np.max(np.abs(rvs))
+
+
+def test_turbulence_clamp_pass_off_unsupported():
+    from atsat_gb300 import abi, dyn
+    g, P, st = case((9, 13, 17), seed=37)
+    with dyn.Dycore(g, P) as d:
+        with pytest.raises(dyn.DycoreError):
+            d.set_turb_params(abi.make_turb_params(clamp_pass=0))
+
+
 def test_pressure_clamp_count():
     from atsat_gb300 import dyn
     g, P, st = case((9, 13, 17), seed=9, pdyn_cap=1e-9)

@@ -5,7 +5,7 @@ import pytest
 from atsat_gb300 import fields as F
 from golden.make_golden import CASES, make_state
 
-from golden_cases import check_inputs, check_outputs, load
+from golden_cases import check_closure_arrays, check_inputs, check_outputs, load
 from helpers import TOL_FP64
 
 pytestmark = pytest.mark.gpu
@@ -29,6 +29,12 @@ def test_gpu_against_reference_fixture(name):
             d.damp_pdyn()
         elif op == "clamp":
             d.clampNegativeSpecies()
+        elif op == "turb":
+            from atsat_gb300 import abi
+            from golden.make_golden import split_over
+            d.set_turb_params(abi.make_turb_params(**split_over(over)[1]))
+            d.TurbulenceSat_run()
+            closure = d.turbulence_diag()
         elif op == "rhs":
             d.computeBuoyancyRefLevel()
             d.computeMetricPressure()
@@ -44,6 +50,8 @@ def test_gpu_against_reference_fixture(name):
         if op in ("clamp", "driver"):
             budget = d.clamp_budget()
     check_outputs(rec, s.arrays, TOL_FP64, name)
+    if op == "turb":
+        check_closure_arrays(rec, closure[0], closure[1], TOL_FP64)
     if budget is not None:
         rb = rec["clamp_budget"]
         n = len(rb) // 4
