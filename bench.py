@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--poisson", action="store_true",
                     help="the standalone pressure-equation solves instead of the dycore iteration")
     ap.add_argument("--sor-sweeps", type=int, default=4000)
+    ap.add_argument("--glue", action="store_true",
+                    help="time the driver's glue (p_dyn filter, species floor, turbulence closure) per call and per iteration")
     ap.add_argument("--press-variants", action="store_true",
                     help="time one pressure call with and without PRESS_LINE / PRESS_BAROTROPIC")
     ap.add_argument("--ensemble", action="store_true",
@@ -479,6 +481,55 @@ def run_press_variants(a, rank, world):
             "variants": out}
 
 
+def run_glue(a, rank, world):
+    """The driver's glue around the dycore at the workload grid: one call each of the p_dyn filter
+    (damp_wiggles), the species floor (clampNegativeSpecies) and the turbulence closure (Turbulence::run),
+    device time from CUDA events around K calls after W warm-up calls, beside the oracle's OpenMP
+    restatement of one call on the host cores; and whole iterations of the resident loop with the glue
+    (params.driver_glue = 1) against the plain dycore loop, mixed and FP64."""
+    if rank != 0:
+        return None
+    from atsat_gb300 import abi, dyn, synth
+    from oracle import oracle
+    g = synth.make_grid(*a.shape)
+    P = abi.default_params()
+    st = synth.saturn_state(g, P, seed=13, exercise=True)
+    calls = {}
+    for name, fn, ofn in (("damp_pdyn", "damp_pdyn", oracle.damp_pdyn),
+                          ("clampNegativeSpecies", "clampNegativeSpecies", oracle.clamp_negative_species),
+                          ("TurbulenceSat_run", "TurbulenceSat_run", oracle.turbulence)):
+        t0 = time.perf_counter()
+        ofn(st.copy(), P)
+        cpu_s = time.perf_counter() - t0
+        with dyn.Dycore(g, P) as d:
+            d.load_state(st)
+            for _ in range(a.warmup):
+                getattr(d, fn)()
+            d.timer_start()
+            for _ in range(a.steps):
+                getattr(d, fn)()
+            ms = d.timer_stop() / a.steps
+        calls[name] = {"device_ms_per_call": ms, "cpu_oracle_s_per_call": cpu_s, "cpu_cores": os.cpu_count()}
+    loops = {}
+    for prec in ("mixed", "fp64"):
+        for glue in (0, 1):
+            with dyn.Dycore(g, dict(P, precision=1 if prec == "mixed" else 0, driver_glue=glue)) as d:
+                d.load_state(st)
+                if prec == "mixed":
+                    d.set_stage_variant(dyn.Dycore.STAGE_NAMES.index("tiled2"))
+                d.iterate(1, a.warmup)
+                d.timer_start()
+                d.iterate(a.warmup + 1, a.steps)
+                ms = d.timer_stop() / a.steps
+            loops[f"{prec}{'_glue' if glue else ''}"] = {"ms_per_iteration": ms,
+                                                          "Mcell_steps_per_s": g.cells / (ms / 1e3) / 1e6}
+    return {"metric": "driver glue around the dycore, 1 GB300, FP64 device time per call and per iteration",
+            "value": loops["mixed_glue"]["Mcell_steps_per_s"], "unit": UNIT + " (mixed, iteration with the glue)",
+            "higher_is_better": True, "n_gpus": 1, "data": "synthetic", "steps": a.steps, "warmup": a.warmup,
+            "config": {"workload": f"{g.im}x{g.jm}x{g.km}, seeded synthetic state with every input exercised"},
+            "calls": calls, "iterations": loops}
+
+
 def run_ensemble(a, rank, world):
     """32 independent members, 16 at 21x91x181, 12 at 41x181x361 and 4 at 61x271x541, each from the seeded
     generator with its own seed and noise amplitude U[0.5, 2], mixed precision, stage kernels autotuned per
@@ -542,6 +593,8 @@ def main():
         res = run_poisson(a, rank, world)
     elif a.press_variants:
         res = run_press_variants(a, rank, world)
+    elif a.glue:
+        res = run_glue(a, rank, world)
     else:
         res = run_reference(a, rank, world) if a.impl == "reference" else run_ours(a, rank, world)
     if rank == 0 and res is not None:
