@@ -1864,6 +1864,190 @@ int atsat_dyn_turbulence_diag(atsat_dyn_t h, double* prod, double* vel_star) {
     return ATSAT_DYN_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// cSaturnModel::restart_arrays and restart_arrays_carried (FileIO_Sat.cpp:513-552), in file order: a device
+// field id, or -1 - n for the caller's host array n. The carried list's last entry (S_precip_ch4) is SAT3 only.
+const int RESTART_MAIN[38] = {
+    ATSAT_F_T, ATSAT_F_U, ATSAT_F_V, ATSAT_F_W, ATSAT_F_TN, ATSAT_F_UN, ATSAT_F_VN, ATSAT_F_WN,
+    ATSAT_F_H2O, ATSAT_F_H2O_CLOUD, ATSAT_F_H2O_ICE, ATSAT_F_H2ON, ATSAT_F_H2O_CLOUDN, ATSAT_F_H2O_ICEN,
+    ATSAT_F_H2S, ATSAT_F_H2SN,
+    ATSAT_F_NH3, ATSAT_F_NH3_CLOUD, ATSAT_F_NH3_ICE, ATSAT_F_NH3N, ATSAT_F_NH3_CLOUDN, ATSAT_F_NH3_ICEN,
+    ATSAT_F_CH4, ATSAT_F_CH4_CLOUD, ATSAT_F_CH4_ICE, ATSAT_F_CH4N, ATSAT_F_CH4_CLOUDN, ATSAT_F_CH4_ICEN,
+    ATSAT_F_NH4SH, ATSAT_F_NH4SHN,
+    ATSAT_F_P_DYN, ATSAT_F_P_DYNN, ATSAT_F_P_STAT,
+    ATSAT_F_TKE, ATSAT_F_DIS, ATSAT_F_TKEN, ATSAT_F_DISN, ATSAT_F_NUE};
+const int RESTART_CARRIED[35] = {
+    ATSAT_F_TKE_SOURCE, ATSAT_F_DIS_SOURCE,
+    -1, -2, -3,                                          // difflux_h2s, _nh3, _nh4sh
+    -4, -5, -6,                                          // j_h2s, _nh3, _nh4sh
+    ATSAT_F_MASSFLUX_H2S, ATSAT_F_MASSFLUX_NH3, ATSAT_F_MASSFLUX_NH4SH,
+    ATSAT_F_THERMALMASSFLUX, ATSAT_F_FLUXLIM_NH4SH,
+    ATSAT_F_RHS_U, ATSAT_F_RHS_V,
+    ATSAT_F_RHO_MIX, ATSAT_F_Q_PRECIP,
+    ATSAT_F_S_PRECIP_H2O, ATSAT_F_S_PRECIP_H2O_CLOUD, ATSAT_F_S_PRECIP_H2O_ICE,
+    ATSAT_F_S_PRECIP_NH3, ATSAT_F_S_PRECIP_NH3_ICE,
+    ATSAT_F_S_PRECIP_NH3_CLOUD, ATSAT_F_S_PRECIP_CH4_CLOUD, ATSAT_F_S_PRECIP_CH4_ICE,
+    -7, -8, -9,                                          // w_h2s, _nh3, _nh4sh
+    -10, -11, -12, -13, -14, -15,                        // BuoyancyForce, PresGradForce, Q_Sensible, jT_*
+    ATSAT_F_S_PRECIP_CH4};
+constexpr int32_t MAGIC_SAT1 = 0x53415431, MAGIC_SAT2 = 0x53415432, MAGIC_SAT3 = 0x53415433;
+
+std::vector<int> restart_list(int format) {
+    std::vector<int> v(RESTART_MAIN, RESTART_MAIN + 38);
+    if (format >= 2) v.insert(v.end(), RESTART_CARRIED, RESTART_CARRIED + (format == 3 ? 35 : 34));
+    return v;
+}
+
+// two pinned buffers of im*jm*km doubles for the restart streams, allocated on first use
+int restart_buffers(atsat_dyn* h, double** buf) {
+    static_assert(sizeof(double) == 8, "double");
+    const size_t bytes = (size_t)h->kc.im * h->kc.jm * h->kc.km * 8;
+    for (int b = 0; b < 2; b++) {
+        const cudaError_t e = cudaHostAlloc(&buf[b], bytes, cudaHostAllocDefault);
+        if (e != cudaSuccess) {
+            if (b) cudaFreeHost(buf[0]);
+            return fail(h, ATSAT_DYN_E_NOMEM, "restart staging: %s", cudaGetErrorString(e));
+        }
+    }
+    return ATSAT_DYN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int atsat_dyn_save_restart(atsat_dyn_t h, const char* path, int32_t iter, int32_t carried,
+                           const double* const* host_arrays) {
+    ENTRY(h);
+    if (!path) return fail(h, ATSAT_DYN_E_INVALID, "save_restart: null path");
+    const KConst& K = h->kc;
+    const size_t n = (size_t)K.im * K.jm * K.km;
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(h, ATSAT_DYN_E_INVALID, "save_restart: cannot open %s", path);
+    const int32_t hdr[5] = {carried ? MAGIC_SAT3 : MAGIC_SAT1, K.im, K.jm, K.km, iter};
+    bool ok = fwrite(hdr, sizeof(hdr), 1, f) == 1;
+    double* buf[2] = {nullptr, nullptr};
+    int rc = restart_buffers(h, buf);
+    if (rc) { fclose(f); return rc; }
+    cudaEvent_t ev[2];
+    cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+    std::vector<double> zeros;
+    const std::vector<int> list = restart_list(carried ? 3 : 1);
+    // device field q: a pitched-to-contiguous copy into buffer q & 1 while the previous one is written out
+    auto fetch = [&](size_t q) -> cudaError_t {
+        const int id = list[q];
+        if (id < 0) return cudaSuccess;
+        const int b = (int)(q & 1);
+        cudaError_t e = cudaMemcpy2DAsync(buf[b], (size_t)K.km * 8, h->f[id], (size_t)K.kp * 8, (size_t)K.km * 8,
+                                          (size_t)K.im * K.jm, cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[b], h->stream);
+        return e;
+    };
+    cudaError_t e = list.empty() ? cudaSuccess : fetch(0);
+    for (size_t q = 0; q < list.size() && ok && e == cudaSuccess; q++) {
+        if (q + 1 < list.size()) e = fetch(q + 1);
+        if (e != cudaSuccess) break;
+        const int id = list[q];
+        const double* src;
+        if (id >= 0) {
+            e = cudaEventSynchronize(ev[q & 1]);
+            src = buf[q & 1];
+        } else {
+            src = host_arrays ? host_arrays[-1 - id] : nullptr;
+            if (!src) {
+                if (zeros.empty()) zeros.assign(n, 0.0);
+                src = zeros.data();
+            }
+        }
+        ok = e == cudaSuccess && fwrite(src, 8, n, f) == n;
+    }
+    cudaStreamSynchronize(h->stream);
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    cudaFreeHost(buf[0]);
+    cudaFreeHost(buf[1]);
+    ok = (fclose(f) == 0) && ok;
+    if (e != cudaSuccess) return fail(h, ATSAT_DYN_E_CUDA, "save_restart: %s", cudaGetErrorString(e));
+    if (!ok) return fail(h, ATSAT_DYN_E_INVALID, "save_restart: write failed on %s (disk full?)", path);
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_load_restart(atsat_dyn_t h, const char* path, int32_t* iter, int32_t* format, double* const* host_arrays) {
+    ENTRY(h);
+    if (!path) return fail(h, ATSAT_DYN_E_INVALID, "load_restart: null path");
+    const KConst& K = h->kc;
+    const size_t n = (size_t)K.im * K.jm * K.km;
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(h, ATSAT_DYN_E_INVALID, "load_restart: no file %s", path);
+    int32_t hdr[5];
+    const bool got = fread(hdr, sizeof(hdr), 1, f) == 1;
+    const int fmt = !got ? 0 : hdr[0] == MAGIC_SAT3 ? 3 : hdr[0] == MAGIC_SAT2 ? 2 : hdr[0] == MAGIC_SAT1 ? 1 : 0;
+    if (!fmt || hdr[1] != K.im || hdr[2] != K.jm || hdr[3] != K.km) {
+        fclose(f);
+        return fail(h, ATSAT_DYN_E_INVALID, "load_restart: bad header / grid mismatch in %s", path);
+    }
+    { int rc0 = unalias(h); if (rc0) { fclose(f); return rc0; } }
+    double* buf[2] = {nullptr, nullptr};
+    int rc = restart_buffers(h, buf);
+    if (rc) { fclose(f); return rc; }
+    cudaEvent_t ev[2];
+    cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+    bool recorded[2] = {false, false};
+    const std::vector<int> list = restart_list(fmt);
+    bool ok = true;
+    cudaError_t e = cudaSuccess;
+    for (size_t q = 0; q < list.size() && ok && e == cudaSuccess; q++) {
+        const int id = list[q];
+        if (id >= 0) {
+            const int b = (int)(q & 1);
+            if (recorded[b]) e = cudaEventSynchronize(ev[b]);      // the buffer's previous upload is done
+            if (e != cudaSuccess) break;
+            ok = fread(buf[b], 8, n, f) == n;
+            if (!ok) break;
+            e = cudaMemcpy2DAsync(h->f[id], (size_t)K.kp * 8, buf[b], (size_t)K.km * 8, (size_t)K.km * 8,
+                                  (size_t)K.im * K.jm, cudaMemcpyHostToDevice, h->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[b], h->stream);
+            recorded[b] = true;
+            mark_dirty(h, id);
+        } else {
+            double* dst = host_arrays ? host_arrays[-1 - id] : nullptr;
+            ok = dst ? fread(dst, 8, n, f) == n : fseek(f, (long)(n * 8), SEEK_CUR) == 0;
+        }
+    }
+    cudaStreamSynchronize(h->stream);
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    cudaFreeHost(buf[0]);
+    cudaFreeHost(buf[1]);
+    fclose(f);
+    if (e != cudaSuccess) return fail(h, ATSAT_DYN_E_CUDA, "load_restart: %s", cudaGetErrorString(e));
+    if (!ok) return fail(h, ATSAT_DYN_E_INVALID, "load_restart: truncated file %s", path);
+    if (iter) *iter = hdr[4];
+    if (format) *format = fmt;
+    return finish(h);
+}
+
+int atsat_dyn_restart_is_clean(atsat_dyn_t h, int32_t* clean) {
+    ENTRY(h);
+    if (!clean) return fail(h, ATSAT_DYN_E_INVALID, "restart_is_clean: null output");
+    const double* fl[38];
+    for (int q = 0; q < 38; q++) fl[q] = h->f[RESTART_MAIN[q]];
+    CK(h, cudaMemsetAsync(h->counter, 0, sizeof(unsigned long long), h->stream));
+    CK(h, launch_nonfinite_fields(h->kc, fl, 38, h->counter, h->stream));
+    h->launches += 1;
+    unsigned long long c = 0;
+    CK(h, cudaMemcpyAsync(&c, h->counter, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+    int rc = finish(h);
+    if (rc) return rc;
+    *clean = c == 0 ? 1 : 0;
+    return ATSAT_DYN_OK;
+}
+
 int atsat_dyn_clamp_budget(atsat_dyn_t h, double* added, int64_t* cells, double* added_bnd, int64_t* cells_bnd) {
     ENTRY(h);
     if (!added || !cells || !added_bnd || !cells_bnd) return fail(h, ATSAT_DYN_E_INVALID, "clamp_budget: null output");

@@ -351,6 +351,9 @@ cudaError_t launch_damp_axis(const KConst& kc, const double* tmp, double* f, dou
 cudaError_t launch_clamp_species(const KConst& kc, double* const f[11], float* const s32[11], double* added,
                                  unsigned long long* cells, cudaStream_t s);
 
+cudaError_t launch_nonfinite_fields(const KConst& kc, const double* const* f, int n, unsigned long long* count,
+                                    cudaStream_t s);
+
 // Turbulence<cSaturnModel>::run (turbulence.cu). Device tables per level i and row j, formed on the host with
 // the reference's expressions; height_m / thick_m from the model's float layer table.
 struct TurbTables {

@@ -250,7 +250,35 @@ __global__ void __launch_bounds__(256) clamp_species_kernel(const KConst K, cons
     }
 }
 
+// cSaturnModel::restart_state_is_clean (FileIO_Sat.cpp:676-695): cells whose exponent bits are all ones
+struct NonfiniteArgs {
+    const double* f[40];
+    int n;
+};
+__global__ void __launch_bounds__(256) nonfinite_fields_kernel(const KConst K, const NonfiniteArgs A,
+                                                               unsigned long long* count) {
+    const int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+    const int q = blockIdx.z / K.im, i = blockIdx.z % K.im;
+    bool bad = false;
+    if (k < K.km && j < K.jm && q < A.n) {
+        const uint64_t b = (uint64_t)__double_as_longlong(A.f[q][((int64_t)i * K.jm + j) * K.kp + k]);
+        bad = (b & 0x7FF0000000000000ull) == 0x7FF0000000000000ull;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(count, (unsigned long long)__popc(m));
+}
+
 }  // namespace
+
+cudaError_t launch_nonfinite_fields(const KConst& kc, const double* const* f, int n, unsigned long long* count,
+                                    cudaStream_t s) {
+    if (n > 40) return cudaErrorInvalidValue;
+    NonfiniteArgs A{};
+    for (int q = 0; q < n; q++) A.f[q] = f[q];
+    A.n = n;
+    nonfinite_fields_kernel<<<dim3((kc.km + 31) / 32, (kc.jm + 7) / 8, kc.im * n), dim3(32, 8), 0, s>>>(kc, A, count);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_damp_axis(const KConst& kc, const double* tmp, double* f, double coeff, int axis, int seam,
                              cudaStream_t s) {

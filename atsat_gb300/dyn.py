@@ -96,6 +96,10 @@ def lib():
         L.atsat_dyn_turb_params_from_env.argtypes = [C.POINTER(abi.TurbParams)]
         L.atsat_dyn_set_turb_params.argtypes = [H, C.POINTER(abi.TurbParams)]
         L.atsat_dyn_turbulence.argtypes = [H]
+        L.atsat_dyn_save_restart.argtypes = [H, C.c_char_p, C.c_int32, C.c_int32, C.POINTER(C.POINTER(C.c_double))]
+        L.atsat_dyn_load_restart.argtypes = [H, C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                             C.POINTER(C.POINTER(C.c_double))]
+        L.atsat_dyn_restart_is_clean.argtypes = [H, C.POINTER(C.c_int32)]
         L.atsat_dyn_turbulence_diag.argtypes = [H, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.atsat_dyn_clamp_negative_species.argtypes = [H]
         L.atsat_dyn_clamp_budget.argtypes = [H, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_double),
@@ -331,6 +335,33 @@ class Dycore:
         vs = np.zeros((g.jm, g.km))
         self._ck(lib().atsat_dyn_turbulence_diag(self.h, abi.dptr(prod), abi.dptr(vs)), "turbulence_diag")
         return prod, vs
+
+    def save_restart(self, path: str, iteration: int, carried: bool = True, host=None):
+        """cSaturnModel::save_state's file (SAT3, or SAT1 without the carried arrays) from the device fields;
+        host: the 15 host-physics arrays (ATSAT_DYN_RESTART_NHOST order) or None for zeros."""
+        ptrs = self._host_ptrs(host)
+        self._ck(lib().atsat_dyn_save_restart(self.h, path.encode(), int(iteration), int(bool(carried)), ptrs),
+                 "save_restart")
+
+    def load_restart(self, path: str, host=None):
+        """cSaturnModel::load_state into the device fields (and the host arrays given); (iteration, format)."""
+        it, fmt = C.c_int32(), C.c_int32()
+        self._ck(lib().atsat_dyn_load_restart(self.h, path.encode(), C.byref(it), C.byref(fmt), self._host_ptrs(host)),
+                 "load_restart")
+        return it.value, fmt.value
+
+    def restart_state_is_clean(self) -> bool:
+        v = C.c_int32()
+        self._ck(lib().atsat_dyn_restart_is_clean(self.h, C.byref(v)), "restart_is_clean")
+        return bool(v.value)
+
+    def _host_ptrs(self, host):
+        if host is None:
+            return None
+        assert len(host) == 15
+        for a in host:
+            assert a is None or (a.dtype == np.float64 and a.flags.c_contiguous and a.shape == self.grid.shape)
+        return (C.POINTER(C.c_double) * 15)(*[abi.dptr(a) if a is not None else None for a in host])
 
     def clampNegativeSpecies(self):
         self._ck(lib().atsat_dyn_clamp_negative_species(self.h), "clamp_negative_species")

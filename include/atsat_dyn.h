@@ -309,6 +309,27 @@ int atsat_dyn_turbulence(atsat_dyn_t h);
  * k fastest) and the friction velocity u_tau (jm*km); either may be null */
 int atsat_dyn_turbulence_diag(atsat_dyn_t h, double* prod, double* vel_star);
 
+/* ---- restart files (cSaturnModel::save_state / load_state, planet/FileIO_Sat.cpp:513-665) ----
+ * The reference's binary format, byte for byte: int32 header {magic, im, jm, km, iteration} with magic
+ * 0x53415433 "SAT3" (0x53415431 "SAT1" without the carried arrays), then each array as im*jm*km doubles
+ * (k fastest) in the order of restart_arrays() and, for SAT2 / SAT3, restart_arrays_carried(). The arrays on
+ * the device are streamed from / into HBM. Fifteen carried arrays belong to the host physics and come
+ * from / go to the caller's buffers (contiguous im*jm*km doubles each; a null entry is written as zeros
+ * and skipped on reading), in this order: */
+#define ATSAT_DYN_RESTART_NHOST 15
+/* difflux_h2s, difflux_nh3, difflux_nh4sh, j_h2s, j_nh3, j_nh4sh, w_h2s, w_nh3, w_nh4sh, BuoyancyForce,
+ * PresGradForce, Q_Sensible, jT_h2s, jT_nh3, jT_nh4sh */
+/* write `path`; carried = 1: SAT3 (the reference's default, ATSAT_RESTART_CARRIED), 0: SAT1 */
+int atsat_dyn_save_restart(atsat_dyn_t h, const char* path, int32_t iter, int32_t carried,
+                           const double* const* host_arrays);
+/* read `path` (SAT1, SAT2 or SAT3) into the device fields and the host buffers; writes the iteration it
+ * belongs to and the format (1, 2, 3). ATSAT_DYN_E_INVALID for a missing file, a bad header, another grid or
+ * a truncated file (the reference then runs from scratch). */
+int atsat_dyn_load_restart(atsat_dyn_t h, const char* path, int32_t* iter, int32_t* format, double* const* host_arrays);
+/* cSaturnModel::restart_state_is_clean (FileIO_Sat.cpp:676-695): 1 when every array of restart_arrays() is
+ * finite everywhere (exponent bits, as the reference tests them), else 0 */
+int atsat_dyn_restart_is_clean(atsat_dyn_t h, int32_t* clean);
+
 /* ---- diagnostics and timing ---- */
 int atsat_dyn_sync(atsat_dyn_t h);
 int atsat_dyn_status(atsat_dyn_t h, atsat_dyn_diag* out);

@@ -21,6 +21,7 @@
 //        driver    as steps, with damp after the pressure call, clamp after the boundary conditions and
 //                  the turbulence closure after restoreVar (cSaturnModel.cpp:894-897, 1101, 1116)
 //        turb      TurbulenceSat(m).run() (Turbulence.h:306-329); writes prod, vel_star and the constants
+//        save      cSaturnModel::save_state(nsteps) into $ORACLE_RESTART_DIR (FileIO_Sat.cpp:578-613)
 // Record format of both files: char name[48]; int64 count; double data[count].
 
 #include "cSaturnModel.h"
@@ -222,6 +223,11 @@ public:
             m.clampNegativeSpecies();
         } else if(op == "turb"){
             TurbulenceSat(m).run();
+        } else if(op == "save"){
+            // cSaturnModel::save_state (FileIO_Sat.cpp:578-613) into ORACLE_RESTART_DIR, iteration = nsteps
+            const char* d = getenv("ORACLE_RESTART_DIR");
+            m.output_path = d ? d : ".";
+            m.save_state(nsteps);
         } else if(op == "driver"){
             // the dycore sequence with the driver's glue around it: the p_dyn filter after the pressure
             // call (cSaturnModel.cpp:894-897) and the species floor after the boundary conditions (:1101)

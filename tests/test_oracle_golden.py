@@ -100,3 +100,21 @@ def test_oracle_pressure_variants_match_reference_bitwise(name):
     oracle.pressure(s, P)
     for fid in range(F.NFIELDS):
         assert np.array_equal(s.arrays[fid], ref[fid]), F.NAMES[fid]
+
+
+def test_restart_format_matches_reference_save_state(tmp_path):
+    """oracle/sat3.py writes the file cSaturnModel::save_state writes, byte for byte (SAT3, 41x181x361)."""
+    from oracle import refrun, sat3
+    if not refrun.available():
+        pytest.skip("reference harness not built here")
+    g, P, st = make_state("rk_s1")
+    refrun.run(st, "save", nsteps=1234, env={"ORACLE_RESTART_DIR": str(tmp_path)}, threads=1)
+    ours = str(tmp_path / "oracle.bin")
+    sat3.write(ours, st.arrays, None, g.shape, 1234, 3)
+    ref = str(tmp_path / "sat_restart_1234.bin")
+    with open(ref, "rb") as a, open(ours, "rb") as b:
+        while True:
+            x, y = a.read(1 << 26), b.read(1 << 26)
+            assert x == y
+            if not x:
+                break
