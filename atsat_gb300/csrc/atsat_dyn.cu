@@ -1003,6 +1003,9 @@ int enqueue_rk4_mixed(atsat_dyn* h, bool resident) {
         Timed t(h, ATSAT_K_RK_STAGE);
         CK(h, launch_stage(h, io, sp, stage == 3 ? MODE_FINAL : MODE_STAGE));
         h->launches += launches_per_stage(h);
+        // the TMA-tiled tracer kernel leaves the final stage's FP64 sum to launch_final_combine
+        const int v = variant_available(h, h->variant) ? h->variant : ATSAT_DYN_STAGE_DIRECT;
+        if (stage == 3 && (v == ATSAT_DYN_STAGE_SPLIT_TILED || v == ATSAT_DYN_STAGE_TILED2)) h->launches += 1;
     }
     return ATSAT_DYN_OK;
 }

@@ -182,7 +182,7 @@ struct MixedIO {
     const float* wlo;              // y_n(w) - yn32(w)
     const float* dl_in[NPROG];     // stage increments; null entries: Y_s = y_n
     float* dl_out[NPROG];          // stages 0..2
-    const float* dl1[NPROG];       // final stage: dl_1 and dl_2
+    float* dl1[NPROG];       // final stage: dl_1 and dl_2
     const float* dl2[NPROG];
     float* acc_turb[2];            // tke, dis
     const double* yn64[NPROG];
@@ -351,6 +351,8 @@ cudaError_t launch_damp_axis(const KConst& kc, const double* tmp, double* f, dou
 cudaError_t launch_clamp_species(const KConst& kc, double* const f[11], float* const s32[11], double* added,
                                  unsigned long long* cells, cudaStream_t s);
 
+// the final stage's FP64 half of fields q0..q1 after a tiled stage kernel (rk_mixed.cu)
+cudaError_t launch_final_combine(const MixedConstF& kf, const MixedIO& io, int q0, int q1, cudaStream_t s);
 cudaError_t launch_nonfinite_fields(const KConst& kc, const double* const* f, int n, unsigned long long* count,
                                     cudaStream_t s);
 

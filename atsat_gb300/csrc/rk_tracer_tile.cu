@@ -6,9 +6,11 @@
 // order the consumers use them, with tensor copies: the halo boxes (40 x 10 x 6 floats) of each field's
 // y_n copy and stage increment into a 4-slot ring, and point boxes (32 x 8 x 4 floats, no halo) of the
 // advecting winds, the eddy viscosity, the sources, the tke/dis running sums and, at the final stage, the
-// increments dl_1 and dl_2 into a 6-slot ring. Eight consumer warps (row j, lane k, four radial levels
-// per lane) read everything from shared memory, so they never wait on a global load except y_n in FP64
-// at the final stage. A field holds at most two halo and four point slots, so a block needs 67 KB of
+// increments dl_1 and dl_2 into a 6-slot ring. At the final stage the kernel writes the FP32 increment of
+// y_{n+1} in place of dl_1 and launch_final_combine (rk_mixed.cu) adds it to y_n in FP64: the FP64 loads, adds and stores
+// then stream in a kernel of their own instead of stalling the stencil kernel. Eight consumer warps (row j,
+// lane k, four radial levels per lane) read everything from shared memory, so they never wait on a global
+// load. A field holds at most two halo and four point slots, so a block needs 67 KB of
 // shared memory and three blocks fit on an SM.
 //
 // The arithmetic is mixed_physics.cuh's scalar() with its constant factors folded: with the raw
@@ -244,24 +246,10 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
 
     const int q_last = K.turb ? ATSAT_F_DIS : ATSAT_F_NH4SH;
     const float pc = K.precip_coupling, chem = K.chem;
-    // final stage: y_n in FP64 of the next field, loaded one field ahead
-    double y64n[TI];
-    if (MODE == MODE_FINAL) {
-#pragma unroll
-        for (int ii = 0; ii < TI; ii++) y64n[ii] = valid[ii] ? ldd(io.yn64[ATSAT_F_H2O] + c[ii]) : 0.0;
-    }
 #pragma unroll
     for (int q = ATSAT_F_H2O; q <= ATSAT_F_DIS; q++) {
         if (q > q_last) break;
         const int hb = h0<HAS_DL>(q), pb = pt0<MODE, HAS_DL>(q), npq = n_pt<MODE>(q);
-        double y64[TI];
-        if (MODE == MODE_FINAL) {
-#pragma unroll
-            for (int ii = 0; ii < TI; ii++) {
-                y64[ii] = y64n[ii];
-                if (q < q_last && valid[ii]) y64n[ii] = ldd(io.yn64[q + 1] + c[ii]);
-            }
-        }
         if (!wait_items<NHS>(rh, hb, hb + (HAS_DL ? 2 : 1)) || !wait_items<NPS>(rp, pb, pb + npq)) { fail(); return; }
         const float* Y = hs + (hb % NHS) * HSLOT_F;
         const float* D = hs + ((hb + 1) % NHS) * HSLOT_F;
@@ -321,11 +309,9 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
                     const float dl1 = (n_src(q) == 2 ? P2 : P1)[x], dl2 = (n_src(q) == 2 ? P3 : P2)[x];
                     inc = THIRD * (dl1 + 2.0f * dl2 + dl_c) + sp.sixth_dt_f * r;
                 }
-                double y = y64[ii] + f2d(inc);
-                if (q == ATSAT_F_TKE) y = smin(smax(y, 0.0), K.tke_max_d);
-                else if (q == ATSAT_F_DIS) y = smax(y, K.dis_min_d);
-                io.out64[q][cc] = y;
-                if (io.out32[q]) io.out32[q][cc] = d2f(y);
+                // the increment of y_{n+1}, in place of dl_1 (read above from this cell's point box);
+                // launch_final_combine adds it to y_n in FP64
+                io.dl1[q][cc] = inc;
                 if (sp.write_all_rhs) io.rhs[q][cc] = f2d(r);
             }
         }
@@ -372,8 +358,10 @@ cudaError_t launch_rk_tracer_tile(const TileMaps& maps, const MixedConstF& kf, c
     if (mode == MODE_STAGE)
         return has_dl ? launch_one<MODE_STAGE, true>(maps, kf, io, sp, plan, grid, s)
                       : launch_one<MODE_STAGE, false>(maps, kf, io, sp, plan, grid, s);
-    return has_dl ? launch_one<MODE_FINAL, true>(maps, kf, io, sp, plan, grid, s)
-                  : launch_one<MODE_FINAL, false>(maps, kf, io, sp, plan, grid, s);
+    cudaError_t e = has_dl ? launch_one<MODE_FINAL, true>(maps, kf, io, sp, plan, grid, s)
+                           : launch_one<MODE_FINAL, false>(maps, kf, io, sp, plan, grid, s);
+    if (e != cudaSuccess) return e;
+    return launch_final_combine(kf, io, ATSAT_F_H2O, kf.turb ? ATSAT_F_DIS : ATSAT_F_NH4SH, s);
 }
 
 // the number of items the kernel consumes (the host's plan must match)

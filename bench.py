@@ -197,8 +197,10 @@ KERNEL_NAME = {"fp64": "rk_stage_fp64_kernel (fused RHSSat + RK4 stage, FP64)",
                "mixed_split": "rk_mom_kernel + rk_tracer_kernel<1> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)",
                "mixed_split3": "rk_mom_kernel + rk_tracer_kernel<3> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)",
                "mixed_split13": "rk_mom_kernel + rk_tracer_kernel<13> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)",
-               "mixed_split_tiled": "rk_mom_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, TMA-tiled tracers)",
-               "mixed_tiled2": "rk_mom_tile_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, all inputs TMA-streamed)"}
+               "mixed_split_tiled": "rk_mom_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, TMA-tiled tracers; "
+                                    "final stage + final_combine_kernel)",
+               "mixed_tiled2": "rk_mom_tile_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, all inputs "
+                               "TMA-streamed; final stage + final_combine_kernel)"}
 
 
 def cpu_baseline(g, P, seed, target_s=3.0):
