@@ -359,6 +359,10 @@ void build_geometry(atsat_dyn* h, const double* vbar0, const double* ubar0) {
             c.p_inv_rm = 1.0 / rm;
             c.p_inv_rmsinthe = 1.0 / (rm * sp);
             c.p_pad_cot_rm = c.cotanthe * c.inv_rm;
+            c.src_r = c.p_exp_rm / (2.0 * g.dr);
+            c.src_the = c.p_inv_rm / (2.0 * g.dthe);
+            c.src_phi = c.p_inv_rmsinthe / (2.0 * g.dphi);
+            c.p_inv_den = 1.0 / c.p_den;
         }
     }
 }
@@ -810,6 +814,8 @@ int enqueue_mixed_prepare(atsat_dyn* h, double* const* base, bool with_dl0, bool
     pr.buoy = h->buoy;
     pr.pgeo = h->pgeo;
     pr.bnum = (h->p.buoy_legacy ? h->p.buoyancy * h->p.g : h->p.g) / (h->kc.rR * h->p.t_ref);
+    pr.bnum_f = (float)pr.bnum;
+    pr.cor_rad = h->kc.cor_rad_on != 0.0;
     pr.inv_2dr_f = (float)h->kc.inv_2dr;
     pr.dps_scale_f = (float)(h->kc.inv_2dr * h->kc.to_nd);
     pr.r_mix_f = (float)h->kc.r_mix;

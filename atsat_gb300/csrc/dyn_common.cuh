@@ -77,8 +77,11 @@ struct alignas(16) ColGeo {
     double ubar0, p_num1, p_num2, p_num3;            // sweep weights
     double p_den, lc_num1, lc_num2, lc_num3;         // sweep denominator, lc_old weights
     double p_exp_rm, p_inv_rm, p_inv_rmsinthe, p_pad_cot_rm; // divergence-source factors; cot / rm
+    // the source factors times the centred-difference scales (exp_rm / (2 dr), 1 / (2 dthe rm),
+    // 1 / (2 dphi rm sin)) and 1 / p_den: one product per term instead of two, no FP64 division
+    double src_r, src_the, src_phi, p_inv_den;
 };
-static_assert(sizeof(ColGeo) == 32 * 8, "ColGeo layout");
+static_assert(sizeof(ColGeo) == 36 * 8, "ColGeo layout");
 
 // Grid-wide constants, every one formed on the host in the reference's own expression order.
 struct KConst {
@@ -242,7 +245,8 @@ struct MixedPrep {
     const double* buoy;
     const PrepGeo* pgeo;
     double bnum;                   // g / (r_mix R_mix t_ref), or buoyancy g / (r_mix R_mix t_ref) legacy
-    float inv_2dr_f, dps_scale_f, r_mix_f;
+    float bnum_f, inv_2dr_f, dps_scale_f, r_mix_f;
+    int cor_rad;                   // the radial Coriolis term is on (coriolis_split off)
 };
 
 // The TMA-tiled stage kernel: the FP32 arrays live in one slab at a fixed stride, addressed by a 4-D

@@ -123,11 +123,60 @@ __global__ void bc_radius_kernel(const KConst K, const BCArgs A) {
         if (!A.turb_on || !inner) return;
         const int q = task - 20;
         const int F = A.turb[q];
-        put(A, F, at(0), smax(A.turb_floor[q], K.c43 * get(A, F, at(1)) - K.c13 * get(A, F, at(2))));
-        put(A, F, at(im - 1), smax(A.turb_floor[q], K.c43 * get(A, F, at(im - 2)) - K.c13 * get(A, F, at(im - 3))));
+        const double a1 = get(A, F, at(1)), a2 = get(A, F, at(2)), b2 = get(A, F, at(im - 2)),
+                     b3 = get(A, F, at(im - 3));
+        put(A, F, at(0), smax(A.turb_floor[q], K.c43 * a1 - K.c13 * a2));
+        put(A, F, at(im - 1), smax(A.turb_floor[q], K.c43 * b2 - K.c13 * b3));
         return;
     }
     const int F = A.radius[task];
+    if (im >= 8) {
+        // The same steps with every load issued before the first store (one memory round trip instead of
+        // several). With im >= 8 the planes read (1..3 and im-4..im-2) are disjoint from the extrapolated
+        // walls (0 and im-1); the taper (v, w only) reads planes nothing before it wrote; the species
+        // copies read planes 1 and im-2, which only the taper writes, and never in a species field.
+        bool species = false;
+        for (int q = 0; q < 11; q++) species = species || (A.species[q] == F);
+        const bool copies = species && (A.lid_copy != 0 || A.wall_copy != 0);
+        const bool taper = (F == ATSAT_F_V || F == ATSAT_F_W) && A.top_taper;
+        const bool rho = copies && A.wall_copy == 2 && A.local_rho;
+        if (!inner && !taper && !copies && !(F == ATSAT_F_U && A.lid_u)) return;
+        const double x1 = get(A, F, at(1)), x2 = get(A, F, at(2)), x3 = get(A, F, at(3));
+        const double y2 = get(A, F, at(im - 2)), y3 = get(A, F, at(im - 3)), y4 = get(A, F, at(im - 4));
+        const double ra = rho ? get(A, ATSAT_F_RHO_MIX, at(0)) : 0.0;
+        const double rb = rho ? get(A, ATSAT_F_RHO_MIX, at(1)) : 0.0;
+        double w0 = 0.0, w1 = 0.0;                        // planes 0 and im-1
+        bool s0 = false, s1 = false;
+        if (inner) {
+            const int fb = (A.bottom_form != 0 && F != ATSAT_F_U) ? A.bottom_form : A.radius_form;
+            w0 = form3(fb, x1, x2, x3, K.c43, K.c13);
+            w1 = form3(A.radius_form, y2, y3, y4, K.c43, K.c13);
+            s0 = s1 = true;
+        }
+        if (F == ATSAT_F_U && A.lid_u) { w0 = 0.0; w1 = 0.0; s0 = s1 = true; }
+        if (taper) {
+            w1 = 0.0;
+            s1 = true;
+            put(A, F, at(im - 2), A.top_taper == 2 ? (1.0 / 3.0) * y4 : y2 * (1.0 / 3.0));
+            put(A, F, at(im - 3), A.top_taper == 2 ? (2.0 / 3.0) * y4 : y3 * (2.0 / 3.0));
+        }
+        if (copies) {
+            double fr = 1.0;
+            if (A.wall_copy == 2) {
+                double r0 = A.r_mix, r1 = A.r_mix;
+                if (A.local_rho) {
+                    r0 = (ra > 0.0 && isfinite(ra)) ? ra : A.r_mix;
+                    r1 = (rb > 0.0 && isfinite(rb)) ? rb : A.r_mix;
+                }
+                fr = r0 / r1;
+            }
+            if (A.lid_copy != 0) { w1 = y2; s1 = true; }
+            if (A.wall_copy != 0) { w0 = x1 * fr; s0 = true; }
+        }
+        if (s0) put(A, F, at(0), w0);
+        if (s1) put(A, F, at(im - 1), w1);
+        return;
+    }
     if (inner) {
         const int fb = (A.bottom_form != 0 && F != ATSAT_F_U) ? A.bottom_form : A.radius_form;
         put(A, F, at(0), form3(fb, get(A, F, at(1)), get(A, F, at(2)), get(A, F, at(3)), K.c43, K.c13));

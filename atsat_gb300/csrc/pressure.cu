@@ -82,30 +82,33 @@ __global__ void __launch_bounds__(256) press_source_kernel(
         const int ke = (k == K.km - 2) ? 0 : k + 1;
         const int64_t cw = c - k + kw, ce = c - k + ke;
         const ColGeo* g = geo + ((int64_t)i * K.jm + j);
-        double du_dr, dv_dthe, dw_dphi;
+        // GB300 issues two FP64 operations per SM per cycle: the scales of each difference are one
+        // product from the column table, the clamp one compare (finiteness is an exponent test), and
+        // lc_old's three second differences accumulate into div by fma (17 operations per cell)
+        double dr_, dthe_, dphi_;
         if (K.press_src == 0) {     // legacy div(aux - rhs), PressureSolver.h:373-381
-            du_dr = ((ldg(aux_u + c + P) - ldg(aux_u + c - P)) - (ldg(rhs_u + c + P) - ldg(rhs_u + c - P))) * K.inv_2dr;
-            dv_dthe = ((ldg(aux_v + c + kp) - ldg(aux_v + c - kp)) - (ldg(rhs_v + c + kp) - ldg(rhs_v + c - kp))) * K.inv_2dthe;
-            dw_dphi = ((ldg(aux_w + ce) - ldg(aux_w + cw)) - (ldg(rhs_w + ce) - ldg(rhs_w + cw))) * K.inv_2dphi;
+            dr_ = (ldg(aux_u + c + P) - ldg(aux_u + c - P)) - (ldg(rhs_u + c + P) - ldg(rhs_u + c - P));
+            dthe_ = (ldg(aux_v + c + kp) - ldg(aux_v + c - kp)) - (ldg(rhs_v + c + kp) - ldg(rhs_v + c - kp));
+            dphi_ = (ldg(aux_w + ce) - ldg(aux_w + cw)) - (ldg(rhs_w + ce) - ldg(rhs_w + cw));
         } else {                    // projection source, rigid-lid zero of S_u on the radial walls (:246-248)
             const bool wall0 = K.press_incr && K.rigid_lid;
             const double sup = (wall0 && i + 1 == K.im - 1) ? 0.0 : ldg(su + c + P);
             const double sdn = (wall0 && i - 1 == 0) ? 0.0 : ldg(su + c - P);
-            du_dr = (sup - sdn) * K.inv_2dr;
-            dv_dthe = (ldg(sv + c + kp) - ldg(sv + c - kp)) * K.inv_2dthe;
-            dw_dphi = (ldg(sw + ce) - ldg(sw + cw)) * K.inv_2dphi;
+            dr_ = sup - sdn;
+            dthe_ = ldg(sv + c + kp) - ldg(sv + c - kp);
+            dphi_ = ldg(sw + ce) - ldg(sw + cw);
         }
-        double div = du_dr * ldg(&g->p_exp_rm) + dv_dthe * ldg(&g->p_inv_rm) + dw_dphi * ldg(&g->p_inv_rmsinthe);
+        double div = fma(dphi_, ldg(&g->src_phi), fma(dthe_, ldg(&g->src_the), dr_ * ldg(&g->src_r)));
         const double src_max = ldg(&g->p_den) * K.pdyn_cap;
-        if (!isfinite(div)) { div = 0.0; clamped = true; }
-        else if (div > src_max) { div = src_max; clamped = true; }
-        else if (div < -src_max) { div = -src_max; clamped = true; }
+        uint32_t lo, hi;
+        split_f64(div, lo, hi);
+        if (((hi >> 20) & 0x7FFu) == 0x7FFu) { div = 0.0; clamped = true; }
+        else if (fabs(div) > src_max) { div = (div > src_max) ? src_max : -src_max; clamped = true; }
         if (K.press_incr) {         // lc_old = Lc(p_dyn) before the sweep (:249-282)
-            const double p0 = ldg(p + c);
-            const double l = ldg(&g->lc_num1) * (ldg(p + c + P) + ldg(p + c - P) - 2.0 * p0)
-                           + ldg(&g->lc_num2) * (ldg(p + c + kp) + ldg(p + c - kp) - 2.0 * p0)
-                           + ldg(&g->lc_num3) * (ldg(p + ce) + ldg(p + cw) - 2.0 * p0);
-            div += l;
+            const double p0 = ldg(p + c);      // fma(-2, p0, s) == s - 2 p0: the product is exact
+            div = fma(ldg(&g->lc_num1), fma(-2.0, p0, ldg(p + c + P) + ldg(p + c - P)), div);
+            div = fma(ldg(&g->lc_num2), fma(-2.0, p0, ldg(p + c + kp) + ldg(p + c - kp)), div);
+            div = fma(ldg(&g->lc_num3), fma(-2.0, p0, ldg(p + ce) + ldg(p + cw)), div);
         }
         src[c] = div;
     }
@@ -127,7 +130,7 @@ __device__ __forceinline__ void sweep_cell(const KConst& K, const ColGeo* __rest
     const ColGeo* g = geo + ((int64_t)i * K.jm + j);
     const double acc = (p[c + P] + p[c - P]) * ldg(&g->p_num1) + (p[c + kp] + p[c - kp]) * ldg(&g->p_num2)
                      + (p[c - k + ke] + p[c - k + kw]) * ldg(&g->p_num3);
-    p[c] = (acc - ldg(src + c)) / ldg(&g->p_den);
+    p[c] = (acc - ldg(src + c)) * ldg(&g->p_inv_den);
 }
 
 __global__ void __launch_bounds__(256) press_sweep_kernel(const KConst K, const ColGeo* __restrict__ geo,

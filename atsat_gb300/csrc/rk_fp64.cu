@@ -297,7 +297,8 @@ __device__ __forceinline__ double recip_nr(double x) {
 }
 
 // the buoyancy g p / (r_mix R_mix T t_ref) = bc p / t of one cell (bc formed on the host); false where
-// the reference skips the cell (!(t > 0), non-finite b)
+// the reference skips the cell (!(t > 0), non-finite b). The level mean's rows take the fast path below
+// and come here only for cells outside it.
 __device__ __forceinline__ bool cell_buoyancy(const KConst& K, double tc, double pc, double& b) {
     if (in_rcp_range(tc)) {
         b = (K.buoy_c * pc) * recip_nr(tc);
@@ -308,6 +309,19 @@ __device__ __forceinline__ bool cell_buoyancy(const KConst& K, double tc, double
     return isfinite(b);
 }
 
+// |x| < 2^512 (zero and subnormals included), finite: an exponent test on the integer pipe
+__device__ __forceinline__ bool moderate(double x) {
+    uint32_t lo, hi;
+    split_f64(x, lo, hi);
+    return ((hi >> 20) & 0x7FFu) < 1023u + 512u;
+}
+
+// GB300 issues two FP64 operations per SM per cycle, so the per-cell work is three of them: each lane
+// sums p / t over its cells of a row (the Newton-Raphson reciprocal and one fma) and the row's weight
+// and the constant bc are applied once per row: sum += sin(theta_j) (bc * sum_k p/t + rest), with the
+// weight sum sin(theta_j) * (cells counted). Cells with t outside the reciprocal's range or a huge p
+// ("rest") take the reference's own expression and skip rule. With |p| < 2^512, 1/t < 2^127 and
+// |bc| < 2^256 every fast-path term and sum is finite, as the reference's isfinite test needs.
 __global__ void __launch_bounds__(LM_THREADS) level_mean_partial_kernel(const KConst K, const double* __restrict__ t,
                                                                          const double* __restrict__ ps,
                                                                          const double* __restrict__ sin_j,
@@ -315,10 +329,12 @@ __global__ void __launch_bounds__(LM_THREADS) level_mean_partial_kernel(const KC
     const int i = blockIdx.x, chunk = blockIdx.y;
     const int j0 = (int)((int64_t)K.jm * chunk / LM_CHUNKS), j1 = (int)((int64_t)K.jm * (chunk + 1) / LM_CHUNKS);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool bc_ok = fabs(K.buoy_c) < 0x1p256;
     double sum = 0.0, wsum = 0.0;
     for (int j = j0 + warp; j < j1; j += LM_THREADS / 32) {
         const int64_t row = ((int64_t)i * K.jm + j) * K.kp;
-        const double wgt = __ldg(sin_j + j);
+        double rs = 0.0, rest = 0.0;
+        int cnt = 0;
         for (int k0 = 0; k0 < K.km; k0 += 128) {
             double tv[4], pv[4];
 #pragma unroll
@@ -329,13 +345,22 @@ __global__ void __launch_bounds__(LM_THREADS) level_mean_partial_kernel(const KC
             }
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                double b;
-                if (cell_buoyancy(K, tv[q], pv[q], b)) {   // tv = 0 past the row end: skipped
-                    sum += wgt * b;
-                    wsum += wgt;
+                if (k0 + q * 32 + lane >= K.km) continue;
+                if (bc_ok && in_rcp_range(tv[q]) && moderate(pv[q])) {
+                    rs = fma(pv[q], recip_nr(tv[q]), rs);
+                    cnt++;
+                } else {
+                    double b;
+                    if (cell_buoyancy(K, tv[q], pv[q], b)) {
+                        rest += b;
+                        cnt++;
+                    }
                 }
             }
         }
+        const double wgt = __ldg(sin_j + j);
+        sum = fma(wgt, fma(K.buoy_c, rs, rest), sum);
+        wsum = fma(wgt, (double)cnt, wsum);
     }
     __shared__ double s_sum[LM_THREADS / 32], s_w[LM_THREADS / 32];
     for (int o = 16; o > 0; o >>= 1) {
@@ -365,7 +390,9 @@ __global__ void level_mean_final_kernel(const KConst K, const double* __restrict
 
 // ---- computeMetricPressure (RungeKutta_Sat_Turb.cpp:60-108): one radial trapezoid scan per column ----
 // The scan is serial in i; the loads of eight levels are issued ahead of the dependent sums. inv_rm holds
-// 1 / rm(i) (a product instead of the reference's quotient: at most one rounding apart).
+// 1 / rm(i) (a product instead of the reference's quotient: at most one rounding apart). Six FP64 operations
+// per cell (seven with p_baro): f = (v^2 + w^2) / rm + cor w as two products and two fmas, and the
+// trapezoid acc += dr/2 (f_{i-1} + f_i) as one add and one fma.
 constexpr int MS_BATCH = 8;
 
 __global__ void __launch_bounds__(128) metric_scan_kernel(const KConst K, const double* __restrict__ v,
@@ -373,7 +400,7 @@ __global__ void __launch_bounds__(128) metric_scan_kernel(const KConst K, const 
                                                           const double* __restrict__ inv_rm,
                                                           const double* __restrict__ cor_j,
                                                           const double* __restrict__ p_baro,
-                                                          double* __restrict__ pm, double dr) {
+                                                          double* __restrict__ pm, double half_dr) {
     const int k = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 4 + threadIdx.y;
     if (k >= K.km || j >= K.jm) return;
@@ -394,8 +421,8 @@ __global__ void __launch_bounds__(128) metric_scan_kernel(const KConst K, const 
         for (int q = 0; q < MS_BATCH; q++) {
             const int i = i0 + q;
             if (i >= K.im) break;
-            const double f = (vv[q] * vv[q] + ww[q] * ww[q]) * __ldg(inv_rm + i) + cor * ww[q];
-            if (i > 0) acc = acc + 0.5 * (f_prev + f) * dr;
+            const double f = fma(fma(ww[q], ww[q], vv[q] * vv[q]), __ldg(inv_rm + i), cor * ww[q]);
+            if (i > 0) acc = fma(half_dr, f_prev + f, acc);
             f_prev = f;
             pm[c0 + (int64_t)i * K.plane] = p_baro ? acc + pb[q] : acc;
         }
@@ -403,18 +430,32 @@ __global__ void __launch_bounds__(128) metric_scan_kernel(const KConst K, const 
 }
 
 // ---- computeMixtureDensity (Pressure_Sat.cpp:49-62) ----
+// rho = p_stat 1e5 / (R_mix t t_ref). Where t is in [2^-60, 2^60), |p_stat| < 2^60 and the constant
+// c2 = 1e5 / (R_mix t_ref) is moderate (`fast`, set by the host), rho = p_stat (c2 / t) with c2 / t the
+// FP32 quotient corrected once in FP64 (q = q0 + (c2 - t q0) rcp(t), relative error ~2^-44): three FP64
+// operations per cell. Elsewhere the reference's expression and skip rules.
 __global__ void __launch_bounds__(256) density_kernel(const KConst K, const double* __restrict__ t,
-                                                      const double* __restrict__ ps, double R_mix,
-                                                      double* __restrict__ rho) {
+                                                      const double* __restrict__ ps, double R_mix, double c2,
+                                                      float c2f, int fast, double* __restrict__ rho) {
     const int k = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
     const int i = blockIdx.z;
     if (k >= K.km || j >= K.jm) return;
     const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
-    const double T = __ldg(t + c) * K.t_ref;
+    const double tc = __ldg(t + c), pc = __ldg(ps + c);
+    uint32_t lo, th, ph;
+    split_f64(tc, lo, th);
+    split_f64(pc, lo, ph);
+    if (fast && ((th >> 20) & 0xFFFu) - 963u < 120u && ((ph >> 20) & 0x7FFu) < 1083u) {
+        const float rf = __frcp_rn(d2f(tc));
+        const double q0 = f2d(c2f * rf);
+        rho[c] = pc * fma(fma(-tc, q0, c2), f2d(rf), q0);
+        return;
+    }
+    const double T = tc * K.t_ref;
     if (!(T > 0.0) || !(R_mix > 0.0)) { rho[c] = 0.0; return; }
     const double den = R_mix * T;
-    const double r = in_rcp_range(den) ? (__ldg(ps + c) * 1.0e5) * recip_nr(den) : (__ldg(ps + c) * 1.0e5) / den;
+    const double r = in_rcp_range(den) ? (pc * 1.0e5) * recip_nr(den) : (pc * 1.0e5) / den;
     rho[c] = isfinite(r) ? r : 0.0;
 }
 
@@ -440,14 +481,16 @@ cudaError_t launch_level_mean(const KConst& kc, const double* t, const double* p
 cudaError_t launch_metric_scan(const KConst& kc, const double* v, const double* w, const double* inv_rm,
                                const double* cor_j, const double* p_baro, double* p_metric, cudaStream_t s) {
     dim3 block(32, 4), grid((kc.km + 31) / 32, (kc.jm + 3) / 4);
-    metric_scan_kernel<<<grid, block, 0, s>>>(kc, v, w, inv_rm, cor_j, p_baro, p_metric, kc.dr);
+    metric_scan_kernel<<<grid, block, 0, s>>>(kc, v, w, inv_rm, cor_j, p_baro, p_metric, 0.5 * kc.dr);
     return cudaGetLastError();
 }
 
 cudaError_t launch_density(const KConst& kc, const double* t, const double* p_stat, double R_mix, double* rho,
                            cudaStream_t s) {
     dim3 block(32, 8), grid((kc.km + 31) / 32, (kc.jm + 7) / 8, kc.im);
-    density_kernel<<<grid, block, 0, s>>>(kc, t, p_stat, R_mix, rho);
+    const double c2 = (R_mix > 0.0 && kc.t_ref > 0.0) ? 1.0e5 / (R_mix * kc.t_ref) : 0.0;
+    const int fast = c2 > 0x1p-60 && c2 < 0x1p60;
+    density_kernel<<<grid, block, 0, s>>>(kc, t, p_stat, R_mix, c2, (float)c2, fast, rho);
     return cudaGetLastError();
 }
 

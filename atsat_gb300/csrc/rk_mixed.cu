@@ -192,10 +192,12 @@ __global__ void __launch_bounds__(256) mixed_prepare_kernel(const KConst K, cons
     const float dpdr = d2f(__ldg(p + c + P) - __ldg(p + c - P)) * pr.inv_2dr_f;
     const float dpdthe = d2f(__ldg(p + c + kp) - __ldg(p + c - kp)) * __ldg(&g->s_the_f);
     const float dpdphi = d2f(__ldg(p + ce) - __ldg(p + cw)) * __ldg(&g->s_phi_f);
-    double dpmdthe = 0.0;
+    // GB300 issues two FP64 operations per SM per cycle: the FP64 work here is the five differences, the
+    // meridional balance (three fmas) and the buoyancy anomaly (three), twelve operations per cell
+    double dpm_the = 0.0;          // the p_metric difference along theta
     float dpmdphi = 0.0f;
     if (K.metric_split) {
-        dpmdthe = (__ldg(pr.p_metric + c + kp) - __ldg(pr.p_metric + c - kp)) * __ldg(&g->s_the);
+        dpm_the = __ldg(pr.p_metric + c + kp) - __ldg(pr.p_metric + c - kp);
         dpmdphi = d2f(__ldg(pr.p_metric + ce) - __ldg(pr.p_metric + cw)) * __ldg(&g->s_phi_f);
     }
     // the adiabatic term only enters rhs_t's small compression work
@@ -207,15 +209,40 @@ __global__ void __launch_bounds__(256) mixed_prepare_kernel(const KConst K, cons
     }
     const double t = __ldg(pr.yn64[ATSAT_F_T] + c);
     const double ps = __ldg(pr.p_stat + c);
-    // buoyancy: numerator B p (so that b = B p / t) and the anomaly at t_n. 1/t: the FP32 reciprocal
-    // refined by one Newton-Raphson step (relative error ~1e-14, far below the FP32 result's)
-    const double bps = K.buoy_legacy ? (ps + __ldg(p + c)) * pr.bnum : ps * pr.bnum;
+    // buoyancy: numerator B p (so that b = B p / t; stored in FP32, so formed in FP32) and the anomaly
+    // B p / t - mean at t_n. p / t: the FP32 quotient q0 = p * rcp(t) corrected once in FP64,
+    // q = q0 + (p - t q0) rcp(t) (relative error ~2^-44), where t and p are moderate (t in [2^-60, 2^60),
+    // |p| < 2^60: no FP32 overflow); elsewhere 1/t refined by one Newton-Raphson step times B p.
     const float tf = d2f(t);
+    float bps_f;
     double ban = 0.0;
-    if (tf > 0.0f) {
-        double r = f2d(__frcp_rn(tf));
-        r = fma(r, fma(-t, r, 1.0), r);
-        ban = K.buoy_legacy ? bps * r : (bps * r - __ldg(pr.buoy + i));
+    if (K.buoy_legacy) {
+        const double bps = (ps + __ldg(p + c)) * pr.bnum;
+        bps_f = d2f(bps);
+        if (tf > 0.0f) {
+            double r = f2d(__frcp_rn(tf));
+            r = fma(r, fma(-t, r, 1.0), r);
+            ban = bps * r;
+        }
+    } else {
+        const float psf = d2f(ps);
+        bps_f = psf * pr.bnum_f;
+        if (tf > 0.0f) {
+            uint32_t lo, th, ph;
+            split_f64(t, lo, th);
+            split_f64(ps, lo, ph);
+            const uint32_t te = (th >> 20) & 0x7FFu, pe = (ph >> 20) & 0x7FFu;
+            const float rf = __frcp_rn(tf);
+            const double r0 = f2d(rf);
+            const double buoy_i = __ldg(pr.buoy + i);
+            if (te - 963u < 120u && pe < 1083u) {
+                const double q0 = f2d(psf * rf);
+                ban = fma(pr.bnum, fma(fma(-t, q0, ps), r0, q0), -buoy_i);
+            } else {
+                const double r = fma(r0, fma(-t, r0, 1.0), r0);
+                ban = ps * pr.bnum * r - buoy_i;
+            }
+        }
     }
     // frozen parts of rhs_u, rhs_v, rhs_w at y_n (RHS_Sat_Turb.cpp:310-350, 388-399, 780-835)
     const double wn = __ldg(pr.yn64[ATSAT_F_W] + c);
@@ -224,9 +251,10 @@ __global__ void __launch_bounds__(256) mixed_prepare_kernel(const KConst K, cons
         const double vn = __ldg(pr.yn64[ATSAT_F_V] + c);
         gu -= (vn * vn + wn * wn) * __ldg(&g->metric_inv_rm);
     }
-    if (K.cor_rad_on != 0.0) gu -= __ldg(&g->cor_rad_c) * wn;
+    if (pr.cor_rad) gu -= __ldg(&g->cor_rad_c) * wn;
     // w (w cot / r) - Coriolis cor_the w, the centrifugal and the p_metric gradient
-    const double gv = wn * fma(wn, __ldg(&g->cot_rm), -__ldg(&g->cor_the_c)) - dpmdthe + __ldg(&g->cent_the_c);
+    const double rest = K.metric_split ? fma(-dpm_the, __ldg(&g->s_the), __ldg(&g->cent_the_c)) : __ldg(&g->cent_the_c);
+    const double gv = fma(wn, fma(wn, __ldg(&g->cot_rm), -__ldg(&g->cor_the_c)), rest);
     pr.fz[FZ_DPR][c] = dpdr;
     pr.fz[FZ_DPTH][c] = dpdthe;
     pr.fz[FZ_DPPH][c] = dpdphi;
@@ -235,7 +263,7 @@ __global__ void __launch_bounds__(256) mixed_prepare_kernel(const KConst K, cons
     pr.fz[FZ_GV][c] = d2f(gv);
     pr.fz[FZ_GW][c] = -dpmdphi;
     pr.fz[FZ_BAN][c] = d2f(ban);
-    pr.fz[FZ_BPS][c] = d2f(bps);
+    pr.fz[FZ_BPS][c] = bps_f;
 }
 
 }  // namespace
