@@ -84,6 +84,12 @@ struct atsat_dyn {
     cudaStream_t cstream = nullptr;
     cudaEvent_t ev_ready[2] = {}, ev_free[2] = {}, ev_join = nullptr;
     int stage_next = 0;
+    // bindings the SMs move in place (host_xfer.cu): host_ok when the device addresses host memory
+    // through the CPU's page tables, host_direct when that path is selected, per field whether its
+    // binding takes it, and the device copy of a ragged binding's row-pointer table
+    bool host_ok = false, host_direct = false;
+    bool direct[ATSAT_NFIELDS] = {};
+    double** dev_rows[ATSAT_NFIELDS] = {};
 
     int64_t launches = 0;
     bool profiling = false;
@@ -646,6 +652,70 @@ int download_one(atsat_dyn* h, int fid) {
     } else {
         return fail(h, ATSAT_DYN_E_UNBOUND, "field %d has no host binding", fid);
     }
+    return ATSAT_DYN_OK;
+}
+
+// The copy-engine path's resources for a binding: pinned staging for ragged rows, the device staging
+// pipeline for contiguous arrays whose rows the device pads.
+int staging_for(atsat_dyn* h, int fid) {
+    if (h->bind_kind[fid] == BIND_ROWS && !h->ev_pin[1]) {
+        CK(h, cudaSetDevice(h->device));
+        cudaError_t e = cudaSuccess;
+        for (int b = 0; b < 2 && e == cudaSuccess; b++) {
+            if (!h->pinned[b]) e = cudaHostAlloc(&h->pinned[b], (size_t)h->kc.fsz * 8, cudaHostAllocDefault);
+            if (e == cudaSuccess && !h->ev_pin[b]) e = cudaEventCreateWithFlags(&h->ev_pin[b], cudaEventDisableTiming);
+        }
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(h, ATSAT_DYN_E_NOMEM, "pinned staging: %s", cudaGetErrorString(e));
+        }
+    }
+    if (h->bind_kind[fid] == BIND_ARRAY && !h->cstream && h->kc.kp != h->kc.km) return stage_pipe_create(h);
+    return ATSAT_DYN_OK;
+}
+
+// Chooses the path of field fid's binding: the SMs in place when selected (a ragged binding's row table
+// then goes to the device once, here), else the copy engines.
+int route_binding(atsat_dyn* h, int fid) {
+    h->direct[fid] = false;
+    if (h->bind_kind[fid] == BIND_NONE) return ATSAT_DYN_OK;
+    bool aligned = (reinterpret_cast<uintptr_t>(h->bind_base[fid]) & 7u) == 0;   // whole doubles only
+    for (double* r : h->bind_rows[fid]) aligned = aligned && (reinterpret_cast<uintptr_t>(r) & 7u) == 0;
+    if (!h->host_direct || !aligned) return staging_for(h, fid);
+    if (h->bind_kind[fid] == BIND_ROWS) {
+        const size_t n = h->bind_rows[fid].size();
+        CK(h, cudaSetDevice(h->device));
+        if (!h->dev_rows[fid]) {
+            const cudaError_t e = cudaMalloc(&h->dev_rows[fid], n * sizeof(double*));
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return fail(h, ATSAT_DYN_E_NOMEM, "row table: %s", cudaGetErrorString(e));
+            }
+        }
+        CK(h, cudaMemcpy(h->dev_rows[fid], h->bind_rows[fid].data(), n * sizeof(double*), cudaMemcpyHostToDevice));
+    }
+    h->direct[fid] = true;
+    return ATSAT_DYN_OK;
+}
+
+int batch_flush(atsat_dyn* h, HostBatch& b, int to_device) {
+    if (b.n == 0) return ATSAT_DYN_OK;
+    const KConst& K = h->kc;
+    CK(h, launch_host_transfer(b, to_device, (int64_t)K.im * K.jm, K.km, K.kp, h->stream));
+    h->launches += 1;
+    b.n = 0;
+    return ATSAT_DYN_OK;
+}
+
+int batch_add(atsat_dyn* h, HostBatch& b, int fid, int to_device) {
+    if (b.n == HOST_BATCH_MAX) {
+        int rc = batch_flush(h, b, to_device);
+        if (rc) return rc;
+    }
+    HostField& f = b.f[b.n++];
+    f.base = h->bind_kind[fid] == BIND_ARRAY ? h->bind_base[fid] : nullptr;
+    f.rows = h->bind_kind[fid] == BIND_ROWS ? h->dev_rows[fid] : nullptr;
+    f.dev = h->f[fid];
     return ATSAT_DYN_OK;
 }
 
@@ -1479,6 +1549,19 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
     if ((e = cudaGetDevice(&h->device)) != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
     if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
         return cuda_fail(e, "cudaStreamCreate");
+    {
+        // host memory the SMs may address in place: both attributes, not just HMM's page migration
+        int pageable = 0, host_tables = 0;
+        if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, h->device) != cudaSuccess ||
+            cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, h->device) !=
+                cudaSuccess) {
+            cudaGetLastError();
+            pageable = host_tables = 0;
+        }
+        h->host_ok = pageable == 1 && host_tables == 1;
+        const char* env = std::getenv("ATSAT_HOST_DIRECT");
+        h->host_direct = h->host_ok && !(env && std::strcmp(env, "0") == 0);
+    }
     // fields, FP64 stage buffers and accumulators (FP64 path only), source; then the small tables
     const bool fp64_stage = p->precision != ATSAT_DYN_MIXED;
     const int64_t nbig = ATSAT_NFIELDS + (fp64_stage ? 2 * NPROG : 0) + 2;
@@ -1583,6 +1666,8 @@ void atsat_dyn_destroy(atsat_dyn_t h) {
         if (h->ev_pin[b]) cudaEventDestroy(h->ev_pin[b]);
     }
     stage_pipe_free(h);
+    for (int f = 0; f < ATSAT_NFIELDS; f++)
+        if (h->dev_rows[f]) cudaFree(h->dev_rows[f]);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -1595,35 +1680,40 @@ int atsat_dyn_bind_host_rows(atsat_dyn_t h, int32_t field, double* const* rows) 
     const size_t n = (size_t)h->kc.im * h->kc.jm;
     for (size_t r = 0; r < n; r++)
         if (!rows[r]) return fail(h, ATSAT_DYN_E_INVALID, "row %zu of field %d is null", r, field);
-    if (!h->ev_pin[1]) {
-        CK(h, cudaSetDevice(h->device));
-        cudaError_t e = cudaSuccess;
-        for (int b = 0; b < 2 && e == cudaSuccess; b++) {
-            if (!h->pinned[b]) e = cudaHostAlloc(&h->pinned[b], (size_t)h->kc.fsz * 8, cudaHostAllocDefault);
-            if (e == cudaSuccess && !h->ev_pin[b]) e = cudaEventCreateWithFlags(&h->ev_pin[b], cudaEventDisableTiming);
-        }
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            return fail(h, ATSAT_DYN_E_NOMEM, "pinned staging: %s", cudaGetErrorString(e));
-        }
-    }
     h->bind_rows[field].assign(rows, rows + n);
     h->bind_kind[field] = BIND_ROWS;
     h->bind_base[field] = nullptr;
-    return ATSAT_DYN_OK;
+    return route_binding(h, field);
 }
 
 int atsat_dyn_bind_host_array(atsat_dyn_t h, int32_t field, double* base) {
     if (!h || !h->slab) return ATSAT_DYN_E_INVALID;
     if (!valid_field(field)) return fail(h, ATSAT_DYN_E_INVALID, "bad field %d", field);
-    if (base && !h->cstream && h->kc.kp != h->kc.km) {
-        int rc = stage_pipe_create(h);
-        if (rc) return rc;
-    }
     h->bind_kind[field] = base ? BIND_ARRAY : BIND_NONE;
     h->bind_base[field] = base;
     h->bind_rows[field].clear();
+    return route_binding(h, field);
+}
+
+int atsat_dyn_set_host_direct(atsat_dyn_t h, int32_t enable) {
+    if (!h || !h->slab || (enable != 0 && enable != 1)) return ATSAT_DYN_E_INVALID;
+    if (enable && !h->host_ok)
+        return fail(h, ATSAT_DYN_E_UNSUPPORTED, "the device does not address host memory through its page tables");
+    CK(h, cudaSetDevice(h->device));
+    h->host_direct = enable != 0;
+    for (int f = 0; f < ATSAT_NFIELDS; f++)
+        if (h->bind_kind[f] != BIND_NONE) {
+            int rc = route_binding(h, f);
+            if (rc) return rc;
+        }
     return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_host_direct(atsat_dyn_t h, int32_t field) {
+    if (!h || !h->slab) return ATSAT_DYN_E_INVALID;
+    if (field == -1) return h->host_direct ? 1 : 0;
+    if (!valid_field(field)) return fail(h, ATSAT_DYN_E_INVALID, "bad field %d", field);
+    return h->direct[field] ? 1 : 0;
 }
 
 int atsat_dyn_upload(atsat_dyn_t h, const int32_t* fields, int32_t n) {
@@ -1635,24 +1725,37 @@ int atsat_dyn_upload(atsat_dyn_t h, const int32_t* fields, int32_t n) {
             if (rc) return rc;
             break;
         }
+    HostBatch b{};
     for (int32_t q = 0; q < n; q++) {
         if (!valid_field(fields[q])) return fail(h, ATSAT_DYN_E_INVALID, "bad field %d", fields[q]);
-        int rc = upload_one(h, fields[q]);
+        const int fid = fields[q];
+        int rc = ATSAT_DYN_OK;
+        if (h->direct[fid] && h->bind_kind[fid] != BIND_NONE) {
+            mark_dirty(h, fid);
+            rc = batch_add(h, b, fid, 1);
+        } else {
+            rc = upload_one(h, fid);
+        }
         if (rc) return rc;
     }
-    int rc = stage_join(h);
+    int rc = batch_flush(h, b, 1);
+    if (!rc) rc = stage_join(h);
     return rc ? rc : finish(h);
 }
 
 int atsat_dyn_download(atsat_dyn_t h, const int32_t* fields, int32_t n) {
     if (!h || !h->slab || (n > 0 && !fields)) return ATSAT_DYN_E_INVALID;
     CK(h, cudaSetDevice(h->device));
+    HostBatch b{};
     for (int32_t q = 0; q < n; q++) {
         if (!valid_field(fields[q])) return fail(h, ATSAT_DYN_E_INVALID, "bad field %d", fields[q]);
-        int rc = download_one(h, fields[q]);
+        const int fid = fields[q];
+        const int rc = (h->direct[fid] && h->bind_kind[fid] != BIND_NONE) ? batch_add(h, b, fid, 0)
+                                                                          : download_one(h, fid);
         if (rc) { h->rows_pending = -1; return rc; }
     }
-    int rc = rows_flush(h);
+    int rc = batch_flush(h, b, 0);
+    if (!rc) rc = rows_flush(h);
     if (!rc) rc = stage_join(h);
     return rc ? rc : finish(h);
 }

@@ -392,6 +392,19 @@ cudaError_t launch_copy_fields(const KConst& kc, double* const* dst, const doubl
 // s32 (may be null): FP32 copies to keep in step, indexed by field id; wlo: the second FP32 word of w.
 cudaError_t launch_boundary_conditions(const KConst& kc, const atsat_dyn_params& p, double* const* f,
                                        float* const* s32, float* wlo, cudaStream_t s);
+// a host binding moved by the SMs (host_xfer.cu): a contiguous array (`base`, rows of km doubles) or a
+// device-resident table of row pointers (`rows`), and the device field (rows of kp doubles)
+constexpr int HOST_BATCH_MAX = 64;
+struct HostField {
+    double* base;
+    double* const* rows;
+    double* dev;
+};
+struct HostBatch {
+    HostField f[HOST_BATCH_MAX];
+    int n;
+};
+cudaError_t launch_host_transfer(const HostBatch& b, int to_device, int64_t nrows, int km, int kp, cudaStream_t s);
 cudaError_t launch_repitch(double* dst, int dst_pitch, const double* src, int src_pitch, int width, int64_t rows,
                            cudaStream_t s);
 cudaError_t launch_count_nonfinite(const KConst& kc, const double* x, unsigned long long* count,

@@ -58,6 +58,8 @@ def lib():
         L.atsat_dyn_bind_host_array.argtypes = [H, C.c_int32, C.POINTER(C.c_double)]
         L.atsat_dyn_upload.argtypes = [H, C.POINTER(C.c_int32), C.c_int32]
         L.atsat_dyn_download.argtypes = [H, C.POINTER(C.c_int32), C.c_int32]
+        L.atsat_dyn_set_host_direct.argtypes = [H, C.c_int32]
+        L.atsat_dyn_host_direct.argtypes = [H, C.c_int32]
         L.atsat_dyn_set_tables.argtypes = [H, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.atsat_dyn_get_buoy_ref_level.argtypes = [H, C.POINTER(C.c_double)]
         for n in ("mixture_density", "buoyancy_ref_level", "metric_pressure", "rhs", "rk4_step",
@@ -216,6 +218,17 @@ class Dycore:
     def download(self, fids):
         ids = (C.c_int32 * len(fids))(*fids)
         self._ck(lib().atsat_dyn_download(self.h, ids, len(fids)), "download")
+
+    def set_host_direct(self, enable: bool):
+        """Move bound fields with one kernel that reads / writes host memory in place (NVLink-C2C, the
+        CPU's page tables), or with the copy engines through staging buffers."""
+        self._ck(lib().atsat_dyn_set_host_direct(self.h, 1 if enable else 0), "set_host_direct")
+
+    def host_direct(self, fid: int = -1) -> bool:
+        """Whether field fid's binding (fid -1: the handle) takes the in-place path."""
+        r = lib().atsat_dyn_host_direct(self.h, fid)
+        self._ck(min(r, 0), "host_direct")
+        return r == 1
 
     def set_tables(self, cell_vbar0=None, cell_ubar0=None, p_baro=None):
         self._tables = [None if a is None else np.ascontiguousarray(a, dtype=np.float64)

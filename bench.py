@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--e2e-rows-steps", type=int, default=4,
                     help="steps of the e2e loop over ragged pageable rows (0 skips it)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--copy-engines", action="store_true",
+                    help="move host bindings with the copy engines even where the SMs can address host memory")
     ap.add_argument("--stage-variant", default="auto",
                     choices=["auto", "direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2"],
                     help="mixed precision: the RK stage kernel (auto: the autotuner's choice)")
@@ -263,6 +265,8 @@ def measure(a, rank, world, g, P, st, pinned, precision):
     import numpy as np
     from atsat_gb300 import abi, dyn, fields as F
     d = dyn.Dycore(g, dict(P, precision=1 if precision == "mixed" else 0))
+    if a.copy_engines and d.host_direct():
+        d.set_host_direct(False)
     for fid in range(F.NFIELDS):
         pinned[fid].array[...] = 0.0 if st.arrays.get(fid) is None else st.arrays[fid]
         d.bind(fid, pinned[fid].array)
@@ -302,6 +306,10 @@ def measure(a, rank, world, g, P, st, pinned, precision):
     ins = F.STEP_INPUTS
     outs = F.STEP_OUTPUTS
 
+    def xfer_path(d):
+        return ("one kernel per upload / download reading and writing host memory in place over NVLink-C2C"
+                if d.host_direct() else "copy engines through staging buffers")
+
     def e2e_step(it):
         """One drop-in step: upload the inputs, pressure call on even steps, RK4, download; bytes moved."""
         up, down = len(ins) * g.cells * 8, len(outs) * g.cells * 8
@@ -332,7 +340,7 @@ def measure(a, rank, world, g, P, st, pinned, precision):
         e2e = {"value": world * a.e2e_steps * g.cells / e2e_s / 1e6, "unit": UNIT,
                "h2d_bytes_per_step": h2d // a.e2e_steps, "d2h_bytes_per_step": d2h // a.e2e_steps,
                "steps": a.e2e_steps, "ms_per_step": e2e_s * 1e3 / a.e2e_steps,
-               "binding": "contiguous pinned arrays (bind_host_array)"}
+               "binding": "contiguous pinned arrays (bind_host_array)", "path": xfer_path(d)}
 
     # the same loop over the reference's own storage: one pageable row of km doubles per (i, j), as
     # lib/Array.cpp allocates it, bound through bind_host_rows (packed on the host into pinned staging)
@@ -353,7 +361,8 @@ def measure(a, rank, world, g, P, st, pinned, precision):
         rows_s = reduce_max(world, time.perf_counter() - t0)
         e2e["rows"] = {"value": world * a.e2e_rows_steps * g.cells / rows_s / 1e6, "unit": UNIT,
                        "steps": a.e2e_rows_steps, "ms_per_step": rows_s * 1e3 / a.e2e_rows_steps,
-                       "binding": "ragged pageable rows (bind_host_rows)", "host_threads": omp_threads()}
+                       "binding": "ragged pageable rows (bind_host_rows)", "path": xfer_path(d),
+                       "host_threads": omp_threads()}
         del keep
 
     peak, peak_kind = peaks()

@@ -221,6 +221,15 @@ int atsat_dyn_bind_host_rows(atsat_dyn_t h, int32_t field, double* const* rows);
 int atsat_dyn_bind_host_array(atsat_dyn_t h, int32_t field, double* base);
 int atsat_dyn_upload(atsat_dyn_t h, const int32_t* fields, int32_t n);
 int atsat_dyn_download(atsat_dyn_t h, const int32_t* fields, int32_t n);
+/* Where the device addresses host memory through the CPU's page tables (Grace-Blackwell, NVLink-C2C:
+ * cudaDevAttrPageableMemoryAccessUsesHostPageTables), bound fields are moved by one kernel per upload or
+ * download that reads or writes the host arrays or rows in place; elsewhere by the copy engines through
+ * staging buffers. On by default where available; ATSAT_HOST_DIRECT=0 in the environment at create, or
+ * atsat_dyn_set_host_direct(h, 0), selects the copy engines. Setting 1 where the device cannot address
+ * host memory returns ATSAT_DYN_E_UNSUPPORTED. atsat_dyn_host_direct returns 1 when `field`'s binding
+ * (or, for field -1, the handle) uses the direct path, 0 when not, a negative code on error. */
+int atsat_dyn_set_host_direct(atsat_dyn_t h, int32_t enable);
+int atsat_dyn_host_direct(atsat_dyn_t h, int32_t field);
 
 /* cell_vbar0 / cell_ubar0: im*jm values or NULL (empty vectors); p_baro: im*jm*km values or NULL. */
 int atsat_dyn_set_tables(atsat_dyn_t h, const double* cell_vbar0, const double* cell_ubar0,
