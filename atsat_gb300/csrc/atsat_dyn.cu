@@ -1175,12 +1175,14 @@ int enqueue_restore(atsat_dyn* h, bool resident = false) {
 }
 
 // Give the n-level fields their own buffers again (a copy of the shared values) before any call that
-// can observe the live and n-level fields separately.
-int unalias(atsat_dyn* h) {
+// can observe the live and n-level fields separately. `overwritten[q]`: n-level field q is about to be
+// replaced as a whole (an upload), so its buffer needs no copy.
+int unalias(atsat_dyn* h, const bool* overwritten = nullptr) {
     if (!h->aliased) return ATSAT_DYN_OK;
     const size_t bytes = (size_t)h->kc.fsz * 8;
     for (int q = 0; q < NPROG; q++) {
-        CK(h, cudaMemcpyAsync(h->spare_n[q], h->f[q], bytes, cudaMemcpyDeviceToDevice, h->stream));
+        if (!(overwritten && overwritten[q]))
+            CK(h, cudaMemcpyAsync(h->spare_n[q], h->f[q], bytes, cudaMemcpyDeviceToDevice, h->stream));
         h->f[ATSAT_F_N_BASE + q] = h->spare_n[q];
     }
     h->aliased = false;
@@ -1719,12 +1721,17 @@ int atsat_dyn_host_direct(atsat_dyn_t h, int32_t field) {
 int atsat_dyn_upload(atsat_dyn_t h, const int32_t* fields, int32_t n) {
     if (!h || !h->slab || (n > 0 && !fields)) return ATSAT_DYN_E_INVALID;
     CK(h, cudaSetDevice(h->device));
-    for (int32_t q = 0; q < n; q++)
-        if (fields[q] >= 0 && fields[q] < ATSAT_F_N_BASE + NPROG) {
-            int rc = unalias(h);
-            if (rc) return rc;
-            break;
-        }
+    bool n_level[NPROG] = {};
+    bool prog = false;
+    for (int32_t q = 0; q < n; q++) {
+        if (fields[q] >= 0 && fields[q] < ATSAT_F_N_BASE + NPROG) prog = true;
+        if (fields[q] >= ATSAT_F_N_BASE && fields[q] < ATSAT_F_N_BASE + NPROG && h->bind_kind[fields[q]] != BIND_NONE)
+            n_level[fields[q] - ATSAT_F_N_BASE] = true;
+    }
+    if (prog) {
+        int rc = unalias(h, n_level);
+        if (rc) return rc;
+    }
     HostBatch b{};
     for (int32_t q = 0; q < n; q++) {
         if (!valid_field(fields[q])) return fail(h, ATSAT_DYN_E_INVALID, "bad field %d", fields[q]);

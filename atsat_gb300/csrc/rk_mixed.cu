@@ -157,6 +157,8 @@ __global__ void __launch_bounds__(256) mixed_prepare_kernel(const KConst K, cons
     const int64_t P = K.plane;
     const int kp = K.kp;
     const int64_t c = ((int64_t)i * K.jm + j) * kp + k;
+    // dl0[0] is the stage-0 input (every cell); dl0[1], dl0[2] need live - y_n only where no stage writes
+    const bool rk_cell = (i >= 1 && i <= K.im - 2 && j >= 2 && j <= K.jm - 3 && k <= K.km - 2);
     if (pr.write_yn32) {
         for (int q = 0; q < NPROG; q++) {
             const double yn = __ldg(pr.yn64[q] + c);
@@ -172,15 +174,14 @@ __global__ void __launch_bounds__(256) mixed_prepare_kernel(const KConst K, cons
                 const float d0 = d2f(__ldg(pr.live64[q] + c) - yn);
 #pragma unroll
                 for (int b = 0; b < 3; b++)
-                    if (pr.dl0[b][q]) pr.dl0[b][q][c] = d0;
+                    if (pr.dl0[b][q] && (b == 0 || !rk_cell)) pr.dl0[b][q][c] = d0;
             }
         }
     }
     for (int q = 0; q < pr.nconv; q++) pr.conv_dst[q][c] = d2f(__ldg(pr.conv_src[q] + c));
     if (pr.skip_frozen) return;
 
-    const bool interior = (i >= 1 && i <= K.im - 2 && j >= 2 && j <= K.jm - 3 && k <= K.km - 2);
-    if (!interior) return;
+    if (!rk_cell) return;
     const int kw = (k == 0) ? K.km - 2 : k - 1;
     const int ke = (k == K.km - 2) ? 0 : k + 1;
     const int64_t cw = c - k + kw, ce = c - k + ke;
