@@ -250,7 +250,7 @@ class Dycore:
         self._ck(lib().atsat_dyn_set_write_all_rhs(self.h, int(bool(on))), "set_write_all_rhs")
 
     STAGE_DIRECT, STAGE_TILED, STAGE_SPLIT, STAGE_SPLIT3, STAGE_SPLIT13, STAGE_SPLIT_TILED, STAGE_TILED2 = range(7)
-    STAGE_NAMES = ["direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2"]
+    STAGE_NAMES = ["direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2", "tiled2_conc"]
 
     def set_stage_variant(self, variant: int):
         """Mixed precision: the RK stage kernel (STAGE_* constants)."""

@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--copy-engines", action="store_true",
                     help="move host bindings with the copy engines even where the SMs can address host memory")
     ap.add_argument("--stage-variant", default="auto",
-                    choices=["auto", "direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2"],
+                    choices=["auto", "direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2", "tiled2_conc"],
                     help="mixed precision: the RK stage kernel (auto: the autotuner's choice)")
     ap.add_argument("--poisson", action="store_true",
                     help="the standalone pressure-equation solves instead of the dycore iteration")
@@ -202,7 +202,10 @@ KERNEL_NAME = {"fp64": "rk_stage_fp64_kernel (fused RHSSat + RK4 stage, FP64)",
                "mixed_split_tiled": "rk_mom_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, TMA-tiled tracers; "
                                     "final stage + final_combine_kernel)",
                "mixed_tiled2": "rk_mom_tile_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, all inputs "
-                               "TMA-streamed; final stage + final_combine_kernel)"}
+                               "TMA-streamed; final stage + final_combine_kernel)",
+               "mixed_tiled2_conc": "rk_mom_tile_kernel || rk_tracer_tile_kernel (split RHSSat + RK4 stage, all "
+                                    "inputs TMA-streamed, the two kernels concurrent on two streams; final stage + "
+                                    "final_combine_kernel)"}
 
 
 def cpu_baseline(g, P, seed, target_s=3.0):

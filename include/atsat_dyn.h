@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define ATSAT_DYN_ABI_VERSION 1
+#define ATSAT_DYN_ABI_VERSION 2
 
 /* ---- status codes ---- */
 enum {
@@ -380,7 +380,9 @@ int atsat_dyn_set_write_all_rhs(atsat_dyn_t h, int32_t on);
  *   SPLIT*   a momentum / temperature kernel, then a tracer kernel with 1, 3 or 13 threads per cell
  *            (not with species_divu on);
  *   SPLIT_TILED  the same momentum kernel, then the tracers TMA-tiled (4 radial levels per thread);
- *   TILED2   both the momentum / temperature and the tracer kernels TMA-tiled, every input streamed.
+ *   TILED2   both the momentum / temperature and the tracer kernels TMA-tiled, every input streamed;
+ *   TILED2_CONC  the TILED2 kernels on two streams at once (their outputs are disjoint and neither reads
+ *            what the other writes), so the latency-bound momentum kernel overlaps the tracer kernel.
  * The default is TILED where available. No reference counterpart (the reference has one CPU loop
  * nest). Setting an unavailable variant returns ATSAT_DYN_E_UNSUPPORTED. */
 enum {
@@ -391,7 +393,8 @@ enum {
     ATSAT_DYN_STAGE_SPLIT13 = 4,
     ATSAT_DYN_STAGE_SPLIT_TILED = 5,
     ATSAT_DYN_STAGE_TILED2 = 6,
-    ATSAT_DYN_STAGE_NVARIANT = 7
+    ATSAT_DYN_STAGE_TILED2_CONC = 7,
+    ATSAT_DYN_STAGE_NVARIANT = 8
 };
 int atsat_dyn_set_stage_variant(atsat_dyn_t h, int32_t variant);
 int atsat_dyn_get_stage_variant(atsat_dyn_t h, int32_t* variant);
