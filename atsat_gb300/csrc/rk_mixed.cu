@@ -160,6 +160,7 @@ __global__ void __launch_bounds__(256) mixed_prepare_kernel(const KConst K, cons
     // dl0[0] is the stage-0 input (every cell); dl0[1], dl0[2] need live - y_n only where no stage writes
     const bool rk_cell = (i >= 1 && i <= K.im - 2 && j >= 2 && j <= K.jm - 3 && k <= K.km - 2);
     if (pr.write_yn32) {
+#pragma unroll 4
         for (int q = 0; q < NPROG; q++) {
             const double yn = __ldg(pr.yn64[q] + c);
             const float hi = d2f(yn);
@@ -178,7 +179,16 @@ __global__ void __launch_bounds__(256) mixed_prepare_kernel(const KConst K, cons
             }
         }
     }
-    for (int q = 0; q < pr.nconv; q++) pr.conv_dst[q][c] = d2f(__ldg(pr.conv_src[q] + c));
+    // the dirty point inputs, four loads in flight per thread
+    for (int q0 = 0; q0 < pr.nconv; q0 += 4) {
+        double v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (q0 + u < pr.nconv) v[u] = __ldg(pr.conv_src[q0 + u] + c);
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (q0 + u < pr.nconv) pr.conv_dst[q0 + u][c] = d2f(v[u]);
+    }
     if (pr.skip_frozen) return;
 
     if (!rk_cell) return;
