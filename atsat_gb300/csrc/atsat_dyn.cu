@@ -38,9 +38,6 @@ struct atsat_dyn {
     KConst kc{};
     int device = 0;
     cudaStream_t stream = nullptr;
-    // the second stream of the concurrent split stage (TILED2_CONC): fork and join events
-    cudaStream_t stream2 = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join2 = nullptr;
 
     double* slab = nullptr;              // one allocation for every device array below
     double* f[ATSAT_NFIELDS] = {};
@@ -96,6 +93,7 @@ struct atsat_dyn {
 
     int64_t launches = 0;
     bool profiling = false;
+    uint32_t prof_mask = ~0u;            // the kernel classes profiled
     std::vector<ProfEvent> pend;
     std::vector<cudaEvent_t> pool;
     int64_t prof_n[ATSAT_K_NCLASS] = {};
@@ -180,14 +178,14 @@ struct Timed {
     int cls;
     cudaEvent_t a = nullptr, b = nullptr;
     Timed(atsat_dyn* h_, int cls_) : h(h_), cls(cls_) {
-        if (h->profiling) {
+        if (h->profiling && ((h->prof_mask >> cls) & 1u)) {
             a = ev_get(h);
             b = ev_get(h);
             cudaEventRecord(a, h->stream);
         }
     }
     ~Timed() {
-        if (h->profiling) {
+        if (a) {
             cudaEventRecord(b, h->stream);
             h->pend.push_back({cls, a, b});
         }
@@ -929,8 +927,6 @@ bool variant_available(const atsat_dyn* h, int v) {
         case ATSAT_DYN_STAGE_SPLIT13: return !h->kc.divu_on;
         case ATSAT_DYN_STAGE_SPLIT_TILED:
         case ATSAT_DYN_STAGE_TILED2: return !h->kc.divu_on && h->tile_ok && !h->kf.fsz_over_int;
-        case ATSAT_DYN_STAGE_TILED2_CONC:
-            return !h->kc.divu_on && h->tile_ok && !h->kf.fsz_over_int && h->stream2 && h->ev_fork && h->ev_join2;
         default: return false;
     }
 }
@@ -1020,27 +1016,15 @@ cudaError_t launch_stage(atsat_dyn* h, const MixedIO& io, const StageParams& sp,
                 return cudaErrorInvalidValue;   // the plan and the kernel disagree: never expected
             return launch_rk_tracer_tile(h->maps, h->kf, io, sp, pl, mode, h->stream);
         }
-        case ATSAT_DYN_STAGE_TILED2:
-        case ATSAT_DYN_STAGE_TILED2_CONC: {
+        case ATSAT_DYN_STAGE_TILED2: {
             const TracerPlan pm = make_plan_mom(h, io);
             const TracerPlan pt = make_plan_tracer(h, io, mode);
             const bool dl = io.dl_in[0] != nullptr;
             if (pm.n_items != mom_plan_items(dl) || pt.n_items != tracer_plan_items(mode, dl, h->kc.turb != 0))
                 return cudaErrorInvalidValue;   // the plans and the kernels disagree: never expected
-            if (v == ATSAT_DYN_STAGE_TILED2) {
-                const cudaError_t e = launch_rk_mom_tile(h->maps, h->kf, io, sp, pm, mode, h->stream);
-                if (e != cudaSuccess) return e;
-                return launch_rk_tracer_tile(h->maps, h->kf, io, sp, pt, mode, h->stream);
-            }
-            // the tracers (and the final stage's combine) on the second stream, forked from and joined back
-            // into the handle's stream: the two kernels write disjoint fields and read only stage inputs
-            cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream2, h->ev_fork, 0);
-            if (e == cudaSuccess) e = launch_rk_tracer_tile(h->maps, h->kf, io, sp, pt, mode, h->stream2);
-            if (e == cudaSuccess) e = launch_rk_mom_tile(h->maps, h->kf, io, sp, pm, mode, h->stream);
-            if (e == cudaSuccess) e = cudaEventRecord(h->ev_join2, h->stream2);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, h->ev_join2, 0);
-            return e;
+            const cudaError_t e = launch_rk_mom_tile(h->maps, h->kf, io, sp, pm, mode, h->stream);
+            if (e != cudaSuccess) return e;
+            return launch_rk_tracer_tile(h->maps, h->kf, io, sp, pt, mode, h->stream);
         }
         default: return launch_rk_stage_mixed(h->kf, io, sp, mode, h->stream);
     }
@@ -1098,9 +1082,7 @@ int enqueue_rk4_mixed(atsat_dyn* h, bool resident) {
         h->launches += launches_per_stage(h);
         // the TMA-tiled tracer kernel leaves the final stage's FP64 sum to launch_final_combine
         const int v = variant_available(h, h->variant) ? h->variant : ATSAT_DYN_STAGE_DIRECT;
-        if (stage == 3 && (v == ATSAT_DYN_STAGE_SPLIT_TILED || v == ATSAT_DYN_STAGE_TILED2 ||
-                           v == ATSAT_DYN_STAGE_TILED2_CONC))
-            h->launches += 1;
+        if (stage == 3 && (v == ATSAT_DYN_STAGE_SPLIT_TILED || v == ATSAT_DYN_STAGE_TILED2)) h->launches += 1;
     }
     return ATSAT_DYN_OK;
 }
@@ -1570,10 +1552,6 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
     if ((e = cudaGetDevice(&h->device)) != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
     if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
         return cuda_fail(e, "cudaStreamCreate");
-    if ((e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
-        (e = cudaEventCreateWithFlags(&h->ev_join2, cudaEventDisableTiming)) != cudaSuccess)
-        return cuda_fail(e, "second stream");
     {
         // host memory the SMs may address in place: both attributes, not just HMM's page migration
         int pageable = 0, host_tables = 0;
@@ -1693,10 +1671,6 @@ void atsat_dyn_destroy(atsat_dyn_t h) {
     stage_pipe_free(h);
     for (int f = 0; f < ATSAT_NFIELDS; f++)
         if (h->dev_rows[f]) cudaFree(h->dev_rows[f]);
-    if (h->stream2) cudaStreamSynchronize(h->stream2);
-    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
-    if (h->ev_join2) cudaEventDestroy(h->ev_join2);
-    if (h->stream2) cudaStreamDestroy(h->stream2);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -2371,6 +2345,15 @@ int atsat_dyn_profile(atsat_dyn_t h, int32_t enable) {
     if (!h) return ATSAT_DYN_E_INVALID;
     int rc = resolve_profile(h);
     h->profiling = enable != 0;
+    h->prof_mask = ~0u;
+    return rc;
+}
+
+int atsat_dyn_profile_classes(atsat_dyn_t h, uint32_t mask) {
+    if (!h) return ATSAT_DYN_E_INVALID;
+    int rc = resolve_profile(h);
+    h->profiling = mask != 0;
+    h->prof_mask = mask;
     return rc;
 }
 

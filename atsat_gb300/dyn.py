@@ -72,6 +72,7 @@ def lib():
         L.atsat_dyn_status.argtypes = [H, C.POINTER(abi.Diag)]
         L.atsat_dyn_count_nonfinite.argtypes = [H, C.c_int32, C.POINTER(C.c_int64)]
         L.atsat_dyn_profile.argtypes = [H, C.c_int32]
+        L.atsat_dyn_profile_classes.argtypes = [H, C.c_uint32]
         L.atsat_dyn_profile_reset.argtypes = [H]
         L.atsat_dyn_profile_read.argtypes = [H, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_double)]
         L.atsat_dyn_device_field.argtypes = [H, C.c_int32, C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_int64)]
@@ -250,7 +251,7 @@ class Dycore:
         self._ck(lib().atsat_dyn_set_write_all_rhs(self.h, int(bool(on))), "set_write_all_rhs")
 
     STAGE_DIRECT, STAGE_TILED, STAGE_SPLIT, STAGE_SPLIT3, STAGE_SPLIT13, STAGE_SPLIT_TILED, STAGE_TILED2 = range(7)
-    STAGE_NAMES = ["direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2", "tiled2_conc"]
+    STAGE_NAMES = ["direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2"]
 
     def set_stage_variant(self, variant: int):
         """Mixed precision: the RK stage kernel (STAGE_* constants)."""
@@ -421,6 +422,13 @@ class Dycore:
 
     def profile(self, on: bool):
         self._ck(lib().atsat_dyn_profile(self.h, int(on)), "profile")
+
+    def profile_classes(self, classes):
+        """Profile only the given kernel classes (abi.K_* ids)."""
+        mask = 0
+        for c in classes:
+            mask |= 1 << int(c)
+        self._ck(lib().atsat_dyn_profile_classes(self.h, mask), "profile_classes")
 
     def profile_reset(self):
         self._ck(lib().atsat_dyn_profile_reset(self.h), "profile_reset")

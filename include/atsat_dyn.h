@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define ATSAT_DYN_ABI_VERSION 2
+#define ATSAT_DYN_ABI_VERSION 1
 
 /* ---- status codes ---- */
 enum {
@@ -359,6 +359,9 @@ enum {
     ATSAT_K_NCLASS
 };
 int atsat_dyn_profile(atsat_dyn_t h, int32_t enable);
+/* Profile only the kernel classes whose bit (1 << ATSAT_K_*) is set in mask (0: none); each timed launch
+ * group adds two event records to the stream, so a narrow mask keeps a timed region close to unprofiled. */
+int atsat_dyn_profile_classes(atsat_dyn_t h, uint32_t mask);
 int atsat_dyn_profile_reset(atsat_dyn_t h);
 int atsat_dyn_profile_read(atsat_dyn_t h, int32_t kclass, int64_t* launches, double* ms);
 /* Wall time of the handle's stream between two marks, from CUDA events recorded on that stream:
@@ -380,9 +383,7 @@ int atsat_dyn_set_write_all_rhs(atsat_dyn_t h, int32_t on);
  *   SPLIT*   a momentum / temperature kernel, then a tracer kernel with 1, 3 or 13 threads per cell
  *            (not with species_divu on);
  *   SPLIT_TILED  the same momentum kernel, then the tracers TMA-tiled (4 radial levels per thread);
- *   TILED2   both the momentum / temperature and the tracer kernels TMA-tiled, every input streamed;
- *   TILED2_CONC  the TILED2 kernels on two streams at once (their outputs are disjoint and neither reads
- *            what the other writes), so the latency-bound momentum kernel overlaps the tracer kernel.
+ *   TILED2   both the momentum / temperature and the tracer kernels TMA-tiled, every input streamed.
  * The default is TILED where available. No reference counterpart (the reference has one CPU loop
  * nest). Setting an unavailable variant returns ATSAT_DYN_E_UNSUPPORTED. */
 enum {
@@ -393,8 +394,7 @@ enum {
     ATSAT_DYN_STAGE_SPLIT13 = 4,
     ATSAT_DYN_STAGE_SPLIT_TILED = 5,
     ATSAT_DYN_STAGE_TILED2 = 6,
-    ATSAT_DYN_STAGE_TILED2_CONC = 7,
-    ATSAT_DYN_STAGE_NVARIANT = 8
+    ATSAT_DYN_STAGE_NVARIANT = 7
 };
 int atsat_dyn_set_stage_variant(atsat_dyn_t h, int32_t variant);
 int atsat_dyn_get_stage_variant(atsat_dyn_t h, int32_t* variant);

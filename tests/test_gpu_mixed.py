@@ -29,10 +29,10 @@ def drift(got, ref, fids):
     return out
 
 
-DIRECT, TILED, SPLIT, SPLIT3, SPLIT13, SPLIT_TILED, TILED2, TILED2_CONC = range(8)
+DIRECT, TILED, SPLIT, SPLIT3, SPLIT13, SPLIT_TILED, TILED2 = range(7)
 VARIANTS = [pytest.param(v, id=n) for v, n in
             [(TILED, "tiled"), (DIRECT, "direct"), (SPLIT, "split"), (SPLIT3, "split3"), (SPLIT13, "split13"),
-             (SPLIT_TILED, "split_tiled"), (TILED2, "tiled2"), (TILED2_CONC, "tiled2_conc")]]
+             (SPLIT_TILED, "split_tiled"), (TILED2, "tiled2")]]
 
 _REF = {}
 
@@ -302,46 +302,3 @@ def test_ensemble_concurrent_equals_sequential():
         for f in F.PROG + [F.P_DYN]:
             assert np.array_equal(runs[0][m].arrays[f], runs[1][m].arrays[f]), (shp, F.NAMES[f])
             assert np.array_equal(runs[0][m].arrays[f], s.arrays[f]), (shp, F.NAMES[f])
-
-
-def test_concurrent_split_stage_is_bitwise_tiled2():
-    """TILED2_CONC runs TILED2's kernels on two streams at once: the same arithmetic on disjoint outputs,
-    so any difference from TILED2 would be a race between them. Bitwise after resident iterations (with
-    turbulence, the pressure call and the boundary conditions) and after a drop-in step."""
-    from atsat_gb300 import dyn
-    g, P, st = case((21, 91, 181), seed=61)
-    out = {}
-    for v in (TILED2, TILED2_CONC):
-        s = st.copy()
-        with dyn.Dycore(g, dict(P, precision=1)) as d:
-            d.set_stage_variant(v)
-            d.load_state(s)
-            d.iterate(1, 4)
-            d.download(ALL)
-            d.RungeKuttaSat()
-            d.download(ALL)
-        out[v] = s
-    for fid in F.PROG + [F.RHS_U, F.RHS_V, F.RHS_W] + F.AUX_FIELDS:
-        assert np.array_equal(out[TILED2].arrays[fid], out[TILED2_CONC].arrays[fid]), F.NAMES[fid]
-
-
-def test_graph_replay_with_concurrent_split_stage():
-    """The two-stream stage inside a captured CUDA graph (forked and joined by events): replays give the
-    state of plain iterations bit for bit."""
-    from atsat_gb300 import dyn
-    g, P, st = case((21, 91, 181), seed=71, exercise=True)
-    a, b = st.copy(), st.copy()
-    with dyn.Dycore(g, dict(P, precision=1)) as d:
-        d.set_stage_variant(TILED2_CONC)
-        d.load_state(a)
-        d.iterate(1, 2)
-        d.graph_capture(3, 2)
-        d.graph_launch(2)
-        d.download(ALL)
-    with dyn.Dycore(g, dict(P, precision=1)) as d:
-        d.set_stage_variant(TILED2_CONC)
-        d.load_state(b)
-        d.iterate(1, 6)
-        d.download(ALL)
-    for f in F.PROG + F.PROG_N + [F.P_DYN, F.RHS_U, F.AUX_W]:
-        assert np.array_equal(a.arrays[f], b.arrays[f], equal_nan=True), F.NAMES[f]
