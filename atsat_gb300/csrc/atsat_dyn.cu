@@ -55,6 +55,7 @@ struct atsat_dyn {
     // clampNegativeSpecies' budget: added[11], added_bnd[11] (doubles), cells[11], cells_bnd[11] (counts)
     double* clamp_added = nullptr;
     unsigned long long* clamp_cells = nullptr;
+    double* clamp_partial = nullptr;     // the floor's per-block sums
     double *line_cp = nullptr, *line_dp = nullptr, *imean_partial = nullptr, *pmean = nullptr;
     BaroTables baro{};
     double* p_baro = nullptr;            // null unless set
@@ -1258,8 +1259,9 @@ int enqueue_clamp(atsat_dyn* h, bool resident = false) {
         f[q] = h->f[CLAMP_SPECIES[q]];
         s32[q] = shadows ? h->yo32[CLAMP_SPECIES[q]] : nullptr;
     }
-    CK(h, launch_clamp_species(h->kc, f, shadows ? s32 : nullptr, h->clamp_added, h->clamp_cells, h->stream));
-    h->launches += 1;
+    CK(h, launch_clamp_species(h->kc, f, shadows ? s32 : nullptr, h->clamp_added, h->clamp_cells, h->clamp_partial,
+                               h->stream));
+    h->launches += 2;
     return ATSAT_DYN_OK;
 }
 
@@ -1644,8 +1646,10 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
         const int trc = setup_turbulence(h);
         if (trc) return trc;
     }
-    if ((e = cudaMalloc(&h->clamp_added, 22 * 8 + 22 * 8)) != cudaSuccess) return cuda_fail(e, "cudaMalloc (budget)");
+    if ((e = cudaMalloc(&h->clamp_added, (44 + clamp_partial_doubles()) * 8)) != cudaSuccess)
+        return cuda_fail(e, "cudaMalloc (budget)");
     h->clamp_cells = reinterpret_cast<unsigned long long*>(h->clamp_added + 22);
+    h->clamp_partial = h->clamp_added + 44;
     if ((e = cudaMemset(h->clamp_added, 0, 44 * 8)) != cudaSuccess) return cuda_fail(e, "cudaMemset (budget)");
     *out = h;
     return setup_press_variants(h);

@@ -352,8 +352,10 @@ cudaError_t launch_press_boundary(const KConst& kc, double* p, cudaStream_t s);
 // the driver's glue (glue.cu): one axis of AtomUtils::damp_wiggles; cSaturnModel::clampNegativeSpecies
 cudaError_t launch_damp_axis(const KConst& kc, const double* tmp, double* f, double coeff, int axis, int seam,
                              cudaStream_t s);
+// the species floor; `partial` holds clamp_partial_doubles() doubles of per-block sums
+size_t clamp_partial_doubles();
 cudaError_t launch_clamp_species(const KConst& kc, double* const f[11], float* const s32[11], double* added,
-                                 unsigned long long* cells, cudaStream_t s);
+                                 unsigned long long* cells, double* partial, cudaStream_t s);
 
 // the final stage's FP64 half of fields q0..q1 after a tiled stage kernel (rk_mixed.cu)
 cudaError_t launch_final_combine(const MixedConstF& kf, const MixedIO& io, int q0, int q1, cudaStream_t s);

@@ -259,44 +259,83 @@ __global__ void __launch_bounds__(256) damp_axis_kernel(const KConst K, const do
 }
 
 // ---- cSaturnModel::clampNegativeSpecies (FileIO_Sat.cpp:716-772) ----
-// blockIdx.z = species * im + i. !(v >= 0) (NaN included) becomes 0 in the FP64 field and, when given,
-// its FP32 copy; the finite amounts clipped and the cells are summed per warp and added to the budget:
-// added[11], added_bnd[11] (doubles), then cells[11], cells_bnd[11] (64-bit counts).
+// !(v >= 0) (NaN included) becomes 0 in the FP64 field and, when given, its FP32 copy. The finite amounts
+// clipped and the cells, in the whole field and on the radial planes i = 0, im-1, form the budget:
+// added[11], added_bnd[11] (doubles), then cells[11], cells_bnd[11] (64-bit counts). An evolved state has
+// undershoots in most cells of some species, so the sums are two-level and deterministic: each of CL_NB
+// blocks per species walks a contiguous range of the field's cells and writes its four sums to `partial`;
+// one small kernel adds the blocks' sums in block order to the budget (no atomics on the 22 totals).
+constexpr int CL_NB = 128, CL_THREADS = 256;
+
 struct ClampArgs {
     double* f[11];
     float* s32[11];
     double* added;
     unsigned long long* cells;
+    double* partial;               // [11][CL_NB][4]
 };
 
-__global__ void __launch_bounds__(256) clamp_species_kernel(const KConst K, const ClampArgs A) {
-    const int k = blockIdx.x * 32 + threadIdx.x;
-    const int j = blockIdx.y * 8 + threadIdx.y;
-    const int q = blockIdx.z / K.im, i = blockIdx.z % K.im;
-    double add = 0.0;
-    unsigned cnt = 0;
-    if (k < K.km && j < K.jm) {
-        const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
-        const double v = A.f[q][c];
+__global__ void __launch_bounds__(CL_THREADS) clamp_species_kernel(const KConst K, const ClampArgs A) {
+    const int q = blockIdx.y;
+    const int64_t n = (int64_t)K.im * K.jm * K.km;
+    const int64_t per = (n + CL_NB - 1) / CL_NB;
+    const int64_t e0 = per * blockIdx.x, e1 = e0 + per < n ? e0 + per : n;
+    const int64_t rb_lo = K.jm, rb_hi = (int64_t)(K.im - 1) * K.jm;   // rows r = i jm + j of i = 0 and im-1
+    const bool small = n < (1 << 24);                                  // the FP32 row estimate is exact
+    const float inv_km = 1.0f / (float)K.km;
+    double* f = A.f[q];
+    float* s32 = A.s32[q];
+    double s[4] = {0.0, 0.0, 0.0, 0.0};                               // added, added_bnd, cells, cells_bnd
+    for (int64_t e = e0 + threadIdx.x; e < e1; e += CL_THREADS) {
+        int64_t r, k;
+        if (small) {
+            int ri = (int)((float)e * inv_km);
+            int ki = (int)e - ri * K.km;
+            if (ki < 0) { ri--; ki += K.km; }
+            else if (ki >= K.km) { ri++; ki -= K.km; }
+            r = ri;
+            k = ki;
+        } else {
+            r = e / K.km;
+            k = e - r * K.km;
+        }
+        const int64_t c = r * K.kp + k;
+        const double v = f[c];
         if (!(v >= 0.0)) {
-            if (isfinite(v)) { add = -v; cnt = 1; }
-            A.f[q][c] = 0.0;
-            if (A.s32[q]) A.s32[q][c] = 0.0f;
+            f[c] = 0.0;
+            if (s32) s32[c] = 0.0f;
+            if (isfinite(v)) {
+                s[0] -= v;
+                s[2] += 1.0;
+                if (r < rb_lo || r >= rb_hi) { s[1] -= v; s[3] += 1.0; }
+            }
         }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        add += __shfl_down_sync(0xffffffffu, add, o);
-        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    __shared__ double red[CL_THREADS / 32][4];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        for (int o = 16; o > 0; o >>= 1) s[m] += __shfl_down_sync(0xffffffffu, s[m], o);
+        if (lane == 0) red[warp][m] = s[m];
     }
-    if ((threadIdx.x & 31) == 0 && cnt) {
-        const bool bnd = (i == 0 || i == K.im - 1);
-        atomicAdd(A.added + q, add);
-        atomicAdd(A.cells + q, (unsigned long long)cnt);
-        if (bnd) {
-            atomicAdd(A.added + 11 + q, add);
-            atomicAdd(A.cells + 11 + q, (unsigned long long)cnt);
-        }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0.0;
+        for (int w = 0; w < CL_THREADS / 32; w++) t += red[w][threadIdx.x];
+        A.partial[((int64_t)q * CL_NB + blockIdx.x) * 4 + threadIdx.x] = t;
     }
+}
+
+__global__ void clamp_budget_kernel(const ClampArgs A) {
+    const int q = threadIdx.x;
+    if (q >= 11) return;
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int b = 0; b < CL_NB; b++)
+        for (int m = 0; m < 4; m++) t[m] += A.partial[((int64_t)q * CL_NB + b) * 4 + m];
+    A.added[q] += t[0];
+    A.added[11 + q] += t[1];
+    A.cells[q] += (unsigned long long)t[2];
+    A.cells[11 + q] += (unsigned long long)t[3];
 }
 
 // cSaturnModel::restart_state_is_clean (FileIO_Sat.cpp:676-695): cells whose exponent bits are all ones
@@ -336,8 +375,10 @@ cudaError_t launch_damp_axis(const KConst& kc, const double* tmp, double* f, dou
     return cudaGetLastError();
 }
 
+size_t clamp_partial_doubles() { return (size_t)11 * CL_NB * 4; }
+
 cudaError_t launch_clamp_species(const KConst& kc, double* const f[11], float* const s32[11], double* added,
-                                 unsigned long long* cells, cudaStream_t s) {
+                                 unsigned long long* cells, double* partial, cudaStream_t s) {
     ClampArgs A{};
     for (int q = 0; q < 11; q++) {
         A.f[q] = f[q];
@@ -345,7 +386,9 @@ cudaError_t launch_clamp_species(const KConst& kc, double* const f[11], float* c
     }
     A.added = added;
     A.cells = cells;
-    clamp_species_kernel<<<dim3((kc.km + 31) / 32, (kc.jm + 7) / 8, kc.im * 11), dim3(32, 8), 0, s>>>(kc, A);
+    A.partial = partial;
+    clamp_species_kernel<<<dim3(CL_NB, 11), CL_THREADS, 0, s>>>(kc, A);
+    clamp_budget_kernel<<<1, 32, 0, s>>>(A);
     return cudaGetLastError();
 }
 

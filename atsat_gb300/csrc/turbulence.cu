@@ -25,6 +25,8 @@ struct TurbArgs {
     int64_t plane;
     double u_0, t_ref, g, cp_mix, r_mix, R_mix, L_m, nue_air, re_turb, nue_max, k_bg_nd, vel_star_max;
     double dr, dthe, dphi, inv_2dr, abl_height, taper_dz;
+    // quotients of constants, formed once on the host
+    double inv_L_m, nue_air_nd, gam_ad, tL2_pr, inv_R_mix, inv_cpR;
     double ep[3], lv[3], ls[3], t_0[3];
     TurbTables tab;
     double *u, *v, *w, *t, *rho, *tke, *dis, *tken, *disn, *nue, *tks, *dss, *prod, *vel_star;
@@ -72,8 +74,7 @@ __device__ void sources_cell(const TurbArgs& A, int i, int j, int k) {
     const int ke = A.periodic ? (k == N - 1 ? 0 : k + 1) : k + 1;
     const int64_t cw = c - k + kw, ce = c - k + ke;
     const double rm = T.rm[i], inv_rm = T.inv_rm[i];
-    const double sinthe = T.sinthe[j], cotanthe = T.cotanthe[j];
-    const double rmsinthe = rm * sinthe;
+    const double cotanthe = T.cotanthe[j];
     const double inv_rm2dthe = T.inv_rm2dthe[i];
     const double inv_rmsinthe2dphi = T.inv_rmsinthe2dphi[(int64_t)i * A.jm + j];
     const double inv_2dr = A.inv_2dr;
@@ -121,23 +122,29 @@ __device__ void sources_cell(const TurbArgs& A, int i, int j, int k) {
     const double L_m = A.L_m;
     double nue, tks, dss;
     if (A.model == 2) {            // compute_k_omega_SST (Turbulence.h:1020-1106)
+        // GB300 issues two FP64 operations per SM per cycle and a division costs about a dozen: the
+        // quotients here are products with 1 / omega, 1 / y*, 1 / CD and 1 / k (four divisions per cell
+        // instead of fifteen), a few ulps from the reference's quotients
         const double a1 = 0.31, bet_star = 0.09, bet1 = 0.0333, bet2 = 0.0368, gam1 = 0.413, gam2 = 0.2, sig_w2 = 1.168;
-        const double nue_air_nd = A.nue_air / (A.u_0 * L_m);
+        const double inv_bet_star = 1.0 / 0.09;
+        const double nue_air_nd = A.nue_air_nd;
         const double dz_layer = dmax(1.0, T.thick_m[i - 1 > 0 ? i - 1 : 0]);
         const double y_phys = A.turb_free ? 1.0e20 : dmax(T.height_m[i] - T.height_m[0], dz_layer);
-        const double y_star = y_phys / L_m;
-        const double dtkedthe = (tk[c + kp] - tk[c - kp]) / (rm * 2.0 * A.dthe);
-        const double ddisdthe = (ds[c + kp] - ds[c - kp]) / (rm * 2.0 * A.dthe);
-        const double dtkedphi = (tk[ce] - tk[cw]) / (rmsinthe * 2.0 * A.dphi);
-        const double ddisdphi = (ds[ce] - ds[cw]) / (rmsinthe * 2.0 * A.dphi);
+        const double y_star = y_phys * A.inv_L_m;
+        const double inv_ys = 1.0 / y_star, inv_ys2 = inv_ys * inv_ys;
+        const double dtkedthe = (tk[c + kp] - tk[c - kp]) * inv_rm2dthe;
+        const double ddisdthe = (ds[c + kp] - ds[c - kp]) * inv_rm2dthe;
+        const double dtkedphi = (tk[ce] - tk[cw]) * inv_rmsinthe2dphi;
+        const double ddisdphi = (ds[ce] - ds[cw]) * inv_rmsinthe2dphi;
         const double grad_dot = dtkedr * ddisdr + dtkedthe * ddisdthe + dtkedphi * ddisdphi;
-        const double CD_kw = dmax(2.0 * sig_w2 / dmax(dsc, 1.0e-20) * grad_dot, 1.0e-20);
         const double dis_safe = dmax(dsc, 1.0e-20);
-        const double arg1 = dmin(dmax(sqrt(tkc) / (bet_star * dis_safe * y_star),
-                                      500.0 * nue_air_nd / (y_star * y_star * dis_safe)),
-                                 4.0 * sig_w2 * tkc / (CD_kw * y_star * y_star));
-        const double arg2 = dmax(2.0 * sqrt(tkc) / (bet_star * dis_safe * y_star),
-                                 500.0 * nue_air_nd / (y_star * y_star * dis_safe));
+        const double inv_dis = 1.0 / dis_safe;
+        const double CD_kw = dmax(2.0 * sig_w2 * inv_dis * grad_dot, 1.0e-20);
+        const double sq_k = sqrt(tkc);
+        const double t_a = sq_k * inv_bet_star * inv_dis * inv_ys;         // sqrt(k) / (beta* omega y*)
+        const double t_b = 500.0 * nue_air_nd * inv_ys2 * inv_dis;         // 500 nu / (y*^2 omega)
+        const double arg1 = dmin(dmax(t_a, t_b), 4.0 * sig_w2 * tkc * inv_ys2 / CD_kw);
+        const double arg2 = dmax(2.0 * t_a, t_b);
         const double a1sq = arg1 * arg1;
         const double F1 = tanh(a1sq * a1sq);
         const double F2 = tanh(arg2 * arg2);
@@ -147,25 +154,27 @@ __device__ void sources_cell(const TurbArgs& A, int i, int j, int k) {
         const double Y_k = bet_star * tke_safe * dis_safe;
         const double P_w = (F1 * gam1 + (1.0 - F1) * gam2) * P_k * dis_safe / tke_safe;
         const double Y_w = (F1 * bet1 + (1.0 - F1) * bet2) * dis_safe * dis_safe;
-        const double D_w = 2.0 * (1.0 - F1) * sig_w2 / dis_safe * grad_dot;
+        const double D_w = 2.0 * (1.0 - F1) * sig_w2 * inv_dis * grad_dot;
         tks = P_k - Y_k;
         dss = P_w - Y_w + D_w;
     } else if (A.model == 1) {     // compute_k_omega (Turbulence.h:929-1017)
         const double bet_star = 0.09, gam = 0.52, C_lim = 0.875, bet_0 = 0.0708;
-        const double dtkedthe = (tk[c + kp] - tk[c - kp]) / (rm * 2.0 * A.dthe);
-        const double ddisdthe = (ds[c + kp] - ds[c - kp]) / (rm * 2.0 * A.dthe);
-        const double dtkedphi = (tk[ce] - tk[cw]) / (rmsinthe * 2.0 * A.dphi);
-        const double ddisdphi = (ds[ce] - ds[cw]) / (rmsinthe * 2.0 * A.dphi);
-        const double d2r = 2.0 * A.dr;
-        const double dudr_k = (u[c + P] - u[c - P]) / d2r / (rm + 1.0);
-        const double dvdthe_k = (v[c + kp] - v[c - kp]) / (rm * 2.0 * A.dthe);
-        const double dwdphi_k = (w[ce] - w[cw]) / (rmsinthe * 2.0 * A.dphi);
-        const double dudthe_u = (u[c + kp] - u[c - kp]) / (rm * 2.0 * A.dthe);
-        const double dudphi_u = (u[ce] - u[cw]) / (rmsinthe * 2.0 * A.dphi);
-        const double dvdr_u = (v[c + P] - v[c - P]) / d2r / (rm + 1.0);
-        const double dwdr_u = (w[c + P] - w[c - P]) / d2r / (rm + 1.0);
-        const double dvdphi_u = (v[ce] - v[cw]) / (rmsinthe * 2.0 * A.dphi);
-        const double dwdthe_u = (w[c + kp] - w[c - kp]) / (rm * 2.0 * A.dthe);
+        // the reference's quotients by rm 2 dthe, rm sin 2 dphi and 2 dr (rm + 1) as products with the
+        // column's reciprocals (one division per cell)
+        const double inv_r1 = A.inv_2dr / (rm + 1.0);
+        const double dtkedthe = (tk[c + kp] - tk[c - kp]) * inv_rm2dthe;
+        const double ddisdthe = (ds[c + kp] - ds[c - kp]) * inv_rm2dthe;
+        const double dtkedphi = (tk[ce] - tk[cw]) * inv_rmsinthe2dphi;
+        const double ddisdphi = (ds[ce] - ds[cw]) * inv_rmsinthe2dphi;
+        const double dudr_k = (u[c + P] - u[c - P]) * inv_r1;
+        const double dvdthe_k = dvdthe;
+        const double dwdphi_k = dwdphi;
+        const double dudthe_u = dudthe;
+        const double dudphi_u = dudphi;
+        const double dvdr_u = (v[c + P] - v[c - P]) * inv_r1;
+        const double dwdr_u = (w[c + P] - w[c - P]) * inv_r1;
+        const double dvdphi_u = dvdphi;
+        const double dwdthe_u = dwdthe;
         const double S11 = dudr_k, S22 = dvdthe_k, S33 = dwdphi_k;
         const double S12 = 0.5 * (dudthe_u + dvdr_u), S13 = 0.5 * (dudphi_u + dwdr_u), S23 = 0.5 * (dvdphi_u + dwdthe_u);
         const double S_mag = sqrt(2.0 * (S11 * S11 + S22 * S22 + S33 * S33 + 2.0 * (S12 * S12 + S13 * S13 + S23 * S23)));
@@ -204,11 +213,12 @@ __device__ void sources_cell(const TurbArgs& A, int i, int j, int k) {
     }
     // the buoyancy sink of k (Turbulence.h:800-835): B = -nu_t N^2 / Pr_t, moist N^2 in saturated cells
     if (A.buoy != 0) {
-        const double Pr_t = 0.9;
+        // quotients as products with 1 / dz, 1 / T, 1 / rho and the host's constant quotients
         const double Tc = A.t[c] * A.t_ref;
         const double dz = T.height_m[i + 1] - T.height_m[i - 1];
         const double dTdz = (A.t[c + P] - A.t[c - P]) * A.t_ref / dz;
-        double Gam = A.g / A.cp_mix, fac = 1.0;
+        const double inv_T = 1.0 / Tc;
+        double Gam = A.gam_ad, fac = 1.0;
         if (A.buoy == 3 && Tc > 0.0) {
             double rho = A.r_mix;
             if (A.local_rho) {
@@ -216,21 +226,19 @@ __device__ void sources_cell(const TurbArgs& A, int i, int j, int k) {
                 rho = (r_ > 0.0 && isfinite(r_)) ? r_ : A.r_mix;
             }
             double a = 0.0, b = 0.0;
+            const double inv_rho = 1.0 / rho;
             for (int n = 0; rho > 0.0 && n < 3; n++) {
-                const double qc = (dmax(0.0, A.gc[n][c]) + dmax(0.0, A.gi[n][c])) / rho;
+                const double qc = (dmax(0.0, A.gc[n][c]) + dmax(0.0, A.gi[n][c])) * inv_rho;
                 if (!(qc > 1.0e-9)) continue;
-                const double qv = dmax(0.0, A.gv[n][c]) / rho;
+                const double qv = dmax(0.0, A.gv[n][c]) * inv_rho;
                 const double L = Tc >= A.t_0[n] ? A.lv[n] : A.ls[n];
-                a += L * qv / (A.R_mix * Tc);
-                b += A.ep[n] * L * L * qv / (A.cp_mix * A.R_mix * Tc * Tc);
+                a += L * qv * A.inv_R_mix * inv_T;
+                b += A.ep[n] * L * L * qv * A.inv_cpR * inv_T * inv_T;
             }
             if (isfinite(a + b)) { Gam *= (1.0 + a) / (1.0 + b); fac = 1.0 + a; }
         }
-        const double N2 = (Tc > 0.0 && dz > 0.0) ? A.g / Tc * (dTdz + Gam) * fac : 0.0;
-        if (isfinite(N2) && (N2 > 0.0 || A.buoy == 2)) {
-            const double tL = L_m / A.u_0;
-            tks -= dmax(0.0, nue) * N2 * tL * tL / Pr_t;
-        }
+        const double N2 = (Tc > 0.0 && dz > 0.0) ? A.g * inv_T * (dTdz + Gam) * fac : 0.0;
+        if (isfinite(N2) && (N2 > 0.0 || A.buoy == 2)) tks -= dmax(0.0, nue) * N2 * A.tL2_pr;
     }
     A.nue[c] = nue;
     A.tks[c] = tks;
@@ -343,6 +351,12 @@ cudaError_t launch_turbulence(const KConst& K, const atsat_dyn_params& p, const 
     A.vel_star_max = tp.vel_star_max;
     A.dr = tab.dr; A.dthe = tab.dthe; A.dphi = tab.dphi;
     A.inv_2dr = 1.0 / (2.0 * tab.dr);
+    A.inv_L_m = 1.0 / A.L_m;
+    A.nue_air_nd = A.nue_air / (A.u_0 * A.L_m);
+    A.gam_ad = p.g / p.cp_mix;
+    A.tL2_pr = (A.L_m / A.u_0) * (A.L_m / A.u_0) / 0.9;
+    A.inv_R_mix = 1.0 / p.R_mix;
+    A.inv_cpR = 1.0 / (p.cp_mix * p.R_mix);
     A.abl_height = tp.abl_height;
     A.taper_dz = tab.taper_dz;
     for (int n = 0; n < 3; n++) { A.ep[n] = tp.ep[n]; A.lv[n] = tp.lv[n]; A.ls[n] = tp.ls[n]; A.t_0[n] = tp.t_0[n]; }

@@ -199,6 +199,24 @@ def test_clamp_negative_species(shape):
     assert rb[11:22].sum() > 0 and rb[33:].sum() > 0
 
 
+def test_clamp_budget_is_deterministic():
+    """The floor's budget is summed in a fixed order (per-block sums, then the blocks in order): two runs
+    on the same state give the same bits, with most cells of a species clipped."""
+    from atsat_gb300 import dyn
+    g, P, st = case((21, 91, 181), seed=33)
+    st.arrays[F.H2O_CLOUD][...] = -np.abs(st.arrays[F.H2O_CLOUD]) - 1e-12
+    budgets = []
+    for _ in range(2):
+        with dyn.Dycore(g, P) as d:
+            d.load_state(st.copy())
+            d.clampNegativeSpecies()
+            budgets.append(d.clamp_budget())
+    assert np.array_equal(budgets[0], budgets[1])
+    q = [F.H2O, F.H2O_CLOUD, F.H2O_ICE, F.H2S, F.NH3, F.NH3_CLOUD, F.NH3_ICE, F.CH4, F.CH4_CLOUD, F.CH4_ICE,
+         F.NH4SH].index(F.H2O_CLOUD)
+    assert budgets[0][11 + q] == g.cells
+
+
 def test_clamp_off_with_no_clamp():
     from atsat_gb300 import dyn
     from helpers import plant_negatives
