@@ -371,6 +371,18 @@ void build_geometry(atsat_dyn* h, const double* vbar0, const double* ubar0) {
             c.src_the = c.p_inv_rm / (2.0 * g.dthe);
             c.src_phi = c.p_inv_rmsinthe / (2.0 * g.dphi);
             c.p_inv_den = 1.0 / c.p_den;
+            {
+                const double i2dr = 1.0 / (2.0 * g.dr), i2dthe = 1.0 / (2.0 * g.dthe), i2dphi = 1.0 / (2.0 * g.dphi);
+                c.t_the = i2dthe * c.inv_rm;
+                c.t_phi = i2dphi * c.inv_rmsinthe;
+                c.d_r1 = c.two_inv_rm * i2dr;
+                c.d_t2 = c.inv_rm2 * inv_dthe2;
+                c.d_t1 = c.costhe_inv_rm2sinthe * i2dthe;
+                c.d_p2 = c.inv_rm2sinthe2 * inv_dphi2;
+                c.x_v1 = 2.0 * c.inv_rm2 * i2dthe;
+                c.x_v2 = 2.0 * c.costhe * c.inv_rm2sinthe2 * i2dphi;
+                c.x_w1 = 2.0 * c.inv_rm2sinthe * i2dphi;
+            }
         }
     }
 }

@@ -80,8 +80,12 @@ struct alignas(16) ColGeo {
     // the source factors times the centred-difference scales (exp_rm / (2 dr), 1 / (2 dthe rm),
     // 1 / (2 dphi rm sin)) and 1 / p_den: one product per term instead of two, no FP64 division
     double src_r, src_the, src_phi, p_inv_den;
+    // the FP64 stage's stencil scales folded into one coefficient per term (raw differences a0 = f(i+1) -
+    // f(i-1), b0, c0 along theta and phi, second differences a1, b1, c1): transport v b0 t_the + w c0 t_phi,
+    // diffusion a0 d_r1 + b1 d_t2 + b0 d_t1 + c1 d_p2, and the cross terms of the u, v, w diffusion
+    double t_the, t_phi, d_r1, d_t2, d_t1, d_p2, x_v1, x_v2, x_w1, pad_c;
 };
-static_assert(sizeof(ColGeo) == 36 * 8, "ColGeo layout");
+static_assert(sizeof(ColGeo) == 46 * 8, "ColGeo layout");
 
 // Grid-wide constants, every one formed on the host in the reference's own expression order.
 struct KConst {

@@ -18,37 +18,7 @@ namespace atsat {
 
 namespace {
 
-struct D6 { double dr, d2r, dthe, d2the, dphi, d2phi; };
-
 __device__ __forceinline__ double ldg(const double* p) { return __ldg(p); }
-
-__device__ __forceinline__ void derivs(const double* __restrict__ f, int64_t c, int64_t plane, int kp,
-                                       int dkw, int dke, const KConst& K, D6& d) {
-    const double x = ldg(f + c);
-    const double rp = ldg(f + c + plane), rn = ldg(f + c - plane);
-    const double tp = ldg(f + c + kp), tn = ldg(f + c - kp);
-    const double pe = ldg(f + c + dke), pw = ldg(f + c + dkw);
-    d.dr = (rp - rn) * K.inv_2dr;
-    d.d2r = (rp - 2.0 * x + rn) * K.inv_dr2;
-    d.dthe = (tp - tn) * K.inv_2dthe;
-    d.d2the = (tp - 2.0 * x + tn) * K.inv_dthe2;
-    d.dphi = (pe - pw) * K.inv_2dphi;
-    d.d2phi = (pe - 2.0 * x + pw) * K.inv_dphi2;
-}
-
-struct GeoR {
-    double inv_rm, inv_rm2, inv_rmsinthe, inv_rm2sinthe, inv_rm2sinthe2, costhe_inv_rm2sinthe, cotanthe;
-    double costhe, two_inv_rm, v_metric;
-};
-
-__device__ __forceinline__ double transport(double u, double v, double w, const D6& d, const GeoR& g) {
-    return u * d.dr + v * d.dthe * g.inv_rm + w * d.dphi * g.inv_rmsinthe;
-}
-
-__device__ __forceinline__ double diffusion(const D6& d, const GeoR& g) {
-    return d.d2r + d.dr * g.two_inv_rm + d.d2the * g.inv_rm2 + d.dthe * g.costhe_inv_rm2sinthe
-         + d.d2phi * g.inv_rm2sinthe2;
-}
 
 __device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
 __device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
@@ -75,6 +45,39 @@ __device__ __forceinline__ void emit(const StageIO<double>& io, const StageParam
     io.out[q][c] = y;
 }
 
+// The stencil of one field as raw differences: a0 = f(i+1) - f(i-1), a1 = f(i+1) - 2 f + f(i-1), and b0, b1
+// along theta, c0, c1 along phi. fma(-2, x, p) equals p - 2x bit for bit (the product is exact).
+struct R6 { double a0, a1, b0, b1, c0, c1; };
+
+__device__ __forceinline__ void raw6(const double* __restrict__ f, int64_t c, int64_t plane, int kp, int dkw,
+                                     int dke, R6& r) {
+    const double x = ldg(f + c);
+    const double rp = ldg(f + c + plane), rn = ldg(f + c - plane);
+    const double tp = ldg(f + c + kp), tn = ldg(f + c - kp);
+    const double pe = ldg(f + c + dke), pw = ldg(f + c + dkw);
+    r.a0 = rp - rn;
+    r.a1 = fma(-2.0, x, rp) + rn;
+    r.b0 = tp - tn;
+    r.b1 = fma(-2.0, x, tp) + tn;
+    r.c0 = pe - pw;
+    r.c1 = fma(-2.0, x, pe) + pw;
+}
+
+// Per-cell factors shared by every field: the advecting velocity times the stencil scales, and the
+// diffusion operator's coefficient per raw difference (from the column table).
+struct Fold {
+    double U, V, W, dr2, dr1, dt2, dt1, dp2;
+    __device__ __forceinline__ double transport(const R6& r) const { return fma(U, r.a0, fma(V, r.b0, W * r.c0)); }
+    __device__ __forceinline__ double diffusion(const R6& r) const {
+        return fma(dr2, r.a1, fma(dr1, r.a0, fma(dt2, r.b1, fma(dt1, r.b0, dp2 * r.c1))));
+    }
+};
+
+// GB300 issues two FP64 operations per SM per cycle, and this kernel is bound by that pipe. The reference
+// scales each of a field's six differences before combining them (RHS_Sat_Turb.cpp:300-1000); here the
+// scales are folded into per-cell factors (Fold) and per-column coefficients (ColGeo), so a field costs its
+// nine differencing operations, three for transport and five for diffusion. Every term is the reference's;
+// the products are associated differently (a few ulps per term).
 template <int MODE>
 __global__ void __launch_bounds__(256) rk_stage_fp64_kernel(const KConst K, const StageIO<double> io,
                                                             const StageParams sp) {
@@ -99,26 +102,26 @@ __global__ void __launch_bounds__(256) rk_stage_fp64_kernel(const KConst K, cons
     const int dkw = kw - k, dke = ke - k;
 
     const ColGeo* gp = io.geo + ((int64_t)i * K.jm + j);
-    GeoR g;
-    g.inv_rm = ldg(&gp->inv_rm);
-    g.inv_rm2 = ldg(&gp->inv_rm2);
-    g.inv_rmsinthe = ldg(&gp->inv_rmsinthe);
-    g.inv_rm2sinthe = ldg(&gp->inv_rm2sinthe);
-    g.inv_rm2sinthe2 = ldg(&gp->inv_rm2sinthe2);
-    g.costhe_inv_rm2sinthe = ldg(&gp->costhe_inv_rm2sinthe);
-    g.cotanthe = ldg(&gp->cotanthe);
-    g.costhe = ldg(&gp->costhe);
-    g.two_inv_rm = ldg(&gp->two_inv_rm);
-    g.v_metric = ldg(&gp->v_metric);
+    const double inv_rm = ldg(&gp->inv_rm), inv_rm2 = ldg(&gp->inv_rm2), inv_rmsinthe = ldg(&gp->inv_rmsinthe);
+    const double cotanthe = ldg(&gp->cotanthe), costhe = ldg(&gp->costhe), v_metric = ldg(&gp->v_metric);
 
     const double u = ldg(io.in[ATSAT_F_U] + c);
     const double v = ldg(io.in[ATSAT_F_V] + c);
     const double w = ldg(io.in[ATSAT_F_W] + c);
+    Fold fd;
+    fd.U = u * K.inv_2dr;
+    fd.V = v * ldg(&gp->t_the);
+    fd.W = w * ldg(&gp->t_phi);
+    fd.dr2 = K.inv_dr2;
+    fd.dr1 = ldg(&gp->d_r1);
+    fd.dt2 = ldg(&gp->d_t2);
+    fd.dt1 = ldg(&gp->d_t1);
+    fd.dp2 = ldg(&gp->d_p2);
 
-    D6 du, dv, dw;
-    derivs(io.in[ATSAT_F_U], c, plane, kp, dkw, dke, K, du);
-    derivs(io.in[ATSAT_F_V], c, plane, kp, dkw, dke, K, dv);
-    derivs(io.in[ATSAT_F_W], c, plane, kp, dkw, dke, K, dw);
+    R6 ru, rv, rw;
+    raw6(io.in[ATSAT_F_U], c, plane, kp, dkw, dke, ru);
+    raw6(io.in[ATSAT_F_V], c, plane, kp, dkw, dke, rv);
+    raw6(io.in[ATSAT_F_W], c, plane, kp, dkw, dke, rw);
     const double dpdr = (ldg(io.p_dyn + c + plane) - ldg(io.p_dyn + c - plane)) * K.inv_2dr;
     const double dpdthe = (ldg(io.p_dyn + c + kp) - ldg(io.p_dyn + c - kp)) * K.inv_2dthe;
     const double dpdphi = (ldg(io.p_dyn + c + dke) - ldg(io.p_dyn + c + dkw)) * K.inv_2dphi;
@@ -133,24 +136,17 @@ __global__ void __launch_bounds__(256) rk_stage_fp64_kernel(const KConst K, cons
         const double cor_rad = ldg(&gp->cor_rad) * w;
         const double cor_the = ldg(&gp->cor_the) * w;
         const double v_cor = v - ldg(&gp->vbar0), u_cor = u - ldg(&gp->ubar0);
-        const double cor_phi = ldg(&gp->cor_phi) * (g.costhe * v_cor + ldg(&gp->sinthe_true) * u_cor);
+        const double cor_phi = ldg(&gp->cor_phi) * (costhe * v_cor + ldg(&gp->sinthe_true) * u_cor);
 
-        double transport_u = u * du.dr + v * du.dthe * g.inv_rm + w * du.dphi * g.inv_rmsinthe;
-        if (!K.metric_split) transport_u = transport_u - K.metric_on * (v * v + w * w) * g.inv_rm;
-        const double transport_v = u * dv.dr + v * dv.dthe * g.inv_rm + w * dv.dphi * g.inv_rmsinthe
-                                 + (u * v - w * w * g.cotanthe) * g.inv_rm;
-        const double transport_w = u * dw.dr + v * dw.dthe * g.inv_rm + w * dw.dphi * g.inv_rmsinthe
-                                 + (w * u + v * w * g.cotanthe) * g.inv_rm;
-        const double diffusion_u = du.d2r + 2.0 * u * g.inv_rm2 + du.d2the * g.inv_rm2 + 4.0 * du.dr * g.inv_rm
-                                 + du.dthe * g.costhe_inv_rm2sinthe + du.d2phi * g.inv_rm2sinthe2;
-        const double diffusion_v = dv.d2r + dv.dr * g.two_inv_rm + dv.d2the * g.inv_rm2
-                                 + dv.dthe * g.costhe_inv_rm2sinthe - g.v_metric * v
-                                 + dv.d2phi * g.inv_rm2sinthe2 + 2.0 * du.dthe * g.inv_rm2
-                                 - dw.dphi * 2.0 * g.costhe * g.inv_rm2sinthe2;
-        const double diffusion_w = dw.d2r + dw.dr * g.two_inv_rm + dw.d2the * g.inv_rm2
-                                 + dw.dthe * g.costhe_inv_rm2sinthe - g.v_metric * w
-                                 + dw.d2phi * g.inv_rm2sinthe2 + 2.0 * du.dphi * g.inv_rm2sinthe
-                                 + dv.dphi * 2.0 * g.costhe * g.inv_rm2sinthe2;
+        double transport_u = fd.transport(ru);
+        if (!K.metric_split) transport_u = transport_u - K.metric_on * (v * v + w * w) * inv_rm;
+        const double transport_v = fd.transport(rv) + (u * v - w * w * cotanthe) * inv_rm;
+        const double transport_w = fd.transport(rw) + (w * u + v * w * cotanthe) * inv_rm;
+        // diffusion_u: 4 du/dr / rm in place of du/dr 2 / rm, and 2 u / rm^2
+        const double diffusion_u = fma(fd.dr1, ru.a0, fd.diffusion(ru)) + 2.0 * u * inv_rm2;
+        const double x_v2 = ldg(&gp->x_v2);
+        const double diffusion_v = fd.diffusion(rv) - v_metric * v + ldg(&gp->x_v1) * ru.b0 - x_v2 * rw.c0;
+        const double diffusion_w = fd.diffusion(rw) - v_metric * w + ldg(&gp->x_w1) * ru.c0 + x_v2 * rv.c0;
 
         double buoyancy_u = 0.0;
         const double t_c = ldg(io.in[ATSAT_F_T] + c);
@@ -159,30 +155,31 @@ __global__ void __launch_bounds__(256) rk_stage_fp64_kernel(const KConst K, cons
             if (K.buoy_legacy) buoyancy_u = K.legacy_buoy * (ps + ldg(io.p_dyn + c)) / (K.rR * t_c * K.t_ref);
             else buoyancy_u = K.kbuoy * (K.g * ps / (K.rR * t_c * K.t_ref) - ldg(io.buoy + i));
         }
-        const double rhs_u = -dpdr + buoyancy_u - transport_u + diffusion_u * K.inv_re + diffusion_u * nue_t
+        const double visc = K.inv_re + nue_t;
+        const double rhs_u = -dpdr + buoyancy_u - transport_u + diffusion_u * visc
                            - K.cor_rad_on * K.Coriolis * cor_rad + K.centrifugal * ldg(&gp->cent_rad);
         double dpmdthe = 0.0, dpmdphi = 0.0;
         if (K.metric_split) {
             dpmdthe = (ldg(io.p_metric + c + kp) - ldg(io.p_metric + c - kp)) * K.inv_2dthe;
             dpmdphi = (ldg(io.p_metric + c + dke) - ldg(io.p_metric + c + dkw)) * K.inv_2dphi;
         }
-        const double rhs_v = -dpdthe * g.inv_rm - dpmdthe * g.inv_rm - transport_v + diffusion_v * K.inv_re
-                           + diffusion_v * nue_t - K.Coriolis * cor_the + K.centrifugal * ldg(&gp->cent_the);
-        const double rhs_w = -dpdphi * g.inv_rmsinthe - dpmdphi * g.inv_rmsinthe - transport_w
-                           + diffusion_w * K.inv_re + diffusion_w * nue_t - K.Coriolis * cor_phi;
+        const double rhs_v = -(dpdthe + dpmdthe) * inv_rm - transport_v + diffusion_v * visc - K.Coriolis * cor_the
+                           + K.centrifugal * ldg(&gp->cent_the);
+        const double rhs_w = -(dpdphi + dpmdphi) * inv_rmsinthe - transport_w + diffusion_w * visc
+                           - K.Coriolis * cor_phi;
         emit<MODE>(io, sp, K, ATSAT_F_U, c, rhs_u);
         emit<MODE>(io, sp, K, ATSAT_F_V, c, rhs_v);
         emit<MODE>(io, sp, K, ATSAT_F_W, c, rhs_w);
         if (MODE != MODE_STAGE) {
             io.aux[0][c] = rhs_u + dpdr;
-            io.aux[1][c] = rhs_v + dpdthe * g.inv_rm;
-            io.aux[2][c] = rhs_w + dpdphi * g.inv_rmsinthe;
+            io.aux[1][c] = rhs_v + dpdthe * inv_rm;
+            io.aux[2][c] = rhs_w + dpdphi * inv_rmsinthe;
         }
     }
 
     // flux-form factor of the species (RHS_Sat_Turb.cpp:979-1009), 0 unless ATSAT_SPECIES_DIVU
-    const double sd = K.divu_on ? K.species_divu * (du.dr + 2.0 * u * g.inv_rm + dv.dthe * g.inv_rm
-                                                    + v * g.cotanthe * g.inv_rm + dw.dphi * g.inv_rmsinthe)
+    const double sd = K.divu_on ? K.species_divu * (ru.a0 * K.inv_2dr + 2.0 * u * inv_rm + rv.b0 * ldg(&gp->t_the)
+                                                    + v * cotanthe * inv_rm + rw.c0 * ldg(&gp->t_phi))
                                 : 0.0;
 
     // ---- temperature (RHS_Sat_Turb.cpp:368-386, 409, 435-437, 611-665, 752-759) ----
@@ -193,12 +190,11 @@ __global__ void __launch_bounds__(256) rk_stage_fp64_kernel(const KConst K, cons
             const double rho_l = ldg(io.rho_mix + c);
             if (K.adiabatic_rho && rho_l > 0.0 && isfinite(rho_l)) dpstatdr *= K.r_mix / rho_l;
         }
-        const double pressure_t = K.coeff_energy_p * (u * (dpdr + dpstatdr) + v * dpdthe * g.inv_rm
-                                                      + w * dpdphi * g.inv_rmsinthe);
-        D6 d;
-        derivs(io.in[ATSAT_F_T], c, plane, kp, dkw, dke, K, d);
-        const double transport_t = transport(u, v, w, d, g);
-        const double diffusion_t = diffusion(d, g);
+        const double pressure_t = K.coeff_energy_p * (u * (dpdr + dpstatdr) + v * dpdthe * inv_rm
+                                                      + w * dpdphi * inv_rmsinthe);
+        R6 rt;
+        raw6(io.in[ATSAT_F_T], c, plane, kp, dkw, dke, rt);
+        const double diffusion_t = fd.diffusion(rt);
         double radiation_t = 0.0;
         if (K.rad_on) {
             const double rho_f = ldg(io.rho_mix + c);
@@ -217,7 +213,7 @@ __global__ void __launch_bounds__(256) rk_stage_fp64_kernel(const KConst K, cons
             else if (precip_t > 0.5) precip_t = 0.5;
             else if (precip_t < -0.5) precip_t = -0.5;
         }
-        double rhs_t = pressure_t - transport_t + diffusion_t * K.inv_re_pr + diffusion_t * nue_t_s;
+        double rhs_t = pressure_t - fd.transport(rt) + diffusion_t * (K.inv_re_pr + nue_t_s);
         if (K.tmf_on) rhs_t = rhs_t - K.tmf_chem * ldg(io.thermalmassflux + c);
         rhs_t = rhs_t + radiation_t + precip_t;
         emit<MODE>(io, sp, K, ATSAT_F_T, c, rhs_t);
@@ -227,48 +223,40 @@ __global__ void __launch_bounds__(256) rk_stage_fp64_kernel(const KConst K, cons
     const double pc = K.precip_coupling;
 #define ATSAT_SPECIES(FID, INV_SC_RE, EXTRA)                                                   \
     {                                                                                          \
-        D6 d;                                                                                  \
-        derivs(io.in[FID], c, plane, kp, dkw, dke, K, d);                                      \
-        const double df = diffusion(d, g);                                                     \
-        double r = -transport(u, v, w, d, g) + df * (INV_SC_RE) + df * nue_t_s EXTRA;          \
+        R6 r6;                                                                                 \
+        raw6(io.in[FID], c, plane, kp, dkw, dke, r6);                                          \
+        double r = fma(fd.diffusion(r6), (INV_SC_RE) + nue_t_s, (EXTRA) - fd.transport(r6));   \
         if (K.divu_on) r -= sd * ldg(io.in[FID] + c);                                          \
         emit<MODE>(io, sp, K, FID, c, r);                                                      \
     }
-    ATSAT_SPECIES(ATSAT_F_H2O, K.inv_sc_re_h2o, +pc * ldg(io.s_precip[0] + c))
-    ATSAT_SPECIES(ATSAT_F_H2O_CLOUD, K.inv_sc_re_h2o, +pc * ldg(io.s_precip[1] + c))
-    ATSAT_SPECIES(ATSAT_F_H2O_ICE, K.inv_sc_re_h2o, +pc * ldg(io.s_precip[2] + c))
-    ATSAT_SPECIES(ATSAT_F_H2S, K.inv_sc_re_h2s, +K.chem * ldg(io.massflux_h2s + c))
-    ATSAT_SPECIES(ATSAT_F_NH3, K.inv_sc_re_nh3, +K.chem * ldg(io.massflux_nh3 + c) + pc * ldg(io.s_precip[3] + c))
-    ATSAT_SPECIES(ATSAT_F_NH3_CLOUD, K.inv_sc_re_nh3, +pc * ldg(io.s_precip[4] + c))
-    ATSAT_SPECIES(ATSAT_F_NH3_ICE, K.inv_sc_re_nh3, +pc * ldg(io.s_precip[5] + c))
-    ATSAT_SPECIES(ATSAT_F_CH4, K.inv_sc_re_ch4, +pc * ldg(io.s_precip[6] + c))
-    ATSAT_SPECIES(ATSAT_F_CH4_CLOUD, K.inv_sc_re_ch4, +pc * ldg(io.s_precip[7] + c))
-    ATSAT_SPECIES(ATSAT_F_CH4_ICE, K.inv_sc_re_ch4, +pc * ldg(io.s_precip[8] + c))
+    ATSAT_SPECIES(ATSAT_F_H2O, K.inv_sc_re_h2o, pc * ldg(io.s_precip[0] + c))
+    ATSAT_SPECIES(ATSAT_F_H2O_CLOUD, K.inv_sc_re_h2o, pc * ldg(io.s_precip[1] + c))
+    ATSAT_SPECIES(ATSAT_F_H2O_ICE, K.inv_sc_re_h2o, pc * ldg(io.s_precip[2] + c))
+    ATSAT_SPECIES(ATSAT_F_H2S, K.inv_sc_re_h2s, K.chem * ldg(io.massflux_h2s + c))
+    ATSAT_SPECIES(ATSAT_F_NH3, K.inv_sc_re_nh3, K.chem * ldg(io.massflux_nh3 + c) + pc * ldg(io.s_precip[3] + c))
+    ATSAT_SPECIES(ATSAT_F_NH3_CLOUD, K.inv_sc_re_nh3, pc * ldg(io.s_precip[4] + c))
+    ATSAT_SPECIES(ATSAT_F_NH3_ICE, K.inv_sc_re_nh3, pc * ldg(io.s_precip[5] + c))
+    ATSAT_SPECIES(ATSAT_F_CH4, K.inv_sc_re_ch4, pc * ldg(io.s_precip[6] + c))
+    ATSAT_SPECIES(ATSAT_F_CH4_CLOUD, K.inv_sc_re_ch4, pc * ldg(io.s_precip[7] + c))
+    ATSAT_SPECIES(ATSAT_F_CH4_ICE, K.inv_sc_re_ch4, pc * ldg(io.s_precip[8] + c))
+    // nh4sh carries the flux-limiter correction (RHS_Sat_Turb.cpp:932-937)
+    ATSAT_SPECIES(ATSAT_F_NH4SH, K.inv_sc_re_nh4sh, ldg(io.fluxlim_nh4sh + c) + K.chem * ldg(io.massflux_nh4sh + c))
 #undef ATSAT_SPECIES
-    {   // nh4sh carries the flux-limiter correction (RHS_Sat_Turb.cpp:932-937)
-        D6 d;
-        derivs(io.in[ATSAT_F_NH4SH], c, plane, kp, dkw, dke, K, d);
-        const double df = diffusion(d, g);
-        double r = -transport(u, v, w, d, g) + ldg(io.fluxlim_nh4sh + c) + df * K.inv_sc_re_nh4sh + df * nue_t_s
-                 + K.chem * ldg(io.massflux_nh4sh + c);
-        if (K.divu_on) r -= sd * ldg(io.in[ATSAT_F_NH4SH] + c);
-        emit<MODE>(io, sp, K, ATSAT_F_NH4SH, c, r);
-    }
 
     // ---- k-omega transport (RHS_Sat_Turb.cpp:511-538) ----
     if (K.turb) {
         {
-            D6 d;
-            derivs(io.in[ATSAT_F_TKE], c, plane, kp, dkw, dke, K, d);
-            const double r = -transport(u, v, w, d, g) + diffusion(d, g) * (K.inv_re + nue_c * K.inv_sig_k)
-                           + ldg(io.tke_source + c);
+            R6 r6;
+            raw6(io.in[ATSAT_F_TKE], c, plane, kp, dkw, dke, r6);
+            const double r = fma(fd.diffusion(r6), K.inv_re + nue_c * K.inv_sig_k,
+                                 ldg(io.tke_source + c) - fd.transport(r6));
             emit<MODE>(io, sp, K, ATSAT_F_TKE, c, r);
         }
         {
-            D6 d;
-            derivs(io.in[ATSAT_F_DIS], c, plane, kp, dkw, dke, K, d);
-            const double r = -transport(u, v, w, d, g) + diffusion(d, g) * (K.inv_re + nue_c * K.inv_sig_w)
-                           + ldg(io.dis_source + c);
+            R6 r6;
+            raw6(io.in[ATSAT_F_DIS], c, plane, kp, dkw, dke, r6);
+            const double r = fma(fd.diffusion(r6), K.inv_re + nue_c * K.inv_sig_w,
+                                 ldg(io.dis_source + c) - fd.transport(r6));
             emit<MODE>(io, sp, K, ATSAT_F_DIS, c, r);
         }
     } else if (MODE == MODE_RHS || (MODE == MODE_FINAL && sp.write_all_rhs)) {
