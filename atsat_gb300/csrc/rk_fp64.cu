@@ -45,6 +45,19 @@ __device__ __forceinline__ void emit(const StageIO<double>& io, const StageParam
     io.out[q][c] = y;
 }
 
+// 1/x for x > 0 in FP32's normal range: the FP32 reciprocal refined by one Newton-Raphson step
+// r <- r + r (1 - x r) (relative error 2^-23 -> ~2^-46, always from below). in_range tests the range on
+// the integer pipe (exponent field of x); x's FP32 copy and the result's widening are integer too.
+__device__ __forceinline__ bool in_rcp_range(double x) {
+    uint32_t lo, hi;
+    split_f64(x, lo, hi);
+    return (hi >> 31) == 0u && ((hi >> 20) & 0x7FFu) - 897u < 250u;   // 0 < x, float-normal with margin
+}
+__device__ __forceinline__ double recip_nr(double x) {
+    const double r = f2d(__frcp_rn(d2f(x)));
+    return fma(r, fma(-x, r, 1.0), r);
+}
+
 // The stencil of one field as raw differences: a0 = f(i+1) - f(i-1), a1 = f(i+1) - 2 f + f(i-1), and b0, b1
 // along theta, c0, c1 along phi. fma(-2, x, p) equals p - 2x bit for bit (the product is exact).
 struct R6 { double a0, a1, b0, b1, c0, c1; };
@@ -153,6 +166,7 @@ __global__ void __launch_bounds__(256) rk_stage_fp64_kernel(const KConst K, cons
         if (t_c > 0.0 && !K.hydro_buoy) {
             const double ps = ldg(io.p_stat + c);
             if (K.buoy_legacy) buoyancy_u = K.legacy_buoy * (ps + ldg(io.p_dyn + c)) / (K.rR * t_c * K.t_ref);
+            else if (in_rcp_range(t_c)) buoyancy_u = K.kbuoy * ((K.buoy_c * ps) * recip_nr(t_c) - ldg(io.buoy + i));
             else buoyancy_u = K.kbuoy * (K.g * ps / (K.rR * t_c * K.t_ref) - ldg(io.buoy + i));
         }
         const double visc = K.inv_re + nue_t;
@@ -188,7 +202,8 @@ __global__ void __launch_bounds__(256) rk_stage_fp64_kernel(const KConst K, cons
         if (K.adiabatic) {
             dpstatdr = (ldg(io.p_stat + c + plane) - ldg(io.p_stat + c - plane)) * K.inv_2dr * K.to_nd;
             const double rho_l = ldg(io.rho_mix + c);
-            if (K.adiabatic_rho && rho_l > 0.0 && isfinite(rho_l)) dpstatdr *= K.r_mix / rho_l;
+            if (K.adiabatic_rho && rho_l > 0.0 && isfinite(rho_l))
+                dpstatdr *= in_rcp_range(rho_l) ? K.r_mix * recip_nr(rho_l) : K.r_mix / rho_l;
         }
         const double pressure_t = K.coeff_energy_p * (u * (dpdr + dpstatdr) + v * dpdthe * inv_rm
                                                       + w * dpdphi * inv_rmsinthe);
@@ -270,19 +285,6 @@ __global__ void __launch_bounds__(256) rk_stage_fp64_kernel(const KConst K, cons
 // so that eight loads are in flight per lane.
 constexpr int LM_CHUNKS = 16;
 constexpr int LM_THREADS = 128;
-
-// 1/x for x > 0 in FP32's normal range: the FP32 reciprocal refined by one Newton-Raphson step
-// r <- r + r (1 - x r) (relative error 2^-23 -> ~2^-46, always from below). in_range tests the range on
-// the integer pipe (exponent field of x); x's FP32 copy and the result's widening are integer too.
-__device__ __forceinline__ bool in_rcp_range(double x) {
-    uint32_t lo, hi;
-    split_f64(x, lo, hi);
-    return (hi >> 31) == 0u && ((hi >> 20) & 0x7FFu) - 897u < 250u;   // 0 < x, float-normal with margin
-}
-__device__ __forceinline__ double recip_nr(double x) {
-    const double r = f2d(__frcp_rn(d2f(x)));
-    return fma(r, fma(-x, r, 1.0), r);
-}
 
 // the buoyancy g p / (r_mix R_mix T t_ref) = bc p / t of one cell (bc formed on the host); false where
 // the reference skips the cell (!(t > 0), non-finite b). The level mean's rows take the fast path below
