@@ -64,6 +64,23 @@ __device__ __forceinline__ float d2f(double d) {
     return d2f_rare(d);
 }
 
+// 1/x for x > 0 in FP32's normal range: the FP32 reciprocal refined by one Newton-Raphson step
+// r <- r + r (1 - x r) (relative error 2^-23 -> ~2^-46, always from below). in_range tests the range on
+// the integer pipe (exponent field of x); x's FP32 copy and the result's widening are integer too.
+__device__ __forceinline__ bool in_rcp_range(double x) {
+    uint32_t lo, hi;
+    split_f64(x, lo, hi);
+    return (hi >> 31) == 0u && ((hi >> 20) & 0x7FFu) - 897u < 250u;   // 0 < x, float-normal with margin
+}
+__device__ __forceinline__ double recip_nr(double x) {
+    const double r = f2d(__frcp_rn(d2f(x)));
+    return fma(r, fma(-x, r, 1.0), r);
+}
+
+// a / b with b's reciprocal refined as above where b is in range (relative error ~2^-46 instead of the
+// division's half ulp, at three FP64 operations instead of about a dozen); the division elsewhere
+__device__ __forceinline__ double qdiv(double a, double b) { return in_rcp_range(b) ? a * recip_nr(b) : a / b; }
+
 // Per-(i,j) metric factors of one column. The RK members follow the CellGeometry that
 // RungeKuttaSat builds (RungeKutta_Sat_Turb.cpp:223-243) plus the (i,j)-only products of RHSSat
 // (Coriolis / centrifugal coefficients, RHS_Sat_Turb.cpp:310-350; v_metric :436); the P members are

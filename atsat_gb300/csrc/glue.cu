@@ -286,8 +286,8 @@ __global__ void __launch_bounds__(CL_THREADS) clamp_species_kernel(const KConst 
     double* f = A.f[q];
     float* s32 = A.s32[q];
     double s[4] = {0.0, 0.0, 0.0, 0.0};                               // added, added_bnd, cells, cells_bnd
-    for (int64_t e = e0 + threadIdx.x; e < e1; e += CL_THREADS) {
-        int64_t r, k;
+    auto cell = [&](int64_t e, int64_t& r) -> int64_t {                // (row, device index) of flat cell e
+        int64_t k;
         if (small) {
             int ri = (int)((float)e * inv_km);
             int ki = (int)e - ri * K.km;
@@ -299,15 +299,29 @@ __global__ void __launch_bounds__(CL_THREADS) clamp_species_kernel(const KConst 
             r = e / K.km;
             k = e - r * K.km;
         }
-        const int64_t c = r * K.kp + k;
-        const double v = f[c];
-        if (!(v >= 0.0)) {
-            f[c] = 0.0;
-            if (s32) s32[c] = 0.0f;
+        return r * K.kp + k;
+    };
+    // four cells per thread and pass: their loads are in flight together
+    constexpr int U = 4;
+    for (int64_t e0t = e0 + threadIdx.x; e0t < e1; e0t += (int64_t)CL_THREADS * U) {
+        int64_t rr[U], cc[U];
+        double vv[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int64_t e = e0t + (int64_t)u * CL_THREADS;
+            cc[u] = e < e1 ? cell(e, rr[u]) : -1;
+            vv[u] = cc[u] >= 0 ? f[cc[u]] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const double v = vv[u];
+            if (cc[u] < 0 || v >= 0.0) continue;
+            f[cc[u]] = 0.0;
+            if (s32) s32[cc[u]] = 0.0f;
             if (isfinite(v)) {
                 s[0] -= v;
                 s[2] += 1.0;
-                if (r < rb_lo || r >= rb_hi) { s[1] -= v; s[3] += 1.0; }
+                if (rr[u] < rb_lo || rr[u] >= rb_hi) { s[1] -= v; s[3] += 1.0; }
             }
         }
     }
@@ -326,16 +340,17 @@ __global__ void __launch_bounds__(CL_THREADS) clamp_species_kernel(const KConst 
     }
 }
 
+// one thread per (species, sum): the blocks' partial sums added in block order
 __global__ void clamp_budget_kernel(const ClampArgs A) {
-    const int q = threadIdx.x;
+    const int q = threadIdx.x >> 2, m = threadIdx.x & 3;
     if (q >= 11) return;
-    double t[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int b = 0; b < CL_NB; b++)
-        for (int m = 0; m < 4; m++) t[m] += A.partial[((int64_t)q * CL_NB + b) * 4 + m];
-    A.added[q] += t[0];
-    A.added[11 + q] += t[1];
-    A.cells[q] += (unsigned long long)t[2];
-    A.cells[11 + q] += (unsigned long long)t[3];
+    double t = 0.0;
+#pragma unroll 8
+    for (int b = 0; b < CL_NB; b++) t += A.partial[((int64_t)q * CL_NB + b) * 4 + m];
+    if (m == 0) A.added[q] += t;
+    else if (m == 1) A.added[11 + q] += t;
+    else if (m == 2) A.cells[q] += (unsigned long long)t;
+    else A.cells[11 + q] += (unsigned long long)t;
 }
 
 // cSaturnModel::restart_state_is_clean (FileIO_Sat.cpp:676-695): cells whose exponent bits are all ones
@@ -388,7 +403,7 @@ cudaError_t launch_clamp_species(const KConst& kc, double* const f[11], float* c
     A.cells = cells;
     A.partial = partial;
     clamp_species_kernel<<<dim3(CL_NB, 11), CL_THREADS, 0, s>>>(kc, A);
-    clamp_budget_kernel<<<1, 32, 0, s>>>(A);
+    clamp_budget_kernel<<<1, 64, 0, s>>>(A);
     return cudaGetLastError();
 }
 

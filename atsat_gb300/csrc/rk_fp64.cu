@@ -45,19 +45,6 @@ __device__ __forceinline__ void emit(const StageIO<double>& io, const StageParam
     io.out[q][c] = y;
 }
 
-// 1/x for x > 0 in FP32's normal range: the FP32 reciprocal refined by one Newton-Raphson step
-// r <- r + r (1 - x r) (relative error 2^-23 -> ~2^-46, always from below). in_range tests the range on
-// the integer pipe (exponent field of x); x's FP32 copy and the result's widening are integer too.
-__device__ __forceinline__ bool in_rcp_range(double x) {
-    uint32_t lo, hi;
-    split_f64(x, lo, hi);
-    return (hi >> 31) == 0u && ((hi >> 20) & 0x7FFu) - 897u < 250u;   // 0 < x, float-normal with margin
-}
-__device__ __forceinline__ double recip_nr(double x) {
-    const double r = f2d(__frcp_rn(d2f(x)));
-    return fma(r, fma(-x, r, 1.0), r);
-}
-
 // The stencil of one field as raw differences: a0 = f(i+1) - f(i-1), a1 = f(i+1) - 2 f + f(i-1), and b0, b1
 // along theta, c0, c1 along phi. fma(-2, x, p) equals p - 2x bit for bit (the product is exact).
 struct R6 { double a0, a1, b0, b1, c0, c1; };

@@ -96,7 +96,7 @@ __device__ void sources_cell(const TurbArgs& A, int i, int j, int k) {
     {
         const double dis_here = dmax(dsc, DIS_MIN);
         const double tke_here = dmax(tkc, 0.0);
-        cnue = (A.model == 0) ? C_NUE * tke_here * tke_here / dis_here : tke_here / dis_here;
+        cnue = (A.model == 0) ? qdiv(C_NUE * tke_here * tke_here, dis_here) : qdiv(tke_here, dis_here);
         cnue = dmin(cnue, A.nue_max);
     }
     const double u_r = A.curv ? u[c] * inv_rm : 0.0;
@@ -124,35 +124,35 @@ __device__ void sources_cell(const TurbArgs& A, int i, int j, int k) {
     if (A.model == 2) {            // compute_k_omega_SST (Turbulence.h:1020-1106)
         // GB300 issues two FP64 operations per SM per cycle and a division costs about a dozen: the
         // quotients here are products with 1 / omega, 1 / y*, 1 / CD and 1 / k (four divisions per cell
-        // instead of fifteen), a few ulps from the reference's quotients
+        // instead of fifteen), and those reciprocals are Newton-refined FP32 ones (qdiv) where in range
         const double a1 = 0.31, bet_star = 0.09, bet1 = 0.0333, bet2 = 0.0368, gam1 = 0.413, gam2 = 0.2, sig_w2 = 1.168;
         const double inv_bet_star = 1.0 / 0.09;
         const double nue_air_nd = A.nue_air_nd;
         const double dz_layer = dmax(1.0, T.thick_m[i - 1 > 0 ? i - 1 : 0]);
         const double y_phys = A.turb_free ? 1.0e20 : dmax(T.height_m[i] - T.height_m[0], dz_layer);
         const double y_star = y_phys * A.inv_L_m;
-        const double inv_ys = 1.0 / y_star, inv_ys2 = inv_ys * inv_ys;
+        const double inv_ys = qdiv(1.0, y_star), inv_ys2 = inv_ys * inv_ys;
         const double dtkedthe = (tk[c + kp] - tk[c - kp]) * inv_rm2dthe;
         const double ddisdthe = (ds[c + kp] - ds[c - kp]) * inv_rm2dthe;
         const double dtkedphi = (tk[ce] - tk[cw]) * inv_rmsinthe2dphi;
         const double ddisdphi = (ds[ce] - ds[cw]) * inv_rmsinthe2dphi;
         const double grad_dot = dtkedr * ddisdr + dtkedthe * ddisdthe + dtkedphi * ddisdphi;
         const double dis_safe = dmax(dsc, 1.0e-20);
-        const double inv_dis = 1.0 / dis_safe;
+        const double inv_dis = qdiv(1.0, dis_safe);
         const double CD_kw = dmax(2.0 * sig_w2 * inv_dis * grad_dot, 1.0e-20);
         const double sq_k = sqrt(tkc);
         const double t_a = sq_k * inv_bet_star * inv_dis * inv_ys;         // sqrt(k) / (beta* omega y*)
         const double t_b = 500.0 * nue_air_nd * inv_ys2 * inv_dis;         // 500 nu / (y*^2 omega)
-        const double arg1 = dmin(dmax(t_a, t_b), 4.0 * sig_w2 * tkc * inv_ys2 / CD_kw);
+        const double arg1 = dmin(dmax(t_a, t_b), qdiv(4.0 * sig_w2 * tkc * inv_ys2, CD_kw));
         const double arg2 = dmax(2.0 * t_a, t_b);
         const double a1sq = arg1 * arg1;
         const double F1 = tanh(a1sq * a1sq);
         const double F2 = tanh(arg2 * arg2);
-        nue = a1 * tkc / dmax(a1 * dis_safe, Omega * F2);
+        nue = qdiv(a1 * tkc, dmax(a1 * dis_safe, Omega * F2));
         const double tke_safe = dmax(tkc, 1.0e-20);
         const double P_k = dmin(prod, 20.0 * bet_star * tke_safe * dis_safe);
         const double Y_k = bet_star * tke_safe * dis_safe;
-        const double P_w = (F1 * gam1 + (1.0 - F1) * gam2) * P_k * dis_safe / tke_safe;
+        const double P_w = qdiv((F1 * gam1 + (1.0 - F1) * gam2) * P_k * dis_safe, tke_safe);
         const double Y_w = (F1 * bet1 + (1.0 - F1) * bet2) * dis_safe * dis_safe;
         const double D_w = 2.0 * (1.0 - F1) * sig_w2 * inv_dis * grad_dot;
         tks = P_k - Y_k;
@@ -161,7 +161,7 @@ __device__ void sources_cell(const TurbArgs& A, int i, int j, int k) {
         const double bet_star = 0.09, gam = 0.52, C_lim = 0.875, bet_0 = 0.0708;
         // the reference's quotients by rm 2 dthe, rm sin 2 dphi and 2 dr (rm + 1) as products with the
         // column's reciprocals (one division per cell)
-        const double inv_r1 = A.inv_2dr / (rm + 1.0);
+        const double inv_r1 = qdiv(A.inv_2dr, rm + 1.0);
         const double dtkedthe = (tk[c + kp] - tk[c - kp]) * inv_rm2dthe;
         const double ddisdthe = (ds[c + kp] - ds[c - kp]) * inv_rm2dthe;
         const double dtkedphi = (tk[ce] - tk[cw]) * inv_rmsinthe2dphi;
@@ -182,14 +182,14 @@ __device__ void sources_cell(const TurbArgs& A, int i, int j, int k) {
         const double gd = dtkedr * ddisdr + dtkedthe * ddisdthe + dtkedphi * ddisdphi;
         const double sig_d = (gd <= 0.0) ? 0.0 : 0.125;
         const double b3 = bet_star * dmax(dsc, 1.0e-20);
-        const double chi_w = fabs(Omega * Omega * S_mag / (b3 * b3 * b3));
-        const double f_bet = (1.0 + 85.0 * chi_w) / (1.0 + 100.0 * chi_w);
-        nue = tkc / dmax(w_hat, 1.0e-20);
+        const double chi_w = fabs(qdiv(Omega * Omega * S_mag, b3 * b3 * b3));
+        const double f_bet = qdiv(1.0 + 85.0 * chi_w, 1.0 + 100.0 * chi_w);
+        nue = qdiv(tkc, dmax(w_hat, 1.0e-20));
         const double P_k = dmin(prod, 20.0 * bet_star * tkc * dsc);
         const double Y_k = bet_star * tkc * dsc;
-        const double P_w = gam * dsc / dmax(tkc, 1.0e-20) * P_k;
+        const double P_w = qdiv(gam * dsc, dmax(tkc, 1.0e-20)) * P_k;
         const double Y_w = bet_0 * f_bet * dsc * dsc;
-        const double D_w = sig_d / dmax(dsc, 1.0e-20) * gd;
+        const double D_w = qdiv(sig_d, dmax(dsc, 1.0e-20)) * gd;
         tks = P_k - Y_k;
         dss = P_w - Y_w + D_w;
     } else {                       // compute_k_epsilon (Turbulence.h:885-926)
@@ -216,8 +216,8 @@ __device__ void sources_cell(const TurbArgs& A, int i, int j, int k) {
         // quotients as products with 1 / dz, 1 / T, 1 / rho and the host's constant quotients
         const double Tc = A.t[c] * A.t_ref;
         const double dz = T.height_m[i + 1] - T.height_m[i - 1];
-        const double dTdz = (A.t[c + P] - A.t[c - P]) * A.t_ref / dz;
-        const double inv_T = 1.0 / Tc;
+        const double dTdz = qdiv((A.t[c + P] - A.t[c - P]) * A.t_ref, dz);
+        const double inv_T = qdiv(1.0, Tc);
         double Gam = A.gam_ad, fac = 1.0;
         if (A.buoy == 3 && Tc > 0.0) {
             double rho = A.r_mix;
@@ -226,7 +226,7 @@ __device__ void sources_cell(const TurbArgs& A, int i, int j, int k) {
                 rho = (r_ > 0.0 && isfinite(r_)) ? r_ : A.r_mix;
             }
             double a = 0.0, b = 0.0;
-            const double inv_rho = 1.0 / rho;
+            const double inv_rho = qdiv(1.0, rho);
             for (int n = 0; rho > 0.0 && n < 3; n++) {
                 const double qc = (dmax(0.0, A.gc[n][c]) + dmax(0.0, A.gi[n][c])) * inv_rho;
                 if (!(qc > 1.0e-9)) continue;
@@ -235,7 +235,7 @@ __device__ void sources_cell(const TurbArgs& A, int i, int j, int k) {
                 a += L * qv * A.inv_R_mix * inv_T;
                 b += A.ep[n] * L * L * qv * A.inv_cpR * inv_T * inv_T;
             }
-            if (isfinite(a + b)) { Gam *= (1.0 + a) / (1.0 + b); fac = 1.0 + a; }
+            if (isfinite(a + b)) { Gam *= qdiv(1.0 + a, 1.0 + b); fac = 1.0 + a; }
         }
         const double N2 = (Tc > 0.0 && dz > 0.0) ? A.g * inv_T * (dTdz + Gam) * fac : 0.0;
         if (isfinite(N2) && (N2 > 0.0 || A.buoy == 2)) tks -= dmax(0.0, nue) * N2 * A.tL2_pr;
