@@ -115,11 +115,14 @@ struct atsat_dyn {
     bool aliased = false;
     bool shadow_valid = false;
     double* spare_n[NPROG] = {};
+    // while aliased: the fields whose n-level has its own storage again (spare_n) because a call after
+    // restoreVar changed the live field alone (the turbulence closure: k* and omega*)
+    uint32_t split_mask = 0;
     // stage increments dl_1, dl_2, dl_3 (the stage-0 input live - y_n sits in C until stage 2)
     float* dlA[NPROG] = {};
     float* dlB[NPROG] = {};
     float* dlC[NPROG] = {};
-    bool dl_edges_zero = false;          // the cells no stage writes hold 0 in A, B and C
+    uint32_t edges_dirty = ~0u;          // fields whose cells no stage writes may hold non-zero A, B, C
     float* acc_turb[2] = {};             // tke, dis: k1 + 2 k2 + 2 k3
     float* fz[NFZ] = {};
     float* conv32[NCONV] = {};
@@ -862,14 +865,14 @@ MixedIO make_mixed_io(atsat_dyn* h, float* const* dl_in, float* const* dl_out, d
     return io;
 }
 
-// Once per RK step: yn32 / wlo <- y_n (`base`), dl_0 <- live - y_n into all three increment buffers
-// when asked (the cells no stage writes keep Y_s = live at every stage), the dirty FP32 input copies,
-// and the frozen FP64 momentum terms.
-int enqueue_mixed_prepare(atsat_dyn* h, double* const* base, bool with_dl0, bool resident) {
+// Once per RK step: yn32 / wlo <- y_n (`base`) unless the resident copies are current, dl_0 <- live - y_n
+// into all three increment buffers for the fields of dl0_mask (the cells no stage writes keep Y_s = live
+// at every stage), the dirty FP32 input copies, and the frozen FP64 momentum terms.
+int enqueue_mixed_prepare(atsat_dyn* h, double* const* base, uint32_t dl0_mask, bool resident) {
     MixedPrep pr{};
     pr.write_yn32 = resident ? 0 : 1;
-    const bool dl0 = with_dl0 && !resident;
     for (int q = 0; q < NPROG; q++) {
+        const bool dl0 = (dl0_mask >> q) & 1u;
         pr.yn64[q] = base[q];
         pr.live64[q] = h->f[q];
         pr.yn32[q] = h->yn32[q];
@@ -878,7 +881,8 @@ int enqueue_mixed_prepare(atsat_dyn* h, double* const* base, bool with_dl0, bool
         pr.dl0[1][q] = dl0 ? h->dlA[q] : nullptr;
         pr.dl0[2][q] = dl0 ? h->dlB[q] : nullptr;
     }
-    if (dl0) h->dl_edges_zero = false;
+    pr.any_dl0 = dl0_mask != 0;
+    h->edges_dirty |= dl0_mask;
     pr.wlo = h->wlo;
     pr.wlo_b = nullptr;
     int n = 0;
@@ -1053,18 +1057,31 @@ int enqueue_rk4_mixed(atsat_dyn* h, bool resident) {
     double* L[NPROG];
     for (int q = 0; q < NPROG; q++) { yn[q] = h->f[ATSAT_F_N_BASE + q]; L[q] = h->f[q]; }
     const bool fast = resident && h->aliased && h->shadow_valid;
-    if ((rc = enqueue_mixed_prepare(h, yn, true, fast))) return rc;
-    if (fast && !h->dl_edges_zero) {
+    // fields whose live values differ from y_n although the run is aliased (split after restoreVar)
+    const uint32_t split = fast ? h->split_mask : 0u;
+    const uint32_t all = (1u << NPROG) - 1u;
+    if (fast && (h->edges_dirty & ~split)) {
         // live == y_n: the cells no stage writes must hold a zero increment in A, B and C (contiguous)
         CK(h, cudaMemsetAsync(h->dlA[0], 0, (size_t)3 * NPROG * h->kc.fsz * sizeof(float), h->stream));
-        h->dl_edges_zero = true;
+        h->edges_dirty = 0;
     }
-    if (resident && !fast) {
+    if (split) {
+        // stage 0 reads C: zero for the aliased fields, live - y_n for the split ones (the prepare's dl_0,
+        // which also writes their A and B at the cells no stage writes)
+        CK(h, cudaMemsetAsync(h->dlC[0], 0, (size_t)NPROG * h->kc.fsz * sizeof(float), h->stream));
+    }
+    if ((rc = enqueue_mixed_prepare(h, yn, fast ? split : all, fast))) return rc;
+    if (resident && (!fast || split)) {
         // the copies of y_{n+1} start as (float) live: cells the step and the BCs leave alone keep them
+        // (every field on the general path, the split ones on the aliased path)
         MixedPrep pr{};
         pr.write_yn32 = 1;
-        for (int q = 0; q < NPROG; q++) { pr.yn64[q] = L[q]; pr.live64[q] = L[q]; pr.yn32[q] = h->yo32[q]; }
-        pr.wlo = h->wlo_o;
+        for (int q = 0; q < NPROG; q++) {
+            pr.yn64[q] = L[q];
+            pr.live64[q] = L[q];
+            pr.yn32[q] = (!fast || ((split >> q) & 1u)) ? h->yo32[q] : nullptr;
+        }
+        pr.wlo = pr.yn32[ATSAT_F_W] ? h->wlo_o : nullptr;
         pr.skip_frozen = 1;
         Timed t(h, ATSAT_K_PREPARE);
         CK(h, launch_mixed_prepare(h->kc, pr, h->stream));
@@ -1073,7 +1090,7 @@ int enqueue_rk4_mixed(atsat_dyn* h, bool resident) {
     const double dt = h->p.dt;
     // increments: stage 0 reads dl_0 (C; none when live == y_n) and writes dl_1 to A, stage 1: A -> B,
     // stage 2: B -> C, the final stage reads C and the point values of A and B
-    float* const* ins[4] = {fast ? nullptr : h->dlC, h->dlA, h->dlB, h->dlC};
+    float* const* ins[4] = {(fast && !split) ? nullptr : h->dlC, h->dlA, h->dlB, h->dlC};
     float* const* outs[4] = {h->dlA, h->dlB, h->dlC, nullptr};
     for (int stage = 0; stage < 4; stage++) {
         StageParams sp{};
@@ -1165,12 +1182,18 @@ int enqueue_restore(atsat_dyn* h, bool resident = false) {
     Timed t(h, ATSAT_K_GLUE);
     const size_t bytes = (size_t)h->kc.fsz * 8;
     if (resident && h->p.precision == ATSAT_DYN_MIXED) {
-        if (!h->aliased) {
+        if (h->aliased) {
+            // the split fields share their live storage again (spare_n keeps their buffers)
+            for (int q = 0; q < NPROG; q++)
+                if ((h->split_mask >> q) & 1u) h->f[ATSAT_F_N_BASE + q] = h->f[q];
+            h->split_mask = 0;
+        } else {
             for (int q = 0; q < NPROG; q++) {
                 h->spare_n[q] = h->f[ATSAT_F_N_BASE + q];
                 h->f[ATSAT_F_N_BASE + q] = h->f[q];
             }
             h->aliased = true;
+            h->split_mask = 0;
             // both FP32 copies must agree on the cells no step or boundary pass writes
             const size_t b32 = (size_t)h->kc.fsz * 4;
             for (int q = 0; q < NPROG; q++)
@@ -1195,12 +1218,29 @@ int unalias(atsat_dyn* h, const bool* overwritten = nullptr) {
     if (!h->aliased) return ATSAT_DYN_OK;
     const size_t bytes = (size_t)h->kc.fsz * 8;
     for (int q = 0; q < NPROG; q++) {
+        if ((h->split_mask >> q) & 1u) continue;           // has its own n-level storage already
         if (!(overwritten && overwritten[q]))
             CK(h, cudaMemcpyAsync(h->spare_n[q], h->f[q], bytes, cudaMemcpyDeviceToDevice, h->stream));
         h->f[ATSAT_F_N_BASE + q] = h->spare_n[q];
     }
     h->aliased = false;
     h->shadow_valid = false;
+    h->split_mask = 0;
+    return ATSAT_DYN_OK;
+}
+
+// In an aliased resident run, give the fields of `mask` their own n-level storage again (a copy of the
+// shared values), the others staying aliased: for a call after restoreVar that changes those live fields
+// alone. The FP32 copies of y_n stay valid.
+int split_fields(atsat_dyn* h, uint32_t mask) {
+    if (!h->aliased) return ATSAT_DYN_OK;
+    const size_t bytes = (size_t)h->kc.fsz * 8;
+    for (int q = 0; q < NPROG; q++) {
+        if (!((mask >> q) & 1u) || ((h->split_mask >> q) & 1u)) continue;
+        CK(h, cudaMemcpyAsync(h->spare_n[q], h->f[q], bytes, cudaMemcpyDeviceToDevice, h->stream));
+        h->f[ATSAT_F_N_BASE + q] = h->spare_n[q];
+    }
+    h->split_mask |= mask;
     return ATSAT_DYN_OK;
 }
 
@@ -1524,7 +1564,9 @@ int enqueue_turbulence(atsat_dyn* h, bool resident = false) {
         if (rc) return rc;
     }
     if (resident && h->p.precision == ATSAT_DYN_MIXED) {
-        int rc = unalias(h);
+        // the closure changes live k* and omega* only (and their n-level copies at the seam and corners):
+        // those two get their own n-level storage, the other fields stay aliased
+        int rc = split_fields(h, (1u << ATSAT_F_TKE) | (1u << ATSAT_F_DIS));
         if (rc) return rc;
     }
     h->ttab.taper_dz = turb_taper_dz(h);
@@ -1620,7 +1662,7 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
         for (int s = 0; s < NPROG; s++) { h->dlA[s] = r; r += K.fsz; }
         for (int s = 0; s < NPROG; s++) { h->dlB[s] = r; r += K.fsz; }
         for (int s = 0; s < NPROG; s++) { h->dlC[s] = r; r += K.fsz; }
-        h->dl_edges_zero = true;
+        h->edges_dirty = 0;
         for (int s = 0; s < 2; s++) { h->acc_turb[s] = r; r += K.fsz; }
         for (int s = 0; s < NFZ; s++) { h->fz[s] = r; r += K.fsz; }
         for (int s = 0; s < NCONV; s++) { h->conv32[s] = r; r += K.fsz; h->conv_dirty[s] = true; }
@@ -1842,7 +1884,7 @@ int atsat_dyn_rhs(atsat_dyn_t h) {
     double* L[NPROG];
     for (int q = 0; q < NPROG; q++) L[q] = h->f[q];
     if (h->p.precision == ATSAT_DYN_MIXED) {
-        int rc = enqueue_mixed_prepare(h, L, false, false);   // the stencils read the live fields
+        int rc = enqueue_mixed_prepare(h, L, 0u, false);   // the stencils read the live fields
         if (rc) return rc;
         MixedIO io = make_mixed_io(h, nullptr, nullptr, nullptr);
         for (int q = 0; q < NPROG; q++) io.yn64[q] = L[q];
@@ -2229,7 +2271,7 @@ int enqueue_iteration(atsat_dyn* h, int32_t it) {
 
 bool resident_steady(const atsat_dyn* h) {
     if (h->p.precision != ATSAT_DYN_MIXED) return true;
-    if (!(h->aliased && h->shadow_valid && h->dl_edges_zero)) return false;
+    if (!(h->aliased && h->shadow_valid && h->edges_dirty == 0 && h->split_mask == 0)) return false;
     for (int s = 0; s < NCONV; s++)
         if (h->conv_dirty[s]) return false;
     return true;

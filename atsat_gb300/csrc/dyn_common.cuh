@@ -246,7 +246,8 @@ struct alignas(16) PrepGeo {
 static_assert(sizeof(PrepGeo) == 64, "PrepGeo layout");
 
 struct MixedPrep {
-    int write_yn32;
+    int write_yn32;                // yn32[q] (where non-null) and wlo from yn64
+    int any_dl0;                   // some dl0[0][q] is non-null
     int skip_frozen;               // conversions only
     const double* yn64[NPROG];
     const double* live64[NPROG];

@@ -159,17 +159,21 @@ __global__ void __launch_bounds__(256) mixed_prepare_kernel(const KConst K, cons
     const int64_t c = ((int64_t)i * K.jm + j) * kp + k;
     // dl0[0] is the stage-0 input (every cell); dl0[1], dl0[2] need live - y_n only where no stage writes
     const bool rk_cell = (i >= 1 && i <= K.im - 2 && j >= 2 && j <= K.jm - 3 && k <= K.km - 2);
-    if (pr.write_yn32) {
+    if (pr.write_yn32 || pr.any_dl0) {
 #pragma unroll 4
         for (int q = 0; q < NPROG; q++) {
+            const bool y32 = pr.write_yn32 && pr.yn32[q];
+            if (!y32 && !pr.dl0[0][q]) continue;
             const double yn = __ldg(pr.yn64[q] + c);
-            const float hi = d2f(yn);
-            pr.yn32[q][c] = hi;
-            if (pr.yn32_b[q]) pr.yn32_b[q][c] = hi;
-            if (q == ATSAT_F_W) {
-                const float lo = d2f(yn - f2d(hi));
-                pr.wlo[c] = lo;
-                if (pr.wlo_b) pr.wlo_b[c] = lo;
+            if (y32) {
+                const float hi = d2f(yn);
+                pr.yn32[q][c] = hi;
+                if (pr.yn32_b[q]) pr.yn32_b[q][c] = hi;
+                if (q == ATSAT_F_W && pr.wlo) {
+                    const float lo = d2f(yn - f2d(hi));
+                    pr.wlo[c] = lo;
+                    if (pr.wlo_b) pr.wlo_b[c] = lo;
+                }
             }
             if (pr.dl0[0][q]) {
                 const float d0 = d2f(__ldg(pr.live64[q] + c) - yn);

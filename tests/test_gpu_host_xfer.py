@@ -120,3 +120,29 @@ def test_rk_step_through_each_path(direct):
         d.download(list(range(F.NFIELDS)))
     got = {fid: np.stack(rows[fid]).reshape(g.shape) for fid in range(F.NFIELDS)}
     compare(got, ref.arrays, F.PROG + [F.RHS_U, F.RHS_V, F.RHS_W], TOL_FP64, "rk step")
+
+
+def test_misaligned_rows_take_the_copy_engines():
+    """A row pointer that is not a whole double (8-byte aligned) sends its binding to the copy engines; the
+    round trip is still exact."""
+    from atsat_gb300 import dyn
+    g, P, _ = case((9, 13, 17), seed=6)
+    n = g.im * g.jm
+    src = rand_field(g, 41)
+    with dyn.Dycore(g, P) as d:
+        need_direct(d)
+        raw = [np.zeros(g.km * 8 + 8, dtype=np.uint8) for _ in range(n)]
+        rows = []
+        for r in range(n):
+            off = 4 if r == 7 else 0
+            a = raw[r][off:off + g.km * 8].view(np.float64)
+            a[...] = src[r // g.jm, r % g.jm]
+            rows.append(a)
+        d.bind_rows(F.T, rows)
+        assert not d.host_direct(F.T)
+        d.upload([F.T])
+        out = np.zeros(g.shape)
+        d.bind(F.T, out)
+        assert d.host_direct(F.T)
+        d.download([F.T])
+    assert np.array_equal(out, src)

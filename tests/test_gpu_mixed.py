@@ -302,3 +302,20 @@ def test_ensemble_concurrent_equals_sequential():
         for f in F.PROG + [F.P_DYN]:
             assert np.array_equal(runs[0][m].arrays[f], runs[1][m].arrays[f]), (shp, F.NAMES[f])
             assert np.array_equal(runs[0][m].arrays[f], s.arrays[f]), (shp, F.NAMES[f])
+
+
+def test_profile_classes_times_only_the_chosen_classes():
+    """atsat_dyn_profile_classes: launch groups of the selected kernel classes are timed, others not."""
+    from atsat_gb300 import abi, dyn
+    g, P, st = case((21, 91, 181), seed=73)
+    with dyn.Dycore(g, dict(P, precision=1)) as d:
+        d.load_state(st.copy())
+        d.iterate(1, 2)
+        d.profile_classes([abi.K_RK_STAGE])
+        d.profile_reset()
+        d.iterate(3, 2)
+        n_rk, ms_rk = d.profile_read(abi.K_RK_STAGE)
+        others = [d.profile_read(c)[0] for c in range(len(abi.K_NAMES)) if c != abi.K_RK_STAGE]
+        d.profile(False)
+    assert n_rk == 8 and ms_rk > 0
+    assert not any(others)
