@@ -97,11 +97,47 @@ def test_mixed_ten_iterations_driver_glue():
     ref = st.copy()
     oracle.steps(ref, P, 10, glue=True)
     got = run_mixed(g, P, st, 10, TILED2)
-    rep = drift(got.arrays, ref.arrays, F.PROG + [F.P_DYN])
+    rep = drift(got.arrays, ref.arrays, F.PROG + F.PROG_N + [F.P_DYN])
+    print("\nglue, 10 iterations:", {k: f"{v[0]:.2e}" for k, v in rep.items()})
     bad = {F.NAMES[f]: rep[F.NAMES[f]][0] for f in CRITERION if not rep[F.NAMES[f]][0] <= TOL_MIXED}
+    assert not bad, bad
+    # k* and omega*: the closure changes them after restoreVar, so their n-level copies part from the live
+    # fields inside the resident loop (split_fields); both levels must follow the oracle. omega* within 1e-2
+    # only: where grad k . grad omega is near zero the SST cross-diffusion term sits at its floor (1e-20) and
+    # the blending F1 switches, so the closure turns the FP32 stages' 1e-7 differences into O(1) source
+    # differences in those cells (the FP64 path follows the oracle to 1e-15 there)
+    bad = {F.NAMES[f]: rep[F.NAMES[f]][0] for f in (F.TKE, F.TKEN) if not rep[F.NAMES[f]][0] <= 1e-5}
+    bad.update({F.NAMES[f]: rep[F.NAMES[f]][0] for f in (F.DIS, F.DISN) if not rep[F.NAMES[f]][0] <= 1e-2})
     assert not bad, bad
     for f in (F.H2O, F.NH3, F.NH4SH, F.CH4_ICE, F.H2S, F.NH3_CLOUD):
         assert np.all(got.arrays[f] >= 0.0), F.NAMES[f]
+
+
+def test_mixed_glue_then_dropin_calls():
+    """Resident iterations with the glue (k* and omega* split from the shared n-level storage after each
+    closure), then drop-in calls that see the live and n-level fields separately."""
+    from atsat_gb300 import dyn
+    g, P, st = case((21, 91, 181), seed=46, exercise=True, driver_glue=1)
+    ref = st.copy()
+    oracle.steps(ref, P, 3, glue=True)
+    s = st.copy()
+    with dyn.Dycore(g, dict(P, precision=1)) as d:
+        d.set_stage_variant(TILED2)
+        d.load_state(s)
+        d.iterate(1, 3)
+        d.download(ALL)
+        rep = drift(s.arrays, ref.arrays, F.PROG + F.PROG_N)
+        bad = {k: v[0] for k, v in rep.items() if not v[0] <= (1e-2 if k in ("dis", "disn") else 1e-5)}
+        assert not bad, ("after 3 glue iterations", bad)
+        s.arrays[F.T][...] *= 1.0 + 1e-4
+        ref.arrays[F.T][...] = s.arrays[F.T]
+        d.upload([F.T])
+        d.RungeKuttaSat()
+        oracle.rk4_step(ref, P)
+        d.download(ALL)
+    rep = drift(s.arrays, ref.arrays, F.PROG)
+    bad = {k: v[0] for k, v in rep.items() if not v[0] <= (1e-2 if k == "dis" else 1e-5)}
+    assert not bad, ("after the drop-in step", bad)
 
 
 @pytest.mark.parametrize("variant", VARIANTS)
