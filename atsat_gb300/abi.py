@@ -27,7 +27,7 @@ class Grid(C.Structure):
 class Params(C.Structure):
     _fields_ = ([(n, C.c_double) for n, _ in F.PARAM_DOUBLES]
                 + [(n, C.c_int32) for n, _ in F.PARAM_INTS]
-                + [("reserved", C.c_int32 * 4)])
+                + [("reserved", C.c_int32 * 3)])
 
 
 class TurbParams(C.Structure):

@@ -1347,7 +1347,7 @@ int atsat_dyn_params_default(atsat_dyn_params* p) {
     p->press_line = 0; p->press_baro = 0; p->precision = ATSAT_DYN_FP64;
     p->bc_radius_form = 2; p->bc_bottom_form = 3; p->bc_pole_form = 1; p->bc_pole_fill = 1; p->bc_lid_u = 1;
     p->bc_top_taper = 2; p->bc_species_lid_copy = 1; p->bc_species_wall_copy = 2; p->local_rho = 1;
-    p->damp_pdyn = 3; p->clamp_species = 1; p->driver_glue = 0;
+    p->damp_pdyn = 3; p->clamp_species = 1; p->driver_glue = 0; p->press_every_step = 0;
     return ATSAT_DYN_OK;
 }
 
@@ -2250,7 +2250,7 @@ namespace {
 // one resident dycore iteration (cSaturnModel.cpp:864-1111 restricted to the dycore), enqueued
 int enqueue_iteration(atsat_dyn* h, int32_t it) {
     int rc;
-    if (it % 2 == 0) {
+    if (it % 2 == 0 || h->p.press_every_step) {
         {
             Timed t(h, ATSAT_K_GLUE);
             CK(h, launch_density(h->kc, h->f[ATSAT_F_T], h->f[ATSAT_F_P_STAT], h->p.R_mix, h->f[ATSAT_F_RHO_MIX],

@@ -67,5 +67,5 @@ PARAM_INTS = [
     ("rigid_lid", 1), ("press_line", 0), ("press_baro", 0), ("precision", 0),
     ("bc_radius_form", 2), ("bc_bottom_form", 3), ("bc_pole_form", 1), ("bc_pole_fill", 1),
     ("bc_lid_u", 1), ("bc_top_taper", 2), ("bc_species_lid_copy", 1), ("bc_species_wall_copy", 2),
-    ("local_rho", 1), ("damp_pdyn", 3), ("clamp_species", 1), ("driver_glue", 0),
+    ("local_rho", 1), ("damp_pdyn", 3), ("clamp_species", 1), ("driver_glue", 0), ("press_every_step", 0),
 ]

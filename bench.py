@@ -387,9 +387,33 @@ def measure(a, rank, world, g, P, st, pinned, precision):
             "launches": n_rk, "mean_launch_ms": avg_ms}
     if precision == "fp64":
         roof["note"] = "bound by GB300's FP64 pipe (2 DFMA per SM per cycle), not by HBM"
+        # the FP64 roofline that binds: FP64 instructions per interior cell and stage counted by ncu
+        # (profiles/rk_stage_fp64_21x91x181.md) over the same CUDA-event stage time, against 2 per SM per cycle
+        sm_hz = (clk.get("sm_mhz") or 2070.0) * 1e6
+        per_cell = 590.0
+        ach = per_cell * interior_rk(g) / (avg_ms / 1e3)
+        peak64 = 2.0 * 152 * sm_hz
+        roof["fp64_pipe"] = {"instructions_per_cell": per_cell, "achieved_per_s": ach, "peak_per_s": peak64,
+                             "frac": ach / peak64, "source": "ncu count, profiles/rk_stage_fp64_21x91x181.md"}
     d.close()
+    # the pressure call on every iteration, beside the reference's even-iteration schedule
+    pe = None
+    if a.steps > 0:
+        d = dyn.Dycore(g, dict(P, precision=1 if precision == "mixed" else 0, press_every_step=1))
+        d.load_state(st.copy())
+        if tune:
+            d.set_stage_variant(dyn.Dycore.STAGE_NAMES.index(tune["stage_variant"]))
+        d.iterate(1, a.warmup)
+        n_pe = max(2, min(a.steps, 100) // 2 * 2)
+        barrier(world)
+        d.timer_start()
+        d.iterate(a.warmup + 1, n_pe)
+        ms_pe = reduce_max(world, d.timer_stop())
+        d.close()
+        pe = {"value": world * n_pe * g.cells / (ms_pe / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms_pe / n_pe,
+              "steps": n_pe}
     return {"value": value, "ms_per_step": ms / a.steps, "e2e": e2e, "roofline": roof, "gpu_launches": launches,
-            "clocks": clk, "kernels_ms": kern, "tune": tune}
+            "clocks": clk, "kernels_ms": kern, "tune": tune, "pressure_every_step": pe}
 
 
 def run_ours(a, rank, world):
@@ -412,9 +436,11 @@ def run_ours(a, rank, world):
            "warmup": a.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32+f64" if head == "mixed" else "f64", "data": "synthetic",
            "config": dict(config(g, head), **(r["tune"] or {})), "e2e": r["e2e"], "roofline": r["roofline"],
-           "gpu_launches": r["gpu_launches"], "clocks": r["clocks"], "kernels_ms": r["kernels_ms"]}
+           "gpu_launches": r["gpu_launches"], "clocks": r["clocks"], "kernels_ms": r["kernels_ms"],
+           "pressure_every_step": r["pressure_every_step"]}
     for p in a.precisions[1:]:
-        out[p] = {k: res[p][k] for k in ("value", "ms_per_step", "e2e", "roofline", "gpu_launches", "clocks")}
+        out[p] = {k: res[p][k] for k in ("value", "ms_per_step", "e2e", "roofline", "gpu_launches", "clocks",
+                                         "pressure_every_step")}
         out["mixed_over_" + p] = r["value"] / res[p]["value"]
     if cpu:
         out["cpu_baseline"] = cpu

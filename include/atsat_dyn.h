@@ -176,7 +176,10 @@ typedef struct atsat_dyn_params {
     int32_t damp_pdyn;         /* ATSAT_DAMP_PDYN, 3 under GEO_BALANCE, else 1 */
     int32_t clamp_species;     /* 1; 0 with ATSAT_NO_CLAMP */
     int32_t driver_glue;       /* 0: atsat_dyn_iterate runs the dycore sequence only; 1: also the two above */
-    int32_t reserved[4];
+    /* 0: atsat_dyn_iterate runs the pressure call on even iterations, as Run does (cSaturnModel.cpp:864-873);
+     * 1: on every iteration (a benchmark schedule; no reference counterpart) */
+    int32_t press_every_step;
+    int32_t reserved[3];
 } atsat_dyn_params;
 
 /* statistics of one pressure call */

@@ -355,3 +355,23 @@ def test_profile_classes_times_only_the_chosen_classes():
         d.profile(False)
     assert n_rk == 8 and ms_rk > 0
     assert not any(others)
+
+
+@pytest.mark.parametrize("precision", [1, 0], ids=["mixed", "fp64"])
+def test_press_every_step_schedule(precision):
+    """press_every_step = 1 runs the pressure call on every iteration: iterations 1 and 2 then equal the
+    default schedule's even iterations 2 and 4, bit for bit."""
+    from atsat_gb300 import dyn
+    g, P, st = case((21, 91, 181), seed=75, exercise=True)
+    a, b = st.copy(), st.copy()
+    with dyn.Dycore(g, dict(P, precision=precision, press_every_step=1)) as d:
+        d.load_state(a)
+        d.iterate(1, 2)
+        d.download(ALL)
+    with dyn.Dycore(g, dict(P, precision=precision)) as d:
+        d.load_state(b)
+        d.iterate(2, 1)
+        d.iterate(4, 1)
+        d.download(ALL)
+    for f in F.PROG + F.PROG_N + [F.P_DYN, F.RHO_MIX]:
+        assert np.array_equal(a.arrays[f], b.arrays[f], equal_nan=True), F.NAMES[f]
