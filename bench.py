@@ -222,6 +222,21 @@ def cpu_baseline(g, P, seed, target_s=3.0):
                       f"{dt:.2f} s wall on {os.cpu_count()} OpenMP threads"}
 
 
+def cpu_baseline_one_thread(shape):
+    """The same bounded sample on one OpenMP thread, in a child process (OpenMP fixes its thread count when
+    the library loads)."""
+    code = ("import json, sys; sys.path.insert(0, %r); import bench; from atsat_gb300 import abi, synth; "
+            "g = synth.make_grid(*%r); r = bench.cpu_baseline(g, abi.default_params(), seed=0, target_s=2.0); "
+            "r['cores'] = 1; r['sample'] = r['sample'].replace('%%d OpenMP threads' %% __import__('os').cpu_count(), "
+            "'1 OpenMP thread'); print(json.dumps(r))") % (ROOT, tuple(shape))
+    try:
+        out = subprocess.run([sys.executable, "-c", code], env=dict(os.environ, OMP_NUM_THREADS="1"),
+                             capture_output=True, text=True, timeout=300)
+        return json.loads(out.stdout.strip().splitlines()[-1])
+    except (subprocess.SubprocessError, ValueError, IndexError, OSError):
+        return None
+
+
 def run_reference(a, rank, world):
     if rank != 0:
         return None
@@ -421,8 +436,10 @@ def run_ours(a, rank, world):
     g = synth.make_grid(*a.shape)
     P = abi.default_params()
     cpu = None
+    cpu1 = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         cpu = cpu_baseline(g, P, seed=0)          # before the first CUDA call
+        cpu1 = cpu_baseline_one_thread(a.shape)
     st = synth.saturn_state(g, P, seed=rank)
     pinned = {fid: dyn.PinnedArray(g.shape) for fid in range(F.NFIELDS)}
     res = {p: measure(a, rank, world, g, P, st, pinned, p) for p in a.precisions}
@@ -444,6 +461,8 @@ def run_ours(a, rank, world):
         out["mixed_over_" + p] = r["value"] / res[p]["value"]
     if cpu:
         out["cpu_baseline"] = cpu
+    if cpu1:
+        out["cpu_baseline_one_thread"] = cpu1
     return out
 
 
