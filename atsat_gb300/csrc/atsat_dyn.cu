@@ -89,6 +89,7 @@ struct atsat_dyn {
     // through the CPU's page tables, host_direct when that path is selected, per field whether its
     // binding takes it, and the device copy of a ragged binding's row-pointer table
     bool host_ok = false, host_direct = false;
+    bool async = false;                  // entry points return without waiting (ATSAT_DYN_ASYNC)
     bool direct[ATSAT_NFIELDS] = {};
     double** dev_rows[ATSAT_NFIELDS] = {};
 
@@ -709,6 +710,8 @@ int route_binding(atsat_dyn* h, int fid) {
                 return fail(h, ATSAT_DYN_E_NOMEM, "row table: %s", cudaGetErrorString(e));
             }
         }
+        // a transfer queued earlier (asynchronous mode) may still read the old table
+        CK(h, cudaStreamSynchronize(h->stream));
         CK(h, cudaMemcpy(h->dev_rows[fid], h->bind_rows[fid].data(), n * sizeof(double*), cudaMemcpyHostToDevice));
     }
     h->direct[fid] = true;
@@ -736,8 +739,11 @@ int batch_add(atsat_dyn* h, HostBatch& b, int fid, int to_device) {
     return ATSAT_DYN_OK;
 }
 
-int finish(atsat_dyn* h) {
+// The end of an entry point: launch errors always; in the asynchronous mode nothing else unless the call
+// hands a device result to the host (host_result), else the wait for the stream and the device status word.
+int finish(atsat_dyn* h, bool host_result = false) {
     CK(h, cudaGetLastError());
+    if (h->async && !host_result) return ATSAT_DYN_OK;
     CK(h, cudaStreamSynchronize(h->stream));
     if (h->dev_err && h->tile_ok) {
         unsigned int v = 0;
@@ -1620,6 +1626,8 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
         h->host_ok = pageable == 1 && host_tables == 1;
         const char* env = std::getenv("ATSAT_HOST_DIRECT");
         h->host_direct = h->host_ok && !(env && std::strcmp(env, "0") == 0);
+        const char* as = std::getenv("ATSAT_DYN_ASYNC");
+        h->async = as && std::strcmp(as, "0") != 0 && as[0] != '\0';
     }
     // fields, FP64 stage buffers and accumulators (FP64 path only), source; then the small tables
     const bool fp64_stage = p->precision != ATSAT_DYN_MIXED;
@@ -1848,7 +1856,7 @@ int atsat_dyn_get_buoy_ref_level(atsat_dyn_t h, double* out) {
     if (!h || !h->slab || !out) return ATSAT_DYN_E_INVALID;
     CK(h, cudaSetDevice(h->device));
     CK(h, cudaMemcpyAsync(out, h->buoy, 8 * (size_t)h->kc.im, cudaMemcpyDeviceToHost, h->stream));
-    return finish(h);
+    return finish(h, true);
 }
 
 #define ENTRY(h)                                              \
@@ -1928,7 +1936,7 @@ int atsat_dyn_pressure(atsat_dyn_t h, atsat_dyn_pstats* out) {
     const int sweeps = h->p.press_sweeps > 0 ? h->p.press_sweeps : 1;
     int rc = enqueue_pressure(h, sweeps);
     if (rc) return rc;
-    rc = finish(h);
+    rc = finish(h, out != nullptr);
     if (rc) return rc;
     if (out) {
         unsigned long long n = 0;
@@ -2207,7 +2215,7 @@ int atsat_dyn_load_restart(atsat_dyn_t h, const char* path, int32_t* iter, int32
     if (!ok) return fail(h, ATSAT_DYN_E_INVALID, "load_restart: truncated file %s", path);
     if (iter) *iter = hdr[4];
     if (format) *format = fmt;
-    return finish(h);
+    return finish(h, true);
 }
 
 int atsat_dyn_restart_is_clean(atsat_dyn_t h, int32_t* clean) {
@@ -2220,7 +2228,7 @@ int atsat_dyn_restart_is_clean(atsat_dyn_t h, int32_t* clean) {
     h->launches += 1;
     unsigned long long c = 0;
     CK(h, cudaMemcpyAsync(&c, h->counter, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
-    int rc = finish(h);
+    int rc = finish(h, true);
     if (rc) return rc;
     *clean = c == 0 ? 1 : 0;
     return ATSAT_DYN_OK;
@@ -2375,7 +2383,18 @@ int atsat_dyn_ensemble_run(const atsat_dyn_t* members, int32_t n, int32_t reps, 
 
 int atsat_dyn_sync(atsat_dyn_t h) {
     ENTRY(h);
-    return finish(h);
+    return finish(h, true);
+}
+
+int atsat_dyn_set_async(atsat_dyn_t h, int32_t enable) {
+    if (!h || !h->slab || (enable != 0 && enable != 1)) return ATSAT_DYN_E_INVALID;
+    if (h->async && !enable) {
+        int rc = finish(h, true);
+        h->async = false;
+        return rc;
+    }
+    h->async = enable != 0;
+    return ATSAT_DYN_OK;
 }
 
 int atsat_dyn_status(atsat_dyn_t h, atsat_dyn_diag* out) {
@@ -2394,7 +2413,7 @@ int atsat_dyn_count_nonfinite(atsat_dyn_t h, int32_t field, int64_t* count) {
     h->launches += 1;
     unsigned long long n = 0;
     CK(h, cudaMemcpyAsync(&n, h->counter, sizeof(n), cudaMemcpyDeviceToHost, h->stream));
-    int rc = finish(h);
+    int rc = finish(h, true);
     *count = (int64_t)n;
     return rc;
 }
@@ -2534,7 +2553,7 @@ int atsat_dyn_autotune(atsat_dyn_t h, int32_t reps, int32_t* chosen, double* ms)
     cudaEventDestroy(ev[1]);
     h->variant = best >= 0 ? best : keep;
     *chosen = h->variant;
-    return finish(h);
+    return finish(h, true);
 }
 
 // ---- standalone pressure-equation solves ----
@@ -2617,7 +2636,7 @@ int atsat_dyn_poisson_solve(atsat_dyn_t h, int32_t method, const double* src, do
         st->rel_residual = rel;
         st->ms = ms;
     }
-    return finish(h);
+    return finish(h, true);
 }
 
 }  // extern "C"

@@ -59,6 +59,7 @@ def lib():
         L.atsat_dyn_upload.argtypes = [H, C.POINTER(C.c_int32), C.c_int32]
         L.atsat_dyn_download.argtypes = [H, C.POINTER(C.c_int32), C.c_int32]
         L.atsat_dyn_set_host_direct.argtypes = [H, C.c_int32]
+        L.atsat_dyn_set_async.argtypes = [H, C.c_int32]
         L.atsat_dyn_host_direct.argtypes = [H, C.c_int32]
         L.atsat_dyn_set_tables.argtypes = [H, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.atsat_dyn_get_buoy_ref_level.argtypes = [H, C.POINTER(C.c_double)]
@@ -319,10 +320,15 @@ class Dycore:
     def prepareProjectionBoundaries(self):
         self._ck(lib().atsat_dyn_prepare_projection_boundaries(self.h), "prepare_projection_boundaries")
 
-    def PressureSolver_run(self) -> abi.PStats:
-        st = abi.PStats()
-        self._ck(lib().atsat_dyn_pressure(self.h, C.byref(st)), "pressure")
+    def PressureSolver_run(self, stats: bool = True):
+        """PressureSolver<cSaturnModel>::run; its statistics when `stats` (which waits for the call)."""
+        st = abi.PStats() if stats else None
+        self._ck(lib().atsat_dyn_pressure(self.h, C.byref(st) if stats else None), "pressure")
         return st
+
+    def set_async(self, enable: bool):
+        """Transfers and compute calls return once queued (sync() before touching bound arrays)."""
+        self._ck(lib().atsat_dyn_set_async(self.h, 1 if enable else 0), "set_async")
 
     def damp_wiggles(self, fid: int, along_i: bool, along_j: bool, along_k: bool, strength: float = 1.0,
                      passes: int = 1):

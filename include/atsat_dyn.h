@@ -21,7 +21,12 @@
  *   - Fields are bound to HOST storage, either as the reference's ragged rows (Array::x[i][j] is
  *     one row of km doubles) or as one contiguous [im][jm][km] block. upload/download copy between
  *     the bound host storage and the device copy; every compute entry point works on the device copy
- *     only and returns when the device work is complete (ATSAT_DYN_ASYNC unset).
+ *     only and returns when the device work is complete. In the asynchronous mode (ATSAT_DYN_ASYNC=1 in
+ *     the environment at create, or atsat_dyn_set_async(h, 1)) transfers and compute calls return once
+ *     queued on the handle's stream: the host must call atsat_dyn_sync before it reads downloaded arrays
+ *     or changes uploaded ones, and errors of the device work (a timed-out wait) surface there. Calls
+ *     that hand a device result to the host (statistics, counts, restart files, autotune, solves) wait
+ *     in either mode.
  *   - There is no CPU fallback: a knob value the device path does not implement makes
  *     atsat_dyn_create return ATSAT_DYN_E_UNSUPPORTED.
  */
@@ -232,6 +237,8 @@ int atsat_dyn_download(atsat_dyn_t h, const int32_t* fields, int32_t n);
  * host memory returns ATSAT_DYN_E_UNSUPPORTED. atsat_dyn_host_direct returns 1 when `field`'s binding
  * (or, for field -1, the handle) uses the direct path, 0 when not, a negative code on error. */
 int atsat_dyn_set_host_direct(atsat_dyn_t h, int32_t enable);
+/* The asynchronous mode on (1) or off (0; waits for the queued work first). See the conventions above. */
+int atsat_dyn_set_async(atsat_dyn_t h, int32_t enable);
 int atsat_dyn_host_direct(atsat_dyn_t h, int32_t field);
 
 /* cell_vbar0 / cell_ubar0: im*jm values or NULL (empty vectors); p_baro: im*jm*km values or NULL. */

@@ -146,3 +146,28 @@ def test_misaligned_rows_take_the_copy_engines():
         assert d.host_direct(F.T)
         d.download([F.T])
     assert np.array_equal(out, src)
+
+
+def test_async_step_equals_sync():
+    """A host-fed step queued in the asynchronous mode (upload, density, pressure without statistics, RK4,
+    download, then one sync) gives the synchronous mode's bits."""
+    from atsat_gb300 import dyn
+    g, P, st = case((21, 91, 181), seed=8)
+    outs = F.PROG + [F.RHS_U, F.RHS_V, F.RHS_W, F.AUX_U, F.AUX_V, F.AUX_W, F.P_DYN]
+    res = []
+    for mode in (False, True):
+        s = st.copy()
+        with dyn.Dycore(g, dict(P, precision=1)) as d:
+            d.load_state(s)
+            d.set_async(mode)
+            for it in (2, 3):
+                d.upload(list(range(F.NFIELDS)))
+                if it % 2 == 0:
+                    d.computeMixtureDensity()
+                    d.PressureSolver_run(stats=False)
+                d.RungeKuttaSat()
+                d.download(outs)
+                d.sync()
+        res.append(s)
+    for fid in outs:
+        assert np.array_equal(res[0].arrays[fid], res[1].arrays[fid], equal_nan=True), F.NAMES[fid]
