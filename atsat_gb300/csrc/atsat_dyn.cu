@@ -736,6 +736,13 @@ int batch_add(atsat_dyn* h, HostBatch& b, int fid, int to_device) {
     f.base = h->bind_kind[fid] == BIND_ARRAY ? h->bind_base[fid] : nullptr;
     f.rows = h->bind_kind[fid] == BIND_ROWS ? h->dev_rows[fid] : nullptr;
     f.dev = h->f[fid];
+    f.dev32 = nullptr;
+    const int slot = conv_slot(fid);
+    if (to_device && slot >= 0 && h->slab32) {
+        // the mixed path's FP32 copy is written in the same pass (d2f: the hardware's rounding) and is current
+        f.dev32 = h->conv32[slot];
+        h->conv_dirty[slot] = false;
+    }
     return ATSAT_DYN_OK;
 }
 

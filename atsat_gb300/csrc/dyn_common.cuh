@@ -423,6 +423,7 @@ struct HostField {
     double* base;
     double* const* rows;
     double* dev;
+    float* dev32;                  // upload only: the field's FP32 copy, written from the same values (or null)
 };
 struct HostBatch {
     HostField f[HOST_BATCH_MAX];

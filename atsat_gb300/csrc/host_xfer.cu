@@ -1,6 +1,7 @@
 // Host <-> device transfers of bound fields by the SMs themselves: one kernel reads (or writes) the host
 // arrays of every field of an upload (download) and the device field in its pitched layout, with no
-// staging copy and no per-field copy-engine hop.
+// staging copy and no per-field copy-engine hop. An upload also writes a field's FP32 copy when asked (the
+// mixed path's copies of the point inputs), from the values it already holds.
 //
 // On a Grace-Blackwell node the GPU reaches host memory over NVLink-C2C through the CPU's page tables
 // (cudaDevAttrPageableMemoryAccessUsesHostPageTables): pinned and pageable memory alike, contiguous arrays
@@ -23,7 +24,7 @@ constexpr int XF_UNROLL = 4;         // 16-byte accesses in flight per lane befo
 // of km doubles starts 8 bytes past one every other row in a contiguous array): one leading and one
 // trailing double go alone, lane 0 takes them. Device rows start on a 16-byte boundary (kp even, fields
 // 256-byte aligned), so the device side uses 16-byte words when the host's boundary falls on its own.
-__device__ __forceinline__ void gather_row(const double* src, double* dst, int km, int lane) {
+__device__ __forceinline__ void gather_row(const double* src, double* dst, float* dst32, int km, int lane) {
     const int a = (int)((reinterpret_cast<uintptr_t>(src) >> 3) & 1u);
     const int np = (km - a) >> 1;
     const double2* s2 = reinterpret_cast<const double2*>(src + a);
@@ -41,11 +42,12 @@ __device__ __forceinline__ void gather_row(const double* src, double* dst, int k
             double* d = dst + a + 2 * p;
             if (a) { d[0] = v[q].x; d[1] = v[q].y; }
             else *reinterpret_cast<double2*>(d) = v[q];
+            if (dst32) { dst32[a + 2 * p] = d2f(v[q].x); dst32[a + 2 * p + 1] = d2f(v[q].y); }
         }
     }
     if (lane == 0) {
-        if (a) dst[0] = src[0];
-        if ((km - a) & 1) dst[km - 1] = src[km - 1];
+        if (a) { dst[0] = src[0]; if (dst32) dst32[0] = d2f(src[0]); }
+        if ((km - a) & 1) { dst[km - 1] = src[km - 1]; if (dst32) dst32[km - 1] = d2f(src[km - 1]); }
     }
 }
 
@@ -99,7 +101,7 @@ host_gather_kernel(const __grid_constant__ HostBatch B, int64_t nrows, int km, i
         const int64_t nw = (int64_t)gridDim.x * XF_WARPS;
         for (int64_t r = (int64_t)blockIdx.x * XF_WARPS + (threadIdx.x >> 5); r < nrows; r += nw) {
             const double* src = fd.rows ? fd.rows[r] : fd.base + r * km;
-            gather_row(src, fd.dev + r * kp, km, lane);
+            gather_row(src, fd.dev + r * kp, fd.dev32 ? fd.dev32 + r * kp : nullptr, km, lane);
         }
         return;
     }
@@ -121,13 +123,21 @@ host_gather_kernel(const __grid_constant__ HostBatch B, int64_t nrows, int km, i
             const uint32_t w = w0 + q * stride;
             if (w >= nwords) continue;
             const uint32_t e = a + 2 * w;
-            fd.dev[pos.dev(e)] = v[q].x;
-            fd.dev[pos.dev(e + 1)] = v[q].y;
+            const int64_t d0 = pos.dev(e), d1 = pos.dev(e + 1);
+            fd.dev[d0] = v[q].x;
+            fd.dev[d1] = v[q].y;
+            if (fd.dev32) { fd.dev32[d0] = d2f(v[q].x); fd.dev32[d1] = d2f(v[q].y); }
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        if (a) fd.dev[pos.dev(0)] = fd.base[0];
-        if ((n - a) & 1u) fd.dev[pos.dev(n - 1)] = fd.base[n - 1];
+        if (a) {
+            fd.dev[pos.dev(0)] = fd.base[0];
+            if (fd.dev32) fd.dev32[pos.dev(0)] = d2f(fd.base[0]);
+        }
+        if ((n - a) & 1u) {
+            fd.dev[pos.dev(n - 1)] = fd.base[n - 1];
+            if (fd.dev32) fd.dev32[pos.dev(n - 1)] = d2f(fd.base[n - 1]);
+        }
     }
 }
 
