@@ -1,0 +1,62 @@
+"""The N > 1 path of bench.py on CPU: replicas with no data-path collective, only the timing barrier and the
+max over ranks of the elapsed time (gloo, world size 2), and the reference arm under torchrun, where rank 0
+alone runs and prints its line."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, out):
+    os.environ.update({"RANK": str(rank), "WORLD_SIZE": str(world), "LOCAL_RANK": str(rank),
+                       "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    sys.path.insert(0, ROOT)
+    import bench
+    r, w, _ = bench.dist()
+    bench.barrier(w)
+    m = bench.reduce_max(w, 1.5 * r + 0.25)
+    out.put((r, w, m))
+    import torch.distributed as td
+    td.destroy_process_group()
+
+
+def test_barrier_and_max_over_ranks_gloo():
+    """Each rank's elapsed time differs; every rank gets the maximum (the value bench.py reports)."""
+    mp = pytest.importorskip("torch.multiprocessing")
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = free_port()
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = [q.get(timeout=120) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert sorted(g[0] for g in got) == [0, 1]
+    assert all(g[1] == 2 and g[2] == 1.75 for g in got)
+
+
+def test_reference_arm_under_torchrun():
+    """`bench.py --impl reference` launched like the driver's N = 2 run: one JSON line, from rank 0."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(free_port()), "bench.py", "--impl", "reference",
+           "--gpus", "2", "--shape", "9,13,17", "--steps", "2", "--warmup", "3"]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
