@@ -8,8 +8,8 @@ import numpy as np
 from . import fields as F
 
 OK = 0
-E_INVALID, E_UNSUPPORTED, E_CUDA, E_TIMEOUT, E_NONFINITE_INPUT, E_NOMEM, E_UNBOUND = (
-    -1, -2, -3, -4, -5, -6, -7)
+E_INVALID, E_UNSUPPORTED, E_CUDA, E_TIMEOUT, E_NONFINITE_INPUT, E_NOMEM, E_UNBOUND, E_TOO_LARGE = (
+    -1, -2, -3, -4, -5, -6, -7, -8)
 FP64, MIXED = 0, 1
 
 K_RK_STAGE, K_LEVEL_MEAN, K_METRIC_SCAN, K_PRESS_SOURCE, K_PRESS_SWEEP, K_PRESS_BOUNDARY, \

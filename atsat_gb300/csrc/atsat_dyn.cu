@@ -132,12 +132,16 @@ struct atsat_dyn {
     ColGeoF* geof = nullptr;
     PrepGeo* pgeo = nullptr;
     MixedConstF kf{};
-    // the TMA-tiled stage kernel: tensor maps over slab32; variant 1 = tiled, 0 = direct
+    // the TMA-tiled stage kernels: tensor maps over slab32; the stage variant (ATSAT_DYN_STAGE_*)
     TileMaps maps{};
     bool tile_ok = false;
     int variant = 1;
     unsigned int* dev_err = nullptr;     // device status word of the bounded waits
     int timeouts = 0;
+    // the bounded waits' limit in SM clocks, and the test hook that leaves the last items of each tiled
+    // block's stream unissued (atsat_dyn_set_wait_test)
+    long long wait_limit = TILE_WAIT_LIMIT;
+    int test_withhold = 0;
     PoissonSolver* poisson = nullptr;    // standalone pressure-equation solver, built on first use
     // a captured CUDA graph of `graph_iters` resident iterations (atsat_dyn_graph_capture)
     cudaGraphExec_t graph = nullptr;
@@ -933,6 +937,7 @@ int32_t arr_index(const atsat_dyn* h, const float* p) { return (int32_t)((p - h-
 TilePlan make_plan(atsat_dyn* h, const MixedIO& io) {
     TilePlan pl{};
     pl.err = h->dev_err;
+    pl.wait_limit = h->wait_limit;
     pl.arr_lo = arr_index(h, io.wlo);
     int n = 0;
     for (int q = 0; q < NPROG; q++) {
@@ -969,6 +974,8 @@ int launches_per_stage(const atsat_dyn* h) { return h->variant >= ATSAT_DYN_STAG
 TracerPlan make_plan_tracer(atsat_dyn* h, const MixedIO& io, int mode) {
     TracerPlan pl{};
     pl.err = h->dev_err;
+    pl.wait_limit = h->wait_limit;
+    pl.withhold = h->test_withhold;
     int n = 0;
     auto add = [&](const float* p, int kind) {
         if (n < TRACER_MAX_ITEMS) { pl.arr[n] = arr_index(h, p); pl.kind[n] = (unsigned char)kind; }
@@ -1011,6 +1018,8 @@ TracerPlan make_plan_tracer(atsat_dyn* h, const MixedIO& io, int mode) {
 TracerPlan make_plan_mom(atsat_dyn* h, const MixedIO& io) {
     TracerPlan pl{};
     pl.err = h->dev_err;
+    pl.wait_limit = h->wait_limit;
+    pl.withhold = h->test_withhold;
     int n = 0;
     auto add = [&](const float* p, int kind) {
         if (n < TRACER_MAX_ITEMS) { pl.arr[n] = arr_index(h, p); pl.kind[n] = (unsigned char)kind; }
@@ -1689,7 +1698,9 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
         h->pgeo = reinterpret_cast<PrepGeo*>(r);
         if ((e = upload_geof(h)) != cudaSuccess) return cuda_fail(e, "FP32 geometry upload");
         h->tile_ok = make_tile_maps(h);
-        if (!h->tile_ok) h->variant = ATSAT_DYN_STAGE_DIRECT;
+        // the default stage kernel: the fastest one measured at every grid tried, where it applies
+        h->variant = variant_available(h, ATSAT_DYN_STAGE_TILED2) ? ATSAT_DYN_STAGE_TILED2
+                   : (h->tile_ok ? ATSAT_DYN_STAGE_TILED : ATSAT_DYN_STAGE_DIRECT);
     }
     // small host tables
     std::vector<double> sin_j(K.jm), rm_tab(K.im), cor_j(K.jm);
@@ -2401,6 +2412,15 @@ int atsat_dyn_set_async(atsat_dyn_t h, int32_t enable) {
         return rc;
     }
     h->async = enable != 0;
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_set_wait_test(atsat_dyn_t h, int64_t clocks, int32_t withhold) {
+    if (!h) return ATSAT_DYN_E_INVALID;
+    if (clocks < 0 || clocks > TILE_WAIT_LIMIT || withhold < 0 || withhold > 8)
+        return fail(h, ATSAT_DYN_E_INVALID, "set_wait_test: clocks in [0, 2^31] (0: default), withhold in [0, 8]");
+    h->wait_limit = clocks ? clocks : TILE_WAIT_LIMIT;
+    h->test_withhold = withhold;
     return ATSAT_DYN_OK;
 }
 

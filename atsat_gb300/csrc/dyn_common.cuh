@@ -278,6 +278,7 @@ struct MixedPrep {
 // The seam box fetches the periodic partner column (k = km-2 for k = 0, k = 0 for k = km-2) when the
 // main box does not hold it.
 constexpr int TILE_K = 32, TILE_J = 8, TILE_I = 2;
+constexpr long long TILE_WAIT_LIMIT = 1LL << 31;   // SM clocks (about a second) before a bounded wait gives up
 constexpr int TILE_BX = TILE_K + 8, TILE_BY = TILE_J + 2, TILE_BZ = TILE_I + 2;
 constexpr int TILE_SEAM_X = 4;
 constexpr int TILE_MAX_ITEMS = 2 * NPROG + 1;
@@ -290,6 +291,7 @@ struct TilePlan {
     int arr_dl[NPROG];
     int arr_lo;
     unsigned int* err;             // device status word: bit 0 producer wait, bit 1 consumer wait, bit 2 plan
+    long long wait_limit;          // SM clocks before a bounded wait gives up
 };
 
 enum StageMode {
@@ -332,6 +334,8 @@ struct TracerPlan {
     int arr[TRACER_MAX_ITEMS];
     unsigned char kind[TRACER_MAX_ITEMS];
     unsigned int* err;
+    long long wait_limit;          // SM clocks before a consumer's or the producer's slot wait gives up
+    int withhold;                  // test hook: the producer leaves the last `withhold` items unissued
 };
 cudaError_t launch_rk_tile(const TileMaps& maps, const MixedConstF& kf, const MixedIO& io, const StageParams& sp,
                            const TilePlan& plan, int mode, cudaStream_t s);

@@ -113,6 +113,21 @@ extern "C" int atsat_dyn_buoyancy_ref_level_noalloc(const double* t, const doubl
                 im, jm, ATSAT_DYN_NOALLOC_MAX_IM, ATSAT_DYN_NOALLOC_MAX_JM);
         return ATSAT_DYN_E_TOO_LARGE;
     }
+    // an error left pending by earlier, unrelated work belongs to its owner: leave it there and stop
+    if (cudaPeekAtLastError() != cudaSuccess) return ATSAT_DYN_E_CUDA;
+    // the kernels run on the current device, so the caller's arrays must live there
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return ATSAT_DYN_E_CUDA;
+    const void* on_device[3] = {t, p_stat, buoy_out};
+    for (const void* q : on_device) {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+            cudaGetLastError();   // the lookup's own error, not a pending one (checked above)
+            return ATSAT_DYN_E_INVALID;
+        }
+        const bool here = (a.type == cudaMemoryTypeDevice && a.device == dev) || a.type == cudaMemoryTypeManaged;
+        if (!here) return ATSAT_DYN_E_INVALID;
+    }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     double* scratch = nullptr;
     if (scratch_address(&scratch) != cudaSuccess) return ATSAT_DYN_E_CUDA;
@@ -122,6 +137,7 @@ extern "C" int atsat_dyn_buoyancy_ref_level_noalloc(const double* t, const doubl
         return ATSAT_DYN_E_CUDA;
     na_partial_kernel<<<dim3(im, NA_CHUNKS), NA_THREADS, 0, s>>>(t, p_stat, pitch, jm, km, g, r_mix * R_mix, t_ref,
                                                                  scratch);
+    if (cudaGetLastError() != cudaSuccess) return ATSAT_DYN_E_CUDA;
     na_final_kernel<<<(im + 63) / 64, 64, 0, s>>>(scratch, im, buoy_out);
     if (cudaGetLastError() != cudaSuccess) return ATSAT_DYN_E_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return ATSAT_DYN_E_CUDA;

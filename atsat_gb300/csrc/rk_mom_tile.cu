@@ -41,10 +41,10 @@ constexpr size_t SMEM_BYTES = (size_t)NHS * HSLOT_F * 4 + (size_t)NPS * PSLOT_F 
 static_assert((HSLOT_F * 4) % 128 == 0 && (PSLOT_F * 4) % 128 == 0 && (BOX_F * 4) % 128 == 0, "slot alignment");
 
 template <int NS>
-__device__ __forceinline__ bool wait_items(const Ring& rg, int n0, int n1) {
+__device__ __forceinline__ bool wait_items(const Ring& rg, int n0, int n1, long long limit) {
     bool ok = true;
 #pragma unroll
-    for (int n = n0; n < n1; n++) ok = ok && mbar_wait(rg.full(n % NS), (uint32_t)((n / NS) & 1));
+    for (int n = n0; n < n1; n++) ok = ok && mbar_wait(rg.full(n % NS), (uint32_t)((n / NS) & 1), limit);
     return !__any_sync(0xffffffffu, !ok);
 }
 
@@ -101,10 +101,14 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
         if (lane == 0) {
             int nh = 0, np = 0;
             bool ok = true;
-            for (int n = 0; n < plan.n_items && ok; n++) {
+            const int n_issue = plan.n_items - plan.withhold;
+            for (int n = 0; n < n_issue && ok; n++) {
                 if (plan.kind[n] == 0) {
                     const int s = nh % NHS;
-                    if (nh >= NHS && !mbar_wait(rh.empty(s), (uint32_t)(((nh / NHS) - 1) & 1))) { ok = false; break; }
+                    if (nh >= NHS && !mbar_wait(rh.empty(s), (uint32_t)(((nh / NHS) - 1) & 1), plan.wait_limit)) {
+                        ok = false;
+                        break;
+                    }
                     const uint32_t dst = smem_u32(hs + s * HSLOT_F);
                     mbar_expect_tx(rh.full(s), BOX_BYTES + (seam ? SEAM_BYTES : 0u));
                     tma_load_4d(dst, &map_main, k0 - 4, j0 - 1, i0 - 1, plan.arr[n], rh.full(s));
@@ -112,7 +116,10 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
                     nh++;
                 } else {
                     const int s = np % NPS;
-                    if (np >= NPS && !mbar_wait(rp.empty(s), (uint32_t)(((np / NPS) - 1) & 1))) { ok = false; break; }
+                    if (np >= NPS && !mbar_wait(rp.empty(s), (uint32_t)(((np / NPS) - 1) & 1), plan.wait_limit)) {
+                        ok = false;
+                        break;
+                    }
                     mbar_expect_tx(rp.full(s), PT_BYTES);
                     tma_load_4d(smem_u32(ps + s * PSLOT_F), &map_pt, k0, j0, i0, plan.arr[n], rp.full(s));
                     np++;
@@ -162,7 +169,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
 
     // nue -> eddy viscosity terms
     float nue_t[TI], nue_t_s[TI];
-    if (!wait_items<NPS>(rp, P_NUE, P_NUE + 1)) { fail(); return; }
+    if (!wait_items<NPS>(rp, P_NUE, P_NUE + 1, plan.wait_limit)) { fail(); return; }
 #pragma unroll
     for (int ii = 0; ii < TI; ii++) {
         const float nue_c = P(P_NUE)[pidx[ii]];
@@ -177,7 +184,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
     float un[TI], du_s[TI], vn[TI], dv_s[TI], wn[TI], dw_s[TI], wyn[TI];
     D6f du[TI], dv[TI];
     // u
-    if (!wait_items<NHS>(rh, hU, hV)) { fail(); return; }
+    if (!wait_items<NHS>(rh, hU, hV, plan.wait_limit)) { fail(); return; }
 #pragma unroll
     for (int ii = 0; ii < TI; ii++) {
         float a[6];
@@ -194,7 +201,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
     }
     release<NHS>(rh, hU, hV);
     // v
-    if (!wait_items<NHS>(rh, hV, hW)) { fail(); return; }
+    if (!wait_items<NHS>(rh, hV, hW, plan.wait_limit)) { fail(); return; }
 #pragma unroll
     for (int ii = 0; ii < TI; ii++) {
         float a[6];
@@ -212,7 +219,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
     release<NHS>(rh, hV, hW);
     // w (y_n, low word, increment) and the momentum equations' transport and viscous parts
     float adv_u[TI], adv_v[TI], adv_w[TI], dif_u[TI], dif_v[TI], dif_w[TI];
-    if (!wait_items<NHS>(rh, hW, hT)) { fail(); return; }
+    if (!wait_items<NHS>(rh, hW, hT, plan.wait_limit)) { fail(); return; }
 #pragma unroll
     for (int ii = 0; ii < TI; ii++) {
         float a[6], b[6];
@@ -253,7 +260,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
     float dpr[TI], dpth[TI], dpph[TI];
     // rhs_u: frozen GU, DPR, the buoyancy anomaly BAN, BPS; needs the stage temperature -> t's centre values
     // come with t's halo items below, so u waits for them
-    if (!wait_items<NHS>(rh, hT, hEnd)) { fail(); return; }
+    if (!wait_items<NHS>(rh, hT, hEnd, plan.wait_limit)) { fail(); return; }
     float tn[TI], dt_s[TI];
     D6f dtd[TI];
 #pragma unroll
@@ -272,7 +279,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
     }
     release<NHS>(rh, hT, hEnd);
 
-    if (!wait_items<NPS>(rp, P_DPR, P_DPTH)) { fail(); return; }
+    if (!wait_items<NPS>(rp, P_DPR, P_DPTH, plan.wait_limit)) { fail(); return; }
 #pragma unroll
     for (int ii = 0; ii < TI; ii++) {
         if (!valid[ii]) continue;
@@ -297,7 +304,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
     }
     release<NPS>(rp, P_DPR, P_DPTH);
 
-    if (!wait_items<NPS>(rp, P_DPTH, P_DPPH)) { fail(); return; }
+    if (!wait_items<NPS>(rp, P_DPTH, P_DPPH, plan.wait_limit)) { fail(); return; }
 #pragma unroll
     for (int ii = 0; ii < TI; ii++) {
         if (!valid[ii]) continue;
@@ -314,7 +321,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
     }
     release<NPS>(rp, P_DPTH, P_DPPH);
 
-    if (!wait_items<NPS>(rp, P_DPPH, P_DPS)) { fail(); return; }
+    if (!wait_items<NPS>(rp, P_DPPH, P_DPS, plan.wait_limit)) { fail(); return; }
 #pragma unroll
     for (int ii = 0; ii < TI; ii++) {
         if (!valid[ii]) continue;
@@ -332,7 +339,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
     release<NPS>(rp, P_DPPH, P_DPS);
 
     // rhs_t (RHS_Sat_Turb.cpp:460-560)
-    if (!wait_items<NPS>(rp, P_DPS, N_PT)) { fail(); return; }
+    if (!wait_items<NPS>(rp, P_DPS, N_PT, plan.wait_limit)) { fail(); return; }
 #pragma unroll
     for (int ii = 0; ii < TI; ii++) {
         if (!valid[ii]) continue;

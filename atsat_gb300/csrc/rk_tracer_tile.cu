@@ -67,10 +67,10 @@ template <bool HAS_DL>
 __host__ __device__ constexpr int h0(int q) { return (q - ATSAT_F_H2O) * (HAS_DL ? 2 : 1); }
 
 template <int NS>
-__device__ __forceinline__ bool wait_items(const Ring& rg, int n0, int n1) {
+__device__ __forceinline__ bool wait_items(const Ring& rg, int n0, int n1, long long limit) {
     bool ok = true;
 #pragma unroll
-    for (int n = n0; n < n1; n++) ok = ok && mbar_wait(rg.full(n % NS), (uint32_t)((n / NS) & 1));
+    for (int n = n0; n < n1; n++) ok = ok && mbar_wait(rg.full(n % NS), (uint32_t)((n / NS) & 1), limit);
     return !__any_sync(0xffffffffu, !ok);
 }
 
@@ -125,10 +125,14 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
         if (lane == 0) {
             int nh = 0, np = 0;
             bool ok = true;
-            for (int n = 0; n < plan.n_items && ok; n++) {
+            const int n_issue = plan.n_items - plan.withhold;
+            for (int n = 0; n < n_issue && ok; n++) {
                 if (plan.kind[n] == 0) {
                     const int s = nh % NHS;
-                    if (nh >= NHS && !mbar_wait(rh.empty(s), (uint32_t)(((nh / NHS) - 1) & 1))) { ok = false; break; }
+                    if (nh >= NHS && !mbar_wait(rh.empty(s), (uint32_t)(((nh / NHS) - 1) & 1), plan.wait_limit)) {
+                        ok = false;
+                        break;
+                    }
                     const uint32_t dst = smem_u32(hs + s * HSLOT_F);
                     mbar_expect_tx(rh.full(s), BOX_BYTES + (seam ? SEAM_BYTES : 0u));
                     tma_load_4d(dst, &map_main, k0 - 4, j0 - 1, i0 - 1, plan.arr[n], rh.full(s));
@@ -136,7 +140,10 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
                     nh++;
                 } else {
                     const int s = np % NPS;
-                    if (np >= NPS && !mbar_wait(rp.empty(s), (uint32_t)(((np / NPS) - 1) & 1))) { ok = false; break; }
+                    if (np >= NPS && !mbar_wait(rp.empty(s), (uint32_t)(((np / NPS) - 1) & 1), plan.wait_limit)) {
+                        ok = false;
+                        break;
+                    }
                     mbar_expect_tx(rp.full(s), PT_BYTES);
                     tma_load_4d(smem_u32(ps + s * PSLOT_F), &map_pt, k0, j0, i0, plan.arr[n], rp.full(s));
                     np++;
@@ -200,7 +207,7 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
         constexpr int DL = HAS_DL ? 1 : 0;
         constexpr int nU = 0, nV = 1 + DL, nW = 2 + 2 * DL, nN = 4 + 3 * DL;
         // u
-        if (!wait_items<NPS>(rp, nU, nV)) { fail(); return; }
+        if (!wait_items<NPS>(rp, nU, nV, plan.wait_limit)) { fail(); return; }
 #pragma unroll
         for (int ii = 0; ii < TI; ii++) {
             const int x = pidx[ii];
@@ -210,7 +217,7 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
         }
         release<NPS>(rp, nU, nV);
         // v
-        if (!wait_items<NPS>(rp, nV, nW)) { fail(); return; }
+        if (!wait_items<NPS>(rp, nV, nW, plan.wait_limit)) { fail(); return; }
 #pragma unroll
         for (int ii = 0; ii < TI; ii++) {
             const int x = pidx[ii];
@@ -221,7 +228,7 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
         }
         release<NPS>(rp, nV, nW);
         // w = (y_n + low word) + increment
-        if (!wait_items<NPS>(rp, nW, nN)) { fail(); return; }
+        if (!wait_items<NPS>(rp, nW, nN, plan.wait_limit)) { fail(); return; }
 #pragma unroll
         for (int ii = 0; ii < TI; ii++) {
             const int x = pidx[ii];
@@ -232,7 +239,7 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
         }
         release<NPS>(rp, nW, nN);
         // nue
-        if (!wait_items<NPS>(rp, nN, nN + 1)) { fail(); return; }
+        if (!wait_items<NPS>(rp, nN, nN + 1, plan.wait_limit)) { fail(); return; }
 #pragma unroll
         for (int ii = 0; ii < TI; ii++) {
             const float nue_c = ps[(nN % NPS) * PSLOT_F + pidx[ii]];
@@ -250,7 +257,11 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
     for (int q = ATSAT_F_H2O; q <= ATSAT_F_DIS; q++) {
         if (q > q_last) break;
         const int hb = h0<HAS_DL>(q), pb = pt0<MODE, HAS_DL>(q), npq = n_pt<MODE>(q);
-        if (!wait_items<NHS>(rh, hb, hb + (HAS_DL ? 2 : 1)) || !wait_items<NPS>(rp, pb, pb + npq)) { fail(); return; }
+        if (!wait_items<NHS>(rh, hb, hb + (HAS_DL ? 2 : 1), plan.wait_limit) ||
+            !wait_items<NPS>(rp, pb, pb + npq, plan.wait_limit)) {
+            fail();
+            return;
+        }
         const float* Y = hs + (hb % NHS) * HSLOT_F;
         const float* D = hs + ((hb + 1) % NHS) * HSLOT_F;
         const float* P0 = ps + (pb % NPS) * PSLOT_F;

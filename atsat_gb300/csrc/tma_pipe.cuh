@@ -16,7 +16,7 @@
 namespace atsat {
 namespace tma {
 
-constexpr long long WAIT_LIMIT = 1LL << 31;   // SM clocks, about a second
+constexpr long long WAIT_LIMIT = TILE_WAIT_LIMIT;   // SM clocks, about a second
 
 enum : unsigned int { ERR_PRODUCER = 1u, ERR_CONSUMER = 2u, ERR_PLAN = 4u, ERR_ALIGN = 8u };
 
@@ -42,13 +42,13 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// wait for the phase of parity `parity` to complete; false after WAIT_LIMIT clocks
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// wait for the phase of parity `parity` to complete; false after `limit` clocks
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit = WAIT_LIMIT) {
     if (mbar_try(bar, parity)) return true;
     const long long t0 = clock64();
     do {
         if (mbar_try(bar, parity)) return true;
-    } while (clock64() - t0 < WAIT_LIMIT);
+    } while (clock64() - t0 < limit);
     return false;
 }
 __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, int w,
@@ -72,7 +72,7 @@ template <int NSLOT>
 __device__ __forceinline__ bool acquire(const Ring& rg, int n0, int n1, const TilePlan& plan, const int* expect) {
     bool ok = true;
 #pragma unroll
-    for (int n = n0; n < n1; n++) ok = ok && mbar_wait(rg.full(n % NSLOT), (uint32_t)((n / NSLOT) & 1));
+    for (int n = n0; n < n1; n++) ok = ok && mbar_wait(rg.full(n % NSLOT), (uint32_t)((n / NSLOT) & 1), plan.wait_limit);
     if (threadIdx.x == 0) {
         bool same = true;
 #pragma unroll
@@ -92,7 +92,8 @@ __device__ __forceinline__ void release(const Ring& rg, int n0, int n1) {
 }
 
 // Producer: stream the plan's items into the ring (main halo box plus, when `seam`, the seam box at xs),
-// then wait (bounded) for the last copy of every slot so that none lands after the block is gone.
+// then wait (bounded, always with the full WAIT_LIMIT: a copy in flight lands by itself) for the last copy
+// of every slot so that none lands after the block is gone.
 template <int NSLOT>
 __device__ __forceinline__ void produce(const Ring& rg, float* smem, int slot_f, uint32_t box_bytes,
                                         uint32_t seam_bytes, const CUtensorMap* map_main, const CUtensorMap* map_seam,
@@ -102,7 +103,10 @@ __device__ __forceinline__ void produce(const Ring& rg, float* smem, int slot_f,
     bool ok = true;
     for (; n < plan.n_items; n++) {
         const int s = n % NSLOT;
-        if (n >= NSLOT && !mbar_wait(rg.empty(s), (uint32_t)(((n / NSLOT) - 1) & 1))) { ok = false; break; }
+        if (n >= NSLOT && !mbar_wait(rg.empty(s), (uint32_t)(((n / NSLOT) - 1) & 1), plan.wait_limit)) {
+            ok = false;
+            break;
+        }
         const uint32_t dst = smem_u32(smem + s * slot_f);
         mbar_expect_tx(rg.full(s), bytes);
         tma_load_4d(dst, map_main, x, y, z, plan.item[n], rg.full(s));

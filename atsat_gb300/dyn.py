@@ -82,6 +82,7 @@ def lib():
         L.atsat_dyn_host_free.argtypes = [C.c_void_p]
         L.atsat_dyn_host_free.restype = None
         L.atsat_dyn_set_write_all_rhs.argtypes = [H, C.c_int32]
+        L.atsat_dyn_set_wait_test.argtypes = [H, C.c_int64, C.c_int32]
         L.atsat_dyn_set_stage_variant.argtypes = [H, C.c_int32]
         L.atsat_dyn_get_stage_variant.argtypes = [H, C.POINTER(C.c_int32)]
         L.atsat_dyn_autotune.argtypes = [H, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
@@ -412,6 +413,17 @@ class Dycore:
         d = abi.Diag()
         self._ck(lib().atsat_dyn_status(self.h, C.byref(d)), "status")
         return int(d.launches)
+
+    def timeouts(self) -> int:
+        """How many synchronisations found a bounded device wait that gave up."""
+        d = abi.Diag()
+        self._ck(lib().atsat_dyn_status(self.h, C.byref(d)), "status")
+        return int(d.timeout)
+
+    def set_wait_test(self, clocks: int = 0, withhold: int = 0):
+        """Failure-detection test hook: the tiled kernels' waits give up after `clocks` SM clocks (0: the
+        default 2^31), and each block's producer leaves its last `withhold` items unissued."""
+        self._ck(lib().atsat_dyn_set_wait_test(self.h, int(clocks), int(withhold)), "set_wait_test")
 
     def count_nonfinite(self, fid: int) -> int:
         n = C.c_int64()

@@ -352,6 +352,14 @@ int atsat_dyn_restart_is_clean(atsat_dyn_t h, int32_t* clean);
 /* ---- diagnostics and timing ---- */
 int atsat_dyn_sync(atsat_dyn_t h);
 int atsat_dyn_status(atsat_dyn_t h, atsat_dyn_diag* out);
+/* Failure-detection test hook (no reference counterpart; the reference has no device waits). The
+ * TMA-tiled stage kernels' bounded waits give up after `clocks` SM clocks instead of 2^31 (0: back to
+ * 2^31); with `withhold` > 0 each block's producer leaves the last `withhold` items of its stream unissued,
+ * so that the consumers' waits for them run out. A wait that gives up makes the block set a bit of the
+ * device status word and return (its producer first waits, always up to 2^31 clocks, for its own copies
+ * in flight); the next synchronising call returns ATSAT_DYN_E_TIMEOUT and atsat_dyn_status counts it. The
+ * model state of such a step is undefined: re-upload it. clocks in [0, 2^31], withhold in [0, 8]. */
+int atsat_dyn_set_wait_test(atsat_dyn_t h, int64_t clocks, int32_t withhold);
 /* Count non-finite cells of a field on the device (the reference's NaN census, FileIO_Sat.cpp:418). */
 int atsat_dyn_count_nonfinite(atsat_dyn_t h, int32_t field, int64_t* count);
 /* Per-kernel CUDA-event timing on the handle's stream: enable, reset, and read the launch count
@@ -481,10 +489,13 @@ void  atsat_dyn_host_free(void* p);
  *   stream     the CUDA stream to run on (NULL: the default stream); the call waits for it before
  *              returning
  * Limits: im <= ATSAT_DYN_NOALLOC_MAX_IM and jm <= ATSAT_DYN_NOALLOC_MAX_JM, else ATSAT_DYN_E_TOO_LARGE.
- * The first call on a device looks up the scratch array's device address there (once per device), so
- * make that first call before capturing any stream into a CUDA graph. All calls share the one scratch
- * array: calls whose GPU work overlaps (different streams or host threads at once) race on it and must
- * be serialised by the caller. Each call rewrites the scratch it reads, so nothing carries over from the
+ * The call runs on the current device: t, p_stat and buoy_out must be device memory of that device (or
+ * managed memory), else ATSAT_DYN_E_INVALID. It returns ATSAT_DYN_E_CUDA without launching anything when a CUDA error from
+ * earlier work is already pending (and leaves that error for its owner).
+ * The first call on a device looks up the scratch array's device address there (once per device); make
+ * that first call before any stream capture begins. All calls on a device share the one scratch array:
+ * calls whose GPU work overlaps (different streams or host threads at once) race on it and must be
+ * serialised by the caller. Each call rewrites the scratch it reads, so nothing carries over from the
  * previous call. */
 #define ATSAT_DYN_NOALLOC_MAX_IM 512
 #define ATSAT_DYN_NOALLOC_MAX_JM 8192

@@ -7,7 +7,8 @@ reference, so no code generation runs. -O2 without -march, so that on x86-64 no 
 happens and the restatement in oracle/atsat_oracle.c (built with -ffp-contract=off) can be compared
 with it bit for bit.
 
-Usage: python oracle/build_ref.py [--ref /root/reference] [--jobs N]
+Usage: python oracle/build_ref.py [--ref PATH] [--jobs N]
+The reference tree is PATH, else $ATSAT_REFERENCE, else /root/reference.
 Produces oracle/_ref/ref_harness. Exits 0 without doing anything when the reference tree is absent.
 """
 from __future__ import annotations
@@ -20,6 +21,11 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
+
+
+def default_ref() -> str:
+    """The reference tree: $ATSAT_REFERENCE when set, else where this container mounts it."""
+    return os.environ.get("ATSAT_REFERENCE") or "/root/reference"
 
 # The translation units of libatsat (the reference Makefile's LIB_OBJ, ATSAT_OBJ, XML_OBJ) and the
 # command-line stream stub, which the harness needs instead of cli/sat.cpp's main().
@@ -62,7 +68,7 @@ def build(ref: str, jobs: int) -> str:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=default_ref())
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
     a = ap.parse_args()
     exe = build(a.ref, a.jobs)

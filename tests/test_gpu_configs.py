@@ -1,0 +1,155 @@
+"""The larger benchmark configurations against the FP64 oracle.
+
+The reference fixes its grid at compile time (planet/cSaturnModel.h:710-711), so at every grid other
+than 41 x 181 x 361 the oracle is the runtime-grid restatement in oracle/atsat_oracle.c (pinned bit for
+bit to the reference at 41 x 181 x 361). These cases are the configurations the throughput figures are
+quoted on:
+
+* the 81 x 361 x 721 shell (about 21 M cells; 6.25 km levels, 0.5 degrees): the FP64 drop-in after one
+  call sequence (density, pressure, RK4) within 1e-10, and the mixed path after 10 iterations within
+  1e-6 on u, v, w and p_dyn;
+* the ensemble's large members, 61 x 271 x 541, mixed, 10 iterations;
+* an ensemble of members of three sizes (one at 41 x 181 x 361) replayed concurrently as CUDA graphs,
+  every member against its own oracle run;
+* the 100-iteration drift of the mixed path at 41 x 181 x 361 with every source term exercised, checked
+  every 10 iterations.
+
+Every case prints each prognostic field's max and RMS relative difference. Host memory: two states of
+the largest grid (13 GB each) plus the oracle's stage buffers.
+"""
+import gc
+
+import numpy as np
+import pytest
+
+from atsat_gb300 import fields as F
+from oracle import oracle
+
+from helpers import TOL_FP64, case
+
+pytestmark = pytest.mark.gpu
+
+TOL_MIXED = 1e-6
+CRITERION = [F.U, F.V, F.W, F.P_DYN]
+
+
+def drift(got, ref, fids):
+    out = {}
+    for fid in fids:
+        a, b = got[fid], ref[fid]
+        m = float(np.max(np.abs(b))) or 1.0
+        d = np.abs(a - b)
+        out[F.NAMES[fid]] = (float(np.max(d)) / m, float(np.sqrt(np.mean(d * d))) / m)
+    return out
+
+
+def report(title, rep):
+    print(f"\n{title}: max / rms relative difference")
+    for k, (mx, rms) in rep.items():
+        print(f"  {k:12s} {mx:.3e} {rms:.3e}")
+
+
+def mixed_vs_oracle(shape, seed, steps):
+    from atsat_gb300 import dyn
+    g, P, st = case(shape, seed=seed, exercise=True)
+    oracle.lib()
+    ref = st.copy()
+    oracle.steps(ref, P, steps)
+    with dyn.Dycore(g, dict(P, precision=1)) as d:
+        d.load_state(st)
+        d.iterate(1, steps)
+        d.download(F.PROG + [F.P_DYN])
+    rep = drift(st.arrays, ref.arrays, F.PROG + [F.P_DYN])
+    del st, ref
+    gc.collect()
+    return rep
+
+
+def test_fp64_one_call_sequence_81x361x721():
+    """FP64 drop-in at 81 x 361 x 721: mixture density, the pressure call and one RK4 step, every prognostic
+    field, p_dyn, rhs_u/v/w and aux_u/v/w within the FP64 bar."""
+    from atsat_gb300 import dyn
+    g, P, st = case((81, 361, 721), seed=5, exercise=True)
+    oracle.lib()
+    ref = st.copy()
+    oracle.mixture_density(ref, P)
+    oracle.pressure(ref, P)
+    oracle.rk4_step(ref, P)
+    fids = F.PROG + [F.P_DYN, F.RHS_U, F.RHS_V, F.RHS_W] + F.AUX_FIELDS
+    with dyn.Dycore(g, P) as d:
+        d.load_state(st)
+        d.computeMixtureDensity()
+        d.PressureSolver_run()
+        d.RungeKuttaSat()
+        d.download(fids)
+    rep = drift(st.arrays, ref.arrays, fids)
+    report("FP64, 81x361x721, one call sequence", rep)
+    bad = {k: v[0] for k, v in rep.items() if not v[0] <= TOL_FP64}
+    assert not bad, bad
+
+
+def test_mixed_ten_iterations_81x361x721():
+    rep = mixed_vs_oracle((81, 361, 721), seed=41, steps=10)
+    report("mixed, 81x361x721, 10 iterations", rep)
+    bad = {F.NAMES[f]: rep[F.NAMES[f]][0] for f in CRITERION if not rep[F.NAMES[f]][0] <= TOL_MIXED}
+    assert not bad, bad
+
+
+def test_mixed_ten_iterations_61x271x541():
+    rep = mixed_vs_oracle((61, 271, 541), seed=43, steps=10)
+    report("mixed, 61x271x541, 10 iterations", rep)
+    bad = {F.NAMES[f]: rep[F.NAMES[f]][0] for f in CRITERION if not rep[F.NAMES[f]][0] <= TOL_MIXED}
+    assert not bad, bad
+
+
+def test_ensemble_members_match_the_oracle():
+    """Members of three sizes (9 x 13 x 17, two at 21 x 91 x 181, one at 41 x 181 x 361), each seeded on its
+    own with noise amplitudes scaled as the ensemble configuration does: two plain resident iterations,
+    then two graph replays of two iterations each, all members concurrently. Each member's state after the
+    six iterations must follow its own oracle run within the mixed bar."""
+    from atsat_gb300 import dyn
+    shapes = [(21, 91, 181), (41, 181, 361), (9, 13, 17), (21, 91, 181)]
+    rng = np.random.default_rng(2024)
+    scales = rng.uniform(0.5, 2.0, len(shapes))
+    oracle.lib()
+    members, states, refs = [], [], []
+    for m, shp in enumerate(shapes):
+        g, P, st = case(shp, seed=80 + m, exercise=True, noise_scale=float(scales[m]))
+        ref = st.copy()
+        oracle.steps(ref, P, 6)
+        refs.append(ref)
+        d = dyn.Dycore(g, dict(P, precision=1))
+        d.load_state(st)
+        d.iterate(1, 2)
+        d.graph_capture(3, 2)
+        members.append(d)
+        states.append(st)
+    try:
+        ms = dyn.ensemble_run(members, reps=2, concurrent=True)
+        assert ms > 0
+        for d in members:
+            d.download(F.PROG + [F.P_DYN])
+    finally:
+        for d in members:
+            d.close()
+    for m, shp in enumerate(shapes):
+        rep = drift(states[m].arrays, refs[m].arrays, F.PROG + [F.P_DYN])
+        report(f"ensemble member {m} {shp}, 6 iterations", rep)
+        bad = {F.NAMES[f]: rep[F.NAMES[f]][0] for f in CRITERION if not rep[F.NAMES[f]][0] <= TOL_MIXED}
+        assert not bad, (shp, bad)
+
+
+def test_hundred_iteration_drift_41x181x361():
+    """100 iterations with every source term exercised: at every 10th the mixed path stays within 1e-6 of
+    the oracle on u, v, w and p_dyn, and the FP64 path within the FP64 bar."""
+    import drift_report
+    rep = drift_report.run((41, 181, 361), steps=100, every=10, seed=2)
+    assert [r["step"] for r in rep["rows"]] == list(range(10, 101, 10))
+    print("\nstep  " + "  ".join(f"{n:>9s}" for n in ("u", "v", "w", "t", "p_dyn", "tke", "h2o")))
+    for row in rep["rows"]:
+        print(f"{row['step']:4d}  " + "  ".join(f"{row['mixed'][n][0]:9.2e}" for n in
+                                                 ("u", "v", "w", "t", "p_dyn", "tke", "h2o")))
+    for row in rep["rows"]:
+        for name in ("u", "v", "w", "p_dyn"):
+            assert row["mixed"][name][0] <= TOL_MIXED, (row["step"], name, row["mixed"][name])
+            assert row["fp64"][name][0] <= TOL_FP64, (row["step"], name, row["fp64"][name])
