@@ -33,6 +33,25 @@ TOL_MIXED = 1e-6
 CRITERION = [F.U, F.V, F.W, F.P_DYN]
 
 
+def host_gb_available() -> float:
+    """MemAvailable of this host in GB (Linux), inf where /proc/meminfo is absent."""
+    try:
+        with open("/proc/meminfo") as fh:
+            for line in fh:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) / 1e6
+    except OSError:
+        pass
+    return float("inf")
+
+
+def need_host_memory(gb: float):
+    """Skip rather than drive the host out of memory: two states and the oracle's buffers must fit."""
+    have = host_gb_available()
+    if have < gb:
+        pytest.skip(f"needs about {gb:.0f} GB of free host memory, {have:.0f} GB available")
+
+
 def drift(got, ref, fids):
     out = {}
     for fid in fids:
@@ -69,6 +88,7 @@ def test_fp64_one_call_sequence_81x361x721():
     """FP64 drop-in at 81 x 361 x 721: mixture density, the pressure call and one RK4 step, every prognostic
     field, p_dyn, rhs_u/v/w and aux_u/v/w within the FP64 bar."""
     from atsat_gb300 import dyn
+    need_host_memory(48)
     g, P, st = case((81, 361, 721), seed=5, exercise=True)
     oracle.lib()
     ref = st.copy()
@@ -89,6 +109,7 @@ def test_fp64_one_call_sequence_81x361x721():
 
 
 def test_mixed_ten_iterations_81x361x721():
+    need_host_memory(48)
     rep = mixed_vs_oracle((81, 361, 721), seed=41, steps=10)
     report("mixed, 81x361x721, 10 iterations", rep)
     bad = {F.NAMES[f]: rep[F.NAMES[f]][0] for f in CRITERION if not rep[F.NAMES[f]][0] <= TOL_MIXED}
@@ -96,6 +117,7 @@ def test_mixed_ten_iterations_81x361x721():
 
 
 def test_mixed_ten_iterations_61x271x541():
+    need_host_memory(24)
     rep = mixed_vs_oracle((61, 271, 541), seed=43, steps=10)
     report("mixed, 61x271x541, 10 iterations", rep)
     bad = {F.NAMES[f]: rep[F.NAMES[f]][0] for f in CRITERION if not rep[F.NAMES[f]][0] <= TOL_MIXED}
