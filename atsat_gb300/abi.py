@@ -80,7 +80,7 @@ POISSON_METHODS = ["sor64", "sor32", "refine_sor", "direct64", "direct32", "refi
 
 class Diag(C.Structure):
     _fields_ = [("launches", C.c_int64), ("nonfinite", C.c_int64), ("timeout", C.c_int32),
-                ("reserved", C.c_int32 * 5)]
+                ("tuned_from_cache", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 # ChemistrySat::ThermalPropertiesSat of the default composition (planet/ChemistrySat.h:475-530),

@@ -12,6 +12,9 @@
 #include <string>
 #include <vector>
 
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <omp.h>
 
 #include <cuda.h>
@@ -142,6 +145,8 @@ struct atsat_dyn {
     // block's stream unissued (atsat_dyn_set_wait_test)
     long long wait_limit = TILE_WAIT_LIMIT;
     int test_withhold = 0;
+    int march_levels = 0;                // radial levels per block of the march kernel (the march depth)
+    bool tuned_from_cache = false;       // the variant and the march depth came from the autotune cache
     PoissonSolver* poisson = nullptr;    // standalone pressure-equation solver, built on first use
     // a captured CUDA graph of `graph_iters` resident iterations (atsat_dyn_graph_capture)
     cudaGraphExec_t graph = nullptr;
@@ -508,8 +513,21 @@ bool make_tile_maps(atsat_dyn* h) {
     const CUresult r6 = enc(reinterpret_cast<CUtensorMap*>(h->maps.pt2), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->slab32,
                             dims, strides, box_pt2, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    // the radial march's planes: one level deep
+    const cuuint32_t box_plane1[4] = {TILE_BX, TILE_BY, 1, 1};
+    const cuuint32_t box_seam1[4] = {TILE_SEAM_X, TILE_J, 1, 1};
+    const cuuint32_t box_pt1[4] = {TILE_K, TILE_J, 1, 1};
+    const CUresult r7 = enc(reinterpret_cast<CUtensorMap*>(h->maps.plane1), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                            h->slab32, dims, strides, box_plane1, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    const CUresult r8 = enc(reinterpret_cast<CUtensorMap*>(h->maps.seam1), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                            h->slab32, dims, strides, box_seam1, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    const CUresult r9 = enc(reinterpret_cast<CUtensorMap*>(h->maps.pt1), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                            h->slab32, dims, strides, box_pt1, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r1 == CUDA_SUCCESS && r2 == CUDA_SUCCESS && r3 == CUDA_SUCCESS && r4 == CUDA_SUCCESS && r5 == CUDA_SUCCESS &&
-           r6 == CUDA_SUCCESS;
+           r6 == CUDA_SUCCESS && r7 == CUDA_SUCCESS && r8 == CUDA_SUCCESS && r9 == CUDA_SUCCESS;
 }
 
 bool valid_field(int f) { return f >= 0 && f < ATSAT_NFIELDS; }
@@ -816,13 +834,28 @@ int do_metric(atsat_dyn* h) {
     return ATSAT_DYN_OK;
 }
 
+// the start of a step: the buoyancy level mean, and the metric pressure where metric_split is on, fused
+// into one pass over the columns where the grid allows
+int do_level_metric(atsat_dyn* h) {
+    if (!h->p.metric_split) return do_level_mean(h);
+    if (h->kc.im > CS_MAX_IM) {
+        const int rc = do_level_mean(h);
+        return rc ? rc : do_metric(h);
+    }
+    Timed t(h, ATSAT_K_LEVEL_MEAN);
+    CK(h, launch_column_scan(h->kc, h->f[ATSAT_F_T], h->f[ATSAT_F_P_STAT], h->f[ATSAT_F_V], h->f[ATSAT_F_W],
+                             h->sin_j, h->rm_tab, h->cor_j, h->has_pbaro ? h->p_baro : nullptr,
+                             h->f[ATSAT_F_P_METRIC], h->partial, h->buoy, h->stream));
+    h->launches += 2;
+    return ATSAT_DYN_OK;
+}
+
 int enqueue_rk4_mixed(atsat_dyn* h, bool resident);
 
 int enqueue_rk4(atsat_dyn* h, bool resident = false) {
     if (h->p.precision == ATSAT_DYN_MIXED) return enqueue_rk4_mixed(h, resident);
     int rc;
-    if ((rc = do_level_mean(h))) return rc;
-    if (h->p.metric_split && (rc = do_metric(h))) return rc;
+    if ((rc = do_level_metric(h))) return rc;
     double* L[NPROG];
     double* S[NPROG];
     for (int q = 0; q < NPROG; q++) { L[q] = h->f[q]; S[q] = h->stage[q]; }
@@ -961,7 +994,8 @@ bool variant_available(const atsat_dyn* h, int v) {
         case ATSAT_DYN_STAGE_SPLIT3:
         case ATSAT_DYN_STAGE_SPLIT13: return !h->kc.divu_on;
         case ATSAT_DYN_STAGE_SPLIT_TILED:
-        case ATSAT_DYN_STAGE_TILED2: return !h->kc.divu_on && h->tile_ok && !h->kf.fsz_over_int;
+        case ATSAT_DYN_STAGE_TILED2:
+        case ATSAT_DYN_STAGE_MARCH: return !h->kc.divu_on && h->tile_ok && !h->kf.fsz_over_int;
         default: return false;
     }
 }
@@ -1039,6 +1073,154 @@ TracerPlan make_plan_mom(atsat_dyn* h, const MixedIO& io) {
     return pl;
 }
 
+// ---- the autotune cache ----
+// One line per tuned configuration: "<im> <jm> <km> <knobs> <gpu> <version> <variant> <levels> <ms>", the
+// GPU's name with blanks replaced by '_', the latest line of a key winning. knobs: bit 0 turbulence, 1
+// radiation source, 2 precipitation source, 3 thermal mass flux (they change the kernels' streams).
+constexpr int TUNE_VERSION = 1;     // raised whenever a stage kernel's speed changes materially
+
+std::string tune_cache_path(const char* path) {
+    if (path && path[0]) return path;
+    const char* env = std::getenv("ATSAT_DYN_TUNE_CACHE");
+    if (env) {
+        if (!env[0] || !std::strcmp(env, "0") || !std::strcmp(env, "off")) return "";
+        return env;
+    }
+    const char* xdg = std::getenv("XDG_CACHE_HOME");
+    const char* home = std::getenv("HOME");
+    std::string dir = (xdg && xdg[0]) ? std::string(xdg) : (home && home[0]) ? std::string(home) + "/.cache" : "";
+    if (dir.empty()) return "";
+    return dir + "/atsat_dyn/autotune.txt";
+}
+
+std::string tune_gpu_token(const char* gpu) {
+    std::string t = gpu && gpu[0] ? gpu : "unknown";
+    for (char& ch : t)
+        if (ch == ' ' || ch == '\t' || ch == '\n') ch = '_';
+    return t;
+}
+
+bool tune_get(const std::string& path, int im, int jm, int km, unsigned knobs, const std::string& gpu, int* variant,
+              int* levels, double* ms) {
+    if (path.empty()) return false;
+    FILE* f = std::fopen(path.c_str(), "r");
+    if (!f) return false;
+    char line[512], g[256];
+    bool found = false;
+    while (std::fgets(line, sizeof(line), f)) {
+        int a, b, c, ver, v, lv;
+        unsigned kn;
+        double t;
+        if (std::sscanf(line, "%d %d %d %u %255s %d %d %d %lf", &a, &b, &c, &kn, g, &ver, &v, &lv, &t) != 9) continue;
+        if (a == im && b == jm && c == km && kn == knobs && gpu == g && ver == TUNE_VERSION) {
+            *variant = v;
+            *levels = lv;
+            if (ms) *ms = t;
+            found = true;
+        }
+    }
+    std::fclose(f);
+    return found;
+}
+
+bool tune_put(const std::string& path, int im, int jm, int km, unsigned knobs, const std::string& gpu, int variant,
+              int levels, double ms) {
+    if (path.empty()) return false;
+    // the parent directories, then keep every other key's lines and append this one (write + rename)
+    for (size_t p = path.find('/', 1); p != std::string::npos; p = path.find('/', p + 1))
+        mkdir(path.substr(0, p).c_str(), 0755);
+    std::vector<std::string> keep;
+    char line[512], g[256];
+    if (FILE* f = std::fopen(path.c_str(), "r")) {
+        while (std::fgets(line, sizeof(line), f)) {
+            int a, b, c, ver, v, lv;
+            unsigned kn;
+            double t;
+            if (std::sscanf(line, "%d %d %d %u %255s %d %d %d %lf", &a, &b, &c, &kn, g, &ver, &v, &lv, &t) != 9) continue;
+            if (a == im && b == jm && c == km && kn == knobs && gpu == g) continue;
+            keep.push_back(line);
+        }
+        std::fclose(f);
+    }
+    const std::string tmp = path + ".tmp." + std::to_string((long)getpid());
+    FILE* f = std::fopen(tmp.c_str(), "w");
+    if (!f) return false;
+    for (const auto& l : keep) std::fputs(l.c_str(), f);
+    std::fprintf(f, "%d %d %d %u %s %d %d %d %.6f\n", im, jm, km, knobs, gpu.c_str(), TUNE_VERSION, variant, levels, ms);
+    const bool ok = std::fclose(f) == 0 && std::rename(tmp.c_str(), path.c_str()) == 0;
+    if (!ok) std::remove(tmp.c_str());
+    return ok;
+}
+
+unsigned tune_knobs(const atsat_dyn* h) {
+    return (h->kc.turb ? 1u : 0u) | (h->kc.rad_on ? 2u : 0u) | (h->kc.precip_on ? 4u : 0u) | (h->kc.tmf_on ? 8u : 0u);
+}
+
+std::string device_name(const atsat_dyn* h) {
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess) {
+        cudaGetLastError();
+        return tune_gpu_token(nullptr);
+    }
+    return tune_gpu_token(prop.name);
+}
+
+void tune_cache_store(atsat_dyn* h, double ms) {
+    tune_put(tune_cache_path(nullptr), h->kc.im, h->kc.jm, h->kc.km, tune_knobs(h), device_name(h), h->variant,
+             h->march_levels, ms);
+}
+
+// The march depth before any tuning: one run of all interior levels per (k, j) tile when the tiles alone
+// give about two blocks per SM, else the levels split into runs so that they do.
+int default_march_levels(const atsat_dyn* h) {
+    const KConst& K = h->kc;
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess || nsm < 1) {
+        cudaGetLastError();
+        nsm = 152;
+    }
+    const int64_t tiles = (int64_t)((K.km - 1 + TILE_K - 1) / TILE_K) * ((K.jm - 4 + TILE_J - 1) / TILE_J);
+    const int interior = K.im - 2;
+    int64_t runs = tiles > 0 ? (2LL * nsm + tiles / 2) / tiles : 1;
+    if (runs < 1) runs = 1;
+    if (runs > interior) runs = interior;
+    return (int)((interior + runs - 1) / runs);
+}
+
+// The radial march's stream per level: the stencil arrays' planes (y_n then the increment, w's low word
+// after its y_n), and the point items nue, the nine frozen terms, the sources the knobs switch on and at the
+// final stage dl_1, dl_2 of u, v, w, t.
+MarchPlan make_plan_march(atsat_dyn* h, const MixedIO& io, int mode) {
+    MarchPlan pl{};
+    pl.err = h->dev_err;
+    pl.wait_limit = h->wait_limit;
+    pl.withhold = h->test_withhold;
+    pl.levels = h->march_levels;
+    const bool dl = io.dl_in[0] != nullptr;
+    int n = 0;
+    auto halo = [&](const float* p) { pl.halo[n++] = arr_index(h, p); };
+    halo(io.yn32[ATSAT_F_U]); if (dl) halo(io.dl_in[ATSAT_F_U]);
+    halo(io.yn32[ATSAT_F_V]); if (dl) halo(io.dl_in[ATSAT_F_V]);
+    halo(io.yn32[ATSAT_F_W]); halo(io.wlo); if (dl) halo(io.dl_in[ATSAT_F_W]);
+    halo(io.yn32[ATSAT_F_T]); if (dl) halo(io.dl_in[ATSAT_F_T]);
+    pl.n_halo = n;
+    n = 0;
+    auto pt = [&](const float* p) { if (n < MARCH_MAX_PT) pl.pt[n] = arr_index(h, p); return n++; };
+    pt(io.nue);
+    for (int f : {FZ_DPR, FZ_GU, FZ_BAN, FZ_BPS, FZ_DPTH, FZ_GV, FZ_DPPH, FZ_GW, FZ_DPS}) pt(io.fz[f]);
+    pl.p_qprecip = h->kc.precip_on ? pt(io.q_precip) : -1;
+    pl.p_rho = h->kc.rad_on ? pt(io.rho_mix) : -1;
+    pl.p_qrad = h->kc.rad_on ? pt(io.q_rad) : -1;
+    pl.p_tmf = h->kc.tmf_on ? pt(io.thermalmassflux) : -1;
+    pl.p_dl = -1;
+    if (mode == MODE_FINAL) {
+        pl.p_dl = n;
+        for (int q = 0; q < 4; q++) { pt(io.dl1[q]); pt(io.dl2[q]); }
+    }
+    pl.n_pt = n;
+    return pl;
+}
+
 cudaError_t launch_stage(atsat_dyn* h, const MixedIO& io, const StageParams& sp, int mode) {
     const int v = (mode == MODE_RHS || !variant_available(h, h->variant)) ? ATSAT_DYN_STAGE_DIRECT : h->variant;
     switch (v) {
@@ -1065,6 +1247,15 @@ cudaError_t launch_stage(atsat_dyn* h, const MixedIO& io, const StageParams& sp,
             if (e != cudaSuccess) return e;
             return launch_rk_tracer_tile(h->maps, h->kf, io, sp, pt, mode, h->stream);
         }
+        case ATSAT_DYN_STAGE_MARCH: {
+            const MarchPlan pm = make_plan_march(h, io, mode);
+            const TracerPlan pt = make_plan_tracer(h, io, mode);
+            if (pt.n_items != tracer_plan_items(mode, io.dl_in[0] != nullptr, h->kc.turb != 0))
+                return cudaErrorInvalidValue;   // the plan and the kernel disagree: never expected
+            const cudaError_t e = launch_rk_mom_march(h->maps, h->kf, io, sp, pm, mode, h->stream);
+            if (e != cudaSuccess) return e;
+            return launch_rk_tracer_tile(h->maps, h->kf, io, sp, pt, mode, h->stream);
+        }
         default: return launch_rk_stage_mixed(h->kf, io, sp, mode, h->stream);
     }
 }
@@ -1073,8 +1264,7 @@ cudaError_t launch_stage(atsat_dyn* h, const MixedIO& io, const StageParams& sp,
 // ends each iteration with the live and n-level fields equal.
 int enqueue_rk4_mixed(atsat_dyn* h, bool resident) {
     int rc;
-    if ((rc = do_level_mean(h))) return rc;
-    if (h->p.metric_split && (rc = do_metric(h))) return rc;
+    if ((rc = do_level_metric(h))) return rc;
     double* yn[NPROG];
     double* L[NPROG];
     for (int q = 0; q < NPROG; q++) { yn[q] = h->f[ATSAT_F_N_BASE + q]; L[q] = h->f[q]; }
@@ -1134,7 +1324,8 @@ int enqueue_rk4_mixed(atsat_dyn* h, bool resident) {
         h->launches += launches_per_stage(h);
         // the TMA-tiled tracer kernel leaves the final stage's FP64 sum to launch_final_combine
         const int v = variant_available(h, h->variant) ? h->variant : ATSAT_DYN_STAGE_DIRECT;
-        if (stage == 3 && (v == ATSAT_DYN_STAGE_SPLIT_TILED || v == ATSAT_DYN_STAGE_TILED2)) h->launches += 1;
+        if (stage == 3 && (v == ATSAT_DYN_STAGE_SPLIT_TILED || v == ATSAT_DYN_STAGE_TILED2 || v == ATSAT_DYN_STAGE_MARCH))
+            h->launches += 1;
     }
     return ATSAT_DYN_OK;
 }
@@ -1648,7 +1839,8 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
     // fields, FP64 stage buffers and accumulators (FP64 path only), source; then the small tables
     const bool fp64_stage = p->precision != ATSAT_DYN_MIXED;
     const int64_t nbig = ATSAT_NFIELDS + (fp64_stage ? 2 * NPROG : 0) + 2;
-    const int64_t nsmall = 2LL * K.im * 16 + K.im + K.jm + K.im + K.jm + 64;
+    const int64_t n_partial = std::max<int64_t>(2LL * K.im * 16, 2LL * K.im * column_scan_blocks(K));
+    const int64_t nsmall = n_partial + K.im + K.jm + K.im + K.jm + 64;
     const size_t bytes = (size_t)(nbig * K.fsz + nsmall) * 8 + sizeof(ColGeo) * (size_t)K.im * K.jm + 4096;
     if ((e = cudaMalloc(&h->slab, bytes)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
     if ((e = cudaMemsetAsync(h->slab, 0, bytes, h->stream)) != cudaSuccess) return cuda_fail(e, "cudaMemset");
@@ -1660,7 +1852,7 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
     }
     h->src = q; q += K.fsz;
     h->p_baro = q; q += K.fsz;
-    h->partial = q; q += 2LL * K.im * 16;
+    h->partial = q; q += n_partial;
     h->buoy = q; q += K.im;
     h->sin_j = q; q += K.jm;
     h->rm_tab = q; q += K.im;
@@ -1698,9 +1890,18 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
         h->pgeo = reinterpret_cast<PrepGeo*>(r);
         if ((e = upload_geof(h)) != cudaSuccess) return cuda_fail(e, "FP32 geometry upload");
         h->tile_ok = make_tile_maps(h);
+        h->march_levels = default_march_levels(h);
         // the default stage kernel: the fastest one measured at every grid tried, where it applies
-        h->variant = variant_available(h, ATSAT_DYN_STAGE_TILED2) ? ATSAT_DYN_STAGE_TILED2
+        h->variant = variant_available(h, ATSAT_DYN_STAGE_MARCH) ? ATSAT_DYN_STAGE_MARCH
                    : (h->tile_ok ? ATSAT_DYN_STAGE_TILED : ATSAT_DYN_STAGE_DIRECT);
+        // an earlier autotune of this configuration on this GPU model
+        int cv = -1, cl = 0;
+        if (tune_get(tune_cache_path(nullptr), K.im, K.jm, K.km, tune_knobs(h), device_name(h), &cv, &cl, nullptr) &&
+            cv >= 0 && cv < ATSAT_DYN_STAGE_NVARIANT && variant_available(h, cv) && cl >= 1 && cl <= K.im - 2) {
+            h->variant = cv;
+            h->march_levels = cl;
+            h->tuned_from_cache = true;
+        }
     }
     // small host tables
     std::vector<double> sin_j(K.jm), rm_tab(K.im), cor_j(K.jm);
@@ -2429,6 +2630,7 @@ int atsat_dyn_status(atsat_dyn_t h, atsat_dyn_diag* out) {
     memset(out, 0, sizeof(*out));
     out->launches = h->launches;
     out->timeout = h->timeouts;
+    out->tuned_from_cache = h->tuned_from_cache ? 1 : 0;
     return ATSAT_DYN_OK;
 }
 
@@ -2534,6 +2736,37 @@ int atsat_dyn_set_stage_variant(atsat_dyn_t h, int32_t variant) {
     return ATSAT_DYN_OK;
 }
 
+int atsat_dyn_tune_cache_get(const char* path, int32_t im, int32_t jm, int32_t km, uint32_t knobs, const char* gpu,
+                             int32_t* variant, int32_t* levels, double* ms) {
+    if (!variant || !levels) return ATSAT_DYN_E_INVALID;
+    int v = -1, l = 0;
+    if (!tune_get(tune_cache_path(path), im, jm, km, knobs, tune_gpu_token(gpu), &v, &l, ms)) return ATSAT_DYN_E_INVALID;
+    *variant = v;
+    *levels = l;
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_tune_cache_put(const char* path, int32_t im, int32_t jm, int32_t km, uint32_t knobs, const char* gpu,
+                             int32_t variant, int32_t levels, double ms) {
+    if (variant < 0 || variant >= ATSAT_DYN_STAGE_NVARIANT || levels < 1) return ATSAT_DYN_E_INVALID;
+    return tune_put(tune_cache_path(path), im, jm, km, knobs, tune_gpu_token(gpu), variant, levels, ms)
+               ? ATSAT_DYN_OK : ATSAT_DYN_E_INVALID;
+}
+
+int atsat_dyn_set_march_levels(atsat_dyn_t h, int32_t levels) {
+    if (!h) return ATSAT_DYN_E_INVALID;
+    if (levels < 1 || levels > h->kc.im - 2)
+        return fail(h, ATSAT_DYN_E_INVALID, "march levels %d outside 1 .. im-2 = %d", levels, h->kc.im - 2);
+    h->march_levels = levels;
+    return ATSAT_DYN_OK;
+}
+
+int atsat_dyn_get_march_levels(atsat_dyn_t h, int32_t* levels) {
+    if (!h || !levels) return ATSAT_DYN_E_INVALID;
+    *levels = h->march_levels;
+    return ATSAT_DYN_OK;
+}
+
 int atsat_dyn_get_stage_variant(atsat_dyn_t h, int32_t* variant) {
     if (!h || !variant) return ATSAT_DYN_E_INVALID;
     *variant = variant_available(h, h->variant) ? h->variant : ATSAT_DYN_STAGE_DIRECT;
@@ -2560,10 +2793,7 @@ int atsat_dyn_autotune(atsat_dyn_t h, int32_t reps, int32_t* chosen, double* ms)
     CK(h, cudaEventCreate(&ev[0]));
     CK(h, cudaEventCreate(&ev[1]));
     int best = -1;
-    for (int v = 0; v < ATSAT_DYN_STAGE_NVARIANT; v++) {
-        ms[v] = -1.0;
-        if (!variant_available(h, v)) continue;
-        h->variant = v;
+    auto time_stage = [&](double* out) -> int {
         for (int r = 0; r < 2 + reps; r++) {
             if (r == 2) CK(h, cudaEventRecord(ev[0], h->stream));
             CK(h, launch_stage(h, io, sp, MODE_STAGE));
@@ -2573,14 +2803,41 @@ int atsat_dyn_autotune(atsat_dyn_t h, int32_t reps, int32_t* chosen, double* ms)
         CK(h, cudaEventSynchronize(ev[1]));
         float t = 0.0f;
         CK(h, cudaEventElapsedTime(&t, ev[0], ev[1]));
-        ms[v] = t / reps;
+        *out = t / reps;
+        return ATSAT_DYN_OK;
+    };
+    int best_levels = h->march_levels;
+    for (int v = 0; v < ATSAT_DYN_STAGE_NVARIANT; v++) {
+        ms[v] = -1.0;
+        if (!variant_available(h, v)) continue;
+        h->variant = v;
+        if (v == ATSAT_DYN_STAGE_MARCH) {
+            // the march depth: whole columns, halves, thirds, quarters, and short runs
+            const int n = h->kc.im - 2;
+            std::vector<int> cand = {default_march_levels(h), n, (n + 1) / 2, (n + 2) / 3, (n + 3) / 4, 8, 4};
+            for (int lv : cand) {
+                if (lv < 1 || lv > n) continue;
+                h->march_levels = lv;
+                double t = 0.0;
+                const int rc = time_stage(&t);
+                if (rc) return rc;
+                if (ms[v] < 0.0 || t < ms[v]) { ms[v] = t; best_levels = lv; }
+            }
+            h->march_levels = best_levels;
+        } else {
+            const int rc = time_stage(&ms[v]);
+            if (rc) return rc;
+        }
         if (best < 0 || ms[v] < ms[best]) best = v;
     }
     cudaEventDestroy(ev[0]);
     cudaEventDestroy(ev[1]);
     h->variant = best >= 0 ? best : keep;
+    h->march_levels = best_levels;
     *chosen = h->variant;
-    return finish(h, true);
+    const int rc = finish(h, true);
+    if (rc == ATSAT_DYN_OK && best >= 0) tune_cache_store(h, ms[best]);
+    return rc;
 }
 
 // ---- standalone pressure-equation solves ----

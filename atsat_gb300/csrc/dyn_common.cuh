@@ -324,6 +324,9 @@ struct TileMaps {
     alignas(64) unsigned char seam4[128];   // box TILE_SEAM_X x TILE_J x TTILE_I
     alignas(64) unsigned char pt4[128];     // box TILE_K x TILE_J x TTILE_I (point values, no halo)
     alignas(64) unsigned char pt2[128];     // box TILE_K x TILE_J x TILE_I (point values, no halo)
+    alignas(64) unsigned char plane1[128];  // box TILE_BX x TILE_BY x 1: one radial plane with its halo
+    alignas(64) unsigned char seam1[128];   // box TILE_SEAM_X x TILE_J x 1
+    alignas(64) unsigned char pt1[128];     // box TILE_K x TILE_J x 1
 };
 
 // The tracer kernel's stream: every array it reads, in consumption order, each either a halo box
@@ -350,6 +353,27 @@ cudaError_t launch_rk_mom_tile(const TileMaps& maps, const MixedConstF& kf, cons
                                const TracerPlan& plan, int mode, cudaStream_t s);
 int mom_plan_items(bool has_dl);
 
+// The radial-march momentum / temperature kernel (rk_mom_march.cu, species_divu off): a block owns
+// TILE_K x TILE_J columns (k, j) and walks `levels` radial levels; per level its producer streams one plane
+// (with its theta / phi halo) of each stencil array and the level's point inputs, and the consumers keep
+// the stencil's radial neighbours in registers. Point items per level, in this order: nue, the frozen DPR,
+// GU, BAN, BPS, DPTH, GV, DPPH, GW, DPS, then the optional ones at the positions below.
+constexpr int MARCH_MAX_PT = 22;
+struct MarchPlan {
+    int n_halo;                    // stencil arrays: u_yn [u_dl] v_yn [v_dl] w_yn w_lo [w_dl] t_yn [t_dl]
+    int halo[9];
+    int n_pt;
+    int pt[MARCH_MAX_PT];
+    int p_qprecip, p_rho, p_qrad, p_tmf;   // positions of the optional point items (-1: absent)
+    int p_dl;                      // final stage: dl_1, dl_2 of u, v, w, t from here on (-1: other stages)
+    int levels;                    // radial levels per block
+    unsigned int* err;
+    long long wait_limit;
+    int withhold;                  // test hook: the producer leaves the last `withhold` level groups unissued
+};
+cudaError_t launch_rk_mom_march(const TileMaps& maps, const MixedConstF& kf, const MixedIO& io, const StageParams& sp,
+                                const MarchPlan& plan, int mode, cudaStream_t s);
+
 // standalone pressure-equation solver (poisson.cu)
 struct PoissonSolver;
 PoissonSolver* poisson_create(const KConst& kc, const ColGeo* geo_dev, const std::vector<ColGeo>& geo_h,
@@ -366,6 +390,13 @@ cudaError_t launch_metric_scan(const KConst& kc, const double* v, const double* 
                                const double* cor_j, const double* p_baro, double* p_metric, cudaStream_t s);
 cudaError_t launch_density(const KConst& kc, const double* t, const double* p_stat, double R_mix,
                            double* rho, cudaStream_t s);
+// the level mean and the metric pressure in one pass (im <= CS_MAX_IM); `partial` holds
+// 2 * im * column_scan_blocks() doubles
+constexpr int CS_MAX_IM = 256;
+int column_scan_blocks(const KConst& kc);
+cudaError_t launch_column_scan(const KConst& kc, const double* t, const double* p_stat, const double* v,
+                               const double* w, const double* sin_j, const double* inv_rm, const double* cor_j,
+                               const double* p_baro, double* p_metric, double* partial, double* buoy, cudaStream_t s);
 cudaError_t launch_projection_prep(const KConst& kc, double* const six[6], cudaStream_t s);
 cudaError_t launch_press_source(const KConst& kc, const ColGeo* geo, const double* su, const double* sv,
                                 const double* sw, const double* aux_u, const double* aux_v, const double* aux_w,

@@ -113,6 +113,149 @@ __global__ void sor_seam_kernel(const KConst K, const ColGeo* __restrict__ geo, 
     sor_cell(K, geo, f, p, i, j, k, w);
 }
 
+// ---- checkerboard-packed red-black SOR, many sweeps per launch ----
+// With an even ring (km-1 = n even) the colour (i + j + k) & 1 is consistent across the periodic seam, and
+// every colour-c cell of row (i, j) is k = 2m + ((i + j + c) & 1), m = k >> 1: colour c is stored packed as
+// Pk[c][(i * jm + j) * kh + m] (kh = n / 2 rounded up to 32). A colour-c cell's four theta / radial
+// neighbours sit at the same m of the other colour's array, its phi neighbours at m and m +- 1; a
+// half-sweep reads the other colour's packed array and its own packed source, and writes its own colour:
+// every access is a coalesced run, none drags the other colour's half of a cache line along.
+//
+// One cooperative launch runs `nsweeps` sweeps; the blocks meet at a grid barrier after each half-sweep.
+// The reference folds the boundary planes after each sweep (p[0] = c43 p[1] - c13 p[2] in r and theta); here
+// the thread that updates the cell at distance two from a boundary writes that boundary cell's folded value
+// itself, at the moment the reference's stored value would hold it: in the first half-sweep from its old
+// value (the other colour reads it in the second half-sweep, as the previous sweep's fold), in the second
+// from its new value (read in the next sweep's first half-sweep, as this sweep's fold). The neighbour at
+// distance one is of the other colour and does not change in that half-sweep. So a sweep is two phases
+// and two barriers, and every value equals the unpacked red, black, fold sequence.
+struct GridBar {
+    unsigned int count, gen, err, pad;
+};
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+// all blocks of the cooperative launch meet here; false (block-uniform) when the wait gave up after
+// `limit` clocks (the error word is then set)
+__device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned nblocks, long long limit) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        int ok = 1;
+        __threadfence();                  // the block's writes of this phase, before its arrival
+        const unsigned g = ld_acquire(&b->gen);
+        if (atom_add_acq_rel(&b->count, 1u) == nblocks - 1) {
+            b->count = 0;
+            st_release(&b->gen, g + 1u);
+        } else {
+            const long long t0 = clock64();
+            while (ld_acquire(&b->gen) == g) {
+                if (clock64() - t0 > limit) {
+                    ok = 0;
+                    atomicOr(&b->err, 1u);
+                    break;
+                }
+            }
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <typename T>
+struct alignas(4 * sizeof(T)) SorW {
+    T num1, num2, num3, den;
+};
+
+constexpr int SORP_WARPS = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(32 * SORP_WARPS) sor_packed_kernel(const KConst K, const SorW<T>* __restrict__ wt,
+                                                                     T* p0, T* p1, const T* __restrict__ f0,
+                                                                     const T* __restrict__ f1, int kh, int nsweeps,
+                                                                     T w, GridBar* bar, long long limit) {
+    const int n = K.km - 1, nh = n >> 1;
+    const int NI = K.im - 2, NJ = K.jm - 2;
+    const int64_t plane = (int64_t)K.jm * kh;
+    const int lane = threadIdx.x;
+    const int gw = blockIdx.x * SORP_WARPS + threadIdx.y, nw = gridDim.x * SORP_WARPS;
+    const T c43 = (T)K.c43, c13 = (T)K.c13;
+    for (int sweep = 0; sweep < nsweeps; sweep++) {
+        for (int c = 0; c < 2; c++) {
+            T* Pc = c ? p1 : p0;
+            const T* Po = c ? p0 : p1;
+            const T* Fc = c ? f1 : f0;
+            for (int r = gw; r < NI * NJ; r += nw) {
+                const int i = 1 + r / NJ, j = 1 + r % NJ;
+                const int64_t row = ((int64_t)i * K.jm + j) * kh;
+                const SorW<T> W = wt[(int64_t)i * K.jm + j];
+                const int s = (i + j + c) & 1;
+                for (int m = lane; m < nh; m += 32) {
+                    const int k = 2 * m + s;
+                    const int me = (k == n - 1) ? 0 : ((k + 1) >> 1);
+                    const int mw = (k == 0) ? ((n - 1) >> 1) : ((k - 1) >> 1);
+                    const T acc = (__ldcg(Po + row + plane + m) + __ldcg(Po + row - plane + m)) * W.num1
+                                + (__ldcg(Po + row + kh + m) + __ldcg(Po + row - kh + m)) * W.num2
+                                + (__ldcg(Po + row + me) + __ldcg(Po + row + mw)) * W.num3;
+                    const T old = __ldcg(Pc + row + m);
+                    const T nv = (acc - Fc[row + m]) / W.den;
+                    const T pn = old + w * (nv - old);
+                    Pc[row + m] = pn;
+                    // the folded boundary cells this cell stands two away from (the same colour as it)
+                    const T self = (c == 0) ? old : pn;
+                    if (i == 2) Pc[row - 2 * plane + m] = c43 * __ldcg(Po + row - plane + m) - c13 * self;
+                    if (i == K.im - 3) Pc[row + 2 * plane + m] = c43 * __ldcg(Po + row + plane + m) - c13 * self;
+                    if (j == 2) Pc[row - 2 * kh + m] = c43 * __ldcg(Po + row - kh + m) - c13 * self;
+                    if (j == K.jm - 3) Pc[row + 2 * kh + m] = c43 * __ldcg(Po + row + kh + m) - c13 * self;
+                }
+            }
+            if (!grid_barrier(bar, gridDim.x, limit)) return;
+        }
+    }
+}
+
+// pitched -> packed (every (i, j) row, the folded boundary rows and planes included); unpacked back for the
+// interior cells only (the fold kernel then sets the boundary)
+template <typename T>
+__global__ void pack_kernel(const KConst K, const T* __restrict__ src, T* __restrict__ d0, T* __restrict__ d1, int kh) {
+    const int m = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i = blockIdx.z;
+    const int n = K.km - 1;
+    if (m >= (n >> 1) || j >= K.jm) return;
+    const int64_t c = ((int64_t)i * K.jm + j) * K.kp;
+    const int64_t o = ((int64_t)i * K.jm + j) * kh + m;
+    d0[o] = src[c + 2 * m + ((i + j) & 1)];
+    d1[o] = src[c + 2 * m + ((i + j + 1) & 1)];
+}
+
+template <typename T>
+__global__ void unpack_kernel(const KConst K, T* __restrict__ dst, const T* __restrict__ s0, const T* __restrict__ s1,
+                              int kh) {
+    const int m = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int i = blockIdx.z;
+    const int n = K.km - 1;
+    if (m >= (n >> 1) || j < 1 || j > K.jm - 2 || i < 1 || i > K.im - 2) return;
+    const int64_t c = ((int64_t)i * K.jm + j) * K.kp;
+    const int64_t o = ((int64_t)i * K.jm + j) * kh + m;
+    dst[c + 2 * m + ((i + j) & 1)] = s0[o];
+    dst[c + 2 * m + ((i + j + 1) & 1)] = s1[o];
+}
+
 // r = f - L p on the interior P cells, in FP64 (p FP64), with an FP32 copy of r and the sums
 // sum r^2 and sum f^2 (sq[0], sq[1])
 __global__ void __launch_bounds__(256) residual_kernel(const KConst K, const ColGeo* __restrict__ geo,
@@ -381,6 +524,16 @@ struct PoissonSolver {
     std::vector<double> ynull;            // left null vector of the zero mode, [jj * NI + ii]
     void* block = nullptr;
     int64_t n_interior = 0;
+    // the checkerboard-packed SOR (even rings only): per precision both colours of p and f, the column
+    // weights, the grid barrier's words, and the cooperative launch's grid
+    int kh = 0;
+    bool packed = false;
+    double *pk64[2] = {}, *fk64[2] = {};
+    float *pk32[2] = {}, *fk32[2] = {};
+    SorW<double>* w64 = nullptr;
+    SorW<float>* w32 = nullptr;
+    GridBar* bar = nullptr;
+    int coop_blocks64 = 0, coop_blocks32 = 0;
 };
 
 namespace {
@@ -528,6 +681,13 @@ PoissonSolver* poisson_create(const KConst& kc, const ColGeo* geo_dev, const std
     const size_t o_W64 = take(nW * 8), o_s64 = take(nspec * 8), o_b = take(nc * 8), o_c = take(nc * 8);
     const size_t o_tw64 = take((size_t)2 * S.n * 8), o_p32 = take(fsz * 4), o_r32 = take(fsz * 4), o_e32 = take(fsz * 4);
     const size_t o_W32 = take(nW * 4), o_s32 = take(nspec * 4), o_tw32 = take((size_t)2 * S.n * 4);
+    // the packed SOR's arrays (even rings): p and f of both colours in each precision, the column weights
+    P->packed = (S.n % 2) == 0;
+    P->kh = ((S.n / 2 + 31) / 32) * 32;
+    const size_t npk = P->packed ? (size_t)kc.im * kc.jm * P->kh : 0, ncol = (size_t)kc.im * kc.jm;
+    const size_t o_pk64 = take(4 * npk * 8), o_pk32 = take(4 * npk * 4);
+    const size_t o_w64 = take(P->packed ? ncol * sizeof(SorW<double>) : 0);
+    const size_t o_w32 = take(P->packed ? ncol * sizeof(SorW<float>) : 0), o_bar = take(sizeof(GridBar));
     cudaError_t e = cudaMalloc(&P->block, bytes);
     if (e != cudaSuccess) { *err = std::string("poisson: cudaMalloc: ") + cudaGetErrorString(e); delete P; return nullptr; }
     char* b0 = static_cast<char*>(P->block);
@@ -546,6 +706,40 @@ PoissonSolver* poisson_create(const KConst& kc, const ColGeo* geo_dev, const std
     P->W32 = reinterpret_cast<float*>(b0 + o_W32);
     P->spec32 = reinterpret_cast<float*>(b0 + o_s32);
     P->tw32 = reinterpret_cast<float*>(b0 + o_tw32);
+    P->bar = reinterpret_cast<GridBar*>(b0 + o_bar);
+    std::vector<SorW<double>> w64h;
+    std::vector<SorW<float>> w32h;
+    if (P->packed) {
+        for (int q = 0; q < 4; q++) {
+            double* d = reinterpret_cast<double*>(b0 + o_pk64) + q * npk;
+            float* f = reinterpret_cast<float*>(b0 + o_pk32) + q * npk;
+            if (q < 2) { P->pk64[q] = d; P->pk32[q] = f; } else { P->fk64[q - 2] = d; P->fk32[q - 2] = f; }
+        }
+        P->w64 = reinterpret_cast<SorW<double>*>(b0 + o_w64);
+        P->w32 = reinterpret_cast<SorW<float>*>(b0 + o_w32);
+        w64h.resize(ncol);
+        w32h.resize(ncol);
+        for (size_t q = 0; q < ncol; q++) {
+            const ColGeo& c = geo_h[q];
+            w64h[q] = SorW<double>{c.p_num1, c.p_num2, c.p_num3, c.p_den};
+            w32h[q] = SorW<float>{(float)c.p_num1, (float)c.p_num2, (float)c.p_num3, (float)c.p_den};
+        }
+        // the cooperative launch's grid: as many blocks as fit on the GPU at once
+        int dev = 0, nsm = 0, b64 = 0, b32 = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b64, sor_packed_kernel<double>, 32 * SORP_WARPS, 0) !=
+                cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b32, sor_packed_kernel<float>, 32 * SORP_WARPS, 0) !=
+                cudaSuccess) {
+            cudaGetLastError();
+            P->packed = false;
+        } else {
+            P->coop_blocks64 = nsm * b64;
+            P->coop_blocks32 = nsm * b32;
+            if (P->coop_blocks64 < 1 || P->coop_blocks32 < 1) P->packed = false;
+        }
+    }
     std::vector<float> W32(nW);
     for (size_t q = 0; q < nW; q++) W32[q] = (float)W[q];
     std::vector<double> tw(2 * S.n);
@@ -562,6 +756,10 @@ PoissonSolver* poisson_create(const KConst& kc, const ColGeo* geo_dev, const std
         (e = cudaMemcpyAsync(P->cvec_d, P->cvec.data(), nc * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
         (e = cudaMemcpyAsync(P->tw64, tw.data(), 2 * S.n * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
         (e = cudaMemcpyAsync(P->tw32, tw32.data(), 2 * S.n * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (!w64h.empty() && (e = cudaMemcpyAsync(P->w64, w64h.data(), w64h.size() * sizeof(SorW<double>),
+                                               cudaMemcpyHostToDevice, s)) != cudaSuccess) ||
+        (!w32h.empty() && (e = cudaMemcpyAsync(P->w32, w32h.data(), w32h.size() * sizeof(SorW<float>),
+                                               cudaMemcpyHostToDevice, s)) != cudaSuccess) ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess) {
         *err = std::string("poisson: upload: ") + cudaGetErrorString(e);
         cudaFree(P->block);
@@ -605,6 +803,51 @@ cudaError_t sor_sweep(PoissonSolver* P, const T* f, T* p, T w) {
         }
     }
     return fold(P, p);
+}
+
+template <typename T> T** packed_p(PoissonSolver* P);
+template <> double** packed_p<double>(PoissonSolver* P) { return P->pk64; }
+template <> float** packed_p<float>(PoissonSolver* P) { return P->pk32; }
+template <typename T> T** packed_f(PoissonSolver* P);
+template <> double** packed_f<double>(PoissonSolver* P) { return P->fk64; }
+template <> float** packed_f<float>(PoissonSolver* P) { return P->fk32; }
+template <typename T> const SorW<T>* packed_w(PoissonSolver* P);
+template <> const SorW<double>* packed_w<double>(PoissonSolver* P) { return P->w64; }
+template <> const SorW<float>* packed_w<float>(PoissonSolver* P) { return P->w32; }
+
+// `nsweeps` sweeps of the checkerboard-packed SOR in one cooperative launch: f and p packed first where
+// asked (p keeps its packed copy between calls), p unpacked and folded after. The barrier's error word is
+// read back: a barrier wait that gave up returns cudaErrorLaunchTimeout.
+template <typename T>
+cudaError_t sor_packed_run(PoissonSolver* P, const T* f, T* p, T w, int nsweeps, bool pack_f, bool pack_p) {
+    const KConst& K = P->K;
+    const int kh = P->kh;
+    T** pk = packed_p<T>(P);
+    T** fk = packed_f<T>(P);
+    const dim3 pg((K.km - 1) / 2 / 32 + 1, (K.jm + 7) / 8, K.im), pb(32, 8);
+    if (pack_f) pack_kernel<T><<<pg, pb, 0, P->stream>>>(K, f, fk[0], fk[1], kh);
+    if (pack_p) pack_kernel<T><<<pg, pb, 0, P->stream>>>(K, p, pk[0], pk[1], kh);
+    cudaError_t e = cudaMemsetAsync(P->bar, 0, sizeof(GridBar), P->stream);
+    if (e != cudaSuccess) return e;
+    const SorW<T>* wt = packed_w<T>(P);
+    T* p0 = pk[0];
+    T* p1 = pk[1];
+    const T* f0 = fk[0];
+    const T* f1 = fk[1];
+    long long limit = TILE_WAIT_LIMIT;
+    void* args[] = {(void*)&K, (void*)&wt, (void*)&p0, (void*)&p1, (void*)&f0, (void*)&f1, (void*)&kh,
+                    (void*)&nsweeps, (void*)&w, (void*)&P->bar, (void*)&limit};
+    const int nb = sizeof(T) == 8 ? P->coop_blocks64 : P->coop_blocks32;
+    e = cudaLaunchCooperativeKernel((const void*)sor_packed_kernel<T>, dim3(nb), dim3(32, SORP_WARPS), args, 0,
+                                    P->stream);
+    if (e != cudaSuccess) return e;
+    unpack_kernel<T><<<pg, pb, 0, P->stream>>>(K, p, pk[0], pk[1], kh);
+    if ((e = fold(P, p)) != cudaSuccess) return e;
+    unsigned herr = 0;
+    if ((e = cudaMemcpyAsync(&herr, &P->bar->err, sizeof(herr), cudaMemcpyDeviceToHost, P->stream)) != cudaSuccess)
+        return e;
+    if ((e = cudaStreamSynchronize(P->stream)) != cudaSuccess) return e;
+    return herr ? cudaErrorLaunchTimeout : cudaSuccess;
 }
 
 // x = L^-1 rhs by the spectral block solve in precision T (rhs and x pitched; x may alias rhs)
@@ -687,6 +930,21 @@ cudaError_t poisson_run_inner(PoissonSolver* P, int method, double tol, int max_
             convert_kernel<float, double><<<cell_grid(K), dim3(32, 8), 0, P->stream>>>(K, P->e32, P->f64);
         }
         *rel = 1.0;
+        if (P->packed) {
+            // runs of `check` sweeps in one launch each, the residual between them
+            for (int it = 0; it < max_iter;) {
+                const int run = std::min(check, max_iter - it);
+                e = (method == 0) ? sor_packed_run<double>(P, P->f64, P->p64, omega, run, it == 0, it == 0)
+                                  : sor_packed_run<float>(P, P->e32, P->p32, (float)omega, run, it == 0, it == 0);
+                if (e != cudaSuccess) return e;
+                it += run;
+                *iters = it;
+                if (method == 1) convert_kernel<double, float><<<cell_grid(K), dim3(32, 8), 0, P->stream>>>(K, P->p64, P->p32);
+                if ((e = residual(P, rel)) != cudaSuccess) return e;
+                if (*rel <= tol) break;
+            }
+            return cudaSuccess;
+        }
         for (int it = 1; it <= max_iter; it++) {
             e = (method == 0) ? sor_sweep<double>(P, P->f64, P->p64, omega)
                               : sor_sweep<float>(P, P->e32, P->p32, (float)omega);
@@ -709,7 +967,9 @@ cudaError_t poisson_run_inner(PoissonSolver* P, int method, double tol, int max_
             *inner_total += 1;
         } else {
             if ((e = cudaMemsetAsync(P->e32, 0, fsz * 4, P->stream)) != cudaSuccess) return e;
-            for (int s = 0; s < inner && e == cudaSuccess; s++) e = sor_sweep<float>(P, P->r32, P->e32, (float)omega);
+            if (P->packed) e = sor_packed_run<float>(P, P->r32, P->e32, (float)omega, inner, true, true);
+            else
+                for (int s = 0; s < inner && e == cudaSuccess; s++) e = sor_sweep<float>(P, P->r32, P->e32, (float)omega);
             *inner_total += inner;
         }
         if (e != cudaSuccess) return e;

@@ -85,6 +85,12 @@ def lib():
         L.atsat_dyn_set_wait_test.argtypes = [H, C.c_int64, C.c_int32]
         L.atsat_dyn_set_stage_variant.argtypes = [H, C.c_int32]
         L.atsat_dyn_get_stage_variant.argtypes = [H, C.POINTER(C.c_int32)]
+        L.atsat_dyn_set_march_levels.argtypes = [H, C.c_int32]
+        L.atsat_dyn_get_march_levels.argtypes = [H, C.POINTER(C.c_int32)]
+        L.atsat_dyn_tune_cache_get.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint32, C.c_char_p,
+                                               C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+        L.atsat_dyn_tune_cache_put.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint32, C.c_char_p,
+                                               C.c_int32, C.c_int32, C.c_double]
         L.atsat_dyn_autotune.argtypes = [H, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
         L.atsat_dyn_graph_capture.argtypes = [H, C.c_int32, C.c_int32]
         L.atsat_dyn_graph_launch.argtypes = [H, C.c_int32]
@@ -252,8 +258,9 @@ class Dycore:
     def set_write_all_rhs(self, on: bool):
         self._ck(lib().atsat_dyn_set_write_all_rhs(self.h, int(bool(on))), "set_write_all_rhs")
 
-    STAGE_DIRECT, STAGE_TILED, STAGE_SPLIT, STAGE_SPLIT3, STAGE_SPLIT13, STAGE_SPLIT_TILED, STAGE_TILED2 = range(7)
-    STAGE_NAMES = ["direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2"]
+    (STAGE_DIRECT, STAGE_TILED, STAGE_SPLIT, STAGE_SPLIT3, STAGE_SPLIT13, STAGE_SPLIT_TILED, STAGE_TILED2,
+     STAGE_MARCH) = range(8)
+    STAGE_NAMES = ["direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2", "march"]
 
     def set_stage_variant(self, variant: int):
         """Mixed precision: the RK stage kernel (STAGE_* constants)."""
@@ -264,9 +271,24 @@ class Dycore:
         self._ck(lib().atsat_dyn_get_stage_variant(self.h, C.byref(v)), "get_stage_variant")
         return v.value
 
+    def set_march_levels(self, levels: int):
+        """MARCH variant: radial levels per block (the march depth)."""
+        self._ck(lib().atsat_dyn_set_march_levels(self.h, int(levels)), "set_march_levels")
+
+    def march_levels(self) -> int:
+        v = C.c_int32(0)
+        self._ck(lib().atsat_dyn_get_march_levels(self.h, C.byref(v)), "get_march_levels")
+        return v.value
+
+    def tuned_from_cache(self) -> bool:
+        d = abi.Diag()
+        self._ck(lib().atsat_dyn_status(self.h, C.byref(d)), "status")
+        return bool(d.tuned_from_cache)
+
     def autotune(self, reps: int = 10):
-        """Time every available stage variant on this grid, keep the fastest; returns (chosen, ms per
-        variant, -1 where unavailable)."""
+        """Time every available stage variant (the MARCH variant at several march depths) on this grid, keep
+        the fastest and record it in the autotune cache; returns (chosen, ms per variant, -1 where
+        unavailable)."""
         chosen = C.c_int32(-1)
         ms = (C.c_double * len(self.STAGE_NAMES))()
         self._ck(lib().atsat_dyn_autotune(self.h, int(reps), C.byref(chosen), ms), "autotune")

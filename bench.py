@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--copy-engines", action="store_true",
                     help="move host bindings with the copy engines even where the SMs can address host memory")
     ap.add_argument("--stage-variant", default="auto",
-                    choices=["auto", "direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2"],
+                    choices=["auto", "direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2",
+                             "march"],
                     help="mixed precision: the RK stage kernel (auto: the autotuner's choice)")
     ap.add_argument("--poisson", action="store_true",
                     help="the standalone pressure-equation solves instead of the dycore iteration")
@@ -64,6 +65,8 @@ def parse():
                     help="time one pressure call with and without PRESS_LINE / PRESS_BAROTROPIC")
     ap.add_argument("--ensemble", action="store_true",
                     help="the 32-member mixed-size ensemble: concurrent graph replays vs one after another")
+    ap.add_argument("--cpu-table", action="store_true",
+                    help="the CPU restatement's throughput per benchmark configuration, build and thread count")
     ap.add_argument("--precision", default="mixed,fp64",
                     help="comma list; the first is the headline value, the others are reported beside it")
     a = ap.parse_args()
@@ -202,7 +205,10 @@ KERNEL_NAME = {"fp64": "rk_stage_fp64_kernel (fused RHSSat + RK4 stage, FP64)",
                "mixed_split_tiled": "rk_mom_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, TMA-tiled tracers; "
                                     "final stage + final_combine_kernel)",
                "mixed_tiled2": "rk_mom_tile_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, all inputs "
-                               "TMA-streamed; final stage + final_combine_kernel)"}
+                               "TMA-streamed; final stage + final_combine_kernel)",
+               "mixed_march": "rk_mom_march_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage: the momentum "
+                              "part as a radial march, one TMA plane per stencil array and level; final stage + "
+                              "final_combine_kernel)"}
 
 
 def cpu_baseline(g, P, seed, target_s=3.0):
@@ -293,7 +299,7 @@ def measure(a, rank, world, g, P, st, pinned, precision):
     tune = None
     if precision == "mixed" and a.stage_variant == "auto":
         chosen, tms = d.autotune(reps=5)
-        tune = {"stage_variant": dyn.Dycore.STAGE_NAMES[chosen],
+        tune = {"stage_variant": dyn.Dycore.STAGE_NAMES[chosen], "march_levels": d.march_levels(),
                 "autotune_ms_per_stage": {n: (t if t > 0 else None) for n, t in zip(dyn.Dycore.STAGE_NAMES, tms)}}
     elif precision == "mixed":
         d.set_stage_variant(dyn.Dycore.STAGE_NAMES.index(a.stage_variant))
@@ -424,6 +430,8 @@ def measure(a, rank, world, g, P, st, pinned, precision):
         d.load_state(st.copy())
         if tune:
             d.set_stage_variant(dyn.Dycore.STAGE_NAMES.index(tune["stage_variant"]))
+            if tune.get("march_levels"):
+                d.set_march_levels(tune["march_levels"])
         d.iterate(1, a.warmup)
         n_pe = max(2, min(a.steps, 100) // 2 * 2)
         barrier(world)
@@ -622,19 +630,33 @@ def run_ensemble(a, rank, world):
         d = dyn.Dycore(g, P)
         d.load_state(st)
         if shp not in tuned:
-            tuned[shp] = d.autotune(reps=3)[0]
+            tuned[shp] = (d.autotune(reps=3)[0], d.march_levels())
         else:
-            d.set_stage_variant(tuned[shp])
+            d.set_stage_variant(tuned[shp][0])
+            d.set_march_levels(tuned[shp][1])
         d.iterate(1, 2)
         members.append(d)
         cells += g.cells
     setup_s = time.perf_counter() - t0
     steps = 10
     seq_plain = 0.0
-    for d in members:
+    per_shape = {}
+    for d, shp in zip(members, shapes):
         d.timer_start()
         d.iterate(3, steps)
-        seq_plain += d.timer_stop()
+        ms = d.timer_stop()
+        seq_plain += ms
+        e = per_shape.setdefault(f"{shp[0]}x{shp[1]}x{shp[2]}", {"members": 0, "ms": 0.0, "cells": 0})
+        e["members"] += 1
+        e["ms"] += ms
+        e["cells"] += shp[0] * shp[1] * shp[2]
+    for e in per_shape.values():
+        e["ms_per_member_iteration"] = e["ms"] / e["members"] / steps
+        e["Mcell_steps_per_s"] = e["cells"] * steps / (e["ms"] / 1e3) / 1e6
+    # the bound on batching: the members of the shapes whose kernels fill the GPU gain nothing from running
+    # beside others; at best every member runs at the best per-cell rate any shape reaches alone
+    best = max(e["Mcell_steps_per_s"] for e in per_shape.values())
+    t_best = cells * steps / (best * 1e6) * 1e3
     for d in members:
         d.graph_capture(3 + steps, 2)
     seq_graph = dyn.ensemble_run(members, reps=steps // 2, concurrent=False)
@@ -647,19 +669,78 @@ def run_ensemble(a, rank, world):
             "value": mcs(conc), "unit": "Mcell-steps/s", "higher_is_better": True, "n_gpus": 1, "steps": steps,
             "data": "synthetic", "dtype": "f32+f64",
             "config": {"workload": "16 x 21x91x181 + 12 x 41x181x361 + 4 x 61x271x541 members, 10 iterations each",
-                       "cells": cells, "stage_variant_per_shape": {f"{s[0]}x{s[1]}x{s[2]}": dyn.Dycore.STAGE_NAMES[v]
+                       "cells": cells, "stage_variant_per_shape": {f"{s[0]}x{s[1]}x{s[2]}":
+                                                                   f"{dyn.Dycore.STAGE_NAMES[v[0]]} (march depth {v[1]})"
                                                                    for s, v in tuned.items()},
                        "setup_s": setup_s},
+            "per_shape_sequential": per_shape,
+            "bound": {"ms_if_every_member_ran_at_the_best_shape_rate": t_best,
+                      "max_batched_over_sequential": seq_plain / t_best},
             "modes": {"sequential_plain": {"ms": seq_plain, "value": mcs(seq_plain)},
                       "sequential_graphs": {"ms": seq_graph, "value": mcs(seq_graph)},
                       "concurrent_graphs": {"ms": conc, "value": mcs(conc)}},
             "batched_over_sequential": seq_plain / conc}
 
 
+# one child process of the CPU table: the restatement's dycore iterations per grid, timed after one
+# untimed iteration; prints one JSON object {grid: {"iterations", "s", "Mcell_steps_per_s"}}
+_CPU_CHILD = r"""
+import json, sys, time
+sys.path.insert(0, %(root)r)
+from atsat_gb300 import abi, synth
+from oracle import oracle
+P = abi.default_params()
+out = {}
+for shape, n in %(work)r:
+    g = synth.make_grid(*shape)
+    st = synth.saturn_state(g, P, seed=0)
+    oracle.steps(st, P, 1, iter0=1)
+    t0 = time.perf_counter()
+    oracle.steps(st, P, n, iter0=2)
+    dt = time.perf_counter() - t0
+    out["%%dx%%dx%%d" %% shape] = {"iterations": n, "s": dt, "Mcell_steps_per_s": n * g.cells / dt / 1e6}
+    del st
+print(json.dumps(out))
+"""
+
+
+def run_cpu_table(a, rank, world):
+    """The CPU restatement of the reference's OpenMP path per benchmark grid: the parity build (-O2, no
+    contraction) and the fast build (-O3, contraction allowed), on all host cores and on one; each a
+    bounded sample of dycore iterations (pressure call on the even ones) after one untimed iteration."""
+    if rank != 0:
+        return None
+    small = [((41, 181, 361), 2), ((21, 91, 181), 4), ((61, 271, 541), 1)]
+    runs = {"o2_all": ("", None, small + [((81, 361, 721), 1)]), "fast_all": ("fast", None, small),
+            "o2_one": ("", "1", [((41, 181, 361), 1), ((21, 91, 181), 2)]),
+            "fast_one": ("fast", "1", [((41, 181, 361), 1), ((21, 91, 181), 2)])}
+    out = {}
+    for name, (build, threads, work) in runs.items():
+        env = dict(os.environ, ATSAT_ORACLE_BUILD=build)
+        if threads:
+            env["OMP_NUM_THREADS"] = threads
+        else:
+            env.pop("OMP_NUM_THREADS", None)
+        code = _CPU_CHILD % {"root": ROOT, "work": work}
+        t0 = time.perf_counter()
+        r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=1800)
+        try:
+            out[name] = json.loads(r.stdout.strip().splitlines()[-1])
+        except (ValueError, IndexError):
+            out[name] = {"error": (r.stderr or r.stdout)[-400:]}
+        out[name]["wall_s"] = time.perf_counter() - t0
+    return {"metric": "CPU restatement of the dycore iteration, Mcell-steps/s per grid, build and threads",
+            "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "runs": out,
+            "builds": {"o2": "gcc -O2 -fopenmp -ffp-contract=off (the parity oracle)",
+                       "fast": "gcc -O3 -fopenmp -ffp-contract=fast (timed baseline only)"}}
+
+
 def main():
     a = parse()
     rank, world, _ = dist()
-    if a.ensemble:
+    if a.cpu_table:
+        res = run_cpu_table(a, rank, world)
+    elif a.ensemble:
         res = run_ensemble(a, rank, world)
     elif a.poisson:
         res = run_poisson(a, rank, world)

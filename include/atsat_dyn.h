@@ -200,7 +200,8 @@ typedef struct atsat_dyn_diag {
     int64_t launches;          /* kernels launched by this handle since create */
     int64_t nonfinite;         /* non-finite cells found by the last atsat_dyn_check_finite */
     int32_t timeout;           /* a bounded device wait gave up */
-    int32_t reserved[5];
+    int32_t tuned_from_cache;  /* 1: the stage variant and march depth came from the autotune cache */
+    int32_t reserved[4];
 } atsat_dyn_diag;
 
 typedef struct atsat_dyn* atsat_dyn_t;
@@ -401,9 +402,13 @@ int atsat_dyn_set_write_all_rhs(atsat_dyn_t h, int32_t on);
  *   SPLIT*   a momentum / temperature kernel, then a tracer kernel with 1, 3 or 13 threads per cell
  *            (not with species_divu on);
  *   SPLIT_TILED  the same momentum kernel, then the tracers TMA-tiled (4 radial levels per thread);
- *   TILED2   both the momentum / temperature and the tracer kernels TMA-tiled, every input streamed.
- * The default is TILED where available. No reference counterpart (the reference has one CPU loop
- * nest). Setting an unavailable variant returns ATSAT_DYN_E_UNSUPPORTED. */
+ *   TILED2   both the momentum / temperature and the tracer kernels TMA-tiled, every input streamed;
+ *   MARCH    the momentum / temperature kernel as a radial march (a block walks a run of radial levels
+ *            of its theta-phi tile, one plane per stencil array and level streamed by TMA, the radial
+ *            neighbours in registers), then the TMA-tiled tracer kernel.
+ * The default is MARCH where available (not with species_divu on, nor without a tensor-map encoder),
+ * else TILED, else DIRECT. No reference counterpart (the reference has one CPU loop nest). Setting an
+ * unavailable variant returns ATSAT_DYN_E_UNSUPPORTED. */
 enum {
     ATSAT_DYN_STAGE_DIRECT = 0,
     ATSAT_DYN_STAGE_TILED = 1,
@@ -412,15 +417,32 @@ enum {
     ATSAT_DYN_STAGE_SPLIT13 = 4,
     ATSAT_DYN_STAGE_SPLIT_TILED = 5,
     ATSAT_DYN_STAGE_TILED2 = 6,
-    ATSAT_DYN_STAGE_NVARIANT = 7
+    ATSAT_DYN_STAGE_MARCH = 7,
+    ATSAT_DYN_STAGE_NVARIANT = 8
 };
 int atsat_dyn_set_stage_variant(atsat_dyn_t h, int32_t variant);
 int atsat_dyn_get_stage_variant(atsat_dyn_t h, int32_t* variant);
+/* The MARCH variant's march depth: radial levels per block (1 .. im-2; the interior levels are split into
+ * runs of this length). The default gives about two blocks per SM; atsat_dyn_autotune tunes it. */
+int atsat_dyn_set_march_levels(atsat_dyn_t h, int32_t levels);
+int atsat_dyn_get_march_levels(atsat_dyn_t h, int32_t* levels);
 /* Time each available stage variant on this handle's grid (`reps` launches of an intermediate RK
  * stage each, CUDA events, after two untimed launches), keep the fastest and report it with the mean
  * milliseconds of every variant in ms[ATSAT_DYN_STAGE_NVARIANT] (< 0: unavailable). The stage writes
  * only scratch buffers, so the model state is unchanged. No reference counterpart. */
 int atsat_dyn_autotune(atsat_dyn_t h, int32_t reps, int32_t* chosen, double* ms);
+/* The autotune cache. atsat_dyn_autotune records its choice (variant and march depth) per grid, source
+ * knobs and GPU model; atsat_dyn_create of a mixed-precision handle starts from the recorded choice, with
+ * no timing pass (atsat_dyn_diag.tuned_from_cache). The file is $ATSAT_DYN_TUNE_CACHE, else
+ * $XDG_CACHE_HOME/atsat_dyn/autotune.txt, else $HOME/.cache/atsat_dyn/autotune.txt; ATSAT_DYN_TUNE_CACHE
+ * set to "", "0" or "off" disables it. One text line per key: im jm km knobs gpu version variant levels ms
+ * (knobs: bit 0 turbulence, 1 radiation source, 2 precipitation source, 3 thermal mass flux; gpu: the
+ * device name with blanks as '_'). get / put read and write it directly (path NULL: the file above); get
+ * returns ATSAT_DYN_E_INVALID when the key is absent. Neither touches the GPU. */
+int atsat_dyn_tune_cache_get(const char* path, int32_t im, int32_t jm, int32_t km, uint32_t knobs, const char* gpu,
+                             int32_t* variant, int32_t* levels, double* ms);
+int atsat_dyn_tune_cache_put(const char* path, int32_t im, int32_t jm, int32_t km, uint32_t knobs, const char* gpu,
+                             int32_t variant, int32_t levels, double ms);
 
 /* ---- CUDA graphs and ensembles (no reference counterpart) ----
  * graph_capture records n (even, >= 2) resident iterations starting at iter0 (the parity of iter0 fixes

@@ -16,8 +16,13 @@ from atsat_gb300 import abi, fields as F
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "atsat_oracle.c")
-LIB = os.path.join(HERE, "liboracle.so")
-CFLAGS = ["-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c99", "-Wall"]
+# The parity oracle: -O2 and no multiply-add contraction, so that on x86-64 it equals the reference bit for
+# bit. ATSAT_ORACLE_BUILD=fast selects a second build used only as a timed CPU baseline: -O3 with
+# contraction allowed (fused multiply-adds wherever the host ISA has them; no -march / -mcpu).
+FAST = os.environ.get("ATSAT_ORACLE_BUILD", "") == "fast"
+LIB = os.path.join(HERE, "liboracle_fast.so" if FAST else "liboracle.so")
+CFLAGS = (["-O3", "-fopenmp", "-ffp-contract=fast", "-fPIC", "-shared", "-std=c99", "-Wall"] if FAST else
+          ["-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c99", "-Wall"])
 
 
 def build(force: bool = False) -> str:

@@ -3,6 +3,10 @@ import sys
 
 import pytest
 
+# tests start from the built-in stage-kernel defaults, not from an autotune cache on this machine
+# (the cache test points the variable at a file of its own)
+os.environ["ATSAT_DYN_TUNE_CACHE"] = "off"
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 TESTS = os.path.dirname(os.path.abspath(__file__))
 for _p in (ROOT, TESTS):

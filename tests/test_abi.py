@@ -94,3 +94,27 @@ def test_unsupported_knobs_are_rejected(lib):
     with pytest.raises(dyn.DycoreError) as e:
         dyn.Dycore(synth.make_grid(9, 13, 17), abi.default_params(chrom=1))
     assert e.value.status == abi.E_UNSUPPORTED
+
+
+def test_autotune_cache_read_and_write(lib, tmp_path):
+    """The autotune cache file: a key is absent until written, the latest write of a key wins, other keys
+    (grid, source knobs, GPU model) are kept apart, and GPU names with blanks are stored as one token."""
+    path = str(tmp_path / "sub" / "tune.txt").encode()
+    v, lv, ms = C.c_int32(-1), C.c_int32(0), C.c_double(0.0)
+
+    def get(im, jm, km, knobs, gpu):
+        return lib.atsat_dyn_tune_cache_get(path, im, jm, km, knobs, gpu, C.byref(v), C.byref(lv), C.byref(ms))
+
+    assert get(41, 181, 361, 5, b"NVIDIA GB300") == abi.E_INVALID
+    assert lib.atsat_dyn_tune_cache_put(path, 41, 181, 361, 5, b"NVIDIA GB300", 7, 39, 0.25) == abi.OK
+    assert lib.atsat_dyn_tune_cache_put(path, 21, 91, 181, 5, b"NVIDIA GB300", 6, 0, 0.05) == abi.E_INVALID
+    assert lib.atsat_dyn_tune_cache_put(path, 21, 91, 181, 5, b"NVIDIA GB300", 7, 4, 0.05) == abi.OK
+    assert get(41, 181, 361, 5, b"NVIDIA GB300") == abi.OK and (v.value, lv.value) == (7, 39)
+    assert abs(ms.value - 0.25) < 1e-9
+    assert get(41, 181, 361, 1, b"NVIDIA GB300") == abi.E_INVALID
+    assert get(41, 181, 361, 5, b"NVIDIA B200") == abi.E_INVALID
+    assert lib.atsat_dyn_tune_cache_put(path, 41, 181, 361, 5, b"NVIDIA GB300", 6, 20, 0.30) == abi.OK
+    assert get(41, 181, 361, 5, b"NVIDIA GB300") == abi.OK and (v.value, lv.value) == (6, 20)
+    assert get(21, 91, 181, 5, b"NVIDIA GB300") == abi.OK and (v.value, lv.value) == (7, 4)
+    lines = open(path.decode()).read().splitlines()
+    assert len(lines) == 2 and all("NVIDIA_GB300" in ln for ln in lines)

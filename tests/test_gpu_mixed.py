@@ -29,10 +29,10 @@ def drift(got, ref, fids):
     return out
 
 
-DIRECT, TILED, SPLIT, SPLIT3, SPLIT13, SPLIT_TILED, TILED2 = range(7)
+DIRECT, TILED, SPLIT, SPLIT3, SPLIT13, SPLIT_TILED, TILED2, MARCH = range(8)
 VARIANTS = [pytest.param(v, id=n) for v, n in
             [(TILED, "tiled"), (DIRECT, "direct"), (SPLIT, "split"), (SPLIT3, "split3"), (SPLIT13, "split13"),
-             (SPLIT_TILED, "split_tiled"), (TILED2, "tiled2")]]
+             (SPLIT_TILED, "split_tiled"), (TILED2, "tiled2"), (MARCH, "march")]]
 
 _REF = {}
 
@@ -231,6 +231,49 @@ def test_stage_variants_agree(variant):
     assert not bad, bad
 
 
+@pytest.mark.parametrize("shape,levels", [((21, 91, 181), 1), ((21, 91, 181), 2), ((21, 91, 181), 5),
+                                          ((21, 91, 181), 19), ((12, 40, 70), 3), ((10, 20, 36), 8)])
+def test_march_depths_agree(shape, levels):
+    """The radial march at several march depths (runs of 1 level to whole columns, runs that do not divide
+    the interior levels evenly, odd-seam grids) runs the same per-cell arithmetic as the direct kernel:
+    after three iterations their states agree far inside the mixed-precision bar."""
+    from atsat_gb300 import dyn
+    g, P, st = case(shape, seed=59, exercise=True)
+    a = st.copy()
+    with dyn.Dycore(g, dict(P, precision=1)) as d:
+        d.set_stage_variant(MARCH)
+        d.set_march_levels(levels)
+        assert d.march_levels() == levels
+        d.load_state(a)
+        d.iterate(1, 3)
+        d.download(ALL)
+    b = run_mixed(g, P, st, 3, DIRECT)
+    rep = drift(a.arrays, b.arrays, F.PROG + [F.P_DYN])
+    bad = {k: v[0] for k, v in rep.items() if not v[0] <= 1e-7}
+    assert not bad, bad
+
+
+def test_autotune_cache_starts_the_next_handle(tmp_path, monkeypatch):
+    """autotune records its choice; a second handle of the same grid starts from it with no timing pass,
+    a handle of another grid does not."""
+    from atsat_gb300 import dyn
+    monkeypatch.setenv("ATSAT_DYN_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    g, P, st = case((21, 91, 181), seed=61, exercise=True)
+    with dyn.Dycore(g, dict(P, precision=1)) as d:
+        assert not d.tuned_from_cache()
+        d.load_state(st.copy())
+        chosen, ms = d.autotune(reps=2)
+        levels = d.march_levels()
+    assert (tmp_path / "tune.txt").exists()
+    with dyn.Dycore(g, dict(P, precision=1)) as d:
+        assert d.tuned_from_cache()
+        assert d.stage_variant() == chosen and d.march_levels() == levels
+        assert d.launches() == 0
+    g2, P2, _ = case((9, 13, 17), seed=61, exercise=True)
+    with dyn.Dycore(g2, dict(P2, precision=1)) as d:
+        assert not d.tuned_from_cache()
+
+
 def test_split_unavailable_with_species_divu():
     """The split kernels leave the divergence term to the fused kernels: asking for them with
     species_divu on is refused, and the default variant still runs."""
@@ -241,6 +284,7 @@ def test_split_unavailable_with_species_divu():
             d.set_stage_variant(SPLIT)
         chosen, ms = d.autotune(reps=2)
         assert chosen in (DIRECT, TILED) and ms[SPLIT] < 0 and ms[SPLIT13] < 0 and ms[SPLIT_TILED] < 0 and ms[TILED2] < 0
+        assert ms[MARCH] < 0
 
 
 def test_autotune_keeps_state():
@@ -250,6 +294,7 @@ def test_autotune_keeps_state():
     g, P, st = case((21, 91, 181), seed=61, exercise=True)
     s = st.copy()
     with dyn.Dycore(g, dict(P, precision=1)) as d:
+        d.set_stage_variant(TILED)
         d.load_state(s)
         d.iterate(1, 2)
         d.download(ALL)

@@ -66,39 +66,79 @@ def test_refine_and_fp32(shape):
         assert er <= 1e-8
 
 
-def test_sor_matches_red_black_reference():
-    """Five red-black sweeps (omega = 1, the reference's update) from p = 0 against a numpy sweep of the
-    same operator; more sweeps lower the residual (slowly: the horizontal modes are weakly coupled), in
-    FP64 and FP32 alike."""
-    from atsat_gb300 import dyn
-    g, P, A, src = problem((9, 13, 17))
+def numpy_sweeps(g, P, f, sweeps, omega=1.0):
+    """The reference's red-black update (over-relaxed by omega), then the boundary fold, per sweep."""
     num1, num2, num3, den = PR.weights(g, P)
-    with dyn.Dycore(g, P) as d:
-        f = d.poisson_project(src)
-        p_gpu, st = d.poisson_solve("sor64", f, tol=0.0, max_iter=5, omega=1.0)
-        _, st10 = d.poisson_solve("sor64", f, tol=0.0, max_iter=400, omega=1.0)
-        _, st32 = d.poisson_solve("sor32", f, tol=0.0, max_iter=400, omega=1.0)
     im, jm, km = g.shape
     n = km - 1
     p = np.zeros(g.shape)
     ii, jj, kk = np.meshgrid(np.arange(1, im - 1), np.arange(1, jm - 1), np.arange(n), indexing="ij")
-    for _ in range(5):
+    for _ in range(sweeps):
         for colour in (0, 1):
             m = ((ii + jj + kk) & 1) == colour
             i, j, k = ii[m], jj[m], kk[m]
             kw, ke = (k - 1) % n, (k + 1) % n
             acc = (p[i + 1, j, k] + p[i - 1, j, k]) * num1[i, j] + (p[i, j + 1, k] + p[i, j - 1, k]) * num2[i, j] \
                 + (p[i, j, ke] + p[i, j, kw]) * num3[i, j]
-            p[i, j, k] = (acc - f[i, j, k]) / den[i, j]
+            p[i, j, k] = p[i, j, k] + omega * ((acc - f[i, j, k]) / den[i, j] - p[i, j, k])
         p[0] = 4 / 3 * p[1] - 1 / 3 * p[2]
         p[-1] = 4 / 3 * p[-2] - 1 / 3 * p[-3]
         p[:, 0] = 4 / 3 * p[:, 1] - 1 / 3 * p[:, 2]
         p[:, -1] = 4 / 3 * p[:, -2] - 1 / 3 * p[:, -3]
         p[:, :, -1] = p[:, :, 0]
     p -= p[1:-1, 1:-1, :n].mean()
-    err = np.max(np.abs(p[1:-1, 1:-1, :n] - p_gpu[1:-1, 1:-1, :n])) / np.max(np.abs(p))
-    print(f"\nsor64 x5 vs numpy: {err:.2e}; residual after 5 / 400 sweeps {st['rel_residual']:.3e} /"
-          f" {st10['rel_residual']:.3e}, fp32 400 sweeps {st32['rel_residual']:.3e}")
-    assert err <= 1e-12
+    return p
+
+
+@pytest.mark.parametrize("shape", [(9, 13, 17), (12, 24, 33)])
+def test_sor_matches_red_black_reference(shape):
+    """Red-black sweeps (omega = 1, the reference's update) from p = 0 against a numpy sweep of the same
+    operator: 5 sweeps, and 53 (more than one launch of the packed solver's 50-sweep runs, its packed state
+    carried from one to the next); more sweeps lower the residual (slowly: the horizontal modes are weakly
+    coupled), in FP64 and FP32 alike."""
+    from atsat_gb300 import dyn
+    g, P, A, src = problem(shape)
+    with dyn.Dycore(g, P) as d:
+        f = d.poisson_project(src)
+        p_gpu, st = d.poisson_solve("sor64", f, tol=0.0, max_iter=5, omega=1.0)
+        p53, _ = d.poisson_solve("sor64", f, tol=0.0, max_iter=53, omega=1.0)
+        p53_32, _ = d.poisson_solve("sor32", f, tol=0.0, max_iter=53, omega=1.0)
+        _, st10 = d.poisson_solve("sor64", f, tol=0.0, max_iter=400, omega=1.0)
+        _, st32 = d.poisson_solve("sor32", f, tol=0.0, max_iter=400, omega=1.0)
+    n = g.km - 1
+    c = (slice(1, -1), slice(1, -1), slice(0, n))
+    p = numpy_sweeps(g, P, f, 5)
+    err = np.max(np.abs(p[c] - p_gpu[c])) / np.max(np.abs(p))
+    q = numpy_sweeps(g, P, f, 53)
+    err53 = np.max(np.abs(q[c] - p53[c])) / np.max(np.abs(q))
+    err53_32 = np.max(np.abs(q[c] - p53_32[c])) / np.max(np.abs(q))
+    print(f"\n{shape} sor64 x5 / x53 vs numpy: {err:.2e} / {err53:.2e}, sor32 x53 {err53_32:.2e}; residual after"
+          f" 5 / 400 sweeps {st['rel_residual']:.3e} / {st10['rel_residual']:.3e}, fp32 400 sweeps"
+          f" {st32['rel_residual']:.3e}")
+    assert err <= 1e-12 and err53 <= 1e-12
+    assert err53_32 <= 1e-5
+    # the folded boundary planes and the seam as the reference leaves them
+    assert np.allclose(p53[0], 4 / 3 * p53[1] - 1 / 3 * p53[2], rtol=0, atol=1e-12 * np.max(np.abs(p53)))
+    assert np.array_equal(p53[:, :, -1], p53[:, :, 0])
     assert st10["rel_residual"] < st["rel_residual"] < 1.0
     assert abs(st32["rel_residual"] - st10["rel_residual"]) <= 1e-3 * st10["rel_residual"]
+
+
+def test_sor_over_relaxed_and_refined():
+    """omega = 1.2 against numpy over 60 sweeps, and FP64 defect correction around FP32 SOR sweeps (two
+    corrections of 200 sweeps) runs its inner sweeps and lowers the residual."""
+    from atsat_gb300 import dyn
+    g, P, A, src = problem((12, 24, 33))
+    with dyn.Dycore(g, P) as d:
+        f = d.poisson_project(src)
+        p15, _ = d.poisson_solve("sor64", f, tol=0.0, max_iter=60, omega=1.2)
+        _, s32 = d.poisson_solve("sor32", f, tol=0.0, max_iter=400, omega=1.0)
+        _, sr = d.poisson_solve("refine_sor", f, tol=0.0, max_iter=2, inner=200, omega=1.0)
+    n = g.km - 1
+    c = (slice(1, -1), slice(1, -1), slice(0, n))
+    q = numpy_sweeps(g, P, f, 60, omega=1.2)
+    err = np.max(np.abs(q[c] - p15[c])) / np.max(np.abs(q))
+    print(f"\nomega 1.2 x60 vs numpy {err:.2e}; sor32 x400 residual {s32['rel_residual']:.3e}, refine_sor 2 x 200"
+          f" {sr['rel_residual']:.3e}")
+    assert err <= 1e-11
+    assert sr["inner"] == 400 and sr["rel_residual"] < 1.0

@@ -26,7 +26,7 @@ def test_bounded_wait_runs_out_and_the_handle_recovers():
     ref = st.copy()
     oracle.steps(ref, P, 2)
     with dyn.Dycore(g, dict(P, precision=1)) as d:
-        assert d.stage_variant() == dyn.Dycore.STAGE_TILED2
+        assert d.stage_variant() == dyn.Dycore.STAGE_MARCH
         d.load_state(st.copy())
         assert d.timeouts() == 0
         d.set_wait_test(clocks=1 << 20, withhold=1)
