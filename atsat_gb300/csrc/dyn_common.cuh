@@ -392,7 +392,7 @@ cudaError_t launch_density(const KConst& kc, const double* t, const double* p_st
                            double* rho, cudaStream_t s);
 // the level mean and the metric pressure in one pass (im <= CS_MAX_IM); `partial` holds
 // 2 * im * column_scan_blocks() doubles
-constexpr int CS_MAX_IM = 256;
+constexpr int CS_MAX_IM = 64;    // 70 KB of shared memory per block at the limit
 int column_scan_blocks(const KConst& kc);
 cudaError_t launch_column_scan(const KConst& kc, const double* t, const double* p_stat, const double* v,
                                const double* w, const double* sin_j, const double* inv_rm, const double* cor_j,

@@ -409,11 +409,14 @@ __global__ void __launch_bounds__(128) metric_scan_kernel(const KConst K, const 
 // ---- computeBuoyancyRefLevel and computeMetricPressure in one pass (RungeKutta_Sat_Turb.cpp:31-108) ----
 // Both walk every (j, k) column over i at the start of a step and read y_n only (t, p_stat for the level
 // mean; v, w for the metric scan), so one kernel reads the four fields once. A thread owns a column and
-// scans it as metric_scan_kernel does; per level its warp (one row j, 32 meridians) sums p / t over its
-// lanes by shuffles, the row's weight sin(theta_j) is applied once, and each warp's per-level sums go to
-// shared memory. At the end the block adds its four rows per level and writes one partial pair per level;
-// level_sum_kernel adds the blocks in a fixed order (deterministic). Dynamic shared memory: im x 4 x 2
-// doubles, so the fused path is used for im <= CS_MAX_IM.
+// scans it as metric_scan_kernel does. For the level mean each lane parks its cell's p / t per level in
+// shared memory; at the end the block adds them up per (level, row) -- 31 adds for 32 cells, each by one
+// thread in lane order -- applies the row's weight sin(theta_j), adds its four rows and writes one partial
+// pair per level; level_sum_kernel adds the blocks in a fixed order (deterministic). GB300 runs FP64 at
+// two operations per SM per cycle, so a butterfly of shuffles per level (five adds on all 32 lanes) would
+// cost five times the additions this needs. Cells counted go by ballot; the rare cells outside the fast
+// path (t or p out of range) by a shuffle sum taken only when a warp has one. Dynamic shared memory:
+// im x 4 x (32 + 2) doubles, so the fused path is used for im <= CS_MAX_IM.
 constexpr int CS_ROWS = 4;
 
 __device__ __forceinline__ double warp_sum(double x) {
@@ -432,7 +435,9 @@ __global__ void __launch_bounds__(32 * CS_ROWS) column_scan_kernel(const KConst 
                                                                   const double* __restrict__ p_baro,
                                                                   double* __restrict__ pm, double half_dr,
                                                                   double* __restrict__ partial) {
-    extern __shared__ double s_lev[];                 // [im][CS_ROWS][2]
+    extern __shared__ double s_cs[];
+    double* s_rs = s_cs;                                   // [im][CS_ROWS][32]: p / t per cell
+    double* s_rr = s_cs + (size_t)K.im * CS_ROWS * 32;     // [im][CS_ROWS][2]: the rest's sum, cells counted
     const int lane = threadIdx.x, row = threadIdx.y;
     const int k = blockIdx.x * 32 + lane;
     const int j = blockIdx.y * CS_ROWS + row;
@@ -440,13 +445,13 @@ __global__ void __launch_bounds__(32 * CS_ROWS) column_scan_kernel(const KConst 
     const bool in = kin && jin;
     const bool bc_ok = fabs(K.buoy_c) < 0x1p256;
     const double cor = jin ? __ldg(cor_j + j) : 0.0;
-    const double wgt = jin ? __ldg(sin_j + j) : 0.0;
     const int64_t c0 = (int64_t)(jin ? j : 0) * K.kp + (kin ? k : 0);
     double f_prev = 0.0, acc = 0.0;
-    for (int i0 = 0; i0 < K.im; i0 += MS_BATCH) {
-        double tt[MS_BATCH], pp[MS_BATCH], vv[MS_BATCH], ww[MS_BATCH], pb[MS_BATCH];
+    constexpr int B = 4;
+    for (int i0 = 0; i0 < K.im; i0 += B) {
+        double tt[B], pp[B], vv[B], ww[B], pb[B];
 #pragma unroll
-        for (int q = 0; q < MS_BATCH; q++) {
+        for (int q = 0; q < B; q++) {
             const int64_t c = c0 + (int64_t)(i0 + q) * K.plane;
             const bool ok = in && i0 + q < K.im;
             tt[q] = ok ? __ldg(t + c) : 0.0;
@@ -456,7 +461,7 @@ __global__ void __launch_bounds__(32 * CS_ROWS) column_scan_kernel(const KConst 
             pb[q] = (ok && p_baro) ? __ldg(p_baro + c) : 0.0;
         }
 #pragma unroll
-        for (int q = 0; q < MS_BATCH; q++) {
+        for (int q = 0; q < B; q++) {
             const int i = i0 + q;
             if (i >= K.im) break;
             // metric pressure, as metric_scan_kernel
@@ -465,36 +470,45 @@ __global__ void __launch_bounds__(32 * CS_ROWS) column_scan_kernel(const KConst 
             f_prev = f;
             if (in) pm[c0 + (int64_t)i * K.plane] = p_baro ? acc + pb[q] : acc;
             // the level mean's cell, as level_mean_partial_kernel
-            double rs = 0.0, rest = 0.0, cnt = 0.0;
+            double rs = 0.0, rest = 0.0;
+            bool counted = false, slow = false;
             if (in) {
                 if (bc_ok && in_rcp_range(tt[q]) && moderate(pp[q])) {
                     rs = pp[q] * recip_nr(tt[q]);
-                    cnt = 1.0;
+                    counted = true;
                 } else {
                     double b;
+                    slow = true;
                     if (cell_buoyancy(K, tt[q], pp[q], b)) {
                         rest = b;
-                        cnt = 1.0;
+                        counted = true;
                     }
                 }
             }
-            rs = warp_sum(rs);
-            rest = warp_sum(rest);
-            cnt = warp_sum(cnt);
+            s_rs[((size_t)i * CS_ROWS + row) * 32 + lane] = rs;
+            const unsigned n = __popc(__ballot_sync(0xffffffffu, counted));
+            if (__any_sync(0xffffffffu, slow)) rest = warp_sum(rest);
             if (lane == 0) {
-                s_lev[(i * CS_ROWS + row) * 2 + 0] = wgt * fma(K.buoy_c, rs, rest);
-                s_lev[(i * CS_ROWS + row) * 2 + 1] = wgt * cnt;
+                s_rr[((size_t)i * CS_ROWS + row) * 2 + 0] = rest;
+                s_rr[((size_t)i * CS_ROWS + row) * 2 + 1] = (double)n;
             }
         }
     }
     __syncthreads();
+    // per level: the four rows' sums, each added over its 32 cells in lane order
     const int nb = gridDim.x * gridDim.y, b = blockIdx.y * gridDim.x + blockIdx.x;
     for (int i = threadIdx.y * 32 + threadIdx.x; i < K.im; i += 32 * CS_ROWS) {
         double a = 0.0, m = 0.0;
 #pragma unroll
         for (int r = 0; r < CS_ROWS; r++) {
-            a += s_lev[(i * CS_ROWS + r) * 2 + 0];
-            m += s_lev[(i * CS_ROWS + r) * 2 + 1];
+            const int jr = blockIdx.y * CS_ROWS + r;
+            if (jr >= K.jm) break;
+            const double* x = s_rs + ((size_t)i * CS_ROWS + r) * 32;
+            double rs = 0.0;
+            for (int l = 0; l < 32; l++) rs += x[l];
+            const double wgt = __ldg(sin_j + jr);
+            a = fma(wgt, fma(K.buoy_c, rs, s_rr[((size_t)i * CS_ROWS + r) * 2 + 0]), a);
+            m = fma(wgt, s_rr[((size_t)i * CS_ROWS + r) * 2 + 1], m);
         }
         partial[((int64_t)i * nb + b) * 2 + 0] = a;
         partial[((int64_t)i * nb + b) * 2 + 1] = m;
@@ -587,7 +601,12 @@ cudaError_t launch_column_scan(const KConst& kc, const double* t, const double* 
                                const double* p_baro, double* p_metric, double* partial, double* buoy, cudaStream_t s) {
     if (kc.im > CS_MAX_IM) return cudaErrorInvalidValue;
     const dim3 block(32, CS_ROWS), grid((kc.km + 31) / 32, (kc.jm + CS_ROWS - 1) / CS_ROWS);
-    const size_t smem = (size_t)kc.im * CS_ROWS * 2 * sizeof(double);
+    const size_t smem = (size_t)kc.im * CS_ROWS * (32 + 2) * sizeof(double);
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(column_scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem);
+        if (e != cudaSuccess) return e;
+    }
     column_scan_kernel<<<grid, block, smem, s>>>(kc, t, p_stat, v, w, sin_j, inv_rm, cor_j, p_baro, p_metric,
                                                  0.5 * kc.dr, partial);
     level_sum_kernel<<<kc.im, 256, 0, s>>>(kc, partial, column_scan_blocks(kc), buoy);
