@@ -56,6 +56,8 @@ def parse():
                     choices=["auto", "direct", "tiled", "split", "split3", "split13", "split_tiled", "tiled2",
                              "march"],
                     help="mixed precision: the RK stage kernel (auto: the autotuner's choice)")
+    ap.add_argument("--march-levels", type=int, default=0,
+                    help="with --stage-variant march: radial levels per block (0: the library's default)")
     ap.add_argument("--poisson", action="store_true",
                     help="the standalone pressure-equation solves instead of the dycore iteration")
     ap.add_argument("--sor-sweeps", type=int, default=4000)
@@ -303,7 +305,9 @@ def measure(a, rank, world, g, P, st, pinned, precision):
                 "autotune_ms_per_stage": {n: (t if t > 0 else None) for n, t in zip(dyn.Dycore.STAGE_NAMES, tms)}}
     elif precision == "mixed":
         d.set_stage_variant(dyn.Dycore.STAGE_NAMES.index(a.stage_variant))
-        tune = {"stage_variant": a.stage_variant}
+        if a.stage_variant == "march" and a.march_levels > 0:
+            d.set_march_levels(a.march_levels)
+        tune = {"stage_variant": a.stage_variant, "march_levels": d.march_levels()}
     it0 = a.warmup + 1
     # the timed region profiles the RK stage kernels only (the roofline's kernel): two event records per
     # stage launch; every class is timed afterwards in a separate pass of its own
