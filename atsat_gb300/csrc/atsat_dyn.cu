@@ -43,6 +43,7 @@ struct atsat_dyn {
     cudaStream_t stream = nullptr;
 
     double* slab = nullptr;              // one allocation for every device array below
+    int64_t n64 = 0;                     // fsz-sized FP64 arrays at the head of the slab
     double* f[ATSAT_NFIELDS] = {};
     double* stage[NPROG] = {};
     double* acc[NPROG] = {};
@@ -86,6 +87,9 @@ struct atsat_dyn {
     // stream, and per buffer an event for "copy landed / re-pitched out" and one for "free again"
     double* dstage[2] = {};
     cudaStream_t cstream = nullptr;
+    // the second stream of the step's start (the metric scan beside the level mean) and its fork / join
+    cudaStream_t astream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_ajoin = nullptr;
     cudaEvent_t ev_ready[2] = {}, ev_free[2] = {}, ev_join = nullptr;
     int stage_next = 0;
     // bindings the SMs move in place (host_xfer.cu): host_ok when the device addresses host memory
@@ -526,8 +530,17 @@ bool make_tile_maps(atsat_dyn* h) {
     const CUresult r9 = enc(reinterpret_cast<CUtensorMap*>(h->maps.pt1), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
                             h->slab32, dims, strides, box_pt1, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    // the FP64 fields (slab, fsz doubles apart) for the tracer kernel's final-stage y_n boxes
+    if ((reinterpret_cast<uintptr_t>(h->slab) & 15u) != 0) return false;
+    const cuuint64_t dims64[4] = {(cuuint64_t)K.kp, (cuuint64_t)K.jm, (cuuint64_t)K.im, (cuuint64_t)h->n64};
+    const cuuint64_t strides64[3] = {(cuuint64_t)K.kp * 8, (cuuint64_t)K.plane * 8, (cuuint64_t)K.fsz * 8};
+    const cuuint32_t box_pt2_f64[4] = {TILE_K, TILE_J, 2, 1};
+    const CUresult r10 = enc(reinterpret_cast<CUtensorMap*>(h->maps.pt2_f64), CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4,
+                             h->slab, dims64, strides64, box_pt2_f64, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r1 == CUDA_SUCCESS && r2 == CUDA_SUCCESS && r3 == CUDA_SUCCESS && r4 == CUDA_SUCCESS && r5 == CUDA_SUCCESS &&
-           r6 == CUDA_SUCCESS && r7 == CUDA_SUCCESS && r8 == CUDA_SUCCESS && r9 == CUDA_SUCCESS;
+           r6 == CUDA_SUCCESS && r7 == CUDA_SUCCESS && r8 == CUDA_SUCCESS && r9 == CUDA_SUCCESS && r10 == CUDA_SUCCESS;
 }
 
 bool valid_field(int f) { return f >= 0 && f < ATSAT_NFIELDS; }
@@ -834,19 +847,26 @@ int do_metric(atsat_dyn* h) {
     return ATSAT_DYN_OK;
 }
 
-// the start of a step: the buoyancy level mean, and the metric pressure where metric_split is on, fused
-// into one pass over the columns where the grid allows
+// the start of a step: the buoyancy level mean and, where metric_split is on, the metric pressure. Both
+// read y_n only and are latency-bound scans (GB300's FP64 pipe sets their pace, not HBM), so the metric scan
+// runs on a second stream beside the level mean, forked from and joined back into the handle's stream by
+// events (CUDA-graph capture records the fork and the join).
 int do_level_metric(atsat_dyn* h) {
     if (!h->p.metric_split) return do_level_mean(h);
-    if (h->kc.im > CS_MAX_IM) {
-        const int rc = do_level_mean(h);
-        return rc ? rc : do_metric(h);
+    if (!h->astream) {
+        CK(h, cudaStreamCreateWithFlags(&h->astream, cudaStreamNonBlocking));
+        CK(h, cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+        CK(h, cudaEventCreateWithFlags(&h->ev_ajoin, cudaEventDisableTiming));
     }
     Timed t(h, ATSAT_K_LEVEL_MEAN);
-    CK(h, launch_column_scan(h->kc, h->f[ATSAT_F_T], h->f[ATSAT_F_P_STAT], h->f[ATSAT_F_V], h->f[ATSAT_F_W],
-                             h->sin_j, h->rm_tab, h->cor_j, h->has_pbaro ? h->p_baro : nullptr,
-                             h->f[ATSAT_F_P_METRIC], h->partial, h->buoy, h->stream));
-    h->launches += 2;
+    CK(h, cudaEventRecord(h->ev_fork, h->stream));
+    CK(h, cudaStreamWaitEvent(h->astream, h->ev_fork, 0));
+    CK(h, launch_metric_scan(h->kc, h->f[ATSAT_F_V], h->f[ATSAT_F_W], h->rm_tab, h->cor_j,
+                             h->has_pbaro ? h->p_baro : nullptr, h->f[ATSAT_F_P_METRIC], h->astream));
+    CK(h, launch_level_mean(h->kc, h->f[ATSAT_F_T], h->f[ATSAT_F_P_STAT], h->sin_j, h->partial, h->buoy, h->stream));
+    CK(h, cudaEventRecord(h->ev_ajoin, h->astream));
+    CK(h, cudaStreamWaitEvent(h->stream, h->ev_ajoin, 0));
+    h->launches += 3;
     return ATSAT_DYN_OK;
 }
 
@@ -1042,6 +1062,16 @@ TracerPlan make_plan_tracer(atsat_dyn* h, const MixedIO& io, int mode) {
         }
         if (turb) add(io.acc_turb[q - ATSAT_F_TKE], 1);
         else if (mode == MODE_FINAL) { add(io.dl1[q], 1); add(io.dl2[q], 1); }
+        if (mode == MODE_FINAL) {
+            // y_n in FP64, two boxes of two levels (kinds 2, 3), indexed among the FP64 fields
+            for (int half = 0; half < 2; half++) {
+                if (n < TRACER_MAX_ITEMS) {
+                    pl.arr[n] = (int)((io.yn64[q] - h->slab) / h->kc.fsz);
+                    pl.kind[n] = (unsigned char)(2 + half);
+                }
+                n++;
+            }
+        }
     }
     pl.n_items = n;
     return pl;
@@ -1322,10 +1352,6 @@ int enqueue_rk4_mixed(atsat_dyn* h, bool resident) {
         Timed t(h, ATSAT_K_RK_STAGE);
         CK(h, launch_stage(h, io, sp, stage == 3 ? MODE_FINAL : MODE_STAGE));
         h->launches += launches_per_stage(h);
-        // the TMA-tiled tracer kernel leaves the final stage's FP64 sum to launch_final_combine
-        const int v = variant_available(h, h->variant) ? h->variant : ATSAT_DYN_STAGE_DIRECT;
-        if (stage == 3 && (v == ATSAT_DYN_STAGE_SPLIT_TILED || v == ATSAT_DYN_STAGE_TILED2 || v == ATSAT_DYN_STAGE_MARCH))
-            h->launches += 1;
     }
     return ATSAT_DYN_OK;
 }
@@ -1839,8 +1865,8 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
     // fields, FP64 stage buffers and accumulators (FP64 path only), source; then the small tables
     const bool fp64_stage = p->precision != ATSAT_DYN_MIXED;
     const int64_t nbig = ATSAT_NFIELDS + (fp64_stage ? 2 * NPROG : 0) + 2;
-    const int64_t n_partial = std::max<int64_t>(2LL * K.im * 16, 2LL * K.im * column_scan_blocks(K));
-    const int64_t nsmall = n_partial + K.im + K.jm + K.im + K.jm + 64;
+    h->n64 = nbig;
+    const int64_t nsmall = 2LL * K.im * 16 + K.im + K.jm + K.im + K.jm + 64;
     const size_t bytes = (size_t)(nbig * K.fsz + nsmall) * 8 + sizeof(ColGeo) * (size_t)K.im * K.jm + 4096;
     if ((e = cudaMalloc(&h->slab, bytes)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
     if ((e = cudaMemsetAsync(h->slab, 0, bytes, h->stream)) != cudaSuccess) return cuda_fail(e, "cudaMemset");
@@ -1852,7 +1878,7 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
     }
     h->src = q; q += K.fsz;
     h->p_baro = q; q += K.fsz;
-    h->partial = q; q += n_partial;
+    h->partial = q; q += 2LL * K.im * 16;
     h->buoy = q; q += K.im;
     h->sin_j = q; q += K.jm;
     h->rm_tab = q; q += K.im;
@@ -1956,6 +1982,12 @@ void atsat_dyn_destroy(atsat_dyn_t h) {
     stage_pipe_free(h);
     for (int f = 0; f < ATSAT_NFIELDS; f++)
         if (h->dev_rows[f]) cudaFree(h->dev_rows[f]);
+    if (h->astream) {
+        cudaStreamSynchronize(h->astream);
+        cudaStreamDestroy(h->astream);
+    }
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_ajoin) cudaEventDestroy(h->ev_ajoin);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }

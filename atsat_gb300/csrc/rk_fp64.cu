@@ -406,138 +406,6 @@ __global__ void __launch_bounds__(128) metric_scan_kernel(const KConst K, const 
     }
 }
 
-// ---- computeBuoyancyRefLevel and computeMetricPressure in one pass (RungeKutta_Sat_Turb.cpp:31-108) ----
-// Both walk every (j, k) column over i at the start of a step and read y_n only (t, p_stat for the level
-// mean; v, w for the metric scan), so one kernel reads the four fields once. A thread owns a column and
-// scans it as metric_scan_kernel does. For the level mean each lane parks its cell's p / t per level in
-// shared memory; at the end the block adds them up per (level, row) -- 31 adds for 32 cells, each by one
-// thread in lane order -- applies the row's weight sin(theta_j), adds its four rows and writes one partial
-// pair per level; level_sum_kernel adds the blocks in a fixed order (deterministic). GB300 runs FP64 at
-// two operations per SM per cycle, so a butterfly of shuffles per level (five adds on all 32 lanes) would
-// cost five times the additions this needs. Cells counted go by ballot; the rare cells outside the fast
-// path (t or p out of range) by a shuffle sum taken only when a warp has one. Dynamic shared memory:
-// im x 4 x (32 + 2) doubles, so the fused path is used for im <= CS_MAX_IM.
-constexpr int CS_ROWS = 4;
-
-__device__ __forceinline__ double warp_sum(double x) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    return x;
-}
-
-__global__ void __launch_bounds__(32 * CS_ROWS) column_scan_kernel(const KConst K, const double* __restrict__ t,
-                                                                  const double* __restrict__ ps,
-                                                                  const double* __restrict__ v,
-                                                                  const double* __restrict__ w,
-                                                                  const double* __restrict__ sin_j,
-                                                                  const double* __restrict__ inv_rm,
-                                                                  const double* __restrict__ cor_j,
-                                                                  const double* __restrict__ p_baro,
-                                                                  double* __restrict__ pm, double half_dr,
-                                                                  double* __restrict__ partial) {
-    extern __shared__ double s_cs[];
-    double* s_rs = s_cs;                                   // [im][CS_ROWS][32]: p / t per cell
-    double* s_rr = s_cs + (size_t)K.im * CS_ROWS * 32;     // [im][CS_ROWS][2]: the rest's sum, cells counted
-    const int lane = threadIdx.x, row = threadIdx.y;
-    const int k = blockIdx.x * 32 + lane;
-    const int j = blockIdx.y * CS_ROWS + row;
-    const bool kin = k < K.km, jin = j < K.jm;
-    const bool in = kin && jin;
-    const bool bc_ok = fabs(K.buoy_c) < 0x1p256;
-    const double cor = jin ? __ldg(cor_j + j) : 0.0;
-    const int64_t c0 = (int64_t)(jin ? j : 0) * K.kp + (kin ? k : 0);
-    double f_prev = 0.0, acc = 0.0;
-    constexpr int B = 4;
-    for (int i0 = 0; i0 < K.im; i0 += B) {
-        double tt[B], pp[B], vv[B], ww[B], pb[B];
-#pragma unroll
-        for (int q = 0; q < B; q++) {
-            const int64_t c = c0 + (int64_t)(i0 + q) * K.plane;
-            const bool ok = in && i0 + q < K.im;
-            tt[q] = ok ? __ldg(t + c) : 0.0;
-            pp[q] = ok ? __ldg(ps + c) : 0.0;
-            vv[q] = ok ? __ldg(v + c) : 0.0;
-            ww[q] = ok ? __ldg(w + c) : 0.0;
-            pb[q] = (ok && p_baro) ? __ldg(p_baro + c) : 0.0;
-        }
-#pragma unroll
-        for (int q = 0; q < B; q++) {
-            const int i = i0 + q;
-            if (i >= K.im) break;
-            // metric pressure, as metric_scan_kernel
-            const double f = fma(fma(ww[q], ww[q], vv[q] * vv[q]), __ldg(inv_rm + i), cor * ww[q]);
-            if (i > 0) acc = fma(half_dr, f_prev + f, acc);
-            f_prev = f;
-            if (in) pm[c0 + (int64_t)i * K.plane] = p_baro ? acc + pb[q] : acc;
-            // the level mean's cell, as level_mean_partial_kernel
-            double rs = 0.0, rest = 0.0;
-            bool counted = false, slow = false;
-            if (in) {
-                if (bc_ok && in_rcp_range(tt[q]) && moderate(pp[q])) {
-                    rs = pp[q] * recip_nr(tt[q]);
-                    counted = true;
-                } else {
-                    double b;
-                    slow = true;
-                    if (cell_buoyancy(K, tt[q], pp[q], b)) {
-                        rest = b;
-                        counted = true;
-                    }
-                }
-            }
-            s_rs[((size_t)i * CS_ROWS + row) * 32 + lane] = rs;
-            const unsigned n = __popc(__ballot_sync(0xffffffffu, counted));
-            if (__any_sync(0xffffffffu, slow)) rest = warp_sum(rest);
-            if (lane == 0) {
-                s_rr[((size_t)i * CS_ROWS + row) * 2 + 0] = rest;
-                s_rr[((size_t)i * CS_ROWS + row) * 2 + 1] = (double)n;
-            }
-        }
-    }
-    __syncthreads();
-    // per level: the four rows' sums, each added over its 32 cells in lane order
-    const int nb = gridDim.x * gridDim.y, b = blockIdx.y * gridDim.x + blockIdx.x;
-    for (int i = threadIdx.y * 32 + threadIdx.x; i < K.im; i += 32 * CS_ROWS) {
-        double a = 0.0, m = 0.0;
-#pragma unroll
-        for (int r = 0; r < CS_ROWS; r++) {
-            const int jr = blockIdx.y * CS_ROWS + r;
-            if (jr >= K.jm) break;
-            const double* x = s_rs + ((size_t)i * CS_ROWS + r) * 32;
-            double rs = 0.0;
-            for (int l = 0; l < 32; l++) rs += x[l];
-            const double wgt = __ldg(sin_j + jr);
-            a = fma(wgt, fma(K.buoy_c, rs, s_rr[((size_t)i * CS_ROWS + r) * 2 + 0]), a);
-            m = fma(wgt, s_rr[((size_t)i * CS_ROWS + r) * 2 + 1], m);
-        }
-        partial[((int64_t)i * nb + b) * 2 + 0] = a;
-        partial[((int64_t)i * nb + b) * 2 + 1] = m;
-    }
-}
-
-// one block per level: the blocks' partial pairs added in a fixed order
-__global__ void __launch_bounds__(256) level_sum_kernel(const KConst K, const double* __restrict__ partial, int nb,
-                                                        double* __restrict__ buoy) {
-    const int i = blockIdx.x;
-    double a = 0.0, m = 0.0;
-    for (int b = threadIdx.x; b < nb; b += 256) {
-        a += partial[((int64_t)i * nb + b) * 2 + 0];
-        m += partial[((int64_t)i * nb + b) * 2 + 1];
-    }
-    __shared__ double sa[256], sm[256];
-    sa[threadIdx.x] = a;
-    sm[threadIdx.x] = m;
-    __syncthreads();
-    for (int h = 128; h > 0; h >>= 1) {
-        if (threadIdx.x < h) {
-            sa[threadIdx.x] += sa[threadIdx.x + h];
-            sm[threadIdx.x] += sm[threadIdx.x + h];
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) buoy[i] = (sm[0] > 0.0) ? sa[0] / sm[0] : 0.0;
-}
-
 // ---- computeMixtureDensity (Pressure_Sat.cpp:49-62) ----
 // rho = p_stat 1e5 / (R_mix t t_ref). Where t is in [2^-60, 2^60), |p_stat| < 2^60 and the constant
 // c2 = 1e5 / (R_mix t_ref) is moderate (`fast`, set by the host), rho = p_stat (c2 / t) with c2 / t the
@@ -591,25 +459,6 @@ cudaError_t launch_metric_scan(const KConst& kc, const double* v, const double* 
                                const double* cor_j, const double* p_baro, double* p_metric, cudaStream_t s) {
     dim3 block(32, 4), grid((kc.km + 31) / 32, (kc.jm + 3) / 4);
     metric_scan_kernel<<<grid, block, 0, s>>>(kc, v, w, inv_rm, cor_j, p_baro, p_metric, 0.5 * kc.dr);
-    return cudaGetLastError();
-}
-
-int column_scan_blocks(const KConst& kc) { return ((kc.km + 31) / 32) * ((kc.jm + CS_ROWS - 1) / CS_ROWS); }
-
-cudaError_t launch_column_scan(const KConst& kc, const double* t, const double* p_stat, const double* v,
-                               const double* w, const double* sin_j, const double* inv_rm, const double* cor_j,
-                               const double* p_baro, double* p_metric, double* partial, double* buoy, cudaStream_t s) {
-    if (kc.im > CS_MAX_IM) return cudaErrorInvalidValue;
-    const dim3 block(32, CS_ROWS), grid((kc.km + 31) / 32, (kc.jm + CS_ROWS - 1) / CS_ROWS);
-    const size_t smem = (size_t)kc.im * CS_ROWS * (32 + 2) * sizeof(double);
-    if (smem > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(column_scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)smem);
-        if (e != cudaSuccess) return e;
-    }
-    column_scan_kernel<<<grid, block, smem, s>>>(kc, t, p_stat, v, w, sin_j, inv_rm, cor_j, p_baro, p_metric,
-                                                 0.5 * kc.dr, partial);
-    level_sum_kernel<<<kc.im, 256, 0, s>>>(kc, partial, column_scan_blocks(kc), buoy);
     return cudaGetLastError();
 }
 
