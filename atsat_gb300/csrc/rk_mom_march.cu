@@ -208,6 +208,7 @@ rk_mom_march_kernel(const __grid_constant__ CUtensorMap map_plane, const __grid_
         prv[a] = hs[a * HP_F + o];
         cur[a] = hs[S::HG_F + a * HP_F + o];
     }
+    slot_reads_done();                   // prv is used at level 0, after plane ib-1's slot is refilled
     __syncwarp();
     if (lane == 0) mbar_arrive(rh.empty(0));
 
@@ -361,6 +362,7 @@ rk_mom_march_kernel(const __grid_constant__ CUtensorMap map_plane, const __grid_
         }
 
         // the current plane and the level's point group are done with
+        slot_reads_done();
         __syncwarp();
         if (lane == 0) {
             mbar_arrive(rh.empty(sc));
