@@ -43,7 +43,6 @@ struct atsat_dyn {
     cudaStream_t stream = nullptr;
 
     double* slab = nullptr;              // one allocation for every device array below
-    int64_t n64 = 0;                     // fsz-sized FP64 arrays at the head of the slab
     double* f[ATSAT_NFIELDS] = {};
     double* stage[NPROG] = {};
     double* acc[NPROG] = {};
@@ -530,17 +529,8 @@ bool make_tile_maps(atsat_dyn* h) {
     const CUresult r9 = enc(reinterpret_cast<CUtensorMap*>(h->maps.pt1), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
                             h->slab32, dims, strides, box_pt1, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    // the FP64 fields (slab, fsz doubles apart) for the tracer kernel's final-stage y_n boxes
-    if ((reinterpret_cast<uintptr_t>(h->slab) & 15u) != 0) return false;
-    const cuuint64_t dims64[4] = {(cuuint64_t)K.kp, (cuuint64_t)K.jm, (cuuint64_t)K.im, (cuuint64_t)h->n64};
-    const cuuint64_t strides64[3] = {(cuuint64_t)K.kp * 8, (cuuint64_t)K.plane * 8, (cuuint64_t)K.fsz * 8};
-    const cuuint32_t box_pt2_f64[4] = {TILE_K, TILE_J, 2, 1};
-    const CUresult r10 = enc(reinterpret_cast<CUtensorMap*>(h->maps.pt2_f64), CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4,
-                             h->slab, dims64, strides64, box_pt2_f64, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r1 == CUDA_SUCCESS && r2 == CUDA_SUCCESS && r3 == CUDA_SUCCESS && r4 == CUDA_SUCCESS && r5 == CUDA_SUCCESS &&
-           r6 == CUDA_SUCCESS && r7 == CUDA_SUCCESS && r8 == CUDA_SUCCESS && r9 == CUDA_SUCCESS && r10 == CUDA_SUCCESS;
+           r6 == CUDA_SUCCESS && r7 == CUDA_SUCCESS && r8 == CUDA_SUCCESS && r9 == CUDA_SUCCESS;
 }
 
 bool valid_field(int f) { return f >= 0 && f < ATSAT_NFIELDS; }
@@ -1062,16 +1052,6 @@ TracerPlan make_plan_tracer(atsat_dyn* h, const MixedIO& io, int mode) {
         }
         if (turb) add(io.acc_turb[q - ATSAT_F_TKE], 1);
         else if (mode == MODE_FINAL) { add(io.dl1[q], 1); add(io.dl2[q], 1); }
-        if (mode == MODE_FINAL) {
-            // y_n in FP64, two boxes of two levels (kinds 2, 3), indexed among the FP64 fields
-            for (int half = 0; half < 2; half++) {
-                if (n < TRACER_MAX_ITEMS) {
-                    pl.arr[n] = (int)((io.yn64[q] - h->slab) / h->kc.fsz);
-                    pl.kind[n] = (unsigned char)(2 + half);
-                }
-                n++;
-            }
-        }
     }
     pl.n_items = n;
     return pl;
@@ -1352,6 +1332,10 @@ int enqueue_rk4_mixed(atsat_dyn* h, bool resident) {
         Timed t(h, ATSAT_K_RK_STAGE);
         CK(h, launch_stage(h, io, sp, stage == 3 ? MODE_FINAL : MODE_STAGE));
         h->launches += launches_per_stage(h);
+        // the TMA-tiled tracer kernel leaves the final stage's FP64 sum to launch_final_combine
+        const int v = variant_available(h, h->variant) ? h->variant : ATSAT_DYN_STAGE_DIRECT;
+        if (stage == 3 && (v == ATSAT_DYN_STAGE_SPLIT_TILED || v == ATSAT_DYN_STAGE_TILED2 || v == ATSAT_DYN_STAGE_MARCH))
+            h->launches += 1;
     }
     return ATSAT_DYN_OK;
 }
@@ -1865,7 +1849,6 @@ int atsat_dyn_create(const atsat_dyn_grid* g, const atsat_dyn_params* p, atsat_d
     // fields, FP64 stage buffers and accumulators (FP64 path only), source; then the small tables
     const bool fp64_stage = p->precision != ATSAT_DYN_MIXED;
     const int64_t nbig = ATSAT_NFIELDS + (fp64_stage ? 2 * NPROG : 0) + 2;
-    h->n64 = nbig;
     const int64_t nsmall = 2LL * K.im * 16 + K.im + K.jm + K.im + K.jm + 64;
     const size_t bytes = (size_t)(nbig * K.fsz + nsmall) * 8 + sizeof(ColGeo) * (size_t)K.im * K.jm + 4096;
     if ((e = cudaMalloc(&h->slab, bytes)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");

@@ -327,13 +327,11 @@ struct TileMaps {
     alignas(64) unsigned char plane1[128];  // box TILE_BX x TILE_BY x 1: one radial plane with its halo
     alignas(64) unsigned char seam1[128];   // box TILE_SEAM_X x TILE_J x 1
     alignas(64) unsigned char pt1[128];     // box TILE_K x TILE_J x 1
-    alignas(64) unsigned char pt2_f64[128]; // over the FP64 fields: box TILE_K x TILE_J x 2 doubles (4 KB)
 };
 
 // The tracer kernel's stream: every array it reads, in consumption order, each either a halo box
-// (kind 0), a point box (kind 1) or, at the final stage, half of a field's FP64 y_n box (kind 2: levels
-// i0, i0+1; kind 3: i0+2, i0+3; `arr` then indexes the FP64 fields).
-constexpr int TRACER_MAX_ITEMS = 112;
+// (kind 0) or a point box (kind 1).
+constexpr int TRACER_MAX_ITEMS = 96;
 struct TracerPlan {
     int n_items;
     int arr[TRACER_MAX_ITEMS];
@@ -409,6 +407,8 @@ size_t clamp_partial_doubles();
 cudaError_t launch_clamp_species(const KConst& kc, double* const f[11], float* const s32[11], double* added,
                                  unsigned long long* cells, double* partial, cudaStream_t s);
 
+// the final stage's FP64 half of fields q0..q1 after a tiled stage kernel (rk_mixed.cu)
+cudaError_t launch_final_combine(const MixedConstF& kf, const MixedIO& io, int q0, int q1, cudaStream_t s);
 cudaError_t launch_nonfinite_fields(const KConst& kc, const double* const* f, int n, unsigned long long* count,
                                     cudaStream_t s);
 

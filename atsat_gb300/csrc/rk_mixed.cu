@@ -322,7 +322,35 @@ cudaError_t launch_rk_split(const MixedConstF& kf, const MixedIO& io, const Stag
 
 namespace {
 
+// The final stage's FP64 half for fields q0..q1: y_{n+1} = y_n + increment, the increment formed in FP32
+// by the tiled stage kernels and left in place of dl_1 (RungeKutta_Sat_Turb.cpp:324-375), the tke / dis
+// clamps, the FP64 field, its FP32 copy and, for w, the copy's low word. A stream over the RK interior.
+__global__ void __launch_bounds__(256) final_combine_kernel(const MixedConstF K, const MixedIO io, int q0, int q1) {
+    const int k = blockIdx.x * 32 + threadIdx.x, j = 2 + blockIdx.y * 8 + threadIdx.y, i = 1 + blockIdx.z;
+    if (k > K.km - 2 || j > K.jm - 3 || i > K.im - 2) return;
+    const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
+#pragma unroll
+    for (int q = 0; q < NPROG; q++) {
+        if (q < q0 || q > q1) continue;
+        double y = ldd(io.yn64[q] + c) + f2d(io.dl1[q][c]);
+        if (q == ATSAT_F_TKE) y = smin(smax(y, 0.0), K.tke_max_d);
+        else if (q == ATSAT_F_DIS) y = smax(y, K.dis_min_d);
+        io.out64[q][c] = y;
+        if (io.out32[q]) {
+            const float hi = d2f(y);
+            io.out32[q][c] = hi;
+            if (q == ATSAT_F_W && io.wlo_out) io.wlo_out[c] = d2f(y - f2d(hi));
+        }
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_final_combine(const MixedConstF& kf, const MixedIO& io, int q0, int q1, cudaStream_t s) {
+    final_combine_kernel<<<dim3((kf.km - 1 + 31) / 32, (kf.jm - 4 + 7) / 8, kf.im - 2), dim3(32, 8), 0, s>>>(kf, io, q0,
+                                                                                                          q1);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_mixed_prepare(const KConst& kc, const MixedPrep& pr, cudaStream_t s) {
     dim3 block(32, 8), grid((kc.km + 31) / 32, (kc.jm + 7) / 8, kc.im);

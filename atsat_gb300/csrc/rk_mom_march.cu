@@ -361,8 +361,8 @@ rk_mom_march_kernel(const __grid_constant__ CUtensorMap map_plane, const __grid_
                       MODE == MODE_FINAL ? P(pdl + 7) : 0.0f, yn64[3]);
         }
 
-        // the current plane and the level's point group are done with
-        slot_reads_done();
+        // the current plane and the level's point group are done with (their values have gone into the
+        // stores above, so every lane's loads from them are complete)
         __syncwarp();
         if (lane == 0) {
             mbar_arrive(rh.empty(sc));

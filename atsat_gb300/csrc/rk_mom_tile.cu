@@ -176,6 +176,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
         nue_t[ii] = (K.turb_coupling != 0.0f && isfinite(nue_c)) ? K.turb_coupling * smaxf(0.0f, nue_c) : 0.0f;
         nue_t_s[ii] = nue_t[ii] * K.inv_pr_t;
     }
+    slot_reads_done();
     release<NPS>(rp, P_NUE, P_NUE + 1);
 
     // halo items: u_yn [u_dl] | v_yn [v_dl] | w_yn w_lo [w_dl] | t_yn [t_dl]
@@ -199,6 +200,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
         un[ii] = H(hU)[o[ii]];
         du_s[ii] = HAS_DL ? H(hU + 1)[o[ii]] : 0.0f;
     }
+    slot_reads_done();
     release<NHS>(rh, hU, hV);
     // v
     if (!wait_items<NHS>(rh, hV, hW, plan.wait_limit)) { fail(); return; }
@@ -216,6 +218,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
         vn[ii] = H(hV)[o[ii]];
         dv_s[ii] = HAS_DL ? H(hV + 1)[o[ii]] : 0.0f;
     }
+    slot_reads_done();
     release<NHS>(rh, hV, hW);
     // w (y_n, low word, increment) and the momentum equations' transport and viscous parts
     float adv_u[TI], adv_v[TI], adv_w[TI], dif_u[TI], dif_v[TI], dif_w[TI];
@@ -255,6 +258,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
                   + dw.d2phi * g.inv_rm2sinthe2 + 2.0f * Du.dphi * g.inv_rm2sinthe
                   + Dv.dphi * 2.0f * g.costhe * g.inv_rm2sinthe2;
     }
+    slot_reads_done();
     release<NHS>(rh, hW, hT);
 
     float dpr[TI], dpth[TI], dpph[TI];
@@ -277,6 +281,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
         tn[ii] = H(hT)[o[ii]];
         dt_s[ii] = HAS_DL ? H(hT + 1)[o[ii]] : 0.0f;
     }
+    slot_reads_done();
     release<NHS>(rh, hT, hEnd);
 
     if (!wait_items<NPS>(rp, P_DPR, P_DPTH, plan.wait_limit)) { fail(); return; }

@@ -6,12 +6,12 @@
 // order the consumers use them, with tensor copies: the halo boxes (40 x 10 x 6 floats) of each field's
 // y_n copy and stage increment into a 4-slot ring, and point boxes (32 x 8 x 4 floats, no halo) of the
 // advecting winds, the eddy viscosity, the sources, the tke/dis running sums and, at the final stage, the
-// increments dl_1 and dl_2 and the field's y_n in FP64 (two 32 x 8 x 2 boxes of doubles, each the 4 KB of a
-// float box) into a 6-slot ring (8 at the final stage). At the final stage the kernel forms
-// y_{n+1} = y_n + increment in FP64 and writes it with its FP32 copy. Eight consumer warps (row j, lane k,
-// four radial levels per lane) read everything from shared memory, so they never wait on a global load. A
-// field holds at most two halo and six point slots; a block needs 67 KB of shared memory (75 KB at the
-// final stage) and three blocks fit on an SM.
+// increments dl_1 and dl_2 into a 6-slot ring. At the final stage the kernel writes the FP32 increment of
+// y_{n+1} in place of dl_1 and launch_final_combine (rk_mixed.cu) adds it to y_n in FP64: the FP64 loads, adds and stores
+// then stream in a kernel of their own instead of stalling the stencil kernel. Eight consumer warps (row j,
+// lane k, four radial levels per lane) read everything from shared memory, so they never wait on a global
+// load. A field holds at most two halo and four point slots, so a block needs 67 KB of
+// shared memory and three blocks fit on an SM.
 //
 // The arithmetic is mixed_physics.cuh's scalar() with its constant factors folded: with the raw
 // differences a0..a5 of the field (each part differenced on its own),
@@ -38,18 +38,13 @@ constexpr int SEAM_F = TILE_SEAM_X * TILE_J * TI;         // 128
 constexpr int HSLOT_F = BOX_F + SEAM_F;                   // 2528 floats = 10112 bytes (79 x 128)
 constexpr int PSLOT_F = TILE_K * TILE_J * TI;             // 1024 floats = 4096 bytes
 constexpr uint32_t BOX_BYTES = BOX_F * 4, SEAM_BYTES = SEAM_F * 4, PT_BYTES = PSLOT_F * 4;
-constexpr int NHS = 4;                                    // halo slots
-template <int MODE> constexpr int nps() { return MODE == MODE_FINAL ? 8 : 6; }   // point slots
+constexpr int NHS = 4, NPS = 6;                           // halo and point slots
 constexpr int NCW = TILE_J;
 constexpr int THREADS = (NCW + 1) * 32;
 constexpr int GEO_F = TI * TILE_J * 16;                   // ColGeoF of the block's columns
 constexpr int COEF_F = TI * TILE_J * 4;                   // the four per-column diffusion factors
-template <int MODE>
-constexpr size_t smem_bytes() {
-    return (size_t)NHS * HSLOT_F * 4 + (size_t)nps<MODE>() * PSLOT_F * 4 + (size_t)(GEO_F + COEF_F) * 4
-         + 2 * (NHS + nps<MODE>()) * 8;
-}
-static_assert(3 * (smem_bytes<MODE_FINAL>() + 1024) <= 228 * 1024, "three blocks per SM");
+constexpr size_t SMEM_BYTES = (size_t)NHS * HSLOT_F * 4 + (size_t)NPS * PSLOT_F * 4 + (size_t)(GEO_F + COEF_F) * 4
+                            + 2 * (NHS + NPS) * 8;
 
 static_assert((HSLOT_F * 4) % 128 == 0 && (PSLOT_F * 4) % 128 == 0 && (BOX_F * 4) % 128 == 0, "slot alignment");
 
@@ -58,8 +53,7 @@ __host__ __device__ constexpr bool turb_field(int q) { return q == ATSAT_F_TKE |
 __host__ __device__ constexpr int n_src(int q) { return (q == ATSAT_F_NH3 || q == ATSAT_F_NH4SH) ? 2 : 1; }
 template <int MODE>
 __host__ __device__ constexpr int n_pt(int q) {
-    return n_src(q) + (turb_field(q) ? 1 : 0) + ((MODE == MODE_FINAL && !turb_field(q)) ? 2 : 0)
-         + (MODE == MODE_FINAL ? 2 : 0);
+    return n_src(q) + (turb_field(q) ? 1 : 0) + ((MODE == MODE_FINAL && !turb_field(q)) ? 2 : 0);
 }
 template <bool HAS_DL>
 __host__ __device__ constexpr int n_state() { return HAS_DL ? 8 : 5; }   // u, [du], v, [dv], w, wlo, [dw], nue
@@ -96,9 +90,8 @@ __device__ __forceinline__ void d7(const float* s, int o, int ow, int oe, float*
 template <int MODE, bool HAS_DL>
 __global__ void __launch_bounds__(THREADS, 3)
 rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_constant__ CUtensorMap map_seam,
-                      const __grid_constant__ CUtensorMap map_pt, const __grid_constant__ CUtensorMap map_f64,
-                      const MixedConstF K, const MixedIO io, const StageParams sp, const TracerPlan plan) {
-    constexpr int NPS = nps<MODE>();
+                      const __grid_constant__ CUtensorMap map_pt, const MixedConstF K, const MixedIO io,
+                      const StageParams sp, const TracerPlan plan) {
     extern __shared__ __align__(128) float smem[];
     float* hs = smem;
     float* ps = hs + NHS * HSLOT_F;
@@ -152,11 +145,7 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
                         break;
                     }
                     mbar_expect_tx(rp.full(s), PT_BYTES);
-                    if (plan.kind[n] == 1)
-                        tma_load_4d(smem_u32(ps + s * PSLOT_F), &map_pt, k0, j0, i0, plan.arr[n], rp.full(s));
-                    else          // half of a field's FP64 y_n box: levels i0 + 2 (kind - 2) and the next
-                        tma_load_4d(smem_u32(ps + s * PSLOT_F), &map_f64, k0, j0, i0 + 2 * (plan.kind[n] - 2),
-                                    plan.arr[n], rp.full(s));
+                    tma_load_4d(smem_u32(ps + s * PSLOT_F), &map_pt, k0, j0, i0, plan.arr[n], rp.full(s));
                     np++;
                 }
             }
@@ -226,6 +215,7 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
                                    : ps[(nU % NPS) * PSLOT_F + x];
             tu[ii] = u * K.inv_2dr;
         }
+        slot_reads_done();
         release<NPS>(rp, nU, nV);
         // v
         if (!wait_items<NPS>(rp, nV, nW, plan.wait_limit)) { fail(); return; }
@@ -237,6 +227,7 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
             const ColGeoF& g = *reinterpret_cast<const ColGeoF*>(sgeo + (ii * TILE_J + warp) * 16);
             tv[ii] = v * (K.inv_2dthe * g.inv_rm);
         }
+        slot_reads_done();
         release<NPS>(rp, nV, nW);
         // w = (y_n + low word) + increment
         if (!wait_items<NPS>(rp, nW, nN, plan.wait_limit)) { fail(); return; }
@@ -248,6 +239,7 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
             const ColGeoF& g = *reinterpret_cast<const ColGeoF*>(sgeo + (ii * TILE_J + warp) * 16);
             tw[ii] = w * (K.inv_2dphi * g.inv_rmsinthe);
         }
+        slot_reads_done();
         release<NPS>(rp, nW, nN);
         // nue
         if (!wait_items<NPS>(rp, nN, nN + 1, plan.wait_limit)) { fail(); return; }
@@ -258,6 +250,7 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
             nts[ii] = nue_t * K.inv_pr_t;
             nuec[ii] = nue_c;
         }
+        slot_reads_done();
         release<NPS>(rp, nN, nN + 1);
         static_assert(nN + 1 == n_state<HAS_DL>(), "state items");
     }
@@ -279,9 +272,6 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
         const float* P1 = ps + ((pb + 1) % NPS) * PSLOT_F;
         const float* P2 = ps + ((pb + 2) % NPS) * PSLOT_F;
         const float* P3 = ps + ((pb + 3) % NPS) * PSLOT_F;
-        // the final stage's FP64 y_n: the field's last two point items, levels (0, 1) and (2, 3)
-        const double* Y0 = reinterpret_cast<const double*>(ps + ((pb + npq - 2) % NPS) * PSLOT_F);
-        const double* Y1 = reinterpret_cast<const double*>(ps + ((pb + npq - 1) % NPS) * PSLOT_F);
         // the field's diffusivity and source weights (RHS_Sat_Turb.cpp:580-1000 via mixed_physics.cuh)
         float kap0, w0 = 0.0f, w1 = 0.0f;
         switch (q) {
@@ -334,13 +324,9 @@ rk_tracer_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid
                     const float dl1 = (n_src(q) == 2 ? P2 : P1)[x], dl2 = (n_src(q) == 2 ? P3 : P2)[x];
                     inc = THIRD * (dl1 + 2.0f * dl2 + dl_c) + sp.sixth_dt_f * r;
                 }
-                // y_{n+1} = y_n + increment: the increment in FP32, the sum in FP64 (mixed_physics.cuh's emit)
-                const double yn = ((ii < 2) ? Y0 : Y1)[((ii & 1) * TILE_J + warp) * TILE_K + lane];
-                double y = yn + f2d(inc);
-                if (q == ATSAT_F_TKE) y = smin(smax(y, 0.0), K.tke_max_d);
-                else if (q == ATSAT_F_DIS) y = smax(y, K.dis_min_d);
-                io.out64[q][cc] = y;
-                if (io.out32[q]) io.out32[q][cc] = d2f(y);
+                // the increment of y_{n+1}, in place of dl_1 (read above from this cell's point box);
+                // launch_final_combine adds it to y_n in FP64
+                io.dl1[q][cc] = inc;
                 if (sp.write_all_rhs) io.rhs[q][cc] = f2d(r);
             }
         }
@@ -361,17 +347,15 @@ template <int MODE, bool HAS_DL>
 cudaError_t launch_one(const TileMaps& maps, const MixedConstF& kf, const MixedIO& io, const StageParams& sp,
                        const TracerPlan& plan, dim3 grid, cudaStream_t s) {
     static bool attr = false;
-    constexpr size_t smem = smem_bytes<MODE>();
     if (!attr) {
         const cudaError_t e = cudaFuncSetAttribute(rk_tracer_tile_kernel<MODE, HAS_DL>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    rk_tracer_tile_kernel<MODE, HAS_DL><<<grid, THREADS, smem, s>>>(
+    rk_tracer_tile_kernel<MODE, HAS_DL><<<grid, THREADS, SMEM_BYTES, s>>>(
         *reinterpret_cast<const CUtensorMap*>(maps.main4), *reinterpret_cast<const CUtensorMap*>(maps.seam4),
-        *reinterpret_cast<const CUtensorMap*>(maps.pt4), *reinterpret_cast<const CUtensorMap*>(maps.pt2_f64), kf, io,
-        sp, plan);
+        *reinterpret_cast<const CUtensorMap*>(maps.pt4), kf, io, sp, plan);
     return cudaGetLastError();
 }
 
@@ -389,8 +373,10 @@ cudaError_t launch_rk_tracer_tile(const TileMaps& maps, const MixedConstF& kf, c
     if (mode == MODE_STAGE)
         return has_dl ? launch_one<MODE_STAGE, true>(maps, kf, io, sp, plan, grid, s)
                       : launch_one<MODE_STAGE, false>(maps, kf, io, sp, plan, grid, s);
-    return has_dl ? launch_one<MODE_FINAL, true>(maps, kf, io, sp, plan, grid, s)
-                  : launch_one<MODE_FINAL, false>(maps, kf, io, sp, plan, grid, s);
+    cudaError_t e = has_dl ? launch_one<MODE_FINAL, true>(maps, kf, io, sp, plan, grid, s)
+                           : launch_one<MODE_FINAL, false>(maps, kf, io, sp, plan, grid, s);
+    if (e != cudaSuccess) return e;
+    return launch_final_combine(kf, io, ATSAT_F_H2O, kf.turb ? ATSAT_F_DIS : ATSAT_F_NH4SH, s);
 }
 
 // the number of items the kernel consumes (the host's plan must match)

@@ -91,15 +91,16 @@ __device__ __forceinline__ bool acquire(const Ring& rg, int n0, int n1, const Ti
 }
 
 // Handing a slot back: the producer refills it by a tensor copy (async proxy) as soon as the empty barrier
-// completes, so every lane's shared-memory loads from it must have been performed before the arrive. Values
-// loaded into registers and used only after the arrive (the compiler is free to schedule the arithmetic
-// there) would otherwise race with that copy and read the next item's data. The proxy fence orders each
-// lane's generic-proxy reads before the async-proxy writes that follow the barrier.
+// completes, so every lane's shared-memory loads from it must have been performed before the arrive. Where
+// the loaded values have gone into global stores before the release, they have. Where they feed registers
+// only (stencil differences, wind factors), the compiler is free to schedule that arithmetic after the
+// arrive, and the copy could then overtake the loads and hand them the next item's data: such a release is
+// preceded by slot_reads_done, a proxy fence that orders each lane's generic-proxy reads before the
+// async-proxy writes that follow the barrier.
 __device__ __forceinline__ void slot_reads_done() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 template <int NSLOT>
 __device__ __forceinline__ void release(const Ring& rg, int n0, int n1) {
-    slot_reads_done();
     __syncwarp();
     if ((threadIdx.x & 31) == 0) {
 #pragma unroll

@@ -204,11 +204,13 @@ KERNEL_NAME = {"fp64": "rk_stage_fp64_kernel (fused RHSSat + RK4 stage, FP64)",
                "mixed_split": "rk_mom_kernel + rk_tracer_kernel<1> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)",
                "mixed_split3": "rk_mom_kernel + rk_tracer_kernel<3> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)",
                "mixed_split13": "rk_mom_kernel + rk_tracer_kernel<13> (split RHSSat + RK4 stage, FP32 stencils / FP64 state)",
-               "mixed_split_tiled": "rk_mom_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, TMA-tiled tracers)",
+               "mixed_split_tiled": "rk_mom_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, TMA-tiled tracers; "
+                                    "final stage + final_combine_kernel)",
                "mixed_tiled2": "rk_mom_tile_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage, all inputs "
-                               "TMA-streamed)",
+                               "TMA-streamed; final stage + final_combine_kernel)",
                "mixed_march": "rk_mom_march_kernel + rk_tracer_tile_kernel (split RHSSat + RK4 stage: the momentum "
-                              "part as a radial march, one TMA plane per stencil array and level)"}
+                              "part as a radial march, one TMA plane per stencil array and level; final stage + "
+                              "final_combine_kernel)"}
 
 
 def cpu_baseline(g, P, seed, target_s=3.0):
