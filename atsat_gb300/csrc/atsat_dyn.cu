@@ -241,6 +241,10 @@ int check_supported(atsat_dyn* h, const atsat_dyn_params& p) {
         {p.t_limiter != 0, "ATSAT_T_LIMITER (reads tn at k-1 = -1 on the periodic seam in the reference)"},
         {p.press_wall != 0, "ATSAT_PRESS_WALL (no solid body exists in ATSAT)"},
         {p.precision != ATSAT_DYN_FP64 && p.precision != ATSAT_DYN_MIXED, "unknown precision"},
+        // the split Coriolis form balances against the metric pressure, which only the metric split computes;
+        // the reference switches it off with the metric split (cSaturnModel.cpp's knob resolution)
+        {p.coriolis_split != 0 && p.metric_split == 0, "ATSAT_CORIOLIS_SPLIT without ATSAT_METRIC_SPLIT"},
+        {p.hydro_buoy != 0 && p.metric_split == 0, "ATSAT_HYDRO_BUOY without ATSAT_METRIC_SPLIT"},
     };
     for (auto& r : rules)
         if (r.bad) return fail(h, ATSAT_DYN_E_UNSUPPORTED, "not implemented on the device: %s", r.what);

@@ -94,6 +94,10 @@ def test_unsupported_knobs_are_rejected(lib):
     with pytest.raises(dyn.DycoreError) as e:
         dyn.Dycore(synth.make_grid(9, 13, 17), abi.default_params(chrom=1))
     assert e.value.status == abi.E_UNSUPPORTED
+    # the split Coriolis form without the metric split: the reference forces it off, the device refuses it
+    with pytest.raises(dyn.DycoreError) as e:
+        dyn.Dycore(synth.make_grid(9, 13, 17), abi.default_params(metric_split=0, coriolis_split=1))
+    assert e.value.status == abi.E_UNSUPPORTED
 
 
 def test_autotune_cache_read_and_write(lib, tmp_path):

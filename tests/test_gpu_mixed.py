@@ -88,6 +88,20 @@ def test_mixed_ten_iterations_line_barotropic(shape):
     assert not bad, bad
 
 
+@pytest.mark.parametrize("variant", [MARCH, TILED2, DIRECT], ids=["march", "tiled2", "direct"])
+def test_mixed_ten_iterations_without_metric_split(variant):
+    """The metric term in rhs_u itself and the radial Coriolis term unsplit (metric_split = coriolis_split = 0):
+    the mixed path's stage corrections in the increments carry them; 10 iterations against the oracle."""
+    g, P, st = case((21, 91, 181), seed=47, exercise=True, metric_split=0, coriolis_split=0)
+    ref = st.copy()
+    oracle.steps(ref, P, 10)
+    got = run_mixed(g, P, st, 10, variant)
+    rep = drift(got.arrays, ref.arrays, F.PROG + [F.P_DYN])
+    print("\nno metric split, 10 iterations:", {k: f"{v[0]:.2e}" for k, v in rep.items()})
+    bad = {F.NAMES[f]: rep[F.NAMES[f]][0] for f in CRITERION if not rep[F.NAMES[f]][0] <= TOL_MIXED}
+    assert not bad, bad
+
+
 def test_mixed_ten_iterations_driver_glue():
     """The mixed path with the driver's glue: the species floor must also reach the FP32 copies the next
     step starts from."""
