@@ -160,7 +160,7 @@ __device__ __forceinline__ CellState momentum_t(const MixedConstF& K, const Mixe
         }
         // stage-dependent parts of the frozen balances (terms in the increments)
         float gu_stage = 0.0f;
-        if (!K.metric_split) gu_stage -= K.metric_on * (dv_s * (2.0f * vn + dv_s) + dw_s * (2.0f * wn + dw_s)) * g.inv_rm;
+        if (!K.metric_split) gu_stage += K.metric_on * (dv_s * (2.0f * vn + dv_s) + dw_s * (2.0f * wn + dw_s)) * g.inv_rm;
         if (K.cor_rad_on != 0.0f) gu_stage -= K.cor_rad_on * g.cor_rad_c * dw_s;
         const float rhs_u = ldf(io.fz[FZ_GU] + c) - fz_dpr + buoy + gu_stage - adv_u + diffusion_u * visc;
         const float rhs_v = ldf(io.fz[FZ_GV] + c) - fz_dpth - adv_v - u * v * g.inv_rm

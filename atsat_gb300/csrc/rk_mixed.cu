@@ -264,7 +264,8 @@ __global__ void __launch_bounds__(256) mixed_prepare_kernel(const KConst K, cons
     double gu = __ldg(&g->cent_rad_c);
     if (!K.metric_split) {
         const double vn = __ldg(pr.yn64[ATSAT_F_V] + c);
-        gu -= (vn * vn + wn * wn) * __ldg(&g->metric_inv_rm);
+        // + metric (v^2 + w^2) / rm: rhs_u subtracts transport_u, which carries - metric (RHS_Sat_Turb.cpp:391-395)
+        gu += (vn * vn + wn * wn) * __ldg(&g->metric_inv_rm);
     }
     if (pr.cor_rad) gu -= __ldg(&g->cor_rad_c) * wn;
     // w (w cot / r) - Coriolis cor_the w, the centrifugal and the p_metric gradient

@@ -313,7 +313,7 @@ rk_mom_march_kernel(const __grid_constant__ CUtensorMap map_plane, const __grid_
             }
             float gu_stage = 0.0f;
             if (!K.metric_split)
-                gu_stage -= K.metric_on * (dv_s * (2.0f * vn + dv_s) + dw_s * (2.0f * wn + dw_s)) * g.inv_rm;
+                gu_stage += K.metric_on * (dv_s * (2.0f * vn + dv_s) + dw_s * (2.0f * wn + dw_s)) * g.inv_rm;
             if (K.cor_rad_on != 0.0f) gu_stage -= K.cor_rad_on * g.cor_rad_c * dw_s;
             const float rhs_u = P(P_GU) - dpr + buoy + gu_stage - adv_u + dif_u * visc;
             put<MODE>(io, sp, ATSAT_F_U, c, rhs_u, du_s, MODE == MODE_FINAL ? P(pdl) : 0.0f,

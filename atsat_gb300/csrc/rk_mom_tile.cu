@@ -300,7 +300,7 @@ rk_mom_tile_kernel(const __grid_constant__ CUtensorMap map_main, const __grid_co
         }
         float gu_stage = 0.0f;
         if (!K.metric_split)
-            gu_stage -= K.metric_on * (dv_s[ii] * (2.0f * vn[ii] + dv_s[ii]) + dw_s[ii] * (2.0f * wn[ii] + dw_s[ii])) * g.inv_rm;
+            gu_stage += K.metric_on * (dv_s[ii] * (2.0f * vn[ii] + dv_s[ii]) + dw_s[ii] * (2.0f * wn[ii] + dw_s[ii])) * g.inv_rm;
         if (K.cor_rad_on != 0.0f) gu_stage -= K.cor_rad_on * g.cor_rad_c * dw_s[ii];
         const float visc = K.inv_re + nue_t[ii];
         const float rhs_u = P(P_GU)[x] - dpr[ii] + buoy + gu_stage - adv_u[ii] + dif_u[ii] * visc;
