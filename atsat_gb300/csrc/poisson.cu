@@ -177,53 +177,60 @@ __device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned nblocks, long 
 
 template <typename T>
 struct alignas(4 * sizeof(T)) SorW {
-    T num1, num2, num3, den;
+    T num1, num2, num3, rden;     // the sweep weights and 1 / den (formed in FP64 on the host)
 };
 
-constexpr int SORP_WARPS = 8;
+constexpr int SORP_WARPS = 32;   // large blocks: few arrivals at each grid barrier
+
+// One half-sweep of colour c over the warps of the grid. A work item is 32 consecutive cells of one packed
+// row; the arrays are distinct (restrict), so the loads of the next items can be issued ahead of this
+// item's stores.
+template <typename T>
+__device__ __forceinline__ void sor_phase(const KConst& K, const SorW<T>* __restrict__ wt, T* __restrict__ Pc,
+                                          const T* __restrict__ Po, const T* __restrict__ Fc, int kh, int c, T w,
+                                          int gw, int nw) {
+    const int n = K.km - 1, nh = n >> 1, nch = (nh + 31) >> 5;
+    const int NJ = K.jm - 2, items = (K.im - 2) * NJ * nch;
+    const int64_t plane = (int64_t)K.jm * kh;
+    const int lane = threadIdx.x;
+    const T c43 = (T)K.c43, c13 = (T)K.c13;
+#pragma unroll 4
+    for (int it = gw; it < items; it += nw) {
+        const int r = it / nch, m = (it - r * nch) * 32 + lane;
+        const int i = 1 + r / NJ, j = 1 + r % NJ;
+        if (m >= nh) continue;
+        const int64_t row = ((int64_t)i * K.jm + j) * kh;
+        const SorW<T> W = wt[(int64_t)i * K.jm + j];
+        const int k = 2 * m + ((i + j + c) & 1);
+        const int me = (k == n - 1) ? 0 : ((k + 1) >> 1);
+        const int mw = (k == 0) ? ((n - 1) >> 1) : ((k - 1) >> 1);
+        const T acc = (__ldcg(Po + row + plane + m) + __ldcg(Po + row - plane + m)) * W.num1
+                    + (__ldcg(Po + row + kh + m) + __ldcg(Po + row - kh + m)) * W.num2
+                    + (__ldcg(Po + row + me) + __ldcg(Po + row + mw)) * W.num3;
+        const T old = __ldcg(Pc + row + m);
+        const T nv = (acc - Fc[row + m]) * W.rden;
+        const T pn = old + w * (nv - old);
+        Pc[row + m] = pn;
+        // the folded boundary cells this cell stands two away from (the same colour as it)
+        const T self = (c == 0) ? old : pn;
+        if (i == 2) Pc[row - 2 * plane + m] = c43 * __ldcg(Po + row - plane + m) - c13 * self;
+        if (i == K.im - 3) Pc[row + 2 * plane + m] = c43 * __ldcg(Po + row + plane + m) - c13 * self;
+        if (j == 2) Pc[row - 2 * kh + m] = c43 * __ldcg(Po + row - kh + m) - c13 * self;
+        if (j == K.jm - 3) Pc[row + 2 * kh + m] = c43 * __ldcg(Po + row + kh + m) - c13 * self;
+    }
+}
 
 template <typename T>
 __global__ void __launch_bounds__(32 * SORP_WARPS) sor_packed_kernel(const KConst K, const SorW<T>* __restrict__ wt,
                                                                      T* p0, T* p1, const T* __restrict__ f0,
                                                                      const T* __restrict__ f1, int kh, int nsweeps,
                                                                      T w, GridBar* bar, long long limit) {
-    const int n = K.km - 1, nh = n >> 1;
-    const int NI = K.im - 2, NJ = K.jm - 2;
-    const int64_t plane = (int64_t)K.jm * kh;
-    const int lane = threadIdx.x;
     const int gw = blockIdx.x * SORP_WARPS + threadIdx.y, nw = gridDim.x * SORP_WARPS;
-    const T c43 = (T)K.c43, c13 = (T)K.c13;
     for (int sweep = 0; sweep < nsweeps; sweep++) {
-        for (int c = 0; c < 2; c++) {
-            T* Pc = c ? p1 : p0;
-            const T* Po = c ? p0 : p1;
-            const T* Fc = c ? f1 : f0;
-            for (int r = gw; r < NI * NJ; r += nw) {
-                const int i = 1 + r / NJ, j = 1 + r % NJ;
-                const int64_t row = ((int64_t)i * K.jm + j) * kh;
-                const SorW<T> W = wt[(int64_t)i * K.jm + j];
-                const int s = (i + j + c) & 1;
-                for (int m = lane; m < nh; m += 32) {
-                    const int k = 2 * m + s;
-                    const int me = (k == n - 1) ? 0 : ((k + 1) >> 1);
-                    const int mw = (k == 0) ? ((n - 1) >> 1) : ((k - 1) >> 1);
-                    const T acc = (__ldcg(Po + row + plane + m) + __ldcg(Po + row - plane + m)) * W.num1
-                                + (__ldcg(Po + row + kh + m) + __ldcg(Po + row - kh + m)) * W.num2
-                                + (__ldcg(Po + row + me) + __ldcg(Po + row + mw)) * W.num3;
-                    const T old = __ldcg(Pc + row + m);
-                    const T nv = (acc - Fc[row + m]) / W.den;
-                    const T pn = old + w * (nv - old);
-                    Pc[row + m] = pn;
-                    // the folded boundary cells this cell stands two away from (the same colour as it)
-                    const T self = (c == 0) ? old : pn;
-                    if (i == 2) Pc[row - 2 * plane + m] = c43 * __ldcg(Po + row - plane + m) - c13 * self;
-                    if (i == K.im - 3) Pc[row + 2 * plane + m] = c43 * __ldcg(Po + row + plane + m) - c13 * self;
-                    if (j == 2) Pc[row - 2 * kh + m] = c43 * __ldcg(Po + row - kh + m) - c13 * self;
-                    if (j == K.jm - 3) Pc[row + 2 * kh + m] = c43 * __ldcg(Po + row + kh + m) - c13 * self;
-                }
-            }
-            if (!grid_barrier(bar, gridDim.x, limit)) return;
-        }
+        sor_phase<T>(K, wt, p0, p1, f0, kh, 0, w, gw, nw);
+        if (!grid_barrier(bar, gridDim.x, limit)) return;
+        sor_phase<T>(K, wt, p1, p0, f1, kh, 1, w, gw, nw);
+        if (!grid_barrier(bar, gridDim.x, limit)) return;
     }
 }
 
@@ -721,8 +728,9 @@ PoissonSolver* poisson_create(const KConst& kc, const ColGeo* geo_dev, const std
         w32h.resize(ncol);
         for (size_t q = 0; q < ncol; q++) {
             const ColGeo& c = geo_h[q];
-            w64h[q] = SorW<double>{c.p_num1, c.p_num2, c.p_num3, c.p_den};
-            w32h[q] = SorW<float>{(float)c.p_num1, (float)c.p_num2, (float)c.p_num3, (float)c.p_den};
+            const double rden = 1.0 / c.p_den;
+            w64h[q] = SorW<double>{c.p_num1, c.p_num2, c.p_num3, rden};
+            w32h[q] = SorW<float>{(float)c.p_num1, (float)c.p_num2, (float)c.p_num3, (float)rden};
         }
         // the cooperative launch's grid: as many blocks as fit on the GPU at once
         int dev = 0, nsm = 0, b64 = 0, b32 = 0;
