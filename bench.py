@@ -230,19 +230,32 @@ def cpu_baseline(g, P, seed, target_s=3.0):
                       f"{dt:.2f} s wall on {os.cpu_count()} OpenMP threads"}
 
 
-def cpu_baseline_one_thread(shape):
-    """The same bounded sample on one OpenMP thread, in a child process (OpenMP fixes its thread count when
-    the library loads)."""
-    code = ("import json, sys; sys.path.insert(0, %r); import bench; from atsat_gb300 import abi, synth; "
+def cpu_baseline_child(shape, threads=None, build=""):
+    """The same bounded sample in a child process: on one OpenMP thread (OpenMP fixes its thread count when
+    the library loads), or with the restatement's fast build (-O3, multiply-add contraction allowed; a timed
+    baseline only, never the parity oracle)."""
+    code = ("import json, os, sys; sys.path.insert(0, %r); import bench; from atsat_gb300 import abi, synth; "
             "g = synth.make_grid(*%r); r = bench.cpu_baseline(g, abi.default_params(), seed=0, target_s=2.0); "
-            "r['cores'] = 1; r['sample'] = r['sample'].replace('%%d OpenMP threads' %% __import__('os').cpu_count(), "
-            "'1 OpenMP thread'); print(json.dumps(r))") % (ROOT, tuple(shape))
+            "n = int(os.environ.get('OMP_NUM_THREADS') or os.cpu_count()); r['cores'] = n; "
+            "r['sample'] = r['sample'].replace('%%d OpenMP threads' %% os.cpu_count(), '%%d OpenMP thread%%s' "
+            "%% (n, '' if n == 1 else 's')); print(json.dumps(r))") % (ROOT, tuple(shape))
+    env = dict(os.environ)
+    if threads:
+        env["OMP_NUM_THREADS"] = str(threads)
+    if build:
+        env["ATSAT_ORACLE_BUILD"] = build
     try:
-        out = subprocess.run([sys.executable, "-c", code], env=dict(os.environ, OMP_NUM_THREADS="1"),
-                             capture_output=True, text=True, timeout=300)
-        return json.loads(out.stdout.strip().splitlines()[-1])
+        out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
+        r = json.loads(out.stdout.strip().splitlines()[-1])
     except (subprocess.SubprocessError, ValueError, IndexError, OSError):
         return None
+    if build == "fast":
+        r["build"] = "gcc -O3 -fopenmp -ffp-contract=fast (no -march/-mcpu: the same flags on x86-64 and Arm)"
+    return r
+
+
+def cpu_baseline_one_thread(shape):
+    return cpu_baseline_child(shape, threads=1)
 
 
 def run_reference(a, rank, world):
@@ -453,11 +466,11 @@ def run_ours(a, rank, world):
     from atsat_gb300 import abi, dyn, fields as F, synth
     g = synth.make_grid(*a.shape)
     P = abi.default_params()
-    cpu = None
-    cpu1 = None
+    cpu = cpu1 = cpu_fast = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         cpu = cpu_baseline(g, P, seed=0)          # before the first CUDA call
         cpu1 = cpu_baseline_one_thread(a.shape)
+        cpu_fast = cpu_baseline_child(a.shape, build="fast")
     st = synth.saturn_state(g, P, seed=rank)
     pinned = {fid: dyn.PinnedArray(g.shape) for fid in range(F.NFIELDS)}
     res = {p: measure(a, rank, world, g, P, st, pinned, p) for p in a.precisions}
@@ -481,6 +494,8 @@ def run_ours(a, rank, world):
         out["cpu_baseline"] = cpu
     if cpu1:
         out["cpu_baseline_one_thread"] = cpu1
+    if cpu_fast:
+        out["cpu_baseline_o3"] = cpu_fast
     return out
 
 

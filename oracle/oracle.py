@@ -20,15 +20,18 @@ SRC = os.path.join(HERE, "atsat_oracle.c")
 # bit. ATSAT_ORACLE_BUILD=fast selects a second build used only as a timed CPU baseline: -O3 with
 # contraction allowed (fused multiply-adds wherever the host ISA has them; no -march / -mcpu).
 FAST = os.environ.get("ATSAT_ORACLE_BUILD", "") == "fast"
-LIB = os.path.join(HERE, "liboracle_fast.so" if FAST else "liboracle.so")
-CFLAGS = (["-O3", "-fopenmp", "-ffp-contract=fast", "-fPIC", "-shared", "-std=c99", "-Wall"] if FAST else
-          ["-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c99", "-Wall"])
+LIB_O2 = os.path.join(HERE, "liboracle.so")
+LIB_FAST = os.path.join(HERE, "liboracle_fast.so")
+CFLAGS_O2 = ["-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c99", "-Wall"]
+CFLAGS_FAST = ["-O3", "-fopenmp", "-ffp-contract=fast", "-fPIC", "-shared", "-std=c99", "-Wall"]
+LIB = LIB_FAST if FAST else LIB_O2
 
 
-def build(force: bool = False) -> str:
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
-        subprocess.run(["gcc", *CFLAGS, SRC, "-o", LIB, "-lm"], check=True)
-    return LIB
+def build(force: bool = False, fast: bool = FAST) -> str:
+    lib, flags = (LIB_FAST, CFLAGS_FAST) if fast else (LIB_O2, CFLAGS_O2)
+    if force or not os.path.exists(lib) or os.path.getmtime(lib) < os.path.getmtime(SRC):
+        subprocess.run(["gcc", *flags, SRC, "-o", lib, "-lm"], check=True)
+    return lib
 
 
 _lib = None
