@@ -72,7 +72,8 @@ class PStats(C.Structure):
 
 class PoissonStats(C.Structure):
     _fields_ = [("method", C.c_int32), ("iterations", C.c_int32), ("inner", C.c_int32), ("converged", C.c_int32),
-                ("rel_residual", C.c_double), ("ms", C.c_double), ("reserved", C.c_double * 4)]
+                ("rel_residual", C.c_double), ("ms", C.c_double), ("sweeps_per_pass", C.c_int32), ("pad", C.c_int32),
+                ("sweep_ms", C.c_double), ("reserved", C.c_double * 2)]
 
 
 POISSON_METHODS = ["sor64", "sor32", "refine_sor", "direct64", "direct32", "refine_direct"]

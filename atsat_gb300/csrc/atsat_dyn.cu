@@ -2938,6 +2938,11 @@ int atsat_dyn_poisson_solve(atsat_dyn_t h, int32_t method, const double* src, do
         st->converged = rel <= tol;
         st->rel_residual = rel;
         st->ms = ms;
+        int spp = 0;
+        double sms = 0.0;
+        poisson_sweep_stats(h->poisson, &spp, &sms);
+        st->sweeps_per_pass = spp;
+        st->sweep_ms = sms;
     }
     return finish(h, true);
 }

@@ -382,6 +382,7 @@ void poisson_destroy(PoissonSolver* P);
 double* poisson_f(PoissonSolver* P);          // device source (pitched)
 double* poisson_p(PoissonSolver* P);          // device solution (pitched)
 const std::vector<double>& poisson_null_vector(PoissonSolver* P);   // [(j-1) * (im-2) + (i-1)]
+void poisson_sweep_stats(PoissonSolver* P, int* sweeps_per_pass, double* sweep_ms);
 cudaError_t poisson_run(PoissonSolver* P, int method, double tol, int max_iter, int inner, double omega,
                         int* iters, int* inner_total, double* rel);
 cudaError_t launch_level_mean(const KConst& kc, const double* t, const double* p_stat,

@@ -18,6 +18,7 @@
 //     e = L^-1 r in FP32, p += e, until ||r|| / ||f|| <= tol.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -162,6 +163,7 @@ __device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned nblocks, long 
         } else {
             const long long t0 = clock64();
             while (ld_acquire(&b->gen) == g) {
+                __nanosleep(32);           // fewer polls of the one line the arrivals update
                 if (clock64() - t0 > limit) {
                     ok = 0;
                     atomicOr(&b->err, 1u);
@@ -182,26 +184,53 @@ struct alignas(4 * sizeof(T)) SorW {
 
 constexpr int SORP_WARPS = 32;   // large blocks: few arrivals at each grid barrier
 
+// A warp's position in the item list (level i, row j, chunk mc of 32 packed columns) and the step of the
+// grid's stride in the same terms, so that the walk needs no division: integer division and int <-> float
+// conversion run at the FP64 rate on this GPU.
+struct ItemWalk {
+    int i, j, mc;          // the first item of this warp
+    int di, dj, dmc;       // the stride nw as levels, rows and chunks (dj < NJ, dmc < nch)
+};
+
+__device__ __forceinline__ ItemWalk item_walk(const KConst& K, int gw, int nw) {
+    const int n = K.km - 1, nch = ((n >> 1) + 31) >> 5, NJ = K.jm - 2;
+    ItemWalk W;
+    int r = gw / nch;
+    W.mc = gw - r * nch;
+    W.i = 1 + r / NJ;
+    W.j = 1 + (r - (W.i - 1) * NJ);
+    r = nw / nch;
+    W.dmc = nw - r * nch;
+    W.di = r / NJ;
+    W.dj = r - W.di * NJ;
+    return W;
+}
+
 // One half-sweep of colour c over the warps of the grid. A work item is 32 consecutive cells of one packed
 // row; the arrays are distinct (restrict), so the loads of the next items can be issued ahead of this
 // item's stores.
 template <typename T>
 __device__ __forceinline__ void sor_phase(const KConst& K, const SorW<T>* __restrict__ wt, T* __restrict__ Pc,
                                           const T* __restrict__ Po, const T* __restrict__ Fc, int kh, int c, T w,
-                                          int gw, int nw) {
+                                          ItemWalk it) {
     const int n = K.km - 1, nh = n >> 1, nch = (nh + 31) >> 5;
-    const int NJ = K.jm - 2, items = (K.im - 2) * NJ * nch;
     const int64_t plane = (int64_t)K.jm * kh;
     const int lane = threadIdx.x;
     const T c43 = (T)K.c43, c13 = (T)K.c13;
+    int i = it.i, j = it.j, mc = it.mc;
 #pragma unroll 4
-    for (int it = gw; it < items; it += nw) {
-        const int r = it / nch, m = (it - r * nch) * 32 + lane;
-        const int i = 1 + r / NJ, j = 1 + r % NJ;
+    for (; i <= K.im - 2;) {
+        const int m = mc * 32 + lane;
+        const int ci = i, cj = j;
+        mc += it.dmc;
+        if (mc >= nch) { mc -= nch; j++; }
+        j += it.dj;
+        if (j > K.jm - 2) { j -= K.jm - 2; i++; }
+        i += it.di;
         if (m >= nh) continue;
-        const int64_t row = ((int64_t)i * K.jm + j) * kh;
-        const SorW<T> W = wt[(int64_t)i * K.jm + j];
-        const int k = 2 * m + ((i + j + c) & 1);
+        const int64_t row = ((int64_t)ci * K.jm + cj) * kh;
+        const SorW<T> W = wt[(int64_t)ci * K.jm + cj];
+        const int k = 2 * m + ((ci + cj + c) & 1);
         const int me = (k == n - 1) ? 0 : ((k + 1) >> 1);
         const int mw = (k == 0) ? ((n - 1) >> 1) : ((k - 1) >> 1);
         const T acc = (__ldcg(Po + row + plane + m) + __ldcg(Po + row - plane + m)) * W.num1
@@ -213,10 +242,10 @@ __device__ __forceinline__ void sor_phase(const KConst& K, const SorW<T>* __rest
         Pc[row + m] = pn;
         // the folded boundary cells this cell stands two away from (the same colour as it)
         const T self = (c == 0) ? old : pn;
-        if (i == 2) Pc[row - 2 * plane + m] = c43 * __ldcg(Po + row - plane + m) - c13 * self;
-        if (i == K.im - 3) Pc[row + 2 * plane + m] = c43 * __ldcg(Po + row + plane + m) - c13 * self;
-        if (j == 2) Pc[row - 2 * kh + m] = c43 * __ldcg(Po + row - kh + m) - c13 * self;
-        if (j == K.jm - 3) Pc[row + 2 * kh + m] = c43 * __ldcg(Po + row + kh + m) - c13 * self;
+        if (ci == 2) Pc[row - 2 * plane + m] = c43 * __ldcg(Po + row - plane + m) - c13 * self;
+        if (ci == K.im - 3) Pc[row + 2 * plane + m] = c43 * __ldcg(Po + row + plane + m) - c13 * self;
+        if (cj == 2) Pc[row - 2 * kh + m] = c43 * __ldcg(Po + row - kh + m) - c13 * self;
+        if (cj == K.jm - 3) Pc[row + 2 * kh + m] = c43 * __ldcg(Po + row + kh + m) - c13 * self;
     }
 }
 
@@ -225,12 +254,187 @@ __global__ void __launch_bounds__(32 * SORP_WARPS) sor_packed_kernel(const KCons
                                                                      T* p0, T* p1, const T* __restrict__ f0,
                                                                      const T* __restrict__ f1, int kh, int nsweeps,
                                                                      T w, GridBar* bar, long long limit) {
-    const int gw = blockIdx.x * SORP_WARPS + threadIdx.y, nw = gridDim.x * SORP_WARPS;
+    const ItemWalk it = item_walk(K, blockIdx.x * SORP_WARPS + threadIdx.y, gridDim.x * SORP_WARPS);
     for (int sweep = 0; sweep < nsweeps; sweep++) {
-        sor_phase<T>(K, wt, p0, p1, f0, kh, 0, w, gw, nw);
+        sor_phase<T>(K, wt, p0, p1, f0, kh, 0, w, it);
         if (!grid_barrier(bar, gridDim.x, limit)) return;
-        sor_phase<T>(K, wt, p1, p0, f1, kh, 1, w, gw, nw);
+        sor_phase<T>(K, wt, p1, p0, f1, kh, 1, w, it);
         if (!grid_barrier(bar, gridDim.x, limit)) return;
+    }
+}
+
+// ---- the same sweeps temporally blocked (FP32): S sweeps per grid barrier ----
+// A block owns a tile of rows j0 .. j1-1 and packed columns m0 .. m1-1 over every radial level (the folded
+// planes i = 0 and im-1 included) and holds it in shared memory, both colours, with a halo of 2S rows and
+// S packed columns (2S cells along phi) on each side: TB_LANES packed columns per shared row, one per lane.
+// A pass loads the halo'd tile from the current packed arrays, runs 2S half-sweeps in shared memory --
+// half-sweep h updates the cells within 2S - h cells of the owned tile, the cone the owned cells depend
+// on -- and writes the owned cells (with the folded rows j = 0 / jm-1 where it owns the rows next to them)
+// to the other pair of packed arrays; the blocks meet at the grid barrier between passes. Every cell gets
+// the operations of sor_phase in the same order (the folds included), so the two kernels agree bit for
+// bit; halo cells are computed by each tile whose cone holds them.
+constexpr int TB_WARPS = 32;
+constexpr int TB_LANES = 32;
+constexpr int TB_MAX_TILES = 1024;
+
+struct TbPlan {
+    int ntiles, RJ, nh;          // tiles, shared rows per tile, n / 2
+};
+
+// one tile: packed columns m0 .. m0+TM-1, rows j0 .. j1-1 (formed on the host: no division on the device,
+// where integer division and int <-> float conversion run at the FP64 rate)
+struct TbTile {
+    int m0, TM, j0, j1;
+};
+
+// shared memory of one tile: both colours of p over im x RJ rows of TB_LANES, then the rows' weights
+__host__ __device__ inline size_t tb_smem_bytes(int im, int RJ) {
+    return (size_t)2 * im * RJ * TB_LANES * sizeof(float) + (size_t)im * RJ * sizeof(SorW<float>);
+}
+
+// (a, b) += step in a row-major walk with b in [0, nb): b wraps into a (b, step >= 0)
+__device__ __forceinline__ void walk(int& a, int& b, int step, int nb) {
+    b += step;
+    while (b >= nb) { b -= nb; a++; }
+}
+
+// 4-byte asynchronous copy global -> shared (no register round trip; many in flight per thread)
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+constexpr int TB_SEG = 4;        // radial levels per work item of a half-sweep
+
+// One work item: the cells of one shared column (row jj, this lane) at levels i0 .. i0+nl-1 of colour c.
+// FOLDS: the item may hold a cell two away from a folded boundary (levels 2 or im-3, rows 2 or jm-3).
+template <bool FOLDS>
+__device__ __forceinline__ void tb_segment(float* __restrict__ own, const float* __restrict__ oth,
+                                           const SorW<float>* wp, const float (&fv)[TB_SEG], int q, int par,
+                                           bool ok0, bool ok1, int PL, int RJ, int nl, int i0, int im, bool jlow,
+                                           bool jhigh, float w, float c43, float c13, int c) {
+#pragma unroll
+    for (int u = 0; u < TB_SEG; u++) {
+        if (u < nl && (par ? ok1 : ok0)) {
+            const SorW<float> W = wp[u * RJ];
+            const float up = oth[q + PL], dn = oth[q - PL], nn = oth[q + TB_LANES], ss = oth[q - TB_LANES];
+            const float acc = (up + dn) * W.num1 + (nn + ss) * W.num2 + (oth[q + par] + oth[q - 1 + par]) * W.num3;
+            const float old = own[q];
+            const float nv = (acc - fv[u]) * W.rden;
+            const float pn = old + w * (nv - old);
+            own[q] = pn;
+            if (FOLDS) {
+                // the folded boundary cells this cell stands two away from (same colour)
+                const float self = (c == 0) ? old : pn;
+                const int i = i0 + u;
+                if (i == 2) own[q - 2 * PL] = c43 * dn - c13 * self;
+                if (i == im - 3) own[q + 2 * PL] = c43 * up - c13 * self;
+                if (jlow) own[q - 2 * TB_LANES] = c43 * ss - c13 * self;
+                if (jhigh) own[q + 2 * TB_LANES] = c43 * nn - c13 * self;
+            }
+        }
+        q += PL;
+        par ^= 1;
+    }
+}
+
+template <int S>
+__global__ void __launch_bounds__(32 * TB_WARPS) sor_tb_kernel(const KConst K, const SorW<float>* __restrict__ wt,
+                                                               const TbTile* __restrict__ tiles,
+                                                               float* A0, float* A1, float* B0, float* B1,
+                                                               const float* __restrict__ f0,
+                                                               const float* __restrict__ f1, int kh, int nsweeps,
+                                                               float w, TbPlan pl, GridBar* bar, long long limit) {
+    extern __shared__ float4 tb_smem[];
+    float* const sp = reinterpret_cast<float*>(tb_smem);
+    const int RJ = pl.RJ, im = K.im, jm = K.jm, nh = pl.nh, NI = im - 2;
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    const int cs = im * RJ * TB_LANES;          // floats per colour
+    const int PL = RJ * TB_LANES;               // floats per radial level
+    const int64_t GP = (int64_t)jm * kh;        // global floats per radial level (packed)
+    const int nseg = (NI + TB_SEG - 1) / TB_SEG;
+    SorW<float>* const sw = reinterpret_cast<SorW<float>*>(sp + 2 * cs);
+    const float c43 = (float)K.c43, c13 = (float)K.c13;
+    for (int done = 0; done < nsweeps;) {
+        const int ns = min(S, nsweeps - done);
+        done += ns;
+        for (int t = blockIdx.x; t < pl.ntiles; t += gridDim.x) {
+            const TbTile T = tiles[t];
+            const int m0 = T.m0, TM = T.TM, j0 = T.j0, j1 = T.j1;
+            const int jb = j0 - 2 * S;          // the row of shared row 0
+            int gm = m0 - S + lane;             // this lane's packed column, wrapped around the ring
+            gm = gm < 0 ? gm + nh : (gm >= nh ? gm - nh : gm);
+            {
+                int i = 0, jj = warp;           // shared row (i, jj), jj fastest
+                walk(i, jj, 0, RJ);
+                for (; i < im; walk(i, jj, TB_WARPS, RJ)) {
+                    const int j = jb + jj;
+                    if (j < 0 || j >= jm) continue;
+                    const int r = i * RJ + jj;
+                    const int64_t g = ((int64_t)i * jm + j) * kh + gm;
+                    if (lane < TM + 2 * S) {
+                        cp_async4(sp + r * TB_LANES + lane, A0 + g);
+                        cp_async4(sp + cs + r * TB_LANES + lane, A1 + g);
+                    }
+                    if (lane < 4) cp_async4(reinterpret_cast<float*>(sw + r) + lane,
+                                            reinterpret_cast<const float*>(wt + (int64_t)i * jm + j) + lane);
+                }
+                cp_async_wait_all();
+            }
+            __syncthreads();
+            for (int h = 1; h <= 2 * ns; h++) {
+                const int c = (h - 1) & 1, e = 2 * ns - h;
+                float* const own = sp + c * cs;
+                const float* const oth = sp + (1 - c) * cs;
+                const float* const fc = c ? f1 : f0;
+                const int jlo = max(1, j0 - e), nj = min(jm - 2, j1 - 1 + e) - jlo + 1;
+                const int klo = -e, khi = 2 * TM + e;          // phi range relative to 2 m0
+                // this lane updates the cell of parity p (k = 2 m + p) of its column where ok[p]
+                const bool ok0 = 2 * (lane - S) >= klo && 2 * (lane - S) < khi;
+                const bool ok1 = 2 * (lane - S) + 1 >= klo && 2 * (lane - S) + 1 < khi;
+                // work items: (row jr, segment sg of TB_SEG levels), segment fastest
+                int jr = 0, sg = warp;
+                walk(jr, sg, 0, nseg);
+                for (; jr < nj; walk(jr, sg, TB_WARPS, nseg)) {
+                    const int j = jlo + jr, jj = j - jb;
+                    const int i0 = 1 + sg * TB_SEG, nl = min(TB_SEG, NI + 1 - i0);
+                    const float* fp = fc + ((int64_t)i0 * jm + j) * kh + gm;
+                    float fv[TB_SEG];
+#pragma unroll
+                    for (int u = 0; u < TB_SEG; u++) fv[u] = (u < nl) ? __ldg(fp + u * GP) : 0.0f;
+                    const bool jlow = (j == 2 && jj >= 2), jhigh = (j == jm - 3 && jj + 2 < RJ);
+                    const int q0 = i0 * PL + jj * TB_LANES + lane, par0 = (i0 + j + c) & 1;
+                    const SorW<float>* wp = sw + i0 * RJ + jj;
+                    if (nl == TB_SEG && i0 > 2 && i0 + TB_SEG <= im - 3 && !jlow && !jhigh)
+                        tb_segment<false>(own, oth, wp, fv, q0, par0, ok0, ok1, PL, RJ, TB_SEG, i0, im, false, false,
+                                          w, c43, c13, c);
+                    else
+                        tb_segment<true>(own, oth, wp, fv, q0, par0, ok0, ok1, PL, RJ, nl, i0, im, jlow, jhigh,
+                                         w, c43, c13, c);
+                }
+                __syncthreads();
+            }
+            // the owned cells, with the folded rows next to the owned boundary rows
+            const int jsl = (j0 == 1) ? 0 : j0, nrow = ((j1 == jm - 1) ? jm - 1 : j1 - 1) - jsl + 1;
+            if (lane >= S && lane < S + TM) {
+                int jr = 0, i = warp;
+                walk(jr, i, 0, im);
+                for (; jr < nrow; walk(jr, i, TB_WARPS, im)) {
+                    const int j = jsl + jr;
+                    const int q = i * PL + (j - jb) * TB_LANES + lane;
+                    const int64_t g = ((int64_t)i * jm + j) * kh + (m0 + lane - S);
+                    B0[g] = sp[q];
+                    B1[g] = sp[cs + q];
+                }
+            }
+            __syncthreads();
+        }
+        if (done < nsweeps) {
+            if (!grid_barrier(bar, gridDim.x, limit)) return;
+            float* t0 = A0; A0 = B0; B0 = t0;
+            float* t1 = A1; A1 = B1; B1 = t1;
+        }
     }
 }
 
@@ -541,6 +745,18 @@ struct PoissonSolver {
     SorW<float>* w32 = nullptr;
     GridBar* bar = nullptr;
     int coop_blocks64 = 0, coop_blocks32 = 0;
+    // the temporally blocked FP32 sweeps: the second pair of packed p arrays (passes alternate between the
+    // pairs), sweeps per pass (0: not available on this grid), the tiling, its shared memory and grid
+    float* pkb32[2] = {};
+    int tb_S = 0, tb_grid = 0;
+    size_t tb_smem = 0;
+    TbPlan tb{};
+    std::vector<TbTile> tb_tiles_h;
+    TbTile* tb_tiles = nullptr;
+    // the last solve's sweeps between barriers and device time of its sweep launches (events around them)
+    cudaEvent_t sev[2] = {};
+    int spp = 0;
+    double sweep_ms = 0.0;
 };
 
 namespace {
@@ -565,6 +781,56 @@ void build_D(const PoissonSolver& P, int m, int jj, std::vector<double>& D, bool
     if (pin && m == 0 && jj == 0) {           // the pinned cell (1, 1)
         for (int q = 0; q < NI; q++) D[q] = 0.0;
         D[0] = 1.0;
+    }
+}
+
+// The tiling of the temporally blocked sweeps with S sweeps per pass: packed columns in tiles of at most
+// TB_LANES - 2S (so that tile and halo fit one shared row); rows split evenly into as many tiles as fill the
+// co-resident blocks, each of at least two rows (so that the tile owning j = 1 or jm-2 also updates j = 2 or
+// jm-3, whose updates write the folded rows it owns), and fewer, larger ones only if the shared memory
+// allows no more. Leaves tb_S = 0 where no tiling fits (the one-sweep-per-phase kernel then runs).
+void plan_tb(PoissonSolver* P, int S, int dev, int nsm) {
+    const KConst& K = P->K;
+    const int nh = P->S.n / 2, NJ = K.jm - 2;
+    const int ntm = (nh + TB_LANES - 2 * S - 1) / (TB_LANES - 2 * S);
+    int optin = 0;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    const void* fn = (S == 2) ? (const void*)sor_tb_kernel<2> : (const void*)sor_tb_kernel<3>;
+    // the kernel's limit: the device's, less the kernel's static shared memory (handles on other grids
+    // share the function)
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    optin -= (int)fa.sharedSizeBytes;
+    if (optin <= 0 || cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    for (int ntj = std::max(1, std::min(nsm / ntm, NJ / 2)); ntj <= NJ / 2 && ntm * ntj <= TB_MAX_TILES; ntj++) {
+        const int tjmax = (NJ + ntj - 1) / ntj;
+        const size_t smem = tb_smem_bytes(K.im, tjmax + 4 * S);
+        if (smem > (size_t)optin) continue;
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, 32 * TB_WARPS, smem) != cudaSuccess || b < 1) {
+            cudaGetLastError();
+            return;
+        }
+        P->tb_tiles_h.clear();
+        for (int t = 0; t < ntm * ntj; t++) {
+            const int tm = t % ntm, tj = t / ntm;
+            const int m0 = tm * nh / ntm, j0 = 1 + tj * NJ / ntj;
+            P->tb_tiles_h.push_back(TbTile{m0, (tm + 1) * nh / ntm - m0, j0, 1 + (tj + 1) * NJ / ntj});
+        }
+        P->tb = TbPlan{ntm * ntj, tjmax + 4 * S, nh};
+        P->tb_S = S;
+        P->tb_smem = smem;
+        P->tb_grid = std::min(ntm * ntj, b * nsm);
+        return;
     }
 }
 
@@ -692,11 +958,17 @@ PoissonSolver* poisson_create(const KConst& kc, const ColGeo* geo_dev, const std
     P->packed = (S.n % 2) == 0;
     P->kh = ((S.n / 2 + 31) / 32) * 32;
     const size_t npk = P->packed ? (size_t)kc.im * kc.jm * P->kh : 0, ncol = (size_t)kc.im * kc.jm;
-    const size_t o_pk64 = take(4 * npk * 8), o_pk32 = take(4 * npk * 4);
+    const size_t o_pk64 = take(4 * npk * 8), o_pk32 = take(4 * npk * 4), o_pkb32 = take(2 * npk * 4);
     const size_t o_w64 = take(P->packed ? ncol * sizeof(SorW<double>) : 0);
     const size_t o_w32 = take(P->packed ? ncol * sizeof(SorW<float>) : 0), o_bar = take(sizeof(GridBar));
+    const size_t o_tiles = take(P->packed ? TB_MAX_TILES * sizeof(TbTile) : 0);
     cudaError_t e = cudaMalloc(&P->block, bytes);
     if (e != cudaSuccess) { *err = std::string("poisson: cudaMalloc: ") + cudaGetErrorString(e); delete P; return nullptr; }
+    if ((e = cudaEventCreate(&P->sev[0])) != cudaSuccess || (e = cudaEventCreate(&P->sev[1])) != cudaSuccess) {
+        *err = std::string("poisson: cudaEventCreate: ") + cudaGetErrorString(e);
+        poisson_destroy(P);
+        return nullptr;
+    }
     char* b0 = static_cast<char*>(P->block);
     P->f64 = reinterpret_cast<double*>(b0 + o_f);
     P->p64 = reinterpret_cast<double*>(b0 + o_p);
@@ -722,6 +994,9 @@ PoissonSolver* poisson_create(const KConst& kc, const ColGeo* geo_dev, const std
             float* f = reinterpret_cast<float*>(b0 + o_pk32) + q * npk;
             if (q < 2) { P->pk64[q] = d; P->pk32[q] = f; } else { P->fk64[q - 2] = d; P->fk32[q - 2] = f; }
         }
+        P->pkb32[0] = reinterpret_cast<float*>(b0 + o_pkb32);
+        P->pkb32[1] = P->pkb32[0] + npk;
+        P->tb_tiles = reinterpret_cast<TbTile*>(b0 + o_tiles);
         P->w64 = reinterpret_cast<SorW<double>*>(b0 + o_w64);
         P->w32 = reinterpret_cast<SorW<float>*>(b0 + o_w32);
         w64h.resize(ncol);
@@ -747,6 +1022,11 @@ PoissonSolver* poisson_create(const KConst& kc, const ColGeo* geo_dev, const std
             P->coop_blocks32 = nsm * b32;
             if (P->coop_blocks64 < 1 || P->coop_blocks32 < 1) P->packed = false;
         }
+        if (P->packed) {
+            const char* ev = std::getenv("ATSAT_SOR_SWEEPS_PER_PASS");
+            const int want = ev ? std::atoi(ev) : 2;
+            if (want == 2 || want == 3) plan_tb(P, want, dev, nsm);
+        }
     }
     std::vector<float> W32(nW);
     for (size_t q = 0; q < nW; q++) W32[q] = (float)W[q];
@@ -768,10 +1048,12 @@ PoissonSolver* poisson_create(const KConst& kc, const ColGeo* geo_dev, const std
                                                cudaMemcpyHostToDevice, s)) != cudaSuccess) ||
         (!w32h.empty() && (e = cudaMemcpyAsync(P->w32, w32h.data(), w32h.size() * sizeof(SorW<float>),
                                                cudaMemcpyHostToDevice, s)) != cudaSuccess) ||
+        (!P->tb_tiles_h.empty() && (e = cudaMemcpyAsync(P->tb_tiles, P->tb_tiles_h.data(),
+                                                        P->tb_tiles_h.size() * sizeof(TbTile),
+                                                        cudaMemcpyHostToDevice, s)) != cudaSuccess) ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess) {
         *err = std::string("poisson: upload: ") + cudaGetErrorString(e);
-        cudaFree(P->block);
-        delete P;
+        poisson_destroy(P);
         return nullptr;
     }
     return P;
@@ -779,8 +1061,15 @@ PoissonSolver* poisson_create(const KConst& kc, const ColGeo* geo_dev, const std
 
 void poisson_destroy(PoissonSolver* P) {
     if (!P) return;
+    for (cudaEvent_t& ev : P->sev)
+        if (ev) cudaEventDestroy(ev);
     if (P->block) cudaFree(P->block);
     delete P;
+}
+
+void poisson_sweep_stats(PoissonSolver* P, int* sweeps_per_pass, double* sweep_ms) {
+    *sweeps_per_pass = P->spp;
+    *sweep_ms = P->sweep_ms;
 }
 
 double* poisson_f(PoissonSolver* P) { return P->f64; }
@@ -824,7 +1113,9 @@ template <> const SorW<double>* packed_w<double>(PoissonSolver* P) { return P->w
 template <> const SorW<float>* packed_w<float>(PoissonSolver* P) { return P->w32; }
 
 // `nsweeps` sweeps of the checkerboard-packed SOR in one cooperative launch: f and p packed first where
-// asked (p keeps its packed copy between calls), p unpacked and folded after. The barrier's error word is
+// asked (p keeps its packed copy between calls), p unpacked and folded after. FP32 runs the temporally
+// blocked kernel where the grid has a tiling (tb_S > 0); its passes alternate between the two pairs of
+// packed p arrays, and the pair holding the result becomes the current one. The barrier's error word is
 // read back: a barrier wait that gave up returns cudaErrorLaunchTimeout.
 template <typename T>
 cudaError_t sor_packed_run(PoissonSolver* P, const T* f, T* p, T w, int nsweeps, bool pack_f, bool pack_p) {
@@ -843,18 +1134,41 @@ cudaError_t sor_packed_run(PoissonSolver* P, const T* f, T* p, T w, int nsweeps,
     const T* f0 = fk[0];
     const T* f1 = fk[1];
     long long limit = TILE_WAIT_LIMIT;
-    void* args[] = {(void*)&K, (void*)&wt, (void*)&p0, (void*)&p1, (void*)&f0, (void*)&f1, (void*)&kh,
-                    (void*)&nsweeps, (void*)&w, (void*)&P->bar, (void*)&limit};
-    const int nb = sizeof(T) == 8 ? P->coop_blocks64 : P->coop_blocks32;
-    e = cudaLaunchCooperativeKernel((const void*)sor_packed_kernel<T>, dim3(nb), dim3(32, SORP_WARPS), args, 0,
-                                    P->stream);
-    if (e != cudaSuccess) return e;
+    if ((e = cudaEventRecord(P->sev[0], P->stream)) != cudaSuccess) return e;
+    P->spp = (sizeof(T) == 4 && P->tb_S > 0) ? P->tb_S : 1;
+    if (sizeof(T) == 4 && P->tb_S > 0) {
+        float* b0 = P->pkb32[0];
+        float* b1 = P->pkb32[1];
+        TbPlan pl = P->tb;
+        const TbTile* tiles = P->tb_tiles;
+        void* args[] = {(void*)&K, (void*)&wt, (void*)&tiles, (void*)&p0, (void*)&p1, (void*)&b0, (void*)&b1,
+                        (void*)&f0, (void*)&f1, (void*)&kh, (void*)&nsweeps, (void*)&w, (void*)&pl,
+                        (void*)&P->bar, (void*)&limit};
+        const void* fn = (P->tb_S == 2) ? (const void*)sor_tb_kernel<2> : (const void*)sor_tb_kernel<3>;
+        e = cudaLaunchCooperativeKernel(fn, dim3(P->tb_grid), dim3(32, TB_WARPS), args, P->tb_smem, P->stream);
+        if (e != cudaSuccess) return e;
+        if ((((nsweeps + P->tb_S - 1) / P->tb_S) & 1) == 1) {     // an odd number of passes: the result is in B
+            std::swap(P->pk32[0], P->pkb32[0]);
+            std::swap(P->pk32[1], P->pkb32[1]);
+        }
+    } else {
+        void* args[] = {(void*)&K, (void*)&wt, (void*)&p0, (void*)&p1, (void*)&f0, (void*)&f1, (void*)&kh,
+                        (void*)&nsweeps, (void*)&w, (void*)&P->bar, (void*)&limit};
+        const int nb = sizeof(T) == 8 ? P->coop_blocks64 : P->coop_blocks32;
+        e = cudaLaunchCooperativeKernel((const void*)sor_packed_kernel<T>, dim3(nb), dim3(32, SORP_WARPS), args, 0,
+                                        P->stream);
+        if (e != cudaSuccess) return e;
+    }
+    if ((e = cudaEventRecord(P->sev[1], P->stream)) != cudaSuccess) return e;
     unpack_kernel<T><<<pg, pb, 0, P->stream>>>(K, p, pk[0], pk[1], kh);
     if ((e = fold(P, p)) != cudaSuccess) return e;
     unsigned herr = 0;
     if ((e = cudaMemcpyAsync(&herr, &P->bar->err, sizeof(herr), cudaMemcpyDeviceToHost, P->stream)) != cudaSuccess)
         return e;
     if ((e = cudaStreamSynchronize(P->stream)) != cudaSuccess) return e;
+    float ms = 0.0f;
+    if ((e = cudaEventElapsedTime(&ms, P->sev[0], P->sev[1])) != cudaSuccess) return e;
+    P->sweep_ms += ms;
     return herr ? cudaErrorLaunchTimeout : cudaSuccess;
 }
 
@@ -915,6 +1229,8 @@ cudaError_t poisson_run_inner(PoissonSolver* P, int method, double tol, int max_
     cudaError_t e;
     *iters = 0;
     *inner_total = 0;
+    P->spp = 0;
+    P->sweep_ms = 0.0;
     const size_t fsz = (size_t)K.fsz;
     if (method == 3) {
         e = direct<double>(P, P->f64, P->p64, P->spec64, P->W64, P->tw64);

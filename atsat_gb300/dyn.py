@@ -322,7 +322,8 @@ class Dycore:
         self._ck(lib().atsat_dyn_poisson_solve(self.h, m, abi.dptr(f), abi.dptr(p), float(tol), int(max_iter),
                                                int(inner), float(omega), C.byref(st)), "poisson_solve")
         return p, {"method": abi.POISSON_METHODS[m], "iterations": st.iterations, "inner": st.inner,
-                   "converged": bool(st.converged), "rel_residual": st.rel_residual, "ms": st.ms}
+                   "converged": bool(st.converged), "rel_residual": st.rel_residual, "ms": st.ms,
+                   "sweeps_per_pass": st.sweeps_per_pass, "sweep_ms": st.sweep_ms}
 
     # ---- the reference's entry points ----
     def computeMixtureDensity(self):

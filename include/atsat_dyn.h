@@ -485,7 +485,11 @@ typedef struct atsat_dyn_poisson_stats {
     int32_t converged;         /* final relative residual <= tol */
     double  rel_residual;      /* ||src - L p||_2 / ||src||_2 in FP64 */
     double  ms;                /* device time of the solve (CUDA events) */
-    double  reserved[4];
+    int32_t sweeps_per_pass;   /* SOR sweeps between grid barriers: > 1 where the FP32 sweeps run
+                                  temporally blocked, 1 for the one-sweep-per-phase kernels */
+    int32_t pad;
+    double  sweep_ms;          /* of ms, the device time of the SOR sweep launches alone (0: no SOR) */
+    double  reserved[2];
 } atsat_dyn_poisson_stats;
 int atsat_dyn_poisson_project(atsat_dyn_t h, double* src);
 int atsat_dyn_poisson_solve(atsat_dyn_t h, int32_t method, const double* src, double* p, double tol,

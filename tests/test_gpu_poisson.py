@@ -90,19 +90,21 @@ def numpy_sweeps(g, P, f, sweeps, omega=1.0):
     return p
 
 
-@pytest.mark.parametrize("shape", [(9, 13, 17), (12, 24, 33)])
+@pytest.mark.parametrize("shape", [(9, 13, 17), (12, 24, 33), (10, 40, 121)])
 def test_sor_matches_red_black_reference(shape):
     """Red-black sweeps (omega = 1, the reference's update) from p = 0 against a numpy sweep of the same
     operator: 5 sweeps, and 53 (more than one launch of the packed solver's 50-sweep runs, its packed state
     carried from one to the next); more sweeps lower the residual (slowly: the horizontal modes are weakly
-    coupled), in FP64 and FP32 alike."""
+    coupled), in FP64 and FP32 alike. FP32 runs the temporally blocked sweeps: one tile along phi on the two
+    smaller grids, three tiles along phi and 19 along theta on 10 x 40 x 121, an odd number of passes with a
+    shorter last one at 53 sweeps."""
     from atsat_gb300 import dyn
     g, P, A, src = problem(shape)
     with dyn.Dycore(g, P) as d:
         f = d.poisson_project(src)
         p_gpu, st = d.poisson_solve("sor64", f, tol=0.0, max_iter=5, omega=1.0)
         p53, _ = d.poisson_solve("sor64", f, tol=0.0, max_iter=53, omega=1.0)
-        p53_32, _ = d.poisson_solve("sor32", f, tol=0.0, max_iter=53, omega=1.0)
+        p53_32, st53_32 = d.poisson_solve("sor32", f, tol=0.0, max_iter=53, omega=1.0)
         _, st10 = d.poisson_solve("sor64", f, tol=0.0, max_iter=400, omega=1.0)
         _, st32 = d.poisson_solve("sor32", f, tol=0.0, max_iter=400, omega=1.0)
     n = g.km - 1
@@ -117,6 +119,7 @@ def test_sor_matches_red_black_reference(shape):
           f" {st32['rel_residual']:.3e}")
     assert err <= 1e-12 and err53 <= 1e-12
     assert err53_32 <= 1e-5
+    assert st53_32["sweeps_per_pass"] > 1 and st["sweeps_per_pass"] == 1     # FP32 temporally blocked
     # the folded boundary planes and the seam as the reference leaves them
     assert np.allclose(p53[0], 4 / 3 * p53[1] - 1 / 3 * p53[2], rtol=0, atol=1e-12 * np.max(np.abs(p53)))
     assert np.array_equal(p53[:, :, -1], p53[:, :, 0])
