@@ -43,9 +43,11 @@ __device__ __forceinline__ double get(const BCArgs& A, int id, int64_t c) { retu
 __device__ __forceinline__ void put(const BCArgs& A, int id, int64_t c, double x) {
     A.f[id][c] = x;
     if (A.s32[id]) {
-        const float hi = (float)x;
+        // the FP32 copy (and w's low word) by the integer-pipe conversions: GB300 runs the hardware
+        // float <-> double conversions at its FP64 rate
+        const float hi = d2f(x);
         A.s32[id][c] = hi;
-        if (id == ATSAT_F_W && A.wlo) A.wlo[c] = (float)(x - (double)hi);
+        if (id == ATSAT_F_W && A.wlo) A.wlo[c] = d2f(x - f2d(hi));
     }
 }
 

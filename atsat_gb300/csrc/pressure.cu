@@ -7,6 +7,8 @@
 // the other colour's p and its own source. The outer boundary of the relaxation (:718-746: radial
 // planes, then polar planes, then the seam copy) is one kernel that writes boundary cells only and
 // reads interior cells only, so it has no ordering hazard of its own.
+#include <algorithm>
+
 #include "dyn_common.cuh"
 
 namespace atsat {
@@ -172,29 +174,25 @@ __device__ __forceinline__ double pval(const KConst& K, const double* p, int i, 
     return pval_i(K, p, i, j, k);
 }
 
+// blockIdx.z picks the part: 0 the seam column k = km-1 of every (i, j) (row blockIdx.y = i, j along x);
+// 1 the radial planes i = 0 and im-1 (row blockIdx.y = side * jm + j, k along x); 2 the polar planes
+// j = 0 and jm-1 at interior i (row blockIdx.y = side * (im-2) + i-1, k along x). Every value is formed from
+// interior cells only, so the parts are independent; no index needs a division.
 __global__ void press_boundary_kernel(const KConst K, double* __restrict__ p) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
     const int im = K.im, jm = K.jm, km = K.km;
-    const int64_t nA = (int64_t)im * jm;                     // seam column, all (i, j)
-    const int64_t nB = 2LL * jm * (km - 1);                  // radial planes
-    const int64_t nC = 2LL * (im - 2) * (km - 1);            // polar planes, interior i
     int i, j, k;
-    if (e < nA) {
-        i = (int)(e / jm); j = (int)(e % jm); k = km - 1;
-    } else if (e < nA + nB) {
-        const int64_t q = e - nA;
-        k = (int)(q % (km - 1));
-        const int64_t r = q / (km - 1);
-        j = (int)(r % jm);
-        i = (r / jm) ? im - 1 : 0;
-    } else if (e < nA + nB + nC) {
-        const int64_t q = e - nA - nB;
-        k = (int)(q % (km - 1));
-        const int64_t r = q / (km - 1);
-        i = 1 + (int)(r % (im - 2));
-        j = (r / (im - 2)) ? jm - 1 : 0;
+    if (blockIdx.z == 0) {
+        if (y >= im || x >= jm) return;
+        i = y; j = x; k = km - 1;
+    } else if (blockIdx.z == 1) {
+        if (y >= 2 * jm || x >= km - 1) return;
+        const bool top = y >= jm;
+        i = top ? im - 1 : 0; j = top ? y - jm : y; k = x;
     } else {
-        return;
+        if (y >= 2 * (im - 2) || x >= km - 1) return;
+        const bool top = y >= im - 2;
+        i = 1 + (top ? y - (im - 2) : y); j = top ? jm - 1 : 0; k = x;
     }
     const int ks = (k == km - 1) ? 0 : k;
     p[((int64_t)i * jm + j) * K.kp + k] = pval(K, p, i, j, ks);
@@ -246,8 +244,8 @@ cudaError_t launch_press_sweep(const KConst& kc, const ColGeo* geo, const double
 }
 
 cudaError_t launch_press_boundary(const KConst& kc, double* p, cudaStream_t s) {
-    const int64_t n = (int64_t)kc.im * kc.jm + 2LL * kc.jm * (kc.km - 1) + 2LL * (kc.im - 2) * (kc.km - 1);
-    press_boundary_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(kc, p);
+    const int width = std::max(kc.jm, kc.km), rows = std::max(kc.im, 2 * std::max(kc.jm, kc.im - 2));
+    press_boundary_kernel<<<dim3((width + 127) / 128, rows, 3), 128, 0, s>>>(kc, p);
     return cudaGetLastError();
 }
 

@@ -113,19 +113,22 @@ def reduce_max(world, x: float) -> float:
 
 
 class Clocks:
-    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi samples of SM clock and throttle reasons, kept for the timed region: the sampler starts
+    ahead of it (nvidia-smi takes a moment to start) and samples every 50 ms with a timestamp; the samples
+    between mark_start() and mark_stop() are the ones reported."""
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self):
         self.p = None
         self.lines = []
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
-                                       "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                                       "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except OSError:
@@ -134,6 +137,20 @@ class Clocks:
     def _read(self):
         for line in self.p.stdout:
             self.lines.append(line.strip())
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_stop(self):
+        self.t1 = time.time()
+
+    @staticmethod
+    def _when(stamp):
+        import datetime
+        try:
+            return datetime.datetime.strptime(stamp.strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return None
 
     def stop(self):
         if not self.p:
@@ -145,22 +162,31 @@ class Clocks:
             self.p.kill()
         self.t.join(timeout=2)
         vis = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
-            if len(f) < 9 or (vis.isdigit() and f[0] != vis):
+            if len(f) < 10 or (vis.isdigit() and f[1] != vis):
                 continue
+            rows.append((self._when(f[0]), f))
+        inside = [f for w, f in rows if w is not None and self.t0 is not None and self.t1 is not None
+                  and self.t0 <= w <= self.t1]
+        window = "timed region"
+        if not inside:                    # no timestamped sample inside: every sample of the run
+            inside = [f for _, f in rows]
+            window = "whole measurement (none inside the timed region)"
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for f in inside:
             try:
-                sm.append(float(f[1]))
-                smax.append(float(f[2]))
+                sm.append(float(f[2]))
+                smax.append(float(f[3]))
             except ValueError:
                 continue
-            for n, v in zip(names, f[5:9]):
+            for n, v in zip(names, f[6:10]):
                 if v.lower() == "active":
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "window": window}
 
 
 def peaks():
@@ -310,6 +336,8 @@ def measure(a, rank, world, g, P, st, pinned, precision):
     d.set_tables(st.cell_vbar0, st.cell_ubar0, st.p_baro)
 
     # ---- device-resident throughput ----
+    clocks = Clocks()
+    clocks.start()                        # ahead of the timed region: nvidia-smi needs a moment to start
     d.iterate(1, a.warmup)
     tune = None
     if precision == "mixed" and a.stage_variant == "auto":
@@ -322,29 +350,45 @@ def measure(a, rank, world, g, P, st, pinned, precision):
             d.set_march_levels(a.march_levels)
         tune = {"stage_variant": a.stage_variant, "march_levels": d.march_levels()}
     it0 = a.warmup + 1
-    # the timed region profiles the RK stage kernels only (the roofline's kernel): two event records per
-    # stage launch; every class is timed afterwards in a separate pass of its own
-    d.profile_classes([abi.K_RK_STAGE])
-    d.profile_reset()
+    d.iterate(it0, 2)                     # untimed: a capture starts from two settled resident iterations
+    it0 += 2
+    # the headline timed region: the resident loop replayed as a CUDA graph of two iterations (the public
+    # atsat_dyn_graph_capture / atsat_dyn_graph_launch path; replays are bit-identical to plain iterations,
+    # the pressure call on the even one), plus one plain iteration when the step count is odd
+    d.graph_capture(it0, 2)
+    d.graph_launch(1)                     # untimed: the first replay uploads the graph
+    d.sync()
+    it0 += 2
     l0 = d.launches()
-    clocks = Clocks()
-    clocks.start()
     barrier(world)
+    clocks.mark_start()
     d.timer_start()
-    d.iterate(it0, a.steps)
+    d.graph_launch(a.steps // 2)
+    if a.steps % 2:
+        d.iterate(it0 + a.steps - 1, 1)
     ms = d.timer_stop()
+    clocks.mark_stop()
     barrier(world)
     clk = clocks.stop()
     launches = d.launches() - l0
-    n_rk, ms_rk = d.profile_read(abi.K_RK_STAGE)
-    d.profile(False)
     ms = reduce_max(world, ms)
     value = world * a.steps * g.cells / (ms / 1e3) / 1e6
+    it0 += a.steps
+    # the roofline's kernel timed live: the same iterations launched one by one, with two event records
+    # around every RK stage launch group (events cannot time single kernels inside a graph replay)
+    d.profile_classes([abi.K_RK_STAGE])
+    d.profile_reset()
+    d.timer_start()
+    d.iterate(it0, a.steps)
+    ms_plain = reduce_max(world, d.timer_stop())
+    n_rk, ms_rk = d.profile_read(abi.K_RK_STAGE)
+    d.profile(False)
+    it0 += a.steps
     # per-class breakdown: an even number of further iterations with every class profiled
     nb = max(2, min(a.steps, 20) // 2 * 2)
     d.profile(True)
     d.profile_reset()
-    d.iterate(it0 + a.steps, nb)
+    d.iterate(it0, nb)
     kern = {abi.K_NAMES[c]: dict(zip(("launches", "ms"), d.profile_read(c))) for c in range(len(abi.K_NAMES))}
     kern["iterations"] = nb
     d.profile(False)
@@ -373,7 +417,7 @@ def measure(a, rank, world, g, P, st, pinned, precision):
         d.sync()
         return up, down
 
-    it = it0 + a.steps + nb
+    it = it0 + nb
     e2e = None
     d.set_async(True)
     if a.e2e_steps > 0:
@@ -428,7 +472,9 @@ def measure(a, rank, world, g, P, st, pinned, precision):
             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
             "traffic": traffic_per_launch("rk_stage_" + precision + ("_" + tune["stage_variant"] if tune else "")),
             "algorithmic_bytes_per_launch": bytes_per_launch,
-            "launches": n_rk, "mean_launch_ms": avg_ms}
+            "launches": n_rk, "mean_launch_ms": avg_ms,
+            "timed_region": f"{a.steps} iterations launched one by one after the graph-timed region "
+                            f"({ms_plain / a.steps:.4f} ms per iteration there)"}
     if precision == "fp64":
         roof["note"] = "bound by GB300's FP64 pipe (2 DFMA per SM per cycle), not by HBM"
         # the FP64 roofline that binds: FP64 instructions per interior cell and stage counted by ncu
@@ -459,6 +505,8 @@ def measure(a, rank, world, g, P, st, pinned, precision):
         pe = {"value": world * n_pe * g.cells / (ms_pe / 1e3) / 1e6, "unit": UNIT, "ms_per_step": ms_pe / n_pe,
               "steps": n_pe}
     return {"value": value, "ms_per_step": ms / a.steps, "e2e": e2e, "roofline": roof, "gpu_launches": launches,
+            "timed_loop": "the resident loop as replays of a captured two-iteration CUDA graph "
+                          "(atsat_dyn_graph_capture / atsat_dyn_graph_launch)",
             "clocks": clk, "kernels_ms": kern, "tune": tune, "pressure_every_step": pe}
 
 
@@ -485,7 +533,7 @@ def run_ours(a, rank, world):
            "vs_baseline": None, "dtype": "f32+f64" if head == "mixed" else "f64", "data": "synthetic",
            "config": dict(config(g, head), **(r["tune"] or {})), "e2e": r["e2e"], "roofline": r["roofline"],
            "gpu_launches": r["gpu_launches"], "clocks": r["clocks"], "kernels_ms": r["kernels_ms"],
-           "pressure_every_step": r["pressure_every_step"]}
+           "pressure_every_step": r["pressure_every_step"], "timed_loop": r["timed_loop"]}
     for p in a.precisions[1:]:
         out[p] = {k: res[p][k] for k in ("value", "ms_per_step", "e2e", "roofline", "gpu_launches", "clocks",
                                          "pressure_every_step")}
