@@ -1248,7 +1248,7 @@ cudaError_t poisson_run_inner(PoissonSolver* P, int method, double tol, int max_
     }
     if ((e = cudaMemsetAsync(P->p64, 0, fsz * 8, P->stream)) != cudaSuccess) return e;
     if (method == 0 || method == 1) {
-        const int check = 50;
+        const int check = 200;     // sweeps per launch between residual checks
         if (method == 1) {
             if ((e = cudaMemsetAsync(P->p32, 0, fsz * 4, P->stream)) != cudaSuccess) return e;
             convert_kernel<float, double><<<cell_grid(K), dim3(32, 8), 0, P->stream>>>(K, P->e32, P->f64);

@@ -462,7 +462,7 @@ int atsat_dyn_ensemble_run(const atsat_dyn_t* members, int32_t n, int32_t reps, 
  * on i = 1..im-2, j = 1..jm-2, k = 0..km-2, p[0] = c43 p[1] - c13 p[2] in r and theta, periodic in phi.
  * No reference counterpart: the reference only smooths (one red-black sweep per call). Methods:
  *   SOR64 / SOR32   red-black SOR (the reference's update, over-relaxed by omega), max_iter sweeps or
- *                   until ||src - L p|| / ||src|| <= tol (checked every 50 sweeps);
+ *                   until ||src - L p|| / ||src|| <= tol (checked every 200 sweeps);
  *   REFINE_SOR      FP64 defect correction, `inner` FP32 SOR sweeps per correction;
  *   DIRECT64 / 32   real DFT over phi and a block-tridiagonal solve per mode (exact up to rounding);
  *   REFINE_DIRECT   FP64 defect correction with FP32 direct inner solves, until tol or max_iter corrections.
