@@ -1186,6 +1186,18 @@ void tune_cache_store(atsat_dyn* h, double ms) {
 
 // The march depth before any tuning: one run of all interior levels per (k, j) tile when the tiles alone
 // give about two blocks per SM, else the levels split into runs so that they do.
+// The compact rings of the march kernel's intermediate stages (three blocks per SM) apply where the stage
+// streams at most 12 point arrays; ATSAT_MARCH_COMPACT=0 keeps the regular rings (two blocks per SM).
+bool march_compact() {
+    static const bool on = [] {
+        const char* e = std::getenv("ATSAT_MARCH_COMPACT");
+        return !(e && e[0] == '0' && e[1] == 0);
+    }();
+    return on;
+}
+
+// The default march depth: runs of radial levels such that the intermediate stage's blocks fill about 1.8
+// waves of the resident blocks (measured best at 41x181x361, where the autotuner picks the same 13 levels).
 int default_march_levels(const atsat_dyn* h) {
     const KConst& K = h->kc;
     int nsm = 0;
@@ -1193,9 +1205,11 @@ int default_march_levels(const atsat_dyn* h) {
         cudaGetLastError();
         nsm = 152;
     }
+    const int n_pt = 10 + (K.precip_on ? 1 : 0) + (K.rad_on ? 2 : 0) + (K.tmf_on ? 1 : 0);
+    const int per_sm = (march_compact() && n_pt <= 12) ? 3 : 2;
     const int64_t tiles = (int64_t)((K.km - 1 + TILE_K - 1) / TILE_K) * ((K.jm - 4 + TILE_J - 1) / TILE_J);
     const int interior = K.im - 2;
-    int64_t runs = tiles > 0 ? (2LL * nsm + tiles / 2) / tiles : 1;
+    int64_t runs = tiles > 0 ? (int64_t)((double)per_sm * nsm * 1.8 / (double)tiles + 0.5) : 1;
     if (runs < 1) runs = 1;
     if (runs > interior) runs = interior;
     return (int)((interior + runs - 1) / runs);
@@ -1210,6 +1224,7 @@ MarchPlan make_plan_march(atsat_dyn* h, const MixedIO& io, int mode) {
     pl.wait_limit = h->wait_limit;
     pl.withhold = h->test_withhold;
     pl.levels = h->march_levels;
+    pl.compact = march_compact();
     const bool dl = io.dl_in[0] != nullptr;
     int n = 0;
     auto halo = [&](const float* p) { pl.halo[n++] = arr_index(h, p); };

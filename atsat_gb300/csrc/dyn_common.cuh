@@ -370,6 +370,7 @@ struct MarchPlan {
     unsigned int* err;
     long long wait_limit;
     int withhold;                  // test hook: the producer leaves the last `withhold` level groups unissued
+    int compact;                   // intermediate stages with at most 12 point arrays: three blocks per SM
 };
 cudaError_t launch_rk_mom_march(const TileMaps& maps, const MixedConstF& kf, const MixedIO& io, const StageParams& sp,
                                 const MarchPlan& plan, int mode, cudaStream_t s);

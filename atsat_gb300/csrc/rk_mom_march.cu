@@ -41,21 +41,28 @@ constexpr int GEO_F = TILE_J * 16;                // 128 floats: eight ColGeoF
 constexpr uint32_t PLANE_BYTES = PLANE_F * 4, SEAM_BYTES = SEAM_F * 4, PT_BYTES = PT_F * 4, GEO_BYTES = GEO_F * 4;
 constexpr int NCW = TILE_J;
 constexpr int THREADS = (NCW + 1) * 32;
-constexpr int NHG = 4;                            // halo slots
 constexpr int NHA_MAX = 9;
 static_assert((HP_F * 4) % 128 == 0 && (PLANE_PAD * 4) % 128 == 0 && (PT_BYTES % 128) == 0 && GEO_BYTES % 128 == 0,
               "slot alignment");
 static_assert(PLANE_PAD >= PLANE_F, "plane padding");
 
-template <int MODE>
+// The rings of one launch. Regular: 4 halo slots and 3 point slots (2 at the final stage), two blocks per
+// SM. Compact (intermediate stages with at most 12 point arrays): 3 halo slots and 2 point slots in 74 KB,
+// three blocks per SM; its producer issues each level's point group one level ahead (H0 H1 P0 H2 P1 ...),
+// so that both rings keep one level in flight.
+template <int MODE, bool CMP>
 struct Shape {
-    static constexpr int NPG = (MODE == MODE_FINAL) ? 2 : 3;            // point slots
-    static constexpr int NPT = (MODE == MODE_FINAL) ? MARCH_MAX_PT : 14;
+    static constexpr int NHG = CMP ? 3 : 4;                                         // halo slots
+    static constexpr int NPG = CMP ? 2 : ((MODE == MODE_FINAL) ? 2 : 3);            // point slots
+    static constexpr int NPT = (MODE == MODE_FINAL) ? MARCH_MAX_PT : (CMP ? 12 : 14);
+    static constexpr int MINB = CMP ? 3 : 2;                                        // blocks per SM
     static constexpr int PG_F = GEO_F + NPT * PT_F;
     static constexpr int HG_F = NHA_MAX * HP_F;
     static constexpr size_t SMEM = (size_t)(NHG * HG_F + NPG * PG_F) * 4 + 2 * (NHG + NPG) * 8;
 };
-static_assert(Shape<MODE_STAGE>::SMEM <= 113 * 1024 && Shape<MODE_FINAL>::SMEM <= 113 * 1024, "two blocks per SM");
+static_assert(Shape<MODE_STAGE, false>::SMEM <= 113 * 1024 && Shape<MODE_FINAL, false>::SMEM <= 113 * 1024,
+              "two blocks per SM");
+static_assert(Shape<MODE_STAGE, true>::SMEM <= 74 * 1024, "three blocks per SM");
 
 // point items before the optional ones
 enum { P_NUE = 0, P_DPR, P_GU, P_BAN, P_BPS, P_DPTH, P_GV, P_DPPH, P_GW, P_DPS, N_PT_FIXED };
@@ -100,12 +107,13 @@ __device__ __forceinline__ void put(const MixedIO& io, const StageParams& sp, in
     if (sp.write_all_rhs || q < 3) io.rhs[q][c] = f2d(r);
 }
 
-template <int MODE, bool HAS_DL>
-__global__ void __launch_bounds__(THREADS, 2)
+template <int MODE, bool HAS_DL, bool CMP>
+__global__ void __launch_bounds__(THREADS, (CMP ? 3 : 2))
 rk_mom_march_kernel(const __grid_constant__ CUtensorMap map_plane, const __grid_constant__ CUtensorMap map_seam,
                     const __grid_constant__ CUtensorMap map_pt, const MixedConstF K, const MixedIO io,
                     const StageParams sp, const MarchPlan plan) {
-    using S = Shape<MODE>;
+    using S = Shape<MODE, CMP>;
+    constexpr int NHG = S::NHG;
     constexpr int NPG = S::NPG;
     constexpr int DL = HAS_DL ? 1 : 0;
     constexpr int hU = 0, hV = 1 + DL, hW = 2 + 2 * DL, hT = 4 + 3 * DL, NHA = 5 + 4 * DL;
@@ -139,7 +147,8 @@ rk_mom_march_kernel(const __grid_constant__ CUtensorMap map_plane, const __grid_
     __syncthreads();
 
     if (warp == NCW) {
-        // ---- producer: H(0), H(1), then per level m: H(m+2), P(m); H(g) is plane ib-1+g, P(m) level ib+m ----
+        // ---- producer: H(0), H(1), then per level m: H(m+2), P(m) (compact: H(0), H(1), P(0), then H(m+2),
+        // P(m+1)); H(g) is plane ib-1+g, P(m) level ib+m ----
         if (lane == 0) {
             const int total = 2 * nlev + 2;
             const int n_issue = total - plan.withhold;
@@ -148,7 +157,7 @@ rk_mom_march_kernel(const __grid_constant__ CUtensorMap map_plane, const __grid_
             int gh = 0, gp = 0;
             bool ok = true;
             for (int n = 0; n < n_issue; n++) {
-                const bool halo = n < 2 || ((n - 2) & 1) == 0;
+                const bool halo = CMP ? (n < 2 || (n >= 3 && ((n - 3) & 1) == 0)) : (n < 2 || ((n - 2) & 1) == 0);
                 if (halo) {
                     const int s = gh % NHG;
                     if (gh >= NHG && !mbar_wait(rh.empty(s), (uint32_t)(((gh / NHG) - 1) & 1), plan.wait_limit)) {
@@ -380,18 +389,18 @@ rk_mom_march_kernel(const __grid_constant__ CUtensorMap map_plane, const __grid_
     }
 }
 
-template <int MODE, bool HAS_DL>
+template <int MODE, bool HAS_DL, bool CMP>
 cudaError_t launch_one(const TileMaps& maps, const MixedConstF& kf, const MixedIO& io, const StageParams& sp,
                        const MarchPlan& plan, dim3 grid, cudaStream_t s) {
     static bool attr = false;
-    constexpr size_t smem = Shape<MODE>::SMEM;
+    constexpr size_t smem = Shape<MODE, CMP>::SMEM;
     if (!attr) {
-        const cudaError_t e = cudaFuncSetAttribute(rk_mom_march_kernel<MODE, HAS_DL>,
+        const cudaError_t e = cudaFuncSetAttribute(rk_mom_march_kernel<MODE, HAS_DL, CMP>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    rk_mom_march_kernel<MODE, HAS_DL><<<grid, THREADS, smem, s>>>(
+    rk_mom_march_kernel<MODE, HAS_DL, CMP><<<grid, THREADS, smem, s>>>(
         *reinterpret_cast<const CUtensorMap*>(maps.plane1), *reinterpret_cast<const CUtensorMap*>(maps.seam1),
         *reinterpret_cast<const CUtensorMap*>(maps.pt1), kf, io, sp, plan);
     return cudaGetLastError();
@@ -406,16 +415,19 @@ cudaError_t launch_rk_mom_march(const TileMaps& maps, const MixedConstF& kf, con
     if (nk <= 0 || nj <= 0 || kf.im < 3) return cudaSuccess;
     const bool has_dl = io.dl_in[0] != nullptr;
     const int nha = has_dl ? 9 : 5;
-    const int npt_max = mode == MODE_FINAL ? Shape<MODE_FINAL>::NPT : Shape<MODE_STAGE>::NPT;
+    const int npt_max = mode == MODE_FINAL ? Shape<MODE_FINAL, false>::NPT : Shape<MODE_STAGE, false>::NPT;
     if (mode == MODE_RHS || kf.divu_on || plan.levels < 1 || plan.n_halo != nha || plan.n_pt < N_PT_FIXED ||
         plan.n_pt > npt_max || (mode == MODE_FINAL) != (plan.p_dl >= 0) || plan.withhold < 0)
         return cudaErrorInvalidValue;
     const dim3 grid(nk, nj, (kf.im - 2 + plan.levels - 1) / plan.levels);
+    if (mode == MODE_STAGE && plan.compact && plan.n_pt <= Shape<MODE_STAGE, true>::NPT)
+        return has_dl ? launch_one<MODE_STAGE, true, true>(maps, kf, io, sp, plan, grid, s)
+                      : launch_one<MODE_STAGE, false, true>(maps, kf, io, sp, plan, grid, s);
     if (mode == MODE_STAGE)
-        return has_dl ? launch_one<MODE_STAGE, true>(maps, kf, io, sp, plan, grid, s)
-                      : launch_one<MODE_STAGE, false>(maps, kf, io, sp, plan, grid, s);
-    return has_dl ? launch_one<MODE_FINAL, true>(maps, kf, io, sp, plan, grid, s)
-                  : launch_one<MODE_FINAL, false>(maps, kf, io, sp, plan, grid, s);
+        return has_dl ? launch_one<MODE_STAGE, true, false>(maps, kf, io, sp, plan, grid, s)
+                      : launch_one<MODE_STAGE, false, false>(maps, kf, io, sp, plan, grid, s);
+    return has_dl ? launch_one<MODE_FINAL, true, false>(maps, kf, io, sp, plan, grid, s)
+                  : launch_one<MODE_FINAL, false, false>(maps, kf, io, sp, plan, grid, s);
 }
 
 }  // namespace atsat

@@ -423,7 +423,10 @@ enum {
 int atsat_dyn_set_stage_variant(atsat_dyn_t h, int32_t variant);
 int atsat_dyn_get_stage_variant(atsat_dyn_t h, int32_t* variant);
 /* The MARCH variant's march depth: radial levels per block (1 .. im-2; the interior levels are split into
- * runs of this length). The default gives about two blocks per SM; atsat_dyn_autotune tunes it. */
+ * runs of this length). The default fills about 1.8 waves of resident blocks; atsat_dyn_autotune tunes it.
+ * Intermediate stages that stream at most 12 point arrays (the radiation, precipitation and thermal
+ * mass-flux sources off) run compact rings, three blocks per SM; ATSAT_MARCH_COMPACT=0 (read once per
+ * process) keeps the regular rings, two blocks per SM. */
 int atsat_dyn_set_march_levels(atsat_dyn_t h, int32_t levels);
 int atsat_dyn_get_march_levels(atsat_dyn_t h, int32_t* levels);
 /* Time each available stage variant on this handle's grid (`reps` launches of an intermediate RK

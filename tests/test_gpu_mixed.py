@@ -245,14 +245,23 @@ def test_stage_variants_agree(variant):
     assert not bad, bad
 
 
-@pytest.mark.parametrize("shape,levels", [((21, 91, 181), 1), ((21, 91, 181), 2), ((21, 91, 181), 5),
-                                          ((21, 91, 181), 19), ((12, 40, 70), 3), ((10, 20, 36), 8)])
-def test_march_depths_agree(shape, levels):
+SOURCES_ON = dict(rad_coupling=1.0, thermal_massflux=1.0)
+
+
+@pytest.mark.parametrize("shape,levels,knobs", [((21, 91, 181), 1, {}), ((21, 91, 181), 2, {}),
+                                               ((21, 91, 181), 5, {}), ((21, 91, 181), 19, {}),
+                                               ((12, 40, 70), 3, {}), ((10, 20, 36), 8, {}),
+                                               ((21, 91, 181), 3, SOURCES_ON), ((21, 91, 181), 7, SOURCES_ON),
+                                               ((12, 40, 70), 4, SOURCES_ON)])
+def test_march_depths_agree(shape, levels, knobs):
     """The radial march at several march depths (runs of 1 level to whole columns, runs that do not divide
     the interior levels evenly, odd-seam grids) runs the same per-cell arithmetic as the direct kernel:
-    after three iterations their states agree far inside the mixed-precision bar."""
+    after three iterations their states agree far inside the mixed-precision bar. At the default knobs the
+    intermediate stages stream 11 point arrays and run the compact rings (three blocks per SM, each level's
+    point group issued a level ahead); with the radiation and thermal mass-flux sources on, 14 point arrays
+    and the regular rings."""
     from atsat_gb300 import dyn
-    g, P, st = case(shape, seed=59, exercise=True)
+    g, P, st = case(shape, seed=59, exercise=True, **knobs)
     a = st.copy()
     with dyn.Dycore(g, dict(P, precision=1)) as d:
         d.set_stage_variant(MARCH)
