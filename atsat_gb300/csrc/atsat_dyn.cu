@@ -492,7 +492,10 @@ bool make_tile_maps(atsat_dyn* h) {
     }
     const KConst& K = h->kc;
     if ((reinterpret_cast<uintptr_t>(h->slab32) & 15u) != 0) return false;
-    const cuuint64_t dims[4] = {(cuuint64_t)K.kp, (cuuint64_t)K.jm, (cuuint64_t)K.im, (cuuint64_t)h->n32};
+    // the innermost extent is km, not the padded row kp: the padding columns are never a cell or a stencil
+    // neighbour (the east neighbour of km-2 is the periodic seam k = 0), so boxes of the last k-tile read
+    // only the row's km values and the tensor copy fills the rest of the box with zeros
+    const cuuint64_t dims[4] = {(cuuint64_t)K.km, (cuuint64_t)K.jm, (cuuint64_t)K.im, (cuuint64_t)h->n32};
     const cuuint64_t strides[3] = {(cuuint64_t)K.kp * 4, (cuuint64_t)K.plane * 4, (cuuint64_t)K.fsz * 4};
     const cuuint32_t box_main[4] = {TILE_BX, TILE_BY, TILE_BZ, 1};
     const cuuint32_t box_seam[4] = {TILE_SEAM_X, TILE_J, TILE_I, 1};
