@@ -298,40 +298,65 @@ __device__ __forceinline__ void walk(int& a, int& b, int step, int nb) {
     while (b >= nb) { b -= nb; a++; }
 }
 
-// 4-byte asynchronous copy global -> shared (no register round trip; many in flight per thread)
-__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+// asynchronous copy of a pair of floats global -> shared (no register round trip; many in flight per thread)
+__device__ __forceinline__ void cp_async8(float* dst, const float* src) {
     const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-constexpr int TB_SEG = 4;        // radial levels per work item of a half-sweep
+constexpr int TB_SEG = 2;        // radial levels per work item of a half-sweep
 
-// One work item: the cells of one shared column (row jj, this lane) at levels i0 .. i0+nl-1 of colour c.
+// One work item of a half-warp: the cells of one shared row jj at levels i0 .. i0+nl-1 of colour c, a pair of
+// adjacent packed columns per lane (8-byte shared loads and stores). The pair's cells share the parity
+// par (k = 2 m + par), so their phi neighbours in the other colour are the pair (q, q+1) and one of q-1,
+// q+2: par 0: east, west = (q, q-1) and (q+1, q); par 1: (q+1, q) and (q+2, q+1). vx / vy: whether each
+// cell of the pair is updated for parity 0 (a) and 1 (b); a cell that is not keeps its value.
 // FOLDS: the item may hold a cell two away from a folded boundary (levels 2 or im-3, rows 2 or jm-3).
 template <bool FOLDS>
 __device__ __forceinline__ void tb_segment(float* __restrict__ own, const float* __restrict__ oth,
-                                           const SorW<float>* wp, const float (&fv)[TB_SEG], int q, int par,
-                                           bool ok0, bool ok1, int PL, int RJ, int nl, int i0, int im, bool jlow,
-                                           bool jhigh, float w, float c43, float c13, int c) {
+                                           const SorW<float>* wp, const float2 (&fv)[TB_SEG], int q, int par,
+                                           bool a0, bool a1, bool b0, bool b1, int PL, int RJ, int nl, int i0,
+                                           int im, bool jlow, bool jhigh, float w, float c43, float c13, int c) {
 #pragma unroll
     for (int u = 0; u < TB_SEG; u++) {
-        if (u < nl && (par ? ok1 : ok0)) {
+        const bool vx = par ? b0 : a0, vy = par ? b1 : a1;
+        if (u < nl && (vx || vy)) {
             const SorW<float> W = wp[u * RJ];
-            const float up = oth[q + PL], dn = oth[q - PL], nn = oth[q + TB_LANES], ss = oth[q - TB_LANES];
-            const float acc = (up + dn) * W.num1 + (nn + ss) * W.num2 + (oth[q + par] + oth[q - 1 + par]) * W.num3;
-            const float old = own[q];
-            const float nv = (acc - fv[u]) * W.rden;
-            const float pn = old + w * (nv - old);
-            own[q] = pn;
+            const float2 up = *reinterpret_cast<const float2*>(oth + q + PL);
+            const float2 dn = *reinterpret_cast<const float2*>(oth + q - PL);
+            const float2 nn = *reinterpret_cast<const float2*>(oth + q + TB_LANES);
+            const float2 ss = *reinterpret_cast<const float2*>(oth + q - TB_LANES);
+            const float2 pq = *reinterpret_cast<const float2*>(oth + q);
+            const float wl = oth[q - 1], er = oth[q + 2];
+            const float ex = par ? pq.y : pq.x, wx = par ? pq.x : wl;
+            const float ey = par ? er : pq.y, wy = par ? pq.y : pq.x;
+            const float accx = (up.x + dn.x) * W.num1 + (nn.x + ss.x) * W.num2 + (ex + wx) * W.num3;
+            const float accy = (up.y + dn.y) * W.num1 + (nn.y + ss.y) * W.num2 + (ey + wy) * W.num3;
+            const float2 old = *reinterpret_cast<const float2*>(own + q);
+            const float nvx = (accx - fv[u].x) * W.rden, nvy = (accy - fv[u].y) * W.rden;
+            const float pnx = old.x + w * (nvx - old.x), pny = old.y + w * (nvy - old.y);
+            *reinterpret_cast<float2*>(own + q) = make_float2(vx ? pnx : old.x, vy ? pny : old.y);
             if (FOLDS) {
-                // the folded boundary cells this cell stands two away from (same colour)
-                const float self = (c == 0) ? old : pn;
+                // the folded boundary cells the pair's cells stand two away from (same colour)
+                const float sx = (c == 0) ? old.x : pnx, sy = (c == 0) ? old.y : pny;
                 const int i = i0 + u;
-                if (i == 2) own[q - 2 * PL] = c43 * dn - c13 * self;
-                if (i == im - 3) own[q + 2 * PL] = c43 * up - c13 * self;
-                if (jlow) own[q - 2 * TB_LANES] = c43 * ss - c13 * self;
-                if (jhigh) own[q + 2 * TB_LANES] = c43 * nn - c13 * self;
+                if (i == 2) {
+                    if (vx) own[q - 2 * PL] = c43 * dn.x - c13 * sx;
+                    if (vy) own[q + 1 - 2 * PL] = c43 * dn.y - c13 * sy;
+                }
+                if (i == im - 3) {
+                    if (vx) own[q + 2 * PL] = c43 * up.x - c13 * sx;
+                    if (vy) own[q + 1 + 2 * PL] = c43 * up.y - c13 * sy;
+                }
+                if (jlow) {
+                    if (vx) own[q - 2 * TB_LANES] = c43 * ss.x - c13 * sx;
+                    if (vy) own[q + 1 - 2 * TB_LANES] = c43 * ss.y - c13 * sy;
+                }
+                if (jhigh) {
+                    if (vx) own[q + 2 * TB_LANES] = c43 * nn.x - c13 * sx;
+                    if (vy) own[q + 1 + 2 * TB_LANES] = c43 * nn.y - c13 * sy;
+                }
             }
         }
         q += PL;
@@ -363,22 +388,26 @@ __global__ void __launch_bounds__(32 * TB_WARPS) sor_tb_kernel(const KConst K, c
             const TbTile T = tiles[t];
             const int m0 = T.m0, TM = T.TM, j0 = T.j0, j1 = T.j1;
             const int jb = j0 - 2 * S;          // the row of shared row 0
-            int gm = m0 - S + lane;             // this lane's packed column, wrapped around the ring
-            gm = gm < 0 ? gm + nh : (gm >= nh ? gm - nh : gm);
             {
-                int i = 0, jj = warp;           // shared row (i, jj), jj fastest
+                // two shared rows per warp instruction, a pair of packed columns per lane: tiles start on
+                // even columns and the half-ring is even, so a pair never straddles the wrap and its
+                // global address is 8-byte aligned
+                const int half = lane >> 4, pc = 2 * (lane & 15);
+                int gp = m0 - S + pc;
+                gp = gp < 0 ? gp + nh : (gp >= nh ? gp - nh : gp);
+                int i = 0, jj = 2 * warp + half;
                 walk(i, jj, 0, RJ);
-                for (; i < im; walk(i, jj, TB_WARPS, RJ)) {
+                for (; i < im; walk(i, jj, 2 * TB_WARPS, RJ)) {
                     const int j = jb + jj;
                     if (j < 0 || j >= jm) continue;
                     const int r = i * RJ + jj;
-                    const int64_t g = ((int64_t)i * jm + j) * kh + gm;
-                    if (lane < TM + 2 * S) {
-                        cp_async4(sp + r * TB_LANES + lane, A0 + g);
-                        cp_async4(sp + cs + r * TB_LANES + lane, A1 + g);
+                    const int64_t g = ((int64_t)i * jm + j) * kh + gp;
+                    if (pc < TM + 2 * S) {
+                        cp_async8(sp + r * TB_LANES + pc, A0 + g);
+                        cp_async8(sp + cs + r * TB_LANES + pc, A1 + g);
                     }
-                    if (lane < 4) cp_async4(reinterpret_cast<float*>(sw + r) + lane,
-                                            reinterpret_cast<const float*>(wt + (int64_t)i * jm + j) + lane);
+                    if (pc < 4) cp_async8(reinterpret_cast<float*>(sw + r) + pc,
+                                          reinterpret_cast<const float*>(wt + (int64_t)i * jm + j) + pc);
                 }
                 cp_async_wait_all();
             }
@@ -390,42 +419,51 @@ __global__ void __launch_bounds__(32 * TB_WARPS) sor_tb_kernel(const KConst K, c
                 const float* const fc = c ? f1 : f0;
                 const int jlo = max(1, j0 - e), nj = min(jm - 2, j1 - 1 + e) - jlo + 1;
                 const int klo = -e, khi = 2 * TM + e;          // phi range relative to 2 m0
-                // this lane updates the cell of parity p (k = 2 m + p) of its column where ok[p]
-                const bool ok0 = 2 * (lane - S) >= klo && 2 * (lane - S) < khi;
-                const bool ok1 = 2 * (lane - S) + 1 >= klo && 2 * (lane - S) + 1 < khi;
-                // work items: (row jr, segment sg of TB_SEG levels), segment fastest
-                int jr = 0, sg = warp;
+                // this lane's pair of packed columns pc, pc+1 (phi 2 (pc - S) + par and 2 (pc + 1 - S) + par
+                // relative to 2 m0) and whether each is updated for parity 0 (a0, a1) and 1 (b0, b1)
+                const int half = lane >> 4, pc = 2 * (lane & 15), kl = 2 * (pc - S);
+                const bool a0 = kl >= klo && kl < khi, a1 = kl + 2 >= klo && kl + 2 < khi;
+                const bool b0 = kl + 1 >= klo && kl + 1 < khi, b1 = kl + 3 >= klo && kl + 3 < khi;
+                int gp = m0 - S + pc;
+                gp = gp < 0 ? gp + nh : (gp >= nh ? gp - nh : gp);
+                // work items of the half-warps: (row jr, segment sg of TB_SEG levels), segment fastest
+                int jr = 0, sg = 2 * warp + half;
                 walk(jr, sg, 0, nseg);
-                for (; jr < nj; walk(jr, sg, TB_WARPS, nseg)) {
+                for (; jr < nj; walk(jr, sg, 2 * TB_WARPS, nseg)) {
                     const int j = jlo + jr, jj = j - jb;
                     const int i0 = 1 + sg * TB_SEG, nl = min(TB_SEG, NI + 1 - i0);
-                    const float* fp = fc + ((int64_t)i0 * jm + j) * kh + gm;
-                    float fv[TB_SEG];
+                    const float* fp = fc + ((int64_t)i0 * jm + j) * kh + gp;
+                    float2 fv[TB_SEG];
 #pragma unroll
-                    for (int u = 0; u < TB_SEG; u++) fv[u] = (u < nl) ? __ldg(fp + u * GP) : 0.0f;
+                    for (int u = 0; u < TB_SEG; u++)
+                        fv[u] = (u < nl) ? __ldg(reinterpret_cast<const float2*>(fp + u * GP)) : make_float2(0.0f, 0.0f);
                     const bool jlow = (j == 2 && jj >= 2), jhigh = (j == jm - 3 && jj + 2 < RJ);
-                    const int q0 = i0 * PL + jj * TB_LANES + lane, par0 = (i0 + j + c) & 1;
+                    const int q0 = i0 * PL + jj * TB_LANES + pc, par0 = (i0 + j + c) & 1;
                     const SorW<float>* wp = sw + i0 * RJ + jj;
                     if (nl == TB_SEG && i0 > 2 && i0 + TB_SEG <= im - 3 && !jlow && !jhigh)
-                        tb_segment<false>(own, oth, wp, fv, q0, par0, ok0, ok1, PL, RJ, TB_SEG, i0, im, false, false,
-                                          w, c43, c13, c);
+                        tb_segment<false>(own, oth, wp, fv, q0, par0, a0, a1, b0, b1, PL, RJ, TB_SEG, i0, im, false,
+                                          false, w, c43, c13, c);
                     else
-                        tb_segment<true>(own, oth, wp, fv, q0, par0, ok0, ok1, PL, RJ, nl, i0, im, jlow, jhigh,
+                        tb_segment<true>(own, oth, wp, fv, q0, par0, a0, a1, b0, b1, PL, RJ, nl, i0, im, jlow, jhigh,
                                          w, c43, c13, c);
                 }
                 __syncthreads();
             }
-            // the owned cells, with the folded rows next to the owned boundary rows
+            // the owned cells, with the folded rows next to the owned boundary rows: a pair of columns per
+            // lane, two rows per warp instruction
             const int jsl = (j0 == 1) ? 0 : j0, nrow = ((j1 == jm - 1) ? jm - 1 : j1 - 1) - jsl + 1;
-            if (lane >= S && lane < S + TM) {
-                int jr = 0, i = warp;
-                walk(jr, i, 0, im);
-                for (; jr < nrow; walk(jr, i, TB_WARPS, im)) {
-                    const int j = jsl + jr;
-                    const int q = i * PL + (j - jb) * TB_LANES + lane;
-                    const int64_t g = ((int64_t)i * jm + j) * kh + (m0 + lane - S);
-                    B0[g] = sp[q];
-                    B1[g] = sp[cs + q];
+            {
+                const int half = lane >> 4, pc = 2 * (lane & 15);
+                if (pc >= S && pc < S + TM) {
+                    int jr = 0, i = 2 * warp + half;
+                    walk(jr, i, 0, im);
+                    for (; jr < nrow; walk(jr, i, 2 * TB_WARPS, im)) {
+                        const int j = jsl + jr;
+                        const int q = i * PL + (j - jb) * TB_LANES + pc;
+                        const int64_t g = ((int64_t)i * jm + j) * kh + (m0 + pc - S);
+                        *reinterpret_cast<float2*>(B0 + g) = *reinterpret_cast<const float2*>(sp + q);
+                        *reinterpret_cast<float2*>(B1 + g) = *reinterpret_cast<const float2*>(sp + cs + q);
+                    }
                 }
             }
             __syncthreads();
@@ -792,13 +830,14 @@ void build_D(const PoissonSolver& P, int m, int jj, std::vector<double>& D, bool
 void plan_tb(PoissonSolver* P, int S, int dev, int nsm) {
     const KConst& K = P->K;
     const int nh = P->S.n / 2, NJ = K.jm - 2;
+    if ((nh & 1) || (S & 1)) return;          // column pairs: an even half-ring, an even halo
     const int ntm = (nh + TB_LANES - 2 * S - 1) / (TB_LANES - 2 * S);
     int optin = 0;
     if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
         cudaGetLastError();
         return;
     }
-    const void* fn = (S == 2) ? (const void*)sor_tb_kernel<2> : (const void*)sor_tb_kernel<3>;
+    const void* fn = (const void*)sor_tb_kernel<2>;
     // the kernel's limit: the device's, less the kernel's static shared memory (handles on other grids
     // share the function)
     cudaFuncAttributes fa{};
@@ -820,11 +859,14 @@ void plan_tb(PoissonSolver* P, int S, int dev, int nsm) {
             cudaGetLastError();
             return;
         }
+        // tile boundaries along m rounded to even columns (the pairs of the tile loads and stores)
+        auto mb = [&](int tm) { return (tm * nh / ntm) & ~1; };
         P->tb_tiles_h.clear();
         for (int t = 0; t < ntm * ntj; t++) {
             const int tm = t % ntm, tj = t / ntm;
-            const int m0 = tm * nh / ntm, j0 = 1 + tj * NJ / ntj;
-            P->tb_tiles_h.push_back(TbTile{m0, (tm + 1) * nh / ntm - m0, j0, 1 + (tj + 1) * NJ / ntj});
+            const int m0 = mb(tm), m1 = (tm + 1 == ntm) ? nh : mb(tm + 1), j0 = 1 + tj * NJ / ntj;
+            if (m1 - m0 < 2 || m1 - m0 + 2 * S > TB_LANES) return;
+            P->tb_tiles_h.push_back(TbTile{m0, m1 - m0, j0, 1 + (tj + 1) * NJ / ntj});
         }
         P->tb = TbPlan{ntm * ntj, tjmax + 4 * S, nh};
         P->tb_S = S;
@@ -1023,9 +1065,9 @@ PoissonSolver* poisson_create(const KConst& kc, const ColGeo* geo_dev, const std
             if (P->coop_blocks64 < 1 || P->coop_blocks32 < 1) P->packed = false;
         }
         if (P->packed) {
+            // ATSAT_SOR_SWEEPS_PER_PASS=1 keeps the one-sweep-per-phase kernel (a comparison switch)
             const char* ev = std::getenv("ATSAT_SOR_SWEEPS_PER_PASS");
-            const int want = ev ? std::atoi(ev) : 2;
-            if (want == 2 || want == 3) plan_tb(P, want, dev, nsm);
+            if (!(ev && std::atoi(ev) == 1)) plan_tb(P, 2, dev, nsm);
         }
     }
     std::vector<float> W32(nW);
@@ -1144,7 +1186,7 @@ cudaError_t sor_packed_run(PoissonSolver* P, const T* f, T* p, T w, int nsweeps,
         void* args[] = {(void*)&K, (void*)&wt, (void*)&tiles, (void*)&p0, (void*)&p1, (void*)&b0, (void*)&b1,
                         (void*)&f0, (void*)&f1, (void*)&kh, (void*)&nsweeps, (void*)&w, (void*)&pl,
                         (void*)&P->bar, (void*)&limit};
-        const void* fn = (P->tb_S == 2) ? (const void*)sor_tb_kernel<2> : (const void*)sor_tb_kernel<3>;
+        const void* fn = (const void*)sor_tb_kernel<2>;
         e = cudaLaunchCooperativeKernel(fn, dim3(P->tb_grid), dim3(32, TB_WARPS), args, P->tb_smem, P->stream);
         if (e != cudaSuccess) return e;
         if ((((nsweeps + P->tb_S - 1) / P->tb_S) & 1) == 1) {     // an odd number of passes: the result is in B
