@@ -266,7 +266,9 @@ __global__ void __launch_bounds__(32 * SORP_WARPS) sor_packed_kernel(const KCons
 // ---- the same sweeps temporally blocked (FP32): S sweeps per grid barrier ----
 // A block owns a tile of rows j0 .. j1-1 and packed columns m0 .. m1-1 over every radial level (the folded
 // planes i = 0 and im-1 included) and holds it in shared memory, both colours, with a halo of 2S rows and
-// S packed columns (2S cells along phi) on each side: TB_LANES packed columns per shared row, one per lane.
+// S packed columns (2S cells along phi) on each side: TB_LANES packed columns per shared row, a pair of them
+// per lane of a half-warp (tiles start on even columns and the half-ring is even, so a pair never straddles
+// the periodic wrap).
 // A pass loads the halo'd tile from the current packed arrays, runs 2S half-sweeps in shared memory --
 // half-sweep h updates the cells within 2S - h cells of the owned tile, the cone the owned cells depend
 // on -- and writes the owned cells (with the folded rows j = 0 / jm-1 where it owns the rows next to them)
