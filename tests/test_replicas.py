@@ -74,3 +74,42 @@ def test_reference_arm_json_contract():
     assert d["n_gpus"] == 1 and d["warmup"] >= 3 and d["higher_is_better"] is True
     assert d["cpu_baseline"]["value"] == d["value"] and d["e2e"]["value"] == d["value"]
     assert "workload" in d["config"]
+
+
+def test_clock_samples_kept_for_the_timed_region():
+    """bench.py's clock sampler keeps the nvidia-smi samples whose timestamps fall inside the timed region,
+    reports the throttle reasons seen there, and falls back to every sample (saying so) when none does."""
+    import datetime
+    sys.path.insert(0, ROOT)
+    import bench
+    c = bench.Clocks()
+
+    def line(t, sm, reason="Not Active"):
+        stamp = datetime.datetime.fromtimestamp(t).strftime("%Y/%m/%d %H:%M:%S.%f")[:-3]
+        return f"{stamp}, 0, {sm}, 2070, 900.0, 0x0, {reason}, Not Active, Not Active, Not Active"
+
+    t0 = 1_700_000_000.0
+    c.lines = [line(t0 - 1.0, 345, "Active"), line(t0 + 0.1, 2070), line(t0 + 0.2, 2055), line(t0 + 0.3, 2070),
+               line(t0 + 2.0, 900, "Active")]
+    c.p = None
+    c.t0, c.t1 = t0, t0 + 0.5
+
+    class _Done:
+        def terminate(self):
+            pass
+
+        def wait(self, timeout=None):
+            return 0
+
+    class _T:
+        def join(self, timeout=None):
+            pass
+
+    c.p, c.t = _Done(), _T()
+    r = c.stop()
+    assert r["samples"] == 3 and r["window"] == "timed region"
+    assert r["sm_mhz"] == 2070.0 and r["sm_max_mhz"] == 2070.0 and r["reasons"] == []
+    c.lines = [line(t0 - 1.0, 345, "Active")]
+    c.t0, c.t1 = t0, t0 + 0.5
+    r = c.stop()
+    assert r["samples"] == 1 and r["window"].startswith("whole") and r["reasons"] == ["hw_slowdown"]
