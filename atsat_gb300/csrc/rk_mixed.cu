@@ -330,10 +330,20 @@ __global__ void __launch_bounds__(256) final_combine_kernel(const MixedConstF K,
     const int k = blockIdx.x * 32 + threadIdx.x, j = 2 + blockIdx.y * 8 + threadIdx.y, i = 1 + blockIdx.z;
     if (k > K.km - 2 || j > K.jm - 3 || i > K.im - 2) return;
     const int64_t c = ((int64_t)i * K.jm + j) * K.kp + k;
+    // every field's loads first: the stores below could alias them as far as the compiler knows, so loads
+    // issued between stores would wait for each other (one field in flight per thread)
+    double yn[NPROG];
+    float inc[NPROG];
+#pragma unroll
+    for (int q = 0; q < NPROG; q++) {
+        const bool in = q >= q0 && q <= q1;
+        yn[q] = in ? ldd(io.yn64[q] + c) : 0.0;
+        inc[q] = in ? __ldg(io.dl1[q] + c) : 0.0f;
+    }
 #pragma unroll
     for (int q = 0; q < NPROG; q++) {
         if (q < q0 || q > q1) continue;
-        double y = ldd(io.yn64[q] + c) + f2d(io.dl1[q][c]);
+        double y = yn[q] + f2d(inc[q]);
         if (q == ATSAT_F_TKE) y = smin(smax(y, 0.0), K.tke_max_d);
         else if (q == ATSAT_F_DIS) y = smax(y, K.dis_min_d);
         io.out64[q][c] = y;
