@@ -160,26 +160,40 @@ __global__ void __launch_bounds__(256) mixed_prepare_kernel(const KConst K, cons
     // dl0[0] is the stage-0 input (every cell); dl0[1], dl0[2] need live - y_n only where no stage writes
     const bool rk_cell = (i >= 1 && i <= K.im - 2 && j >= 2 && j <= K.jm - 3 && k <= K.km - 2);
     if (pr.write_yn32 || pr.any_dl0) {
-#pragma unroll 4
-        for (int q = 0; q < NPROG; q++) {
-            const bool y32 = pr.write_yn32 && pr.yn32[q];
-            if (!y32 && !pr.dl0[0][q]) continue;
-            const double yn = __ldg(pr.yn64[q] + c);
-            if (y32) {
-                const float hi = d2f(yn);
-                pr.yn32[q][c] = hi;
-                if (pr.yn32_b[q]) pr.yn32_b[q][c] = hi;
-                if (q == ATSAT_F_W && pr.wlo) {
-                    const float lo = d2f(yn - f2d(hi));
-                    pr.wlo[c] = lo;
-                    if (pr.wlo_b) pr.wlo_b[c] = lo;
-                }
-            }
-            if (pr.dl0[0][q]) {
-                const float d0 = d2f(__ldg(pr.live64[q] + c) - yn);
+        // four fields at a time, their loads issued before their stores (the FP32 stores could alias the FP64
+        // loads as far as the compiler knows, so loads left between them would wait one field at a time)
+        for (int q0 = 0; q0 < NPROG; q0 += 4) {
+            double ynv[4], lvv[4];
 #pragma unroll
-                for (int b = 0; b < 3; b++)
-                    if (pr.dl0[b][q] && (b == 0 || !rk_cell)) pr.dl0[b][q][c] = d0;
+            for (int u = 0; u < 4; u++) {
+                const int q = q0 + u;
+                const bool have = q < NPROG, dl = have && pr.dl0[0][q];
+                ynv[u] = (have && ((pr.write_yn32 && pr.yn32[q]) || dl)) ? __ldg(pr.yn64[q] + c) : 0.0;
+                lvv[u] = dl ? __ldg(pr.live64[q] + c) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int q = q0 + u;
+                if (q >= NPROG) break;
+                const bool y32 = pr.write_yn32 && pr.yn32[q];
+                if (!y32 && !pr.dl0[0][q]) continue;
+                const double yn = ynv[u];
+                if (y32) {
+                    const float hi = d2f(yn);
+                    pr.yn32[q][c] = hi;
+                    if (pr.yn32_b[q]) pr.yn32_b[q][c] = hi;
+                    if (q == ATSAT_F_W && pr.wlo) {
+                        const float lo = d2f(yn - f2d(hi));
+                        pr.wlo[c] = lo;
+                        if (pr.wlo_b) pr.wlo_b[c] = lo;
+                    }
+                }
+                if (pr.dl0[0][q]) {
+                    const float d0 = d2f(lvv[u] - yn);
+#pragma unroll
+                    for (int b = 0; b < 3; b++)
+                        if (pr.dl0[b][q] && (b == 0 || !rk_cell)) pr.dl0[b][q][c] = d0;
+                }
             }
         }
     }
