@@ -521,8 +521,9 @@ void  atsat_dyn_host_free(void* p);
  * The call runs on the current device: t, p_stat and buoy_out must be device memory of that device (or
  * managed memory), else ATSAT_DYN_E_INVALID. It returns ATSAT_DYN_E_CUDA without launching anything when a CUDA error from
  * earlier work is already pending (and leaves that error for its owner).
- * The first call on a device looks up the scratch array's device address there (once per device); make
- * that first call before any stream capture begins. All calls on a device share the one scratch array:
+ * The call cannot be captured into a CUDA graph: it copies the_z from pageable host memory and waits for
+ * its stream. The first call on a device also looks up the scratch array's device address there (once per
+ * device). All calls on a device share the one scratch array:
  * calls whose GPU work overlaps (different streams or host threads at once) race on it and must be
  * serialised by the caller. Each call rewrites the scratch it reads, so nothing carries over from the
  * previous call. */
