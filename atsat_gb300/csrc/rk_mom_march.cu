@@ -48,8 +48,9 @@ static_assert(PLANE_PAD >= PLANE_F, "plane padding");
 
 // The rings of one launch. Regular: 4 halo slots and 3 point slots (2 at the final stage), two blocks per
 // SM. Compact (intermediate stages with at most 12 point arrays): 3 halo slots and 2 point slots in 74 KB,
-// three blocks per SM; its producer issues each level's point group one level ahead (H0 H1 P0 H2 P1 ...),
-// so that both rings keep one level in flight.
+// three blocks per SM, its producer issuing H0 H1 P0 H2 P1 ... The consumers free the slot of plane m+1 at
+// the end of level m, so with either ring size and either order each group is issued a level before the
+// level that reads it (tests/test_march_rings.py replays both schedules).
 template <int MODE, bool CMP>
 struct Shape {
     static constexpr int NHG = CMP ? 3 : 4;                                         // halo slots

@@ -257,9 +257,9 @@ def test_march_depths_agree(shape, levels, knobs):
     """The radial march at several march depths (runs of 1 level to whole columns, runs that do not divide
     the interior levels evenly, odd-seam grids) runs the same per-cell arithmetic as the direct kernel:
     after three iterations their states agree far inside the mixed-precision bar. At the default knobs the
-    intermediate stages stream 11 point arrays and run the compact rings (three blocks per SM, each level's
-    point group issued a level ahead); with the radiation and thermal mass-flux sources on, 14 point arrays
-    and the regular rings."""
+    intermediate stages stream 11 point arrays and run the compact rings (3 halo and 2 point slots, three
+    blocks per SM); with the radiation and thermal mass-flux sources on, 14 point arrays and the regular
+    rings."""
     from atsat_gb300 import dyn
     g, P, st = case(shape, seed=59, exercise=True, **knobs)
     a = st.copy()
