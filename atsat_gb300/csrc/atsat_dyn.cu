@@ -1501,8 +1501,10 @@ int enqueue_bc(atsat_dyn* h, bool resident = false) {
     const int bc_inputs[6] = {ATSAT_F_NUE, ATSAT_F_MASSFLUX_H2S, ATSAT_F_MASSFLUX_NH3, ATSAT_F_MASSFLUX_NH4SH,
                               ATSAT_F_FLUXLIM_NH4SH, ATSAT_F_THERMALMASSFLUX};
     if (mixed)
-        for (int fid : bc_inputs)
-            if (!h->conv_dirty[conv_slot(fid)]) s32[fid] = h->conv32[conv_slot(fid)];
+        for (int fid : bc_inputs) {
+            const int slot = conv_slot(fid);
+            if (slot >= 0 && !h->conv_dirty[slot]) s32[fid] = h->conv32[slot];
+        }
     CK(h, launch_boundary_conditions(h->kc, h->p, h->f, mixed ? s32 : nullptr, shadows ? h->wlo_o : nullptr,
                                      h->stream));
     h->launches += 3;

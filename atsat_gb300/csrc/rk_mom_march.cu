@@ -56,7 +56,6 @@ struct Shape {
     static constexpr int NHG = CMP ? 3 : 4;                                         // halo slots
     static constexpr int NPG = CMP ? 2 : ((MODE == MODE_FINAL) ? 2 : 3);            // point slots
     static constexpr int NPT = (MODE == MODE_FINAL) ? MARCH_MAX_PT : (CMP ? 12 : 14);
-    static constexpr int MINB = CMP ? 3 : 2;                                        // blocks per SM
     static constexpr int PG_F = GEO_F + NPT * PT_F;
     static constexpr int HG_F = NHA_MAX * HP_F;
     static constexpr size_t SMEM = (size_t)(NHG * HG_F + NPG * PG_F) * 4 + 2 * (NHG + NPG) * 8;
